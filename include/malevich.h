@@ -1,0 +1,329 @@
+/* malevich.h: C ABI of the GB300-native Malevich draw path.
+ *
+ * A Direct3D-11-flavoured API over hand-written CUDA kernels for sm_103a. The reference
+ * (OzgurCerlet/Malevich) has no device, context or resource objects: it draws through one global
+ * `Pipeline graphics_pipeline` whose fields are assigned directly (source/main.c:109-115,222,
+ * 1276-1294) and three functions, draw_indexed (main.c:1219), clear_render_target_view
+ * (main.c:1191) and clear_depth_stencil_view (main.c:1204). Every entry point below names the
+ * reference field or function it replaces. Each function returns an mlv_status; nothing aborts.
+ *
+ * Threading: a device may be used from several threads for resource creation; a context is
+ * one CUDA stream and, like an ID3D11DeviceContext, is not thread-safe. Work is queued
+ * asynchronously; readbacks and mlv_finish synchronise and report device-side errors.
+ */
+#ifndef MALEVICH_H
+#define MALEVICH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define MLV_API __attribute__((visibility("default")))
+#else
+#define MLV_API
+#endif
+
+#define MLV_ABI_VERSION 1
+
+/* ------------------------------------------------------------------ status */
+
+typedef enum mlv_status {
+    MLV_OK = 0,
+    MLV_ERROR_INVALID_ARG = 1,        /* a NULL handle, a size or format the call cannot take */
+    MLV_ERROR_OUT_OF_MEMORY = 2,
+    MLV_ERROR_CAPACITY_EXCEEDED = 3,  /* an internal buffer overflowed and could not be regrown */
+    MLV_ERROR_DEVICE = 4,             /* a CUDA error; see mlv_get_last_error_string */
+    MLV_ERROR_TIMEOUT = 5,            /* a bounded device-side wait gave up */
+    MLV_ERROR_UNSUPPORTED = 6,
+    MLV_ERROR_INVALID_STATE = 7       /* e.g. a draw with no render target bound */
+} mlv_status;
+
+/* Message of the last failing call on this thread (never NULL). */
+MLV_API const char *mlv_get_last_error_string(void);
+MLV_API int mlv_get_abi_version(void);
+
+/* ------------------------------------------------------------------ handles */
+
+typedef struct mlv_device_t *mlv_device;
+typedef struct mlv_context_t *mlv_context;
+typedef struct mlv_buffer_t *mlv_buffer;
+typedef struct mlv_texture2d_t *mlv_texture2d;
+typedef struct mlv_command_list_t *mlv_command_list;
+
+/* ------------------------------------------------------------------ formats and descriptors */
+
+typedef enum mlv_format {
+    MLV_FORMAT_UNKNOWN = 0,
+    /* 32-bit texel, R in the low byte (common_shader_core.h:26-36, math.h:326-344). Also the
+     * render-target format: the reference's clear packs R in the low byte (math.h:322-324) and its
+     * output merger stores R<<16 | G<<8 | B (main.c:1176-1178); both packings are kept. */
+    MLV_FORMAT_R8G8B8A8_UNORM = 1,
+    MLV_FORMAT_R16G16B16A16_FLOAT = 2,  /* new: widened exactly to float before filtering */
+    MLV_FORMAT_R32G32B32A32_FLOAT = 3,  /* float4 texels (common_shader_core.h:38-53) */
+    MLV_FORMAT_D32_FLOAT = 4,           /* depth buffer (main.c:36) */
+    MLV_FORMAT_R32_UINT = 5,            /* index buffers (main.c:72); triangle-ID targets */
+    MLV_FORMAT_R32G32_FLOAT = 6         /* barycentric targets */
+} mlv_format;
+
+typedef enum mlv_bind_flag {
+    MLV_BIND_VERTEX_BUFFER = 0x1,
+    MLV_BIND_INDEX_BUFFER = 0x2,
+    MLV_BIND_CONSTANT_BUFFER = 0x4,
+    MLV_BIND_SHADER_RESOURCE = 0x8,
+    MLV_BIND_RENDER_TARGET = 0x20,
+    MLV_BIND_DEPTH_STENCIL = 0x40,
+    MLV_BIND_UNORDERED_ACCESS = 0x80
+} mlv_bind_flag;
+
+typedef struct mlv_buffer_desc {
+    uint64_t byte_width;
+    uint32_t bind_flags;
+    uint32_t reserved;
+} mlv_buffer_desc;
+
+typedef struct mlv_texture2d_desc {
+    uint32_t width, height;
+    mlv_format format;
+    uint32_t bind_flags;
+} mlv_texture2d_desc;
+
+/* Viewport, main.c:85-92 */
+typedef struct mlv_viewport {
+    float top_left_x, top_left_y, width, height, min_depth, max_depth;
+} mlv_viewport;
+
+/* PrimitiveTopology, main.c:66-69: triangle lists only */
+typedef enum mlv_primitive_topology {
+    MLV_PRIMITIVE_TOPOLOGY_UNDEFINED = 0,
+    MLV_PRIMITIVE_TOPOLOGY_TRIANGLELIST = 1
+} mlv_primitive_topology;
+
+/* Culling. The reference always culls triangles whose signed screen-space area (y down, 28.4
+ * fixed point) is positive (main.c:851-856): that is MLV_CULL_BACK, the default. */
+typedef enum mlv_cull_mode { MLV_CULL_NONE = 1, MLV_CULL_FRONT = 2, MLV_CULL_BACK = 3 } mlv_cull_mode;
+
+typedef struct mlv_rasterizer_desc {
+    mlv_cull_mode cull_mode;
+} mlv_rasterizer_desc;
+
+/* Depth test. The reference tests GREATER_EQUAL (reversed Z, main.c:1166) against a tile
+ * minimum for hierarchical Z (main.c:1005-1006). LESS is new; it keeps a mirrored tile maximum. */
+typedef enum mlv_comparison_func {
+    MLV_COMPARISON_LESS = 2,
+    MLV_COMPARISON_GREATER_EQUAL = 7
+} mlv_comparison_func;
+
+typedef struct mlv_depth_stencil_desc {
+    int32_t depth_enable;              /* must be 1 */
+    mlv_comparison_func depth_func;
+} mlv_depth_stencil_desc;
+
+/* ------------------------------------------------------------------ shaders
+ * The reference calls shaders through host function pointers (VS::shader, PS::shader,
+ * main.c:79,99; common_shader_core.h:10-18). A GPU cannot call those, so shaders are built-in
+ * and selected by id. Each keeps the reference's stage input/output layout, given below for one
+ * vertex or fragment (the reference stores them 8-wide SoA: v3f256 = three __m256). */
+typedef enum mlv_vertex_shader_id {
+    MLV_VS_BASIC = 1,            /* basic_vs.c:22-35 */
+    MLV_VS_VERTEX_LIGHTING = 2,  /* vertex_lighting_vs.c:22-41 (VS SRV 0: float lat-long map) */
+    MLV_VS_PASSTHROUGH = 3,      /* passthrough_vs.c:16-27 */
+    MLV_VS_FULLSCREEN = 4,       /* fullscreen_vs.c:22-41 */
+    MLV_VS_PASSTHROUGH_UV = 5    /* new: passthrough with a UV, for the differentiable path */
+} mlv_vertex_shader_id;
+
+typedef enum mlv_pixel_shader_id {
+    MLV_PS_BASIC = 1,            /* basic_ps.c:16-29 (PS SRV 0: RGBA8) */
+    MLV_PS_PASSTHROUGH = 2,      /* passthrough_ps.c:13-22 */
+    MLV_PS_ENV_LIGHTING = 3,     /* env_lighting_ps.c:13-26 (PS SRV 0: float lat-long map) */
+    MLV_PS_COLOR_TIMES_TEXEL = 4 /* new: COLOR * bilinear(SRV 0, UV).xyz */
+} mlv_pixel_shader_id;
+
+/* Vs_Input of basic_vs / vertex_lighting_vs (basic_vs.c:3-7): 32 bytes */
+typedef struct mlv_vertex_basic { float position[3]; float normal[3]; float uv[2]; } mlv_vertex_basic;
+/* Vs_Input of passthrough_vs (passthrough_vs.c:3-7): position already in [0,1] screen space */
+typedef struct mlv_vertex_passthrough { float position[4]; float color[3]; float pad; } mlv_vertex_passthrough;
+/* Vs_Input of fullscreen_vs (fullscreen_vs.c:3-7) */
+typedef struct mlv_vertex_fullscreen { float position[4]; float view_dir[3]; float pad; } mlv_vertex_fullscreen;
+/* Vs_Input of MLV_VS_PASSTHROUGH_UV (new): x, y in [0,1] screen space, z depth, w = 1 */
+typedef struct mlv_vertex_passthrough_uv { float position[3]; float color[3]; float uv[2]; } mlv_vertex_passthrough_uv;
+
+/* Vs_Output (basic_vs.c:9-14): three float4 registers per vertex, r0 = SV_POSITION,
+ * r1 = (NORMAL|COLOR|VIEW_DIR).xyz + UV.x, r2 = UV.y + 3 pad (main.c:1286-1287: 12 floats) */
+typedef struct mlv_vs_output { float sv_position[4]; float attr[3]; float uv[2]; float pad[3]; } mlv_vs_output;
+/* Ps_Input (basic_ps.c:3-7) and Ps_Output (basic_ps.c:9-11) */
+typedef struct mlv_ps_input { float sv_position[4]; float attr[3]; float uv[2]; } mlv_ps_input;
+typedef struct mlv_ps_output { float sv_target[4]; } mlv_ps_output;
+
+/* VS constant buffer slot 0 of the reference's shaders: PerFrameCB (main.c:169-173), row-major
+ * matrices applied to column vectors. */
+typedef struct mlv_per_frame_cb {
+    float clip_from_world[16];
+    float view_from_clip[16];
+    float world_from_view[16];
+} mlv_per_frame_cb;
+
+#define MLV_CONSTANT_BUFFER_SLOT_COUNT 16   /* main.c:41 */
+#define MLV_SHADER_RESOURCE_SLOT_COUNT 16   /* main.c:42 */
+
+/* ------------------------------------------------------------------ device and contexts */
+
+/* Creates a device on CUDA device `cuda_ordinal` (the reference has one implicit global). */
+MLV_API mlv_status mlv_create_device(int cuda_ordinal, mlv_device *out_device);
+MLV_API mlv_status mlv_destroy_device(mlv_device device);
+/* The immediate context: draws execute as they are issued (main.c:1284-1296 calls
+ * draw_indexed once per object). */
+MLV_API mlv_status mlv_get_immediate_context(mlv_device device, mlv_context *out_context);
+/* A deferred context records commands into a command list; executing the list runs all its
+ * draws, across all the render targets they use, as one batched launch sequence that is captured
+ * in a CUDA graph on first execution and replayed afterwards. */
+MLV_API mlv_status mlv_create_deferred_context(mlv_device device, mlv_context *out_context);
+MLV_API mlv_status mlv_destroy_context(mlv_context context);
+
+/* ------------------------------------------------------------------ resources
+ * The reference borrows caller pointers (IA::p_index_buffer, IA::p_vertex_buffer, Texture2D::p_data,
+ * OM::p_colors/p_depth, main.c:71-107). Here resources own device memory; init data is copied. */
+MLV_API mlv_status mlv_create_buffer(mlv_device device, const mlv_buffer_desc *desc, const void *init_data,
+                                     mlv_buffer *out_buffer);
+MLV_API mlv_status mlv_destroy_buffer(mlv_buffer buffer);
+/* row_pitch: bytes between rows of init_data (0 = tightly packed). Depth textures carry the
+ * per-8x8-tile hierarchical-Z state (main.c:230). */
+MLV_API mlv_status mlv_create_texture2d(mlv_device device, const mlv_texture2d_desc *desc, const void *init_data,
+                                        uint32_t row_pitch, mlv_texture2d *out_texture);
+MLV_API mlv_status mlv_destroy_texture2d(mlv_texture2d texture);
+/* Raw device addresses for zero-copy interop (e.g. wrapping a render target as a tensor). */
+MLV_API mlv_status mlv_buffer_device_pointer(mlv_buffer buffer, void **out_ptr);
+MLV_API mlv_status mlv_texture2d_device_pointer(mlv_texture2d texture, void **out_ptr);
+
+/* Copies host data into a resource, ordered with the context's queued work. */
+MLV_API mlv_status mlv_update_buffer(mlv_context context, mlv_buffer buffer, uint64_t offset, const void *data,
+                                     uint64_t size);
+MLV_API mlv_status mlv_update_texture2d(mlv_context context, mlv_texture2d texture, const void *data,
+                                        uint32_t row_pitch);
+/* Waits for the context's queued work, then copies the texture to host memory. */
+MLV_API mlv_status mlv_read_texture2d(mlv_context context, mlv_texture2d texture, void *dst, uint32_t row_pitch);
+
+/* ------------------------------------------------------------------ pipeline state (Pipeline, main.c:109-115) */
+
+/* IA::primitive_topology (main.c:75) */
+MLV_API mlv_status mlv_ia_set_primitive_topology(mlv_context context, mlv_primitive_topology topology);
+/* IA::p_index_buffer (main.c:72); format must be MLV_FORMAT_R32_UINT, offset in bytes */
+MLV_API mlv_status mlv_ia_set_index_buffer(mlv_context context, mlv_buffer buffer, mlv_format format,
+                                           uint32_t offset);
+/* IA::p_vertex_buffer and IA::input_layout (main.c:73-74); one slot; stride >= 32 bytes, the VS
+ * reads the first 32 bytes of each vertex (main.c:684-691) */
+MLV_API mlv_status mlv_ia_set_vertex_buffers(mlv_context context, uint32_t start_slot, uint32_t num_buffers,
+                                             const mlv_buffer *buffers, const uint32_t *strides,
+                                             const uint32_t *offsets);
+/* VS::shader and VS::output_register_count (main.c:79-80, 1287-1288) */
+MLV_API mlv_status mlv_vs_set_shader(mlv_context context, mlv_vertex_shader_id shader);
+/* VS::p_constant_buffers (main.c:81, 1281) */
+MLV_API mlv_status mlv_vs_set_constant_buffers(mlv_context context, uint32_t start_slot, uint32_t num_buffers,
+                                               const mlv_buffer *buffers);
+/* VS::p_shader_resource_views (main.c:82, 1293) */
+MLV_API mlv_status mlv_vs_set_shader_resources(mlv_context context, uint32_t start_slot, uint32_t num_views,
+                                               const mlv_texture2d *textures);
+/* PS::shader (main.c:99, 1289) */
+MLV_API mlv_status mlv_ps_set_shader(mlv_context context, mlv_pixel_shader_id shader);
+/* PS::p_shader_resource_views (main.c:100, 1294) */
+MLV_API mlv_status mlv_ps_set_shader_resources(mlv_context context, uint32_t start_slot, uint32_t num_views,
+                                               const mlv_texture2d *textures);
+/* RS::viewport (main.c:94-96, 1277-1278); one viewport */
+MLV_API mlv_status mlv_rs_set_viewports(mlv_context context, uint32_t num_viewports, const mlv_viewport *viewports);
+/* cull mode (the reference hard-codes back-face culling, main.c:856) */
+MLV_API mlv_status mlv_rs_set_state(mlv_context context, const mlv_rasterizer_desc *desc);
+/* depth function (the reference hard-codes GREATER_EQUAL, main.c:1166) */
+MLV_API mlv_status mlv_om_set_depth_stencil_state(mlv_context context, const mlv_depth_stencil_desc *desc);
+/* OM::p_colors, OM::p_depth (main.c:103-107, 1279-1280). The render target is
+ * MLV_FORMAT_R8G8B8A8_UNORM, the depth target MLV_FORMAT_D32_FLOAT, of the same size. */
+MLV_API mlv_status mlv_om_set_render_targets(mlv_context context, mlv_texture2d render_target,
+                                             mlv_texture2d depth_stencil);
+/* Optional visibility targets (new): for every pixel the last writer's triangle id (the index the
+ * reference's primitive assembly gives it within its draw, main.c:873-875) in an R32_UINT texture,
+ * its draw number within the bound render target's draws since the last clear in a second
+ * R32_UINT texture, and its quantised barycentrics (b1, b2) (main.c:1092-1102) in an R32G32_FLOAT
+ * texture. Pixels no draw wrote keep their values. Any of the three may be NULL. */
+MLV_API mlv_status mlv_om_set_visibility_targets(mlv_context context, mlv_texture2d triangle_id,
+                                                 mlv_texture2d draw_id, mlv_texture2d barycentrics);
+
+/* ------------------------------------------------------------------ clears and draws */
+
+/* clear_render_target_view, main.c:1191-1202 (R in the low byte, truncating) */
+MLV_API mlv_status mlv_clear_render_target_view(mlv_context context, mlv_texture2d render_target,
+                                                const float rgba[4]);
+/* clear_depth_stencil_view, main.c:1204-1217: also resets the hierarchical-Z tile minima to 0
+ * (and the tile maxima used by LESS to 1) */
+MLV_API mlv_status mlv_clear_depth_stencil_view(mlv_context context, mlv_texture2d depth_stencil, float depth);
+/* Fills a 32-bit-per-channel texture (e.g. a visibility target) with one value per channel. */
+MLV_API mlv_status mlv_clear_texture_u32(mlv_context context, mlv_texture2d texture, uint32_t value);
+/* draw_indexed, main.c:1219-1261; start_index_location and base_vertex_location are the
+ * reference's TODO (main.c:1219). index_count need not be a multiple of 8 (main.c:670). */
+MLV_API mlv_status mlv_draw_indexed(mlv_context context, uint32_t index_count, uint32_t start_index_location,
+                                    int32_t base_vertex_location);
+/* Non-indexed draw: vertex i of the draw is vertex start + i of the buffer. */
+MLV_API mlv_status mlv_draw(mlv_context context, uint32_t vertex_count, uint32_t start_vertex_location);
+
+/* ------------------------------------------------------------------ submission */
+
+MLV_API mlv_status mlv_flush(mlv_context context);
+/* Blocks until the context's work is done; reports device-side errors (overflows are handled by
+ * regrowing buffers and re-running the affected work before returning). */
+MLV_API mlv_status mlv_finish(mlv_context context);
+MLV_API mlv_status mlv_finish_command_list(mlv_context deferred_context, mlv_command_list *out_list);
+MLV_API mlv_status mlv_execute_command_list(mlv_context immediate_context, mlv_command_list list);
+MLV_API mlv_status mlv_destroy_command_list(mlv_command_list list);
+/* The CUDA stream (cudaStream_t) the context's work runs on. */
+MLV_API mlv_status mlv_get_stream(mlv_context context, void **out_stream);
+
+/* ------------------------------------------------------------------ statistics and tuning */
+
+/* Stats, main.c:199-206, accumulated since the last reset (render() resets them per frame,
+ * main.c:1268). Reading them synchronises. */
+typedef struct mlv_stats {
+    uint64_t vertex_count;
+    uint64_t input_triangle_count;
+    uint64_t assembled_triangle_count;
+    uint64_t active_bin_count;
+    uint64_t total_triangle_count_in_bins;
+    uint64_t draw_count;
+    uint64_t batch_count;
+    uint64_t kernel_launches;
+} mlv_stats;
+
+MLV_API mlv_status mlv_get_stats(mlv_context context, mlv_stats *out_stats);
+MLV_API mlv_status mlv_reset_stats(mlv_context context);
+
+/* Launch-shape knobs of the tile kernel, picked by the autotuner (malevich_gb300/autotune.py).
+ * The hierarchical-Z tile stays 8x8 pixels: it is observable (main.c:1005-1010). */
+typedef struct mlv_tuning {
+    uint32_t tile_warps_per_block;    /* warps per CTA of the tile kernel, 1..16 */
+    uint32_t lanes_per_triangle;      /* lanes that share one triangle's pixels: 1, 2, 4, 8, 16 or 32 */
+    uint32_t big_triangle_tiles;      /* triangles spanning more tiles are binned cooperatively */
+    uint32_t geometry_block;          /* threads per CTA of the geometry kernel: 128, 256 or 512 */
+} mlv_tuning;
+
+MLV_API mlv_status mlv_get_tuning(mlv_context context, mlv_tuning *out_tuning);
+MLV_API mlv_status mlv_set_tuning(mlv_context context, const mlv_tuning *tuning);
+
+/* Per-stage device time (replaces the reference's Remotery CPU samples, main.c:663-1260).
+ * When enabled, CUDA events bracket every stage on the context's stream; reading synchronises.
+ * Stages: 0 clear, 1 geometry (IA+VS+PA+bin count), 2 bin scan, 3 bin scatter, 4 tile
+ * (raster+PS+OM). Times in milliseconds, summed since the last reset. */
+#define MLV_STAGE_COUNT 5
+MLV_API mlv_status mlv_set_profiling(mlv_context context, int enable);
+MLV_API mlv_status mlv_get_stage_times(mlv_context context, double *ms, uint64_t *launches);
+
+/* Debug capture of the last executed single-draw batch: for every (8x8 tile, assembled triangle)
+ * pair the draw binned, its 64-bit coverage mask after the hierarchical-Z test (TileInfo,
+ * main.c:159-162; bit row*8+col). Entries are sorted by tile, then triangle. */
+MLV_API mlv_status mlv_set_debug_capture(mlv_context context, int enable);
+MLV_API mlv_status mlv_get_tile_infos(mlv_context context, uint32_t *tile_index, uint32_t *triangle_id,
+                                      uint64_t *mask, uint64_t capacity, uint64_t *out_count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

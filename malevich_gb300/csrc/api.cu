@@ -1,0 +1,1454 @@
+// Host runtime behind include/malevich.h: devices, contexts, resources, pipeline state, batch
+// planning, workspace management, command lists (CUDA graphs) and error reporting.
+//
+// The reference keeps its pipeline state in one global struct (source/main.c:109-115,222) and
+// mallocs/frees every stage buffer per draw (main.c:675,705,745-746,947,965,986,1253-1259).
+// Here a context owns its state and a workspace that only grows; all buffers are sized on the
+// host before launch. Capacities that only the device knows (assembled triangles, bin entries)
+// are checked by the kernels: on overflow the later kernels of the batch skip their work, the
+// render targets stay untouched, and the next synchronisation regrows the workspace and re-runs
+// the affected batches.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/malevich.h"
+#include "internal.h"
+
+namespace mlv {
+void set_clip_planes(const float planes[6][4], cudaStream_t stream);
+cudaError_t launch_fill_u32(uint32_t *p, size_t n, uint32_t value, const uint32_t *error, cudaStream_t stream);
+cudaError_t launch_geometry(const BatchParams &bp, uint32_t block, cudaStream_t stream);
+cudaError_t launch_scan(const BatchParams &bp, cudaStream_t stream);
+cudaError_t launch_scatter(const BatchParams &bp, int num_sms, cudaStream_t stream);
+cudaError_t launch_tile(const BatchParams &bp, uint32_t warps, cudaStream_t stream);
+}  // namespace mlv
+
+using namespace mlv;
+
+// ------------------------------------------------------------------ errors
+
+static thread_local std::string g_last_error = "no error";
+
+static mlv_status fail(mlv_status st, const std::string &msg) {
+    g_last_error = msg;
+    return st;
+}
+
+#define CUDA_TRY(expr)                                                                               \
+    do {                                                                                             \
+        cudaError_t _e = (expr);                                                                     \
+        if (_e != cudaSuccess)                                                                       \
+            return fail(_e == cudaErrorMemoryAllocation ? MLV_ERROR_OUT_OF_MEMORY : MLV_ERROR_DEVICE, \
+                        std::string(#expr) + ": " + cudaGetErrorString(_e));                         \
+    } while (0)
+
+#define MLV_TRY(expr)                   \
+    do {                                \
+        mlv_status _s = (expr);         \
+        if (_s != MLV_OK) return _s;    \
+    } while (0)
+
+// ------------------------------------------------------------------ objects
+
+struct mlv_context_t;
+
+struct mlv_device_t {
+    int ordinal = 0;
+    int num_sms = 0;
+    float clip_planes[6][4];
+    mlv_context_t *immediate = nullptr;
+    std::mutex mu;
+};
+
+struct mlv_buffer_t {
+    mlv_device device = nullptr;
+    uint8_t *ptr = nullptr;
+    uint64_t size = 0;
+    uint32_t bind = 0;
+    std::vector<uint8_t> shadow;   // host copy of constant buffers (snapshotted at draw time)
+};
+
+struct mlv_texture2d_t {
+    mlv_device device = nullptr;
+    uint8_t *ptr = nullptr;
+    uint32_t width = 0, height = 0;
+    mlv_format format = MLV_FORMAT_UNKNOWN;
+    uint32_t bind = 0;
+    uint32_t texel_bytes = 0;
+    float *tile_min = nullptr, *tile_max = nullptr;   // hierarchical Z (depth textures)
+    uint32_t tiles_x = 0, tiles_y = 0;
+    uint32_t draws_since_clear = 0;                    // render targets: numbers draws for visibility
+};
+
+static uint32_t texel_bytes(mlv_format f) {
+    switch (f) {
+        case MLV_FORMAT_R8G8B8A8_UNORM: return 4;
+        case MLV_FORMAT_R16G16B16A16_FLOAT: return 8;
+        case MLV_FORMAT_R32G32B32A32_FLOAT: return 16;
+        case MLV_FORMAT_D32_FLOAT: return 4;
+        case MLV_FORMAT_R32_UINT: return 4;
+        case MLV_FORMAT_R32G32_FLOAT: return 8;
+        default: return 0;
+    }
+}
+
+struct PipelineState {
+    mlv_buffer ib = nullptr;
+    uint32_t ib_offset = 0;
+    mlv_buffer vb = nullptr;
+    uint32_t vb_stride = 0, vb_offset = 0;
+    int vs = 0, ps = 0;
+    mlv_buffer vs_cb[MLV_CONSTANT_BUFFER_SLOT_COUNT] = {};
+    mlv_texture2d vs_srv[MLV_SHADER_RESOURCE_SLOT_COUNT] = {};
+    mlv_texture2d ps_srv[MLV_SHADER_RESOURCE_SLOT_COUNT] = {};
+    mlv_viewport viewport = {0, 0, 0, 0, 0, 1};
+    bool viewport_set = false;
+    int cull = 1;          // internal: 0 none, 1 back, 2 front
+    int depth_less = 0;
+    mlv_texture2d rtv = nullptr, dsv = nullptr;
+    mlv_texture2d vis_tri = nullptr, vis_draw = nullptr, vis_bary = nullptr;
+    mlv_primitive_topology topology = MLV_PRIMITIVE_TOPOLOGY_TRIANGLELIST;
+};
+
+struct DrawCmd {
+    DrawDesc desc;                 // view / draw_in_view / tri_begin filled by the planner
+    mlv_texture2d rtv, dsv, vis_tri, vis_draw, vis_bary;
+    uint32_t index_count;
+};
+
+struct ClearCmd {
+    mlv_texture2d target;
+    int kind;                      // 0 colour, 1 depth, 2 u32 fill
+    uint32_t value;
+    float depth;
+};
+
+// A segment: clears, then draws that no clear of the segment follows on the same target.
+struct Segment {
+    std::vector<ClearCmd> clears;
+    std::vector<DrawCmd> draws;
+    uint64_t input_triangles = 0, vertex_count = 0;
+};
+
+struct Workspace {
+    TriRaster *raster = nullptr;
+    TriShade *shade = nullptr;
+    TriGeom *geom = nullptr;
+    uint32_t record_cap = 0;
+    bool keep_geom = false;
+    uint32_t *draw_record_begin = nullptr;
+    uint32_t draw_cap = 0;
+    uint32_t *bin_count = nullptr, *bin_start = nullptr;
+    uint32_t bin_cap = 0;
+    uint32_t *list = nullptr;
+    uint64_t *info_mask = nullptr;
+    uint32_t list_cap = 0;
+    unsigned long long *scan_status = nullptr, *scan_status2 = nullptr;
+    uint32_t status_cap = 0, status2_cap = 0;
+    uint32_t *counters = nullptr;
+    unsigned long long *stats = nullptr;
+    uint32_t *error = nullptr;
+    DrawDesc *d_draws = nullptr;
+    ViewDesc *d_views = nullptr;
+    uint32_t desc_draw_cap = 0, desc_view_cap = 0;
+    uint64_t generation = 0;
+};
+
+struct mlv_command_list_t {
+    mlv_device device = nullptr;
+    std::vector<Segment> segments;
+    // graph replay state
+    cudaGraphExec_t exec = nullptr;
+    uint64_t exec_generation = ~0ull;
+    mlv_context_t *exec_context = nullptr;
+    int executions = 0;
+    DrawDesc *d_draws = nullptr;   // per-segment descriptor copies owned by the list
+    ViewDesc *d_views = nullptr;
+    std::vector<size_t> draw_off, view_off;
+    size_t draws_total = 0, views_total = 0;
+};
+
+struct PendingJob {
+    const Segment *segment;        // immediate segments are owned by `owned`
+    std::shared_ptr<Segment> owned;
+    mlv_command_list list;         // or a command list executed as a whole
+    uint32_t seq;
+};
+
+struct mlv_context_t {
+    mlv_device device = nullptr;
+    bool deferred = false;
+    cudaStream_t stream = nullptr;
+    PipelineState st;
+    std::vector<Segment> recorded;     // deferred contexts
+    Workspace ws;
+    mlv_tuning tuning = {4, 1, 16, 256};
+    uint64_t host_stats[8] = {};       // vertex_count, input triangles, draws, batches, launches
+    bool profiling = false;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pool;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_pending;
+    size_t ev_next = 0;
+    double stage_ms[MLV_STAGE_COUNT] = {};
+    uint64_t stage_launches[MLV_STAGE_COUNT] = {};
+    bool capture_infos = false;
+    bool capturing_graph = false;
+    uint32_t batch_seq = 0;
+    std::vector<PendingJob> pending;
+    uint32_t *h_error = nullptr;       // pinned mirror of the device error words + counters
+    // last single-draw segment, for mlv_get_tile_infos
+    bool last_single = false;
+    uint32_t last_total_bins = 0, last_tiles_x = 0, last_draw_count = 0;
+    uint32_t last_records = 0;
+};
+
+// ------------------------------------------------------------------ small helpers
+
+static mlv_status dev_alloc(void **p, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        return fail(MLV_ERROR_OUT_OF_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    return MLV_OK;
+}
+
+template <class T>
+static mlv_status grow(T **p, uint32_t &cap, uint64_t need, uint64_t elem = sizeof(T), bool zero = false) {
+    if (need <= cap && *p) return MLV_OK;
+    uint64_t n = std::max<uint64_t>(need, 1024);
+    n = std::max<uint64_t>(n, (uint64_t)cap + cap / 2);
+    if (n > 0xFFFFFFF0ull) n = 0xFFFFFFF0ull;
+    if (need > n) return fail(MLV_ERROR_CAPACITY_EXCEEDED, "workspace larger than 2^32 elements");
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    MLV_TRY(dev_alloc((void **)p, n * elem));
+    if (zero) CUDA_TRY(cudaMemset(*p, 0, n * elem));
+    cap = (uint32_t)n;
+    return MLV_OK;
+}
+
+static mlv_status set_device(mlv_device d) {
+    CUDA_TRY(cudaSetDevice(d->ordinal));
+    return MLV_OK;
+}
+
+// screen_from_ndc, main.c:825-830, with the reference's mixed float/double arithmetic
+static void screen_from_ndc(const mlv_viewport &vp, float *m) {
+    float r[16] = {(float)(vp.width * 0.5), 0, 0, (float)(vp.width * 0.5 + vp.top_left_x),
+                   0, (float)(-vp.height * 0.5), 0, (float)(vp.height * 0.5 + vp.top_left_y),
+                   0, 0, vp.max_depth - vp.min_depth, vp.min_depth,
+                   0, 0, 0, 1};
+    memcpy(m, r, sizeof(r));
+}
+
+static TexDesc tex_desc(mlv_texture2d t) {
+    TexDesc d = {};
+    if (!t) return d;
+    d.data = t->ptr;
+    d.width = t->width;
+    d.height = t->height;
+    d.format = t->format == MLV_FORMAT_R8G8B8A8_UNORM ? 1 : t->format == MLV_FORMAT_R16G16B16A16_FLOAT ? 2 : 3;
+    return d;
+}
+
+// ------------------------------------------------------------------ workspace
+
+// error words: [0] error bits, [1] first failing batch number (min), [2] warnings, [3] bin
+// entries a list overflow needed
+static mlv_status reset_error_words(Workspace &w) {
+    const uint32_t init[8] = {0, 0xFFFFFFFFu, 0, 0, 0, 0, 0, 0};
+    CUDA_TRY(cudaMemcpy(w.error, init, sizeof(init), cudaMemcpyHostToDevice));
+    return MLV_OK;
+}
+
+static mlv_status ensure_fixed(mlv_context_t *c) {
+    Workspace &w = c->ws;
+    if (!w.counters) {
+        MLV_TRY(dev_alloc((void **)&w.counters, sizeof(uint32_t) * kCtrCount));
+        MLV_TRY(dev_alloc((void **)&w.stats, sizeof(unsigned long long) * kStatCount));
+        MLV_TRY(dev_alloc((void **)&w.error, sizeof(uint32_t) * 8));
+        CUDA_TRY(cudaMemset(w.counters, 0, sizeof(uint32_t) * kCtrCount));
+        CUDA_TRY(cudaMemset(w.stats, 0, sizeof(unsigned long long) * kStatCount));
+        MLV_TRY(reset_error_words(w));
+        CUDA_TRY(cudaMallocHost((void **)&c->h_error, sizeof(uint32_t) * 32));
+        memset(c->h_error, 0, sizeof(uint32_t) * 32);
+    }
+    return MLV_OK;
+}
+
+struct BatchSizes {
+    uint64_t tris = 0, records = 0, bins = 0, tiles = 0, draws = 0, views = 0;
+};
+
+static mlv_status reset_scan_state(Workspace &w) {
+    // fresh look-back state: every status word "not ready" in epoch 0, counters at epoch 0
+    CUDA_TRY(cudaMemset(w.scan_status, 0, sizeof(unsigned long long) * w.status_cap));
+    CUDA_TRY(cudaMemset(w.scan_status2, 0, sizeof(unsigned long long) * w.status2_cap));
+    CUDA_TRY(cudaMemset(w.counters, 0, sizeof(uint32_t) * kCtrCount));
+    return MLV_OK;
+}
+
+static mlv_status ensure_workspace(mlv_context_t *c, const BatchSizes &s, bool keep_geom) {
+    Workspace &w = c->ws;
+    MLV_TRY(ensure_fixed(c));
+    bool changed = false;
+    if (s.records > w.record_cap || !w.raster || (keep_geom && !w.geom)) {
+        uint64_t n = std::max<uint64_t>(s.records, (uint64_t)w.record_cap + w.record_cap / 2);
+        n = std::max<uint64_t>(n, 4096);
+        if (n > 0x7FFFFFFFull) return fail(MLV_ERROR_CAPACITY_EXCEEDED, "more than 2^31 assembled triangles");
+        cudaFree(w.raster); cudaFree(w.shade); cudaFree(w.geom);
+        w.raster = nullptr; w.shade = nullptr; w.geom = nullptr;
+        MLV_TRY(dev_alloc((void **)&w.raster, n * sizeof(TriRaster)));
+        MLV_TRY(dev_alloc((void **)&w.shade, n * sizeof(TriShade)));
+        w.keep_geom = keep_geom || w.keep_geom;
+        if (w.keep_geom) MLV_TRY(dev_alloc((void **)&w.geom, n * sizeof(TriGeom)));
+        w.record_cap = (uint32_t)n;
+        changed = true;
+    }
+    {
+        uint32_t *before = w.draw_record_begin;
+        MLV_TRY(grow(&w.draw_record_begin, w.draw_cap, s.draws));
+        if (before != w.draw_record_begin) changed = true;
+    }
+    {
+        uint32_t *before = w.bin_count;
+        uint32_t cap = w.bin_cap;
+        MLV_TRY(grow(&w.bin_count, cap, s.bins + 1, sizeof(uint32_t), true));
+        if (before != w.bin_count) {
+            uint32_t cap2 = 0;
+            cudaFree(w.bin_start);
+            w.bin_start = nullptr;
+            MLV_TRY(grow(&w.bin_start, cap2, cap, sizeof(uint32_t)));
+            changed = true;
+        }
+        w.bin_cap = cap;
+    }
+    {
+        uint64_t want = std::max<uint64_t>(s.records * 2, 1u << 16);
+        uint32_t *before = w.list;
+        if (want > w.list_cap || !w.list) {
+            uint32_t cap = w.list_cap;
+            MLV_TRY(grow(&w.list, cap, want, sizeof(uint32_t)));
+            w.list_cap = cap;
+        }
+        if (before != w.list) {
+            changed = true;
+            cudaFree(w.info_mask);
+            w.info_mask = nullptr;
+        }
+        if (c->capture_infos && !w.info_mask) MLV_TRY(dev_alloc((void **)&w.info_mask, (size_t)w.list_cap * 8));
+    }
+    {
+        unsigned long long *b1 = w.scan_status, *b2 = w.scan_status2;
+        MLV_TRY(grow(&w.scan_status, w.status_cap, s.tris / 128 + 2, sizeof(unsigned long long)));
+        MLV_TRY(grow(&w.scan_status2, w.status2_cap, s.bins / 2048 + 2, sizeof(unsigned long long)));
+        if (b1 != w.scan_status || b2 != w.scan_status2) {
+            MLV_TRY(reset_scan_state(w));
+            changed = true;
+        }
+    }
+    {
+        DrawDesc *b1 = w.d_draws;
+        ViewDesc *b2 = w.d_views;
+        MLV_TRY(grow(&w.d_draws, w.desc_draw_cap, s.draws));
+        MLV_TRY(grow(&w.d_views, w.desc_view_cap, s.views));
+        if (b1 != w.d_draws || b2 != w.d_views) changed = true;
+    }
+    if (changed) ++w.generation;
+    return MLV_OK;
+}
+
+// ------------------------------------------------------------------ batch planning
+
+struct Plan {
+    std::vector<DrawDesc> draws;
+    std::vector<ViewDesc> views;
+    BatchSizes sizes;
+};
+
+static mlv_status plan_segment(const Segment &seg, Plan &p) {
+    p.draws.clear();
+    p.views.clear();
+    p.sizes = BatchSizes();
+    // group draws by (render target, depth) keeping their order inside a view
+    std::vector<std::pair<std::pair<mlv_texture2d, mlv_texture2d>, std::vector<size_t>>> groups;
+    for (size_t i = 0; i < seg.draws.size(); ++i) {
+        auto key = std::make_pair(seg.draws[i].rtv, seg.draws[i].dsv);
+        size_t g = 0;
+        for (; g < groups.size(); ++g)
+            if (groups[g].first == key) break;
+        if (g == groups.size()) groups.push_back({key, {}});
+        groups[g].second.push_back(i);
+    }
+    uint32_t tri = 0, tiles = 0;
+    uint64_t bins = 0, records = 0;
+    for (size_t g = 0; g < groups.size(); ++g) {
+        const DrawCmd &first = seg.draws[groups[g].second[0]];
+        ViewDesc v = {};
+        mlv_texture2d rt = first.rtv, ds = first.dsv;
+        v.color = (uint32_t *)rt->ptr;
+        v.depth = (float *)ds->ptr;
+        v.tile_min = ds->tile_min;
+        v.tile_max = ds->tile_max;
+        v.vis_tri = first.vis_tri ? (uint32_t *)first.vis_tri->ptr : nullptr;
+        v.vis_draw = first.vis_draw ? (uint32_t *)first.vis_draw->ptr : nullptr;
+        v.vis_bary = first.vis_bary ? (float *)first.vis_bary->ptr : nullptr;
+        v.width = rt->width;
+        v.height = rt->height;
+        v.tiles_x = ds->tiles_x;
+        v.tiles_y = ds->tiles_y;
+        v.tile_base = tiles;
+        v.draw_begin = (uint32_t)p.draws.size();
+        v.draw_count = (uint32_t)groups[g].second.size();
+        v.bin_base = (uint32_t)bins;
+        for (size_t k = 0; k < groups[g].second.size(); ++k) {
+            const DrawCmd &dc = seg.draws[groups[g].second[k]];
+            DrawDesc d = dc.desc;
+            d.view = (uint32_t)g;
+            d.draw_in_view = (uint32_t)k;
+            d.tri_begin = tri;
+            tri += d.tri_count;
+            records += (uint64_t)d.tri_count + std::max<uint64_t>(2ull * d.tri_count, 512);
+            p.draws.push_back(d);
+        }
+        tiles += v.tiles_x * v.tiles_y;
+        bins += (uint64_t)v.tiles_x * v.tiles_y * v.draw_count;
+        p.views.push_back(v);
+    }
+    if (bins > 0x7FFFFFFFull || tiles > 0x7FFFFFFFu)
+        return fail(MLV_ERROR_CAPACITY_EXCEEDED, "batch has too many bins");
+    p.sizes.tris = tri;
+    p.sizes.records = records;
+    p.sizes.bins = bins;
+    p.sizes.tiles = tiles;
+    p.sizes.draws = p.draws.size();
+    p.sizes.views = p.views.size();
+    return MLV_OK;
+}
+
+// ------------------------------------------------------------------ execution
+
+static void ev_begin(mlv_context_t *c, int stage, cudaEvent_t *end_out) {
+    *end_out = nullptr;
+    if (!c->profiling || c->capturing_graph) return;
+    if (c->ev_next >= c->ev_pool.size()) {
+        cudaEvent_t a, b;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        c->ev_pool.push_back({a, b});
+    }
+    auto pr = c->ev_pool[c->ev_next++];
+    cudaEventRecord(pr.first, c->stream);
+    c->ev_pending.push_back({stage, pr});
+    *end_out = pr.second;
+}
+
+static void ev_end(mlv_context_t *c, cudaEvent_t e) {
+    if (e) cudaEventRecord(e, c->stream);
+}
+
+static void collect_events(mlv_context_t *c) {
+    for (auto &pe : c->ev_pending) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, pe.second.first, pe.second.second) == cudaSuccess) {
+            c->stage_ms[pe.first] += ms;
+            c->stage_launches[pe.first] += 1;
+        }
+    }
+    cudaGetLastError();
+    c->ev_pending.clear();
+    c->ev_next = 0;
+}
+
+static mlv_status run_clears(mlv_context_t *c, const Segment &seg) {
+    for (const ClearCmd &cl : seg.clears) {
+        cudaEvent_t e;
+        ev_begin(c, 0, &e);
+        mlv_texture2d t = cl.target;
+        size_t n = (size_t)t->width * t->height * (t->texel_bytes / 4);
+        uint32_t value = cl.value;
+        if (cl.kind == 1) memcpy(&value, &cl.depth, 4);
+        CUDA_TRY(launch_fill_u32((uint32_t *)t->ptr, n, value, c->ws.error, c->stream));
+        if (cl.kind == 1) {
+            // clear_depth_stencil_view resets the tile minima to 0 (main.c:1212-1214); the tile
+            // maxima that depth LESS uses start at 1
+            size_t nt = (size_t)t->tiles_x * t->tiles_y;
+            CUDA_TRY(launch_fill_u32((uint32_t *)t->tile_min, nt, 0u, c->ws.error, c->stream));
+            CUDA_TRY(launch_fill_u32((uint32_t *)t->tile_max, nt, 0x3F800000u, c->ws.error, c->stream));
+            c->host_stats[4] += 2;
+        }
+        c->host_stats[4] += 1;
+        ev_end(c, e);
+    }
+    return MLV_OK;
+}
+
+// Launches the kernels of one segment's draws. `d_draws`/`d_views` hold the plan's descriptors
+// on the device (uploaded by the caller).
+static mlv_status launch_draws(mlv_context_t *c, const Plan &p, DrawDesc *d_draws, ViewDesc *d_views, uint32_t seq) {
+    Workspace &w = c->ws;
+    BatchParams bp = {};
+    bp.draws = d_draws;
+    bp.views = d_views;
+    bp.num_draws = (uint32_t)p.draws.size();
+    bp.num_views = (uint32_t)p.views.size();
+    bp.total_tris = (uint32_t)p.sizes.tris;
+    bp.total_tiles = (uint32_t)p.sizes.tiles;
+    bp.total_bins = (uint32_t)p.sizes.bins;
+    bp.record_capacity = w.record_cap;
+    bp.list_capacity = w.list_cap;
+    bp.big_capacity = 0;
+    bp.big_tiles = c->tuning.big_triangle_tiles;
+    bp.batch_seq = seq;
+    bp.raster = w.raster;
+    bp.shade = w.shade;
+    bp.geom = w.keep_geom ? w.geom : nullptr;
+    bp.draw_record_begin = w.draw_record_begin;
+    bp.bin_count = w.bin_count;
+    bp.bin_start = w.bin_start;
+    bp.list = w.list;
+    bp.info_mask = c->capture_infos ? w.info_mask : nullptr;
+    bp.scan_status = w.scan_status;
+    bp.scan_status2 = w.scan_status2;
+    bp.counters = w.counters;
+    bp.stats = w.stats;
+    bp.error = w.error;
+    c->host_stats[3] += 1;
+    if (bp.total_tris == 0) return MLV_OK;   // nothing to assemble: no kernel has work
+    cudaEvent_t e;
+    ev_begin(c, 1, &e);
+    CUDA_TRY(launch_geometry(bp, c->tuning.geometry_block, c->stream));
+    ev_end(c, e);
+    ev_begin(c, 2, &e);
+    CUDA_TRY(launch_scan(bp, c->stream));
+    ev_end(c, e);
+    ev_begin(c, 3, &e);
+    CUDA_TRY(launch_scatter(bp, c->device->num_sms, c->stream));
+    ev_end(c, e);
+    ev_begin(c, 4, &e);
+    CUDA_TRY(launch_tile(bp, c->tuning.tile_warps_per_block, c->stream));
+    ev_end(c, e);
+    c->host_stats[4] += 4;
+    return MLV_OK;
+}
+
+static mlv_status execute_segment_eager(mlv_context_t *c, const Segment &seg, uint32_t seq) {
+    MLV_TRY(run_clears(c, seg));
+    if (seg.draws.empty()) return MLV_OK;
+    Plan p;
+    MLV_TRY(plan_segment(seg, p));
+    MLV_TRY(ensure_workspace(c, p.sizes, false));
+    CUDA_TRY(cudaMemcpyAsync(c->ws.d_draws, p.draws.data(), sizeof(DrawDesc) * p.draws.size(),
+                             cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(cudaMemcpyAsync(c->ws.d_views, p.views.data(), sizeof(ViewDesc) * p.views.size(),
+                             cudaMemcpyHostToDevice, c->stream));
+    MLV_TRY(launch_draws(c, p, c->ws.d_draws, c->ws.d_views, seq));
+    c->host_stats[0] += seg.vertex_count;
+    c->host_stats[1] += seg.input_triangles;
+    c->host_stats[2] += seg.draws.size();
+    c->last_single = seg.draws.size() == 1;
+    if (c->last_single) {
+        c->last_total_bins = (uint32_t)p.sizes.bins;
+        c->last_tiles_x = p.views[0].tiles_x;
+        c->last_draw_count = 1;
+    }
+    return MLV_OK;
+}
+
+// Reads the device error words; on an overflow regrows the workspace and re-runs the pending
+// work from the failed batch on. Called with the stream idle.
+static mlv_status check_and_recover(mlv_context_t *c) {
+    if (!c->ws.error) {
+        c->pending.clear();
+        return MLV_OK;
+    }
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        CUDA_TRY(cudaMemcpy(c->h_error, c->ws.error, sizeof(uint32_t) * 8, cudaMemcpyDeviceToHost));
+        CUDA_TRY(cudaMemcpy(c->h_error + 8, c->ws.counters, sizeof(uint32_t) * kCtrCount, cudaMemcpyDeviceToHost));
+        const uint32_t err = c->h_error[0];
+        if (c->h_error[2]) {
+            // out-of-range indices read zeros, as Direct3D 11 does; report once
+            uint32_t z = 0;
+            CUDA_TRY(cudaMemcpy(c->ws.error + 2, &z, 4, cudaMemcpyHostToDevice));
+            g_last_error = "a draw read vertices outside its vertex buffer (zeros were used)";
+        }
+        if (err == 0) {
+            c->pending.clear();
+            return MLV_OK;
+        }
+        if (err & kErrLookbackTimeout) {
+            MLV_TRY(reset_error_words(c->ws));
+            CUDA_TRY(cudaMemset(c->ws.bin_count, 0, sizeof(uint32_t) * c->ws.bin_cap));
+            MLV_TRY(reset_scan_state(c->ws));
+            c->pending.clear();
+            return fail(MLV_ERROR_TIMEOUT, "a bounded device-side wait gave up (decoupled look-back)");
+        }
+        // regrow: records from the device's assembled count, list from the reported entry count
+        const uint32_t need_records = c->h_error[8 + kCtrGeomTotal];
+        const uint32_t need_list = c->h_error[3];
+        Workspace &w = c->ws;
+        if ((err & kErrRecordOverflow) && need_records >= w.record_cap) {
+            BatchSizes s;
+            s.records = (uint64_t)need_records + need_records / 4 + 1024;
+            MLV_TRY(ensure_workspace(c, s, false));
+        }
+        if ((err & kErrListOverflow) && need_list > w.list_cap) {
+            uint32_t cap = w.list_cap;
+            MLV_TRY(grow(&w.list, cap, (uint64_t)need_list + need_list / 4 + 1024, sizeof(uint32_t)));
+            w.list_cap = cap;
+            cudaFree(w.info_mask);
+            w.info_mask = nullptr;
+            if (c->capture_infos) MLV_TRY(dev_alloc((void **)&w.info_mask, (size_t)w.list_cap * 8));
+            ++w.generation;
+        }
+        // reset the device state the skipped kernels left behind
+        CUDA_TRY(cudaMemset(w.bin_count, 0, sizeof(uint32_t) * w.bin_cap));
+        MLV_TRY(reset_scan_state(w));
+        MLV_TRY(reset_error_words(w));
+        // Jobs before the first failing batch completed; from it on every kernel that writes a
+        // render target skipped its work, so those jobs are re-run, in order.
+        std::vector<PendingJob> jobs;
+        jobs.swap(c->pending);
+        const uint32_t failed = c->h_error[1];
+        for (const PendingJob &j : jobs) {
+            if (j.seq < failed) continue;
+            if (j.segment) {
+                MLV_TRY(execute_segment_eager(c, *j.segment, j.seq));
+            } else {
+                for (const Segment &s : j.list->segments) MLV_TRY(execute_segment_eager(c, s, j.seq));
+            }
+        }
+        CUDA_TRY(cudaStreamSynchronize(c->stream));
+    }
+    return fail(MLV_ERROR_CAPACITY_EXCEEDED, "workspace overflow persisted after regrowing");
+}
+
+static mlv_status sync_context(mlv_context_t *c) {
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    collect_events(c);
+    return check_and_recover(c);
+}
+
+static mlv_status submit_segment(mlv_context_t *c, Segment &&seg) {
+    if (c->deferred) {
+        c->recorded.push_back(std::move(seg));
+        return MLV_OK;
+    }
+    MLV_TRY(set_device(c->device));
+    auto owned = std::make_shared<Segment>(std::move(seg));
+    const uint32_t seq = ++c->batch_seq;
+    MLV_TRY(execute_segment_eager(c, *owned, seq));
+    c->pending.push_back({owned.get(), owned, nullptr, seq});
+    if (c->pending.size() > 4096) MLV_TRY(sync_context(c));
+    return MLV_OK;
+}
+
+// ------------------------------------------------------------------ C ABI
+
+extern "C" {
+
+MLV_API const char *mlv_get_last_error_string(void) { return g_last_error.c_str(); }
+MLV_API int mlv_get_abi_version(void) { return MLV_ABI_VERSION; }
+
+MLV_API mlv_status mlv_create_device(int ordinal, mlv_device *out) {
+    if (!out) return fail(MLV_ERROR_INVALID_ARG, "out_device is NULL");
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || ordinal < 0 || ordinal >= n) {
+        cudaGetLastError();
+        return fail(MLV_ERROR_DEVICE, "no such CUDA device");
+    }
+    CUDA_TRY(cudaSetDevice(ordinal));
+    auto *d = new mlv_device_t();
+    d->ordinal = ordinal;
+    cudaDeviceGetAttribute(&d->num_sms, cudaDevAttrMultiProcessorCount, ordinal);
+    // the clipper's plane normals: v4f32_normalize (math.h:267-270) of the six planes of
+    // main.c:652-657, evaluated with the reference's float/double mix
+    static const float raw[6][4] = {{1, 0, 0, 1}, {-1, 0, 0, 1}, {0, 1, 0, 1}, {0, -1, 0, 1}, {0, 0, 1, 1}, {0, 0, -1, 1}};
+    for (int p = 0; p < 6; ++p) {
+        float dot = raw[p][0] * raw[p][0] + raw[p][1] * raw[p][1] + raw[p][2] * raw[p][2] + raw[p][3] * raw[p][3];
+        float len = (float)sqrt((double)dot);
+        float inv = (float)(1.0 / (double)len);
+        for (int k = 0; k < 4; ++k) d->clip_planes[p][k] = raw[p][k] * inv;
+    }
+    set_clip_planes(d->clip_planes, 0);
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        delete d;
+        return fail(MLV_ERROR_DEVICE, std::string("device init: ") + cudaGetErrorString(e));
+    }
+    auto *c = new mlv_context_t();
+    c->device = d;
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        delete d;
+        return fail(MLV_ERROR_DEVICE, "cudaStreamCreate failed");
+    }
+    d->immediate = c;
+    *out = d;
+    return MLV_OK;
+}
+
+static void free_workspace(Workspace &w) {
+    cudaFree(w.raster); cudaFree(w.shade); cudaFree(w.geom); cudaFree(w.draw_record_begin);
+    cudaFree(w.bin_count); cudaFree(w.bin_start); cudaFree(w.list); cudaFree(w.info_mask);
+    cudaFree(w.scan_status); cudaFree(w.scan_status2); cudaFree(w.counters); cudaFree(w.stats);
+    cudaFree(w.error); cudaFree(w.d_draws); cudaFree(w.d_views);
+    w = Workspace();
+}
+
+static void destroy_context_internal(mlv_context_t *c) {
+    if (!c) return;
+    cudaSetDevice(c->device->ordinal);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    free_workspace(c->ws);
+    for (auto &pr : c->ev_pool) {
+        cudaEventDestroy(pr.first);
+        cudaEventDestroy(pr.second);
+    }
+    if (c->h_error) cudaFreeHost(c->h_error);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+MLV_API mlv_status mlv_destroy_device(mlv_device d) {
+    if (!d) return fail(MLV_ERROR_INVALID_ARG, "device is NULL");
+    destroy_context_internal(d->immediate);
+    delete d;
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_get_immediate_context(mlv_device d, mlv_context *out) {
+    if (!d || !out) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
+    *out = d->immediate;
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_create_deferred_context(mlv_device d, mlv_context *out) {
+    if (!d || !out) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
+    auto *c = new mlv_context_t();
+    c->device = d;
+    c->deferred = true;
+    *out = c;
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_destroy_context(mlv_context c) {
+    if (!c) return fail(MLV_ERROR_INVALID_ARG, "context is NULL");
+    if (!c->deferred) return fail(MLV_ERROR_INVALID_ARG, "the immediate context is owned by its device");
+    delete c;
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_create_buffer(mlv_device d, const mlv_buffer_desc *desc, const void *init, mlv_buffer *out) {
+    if (!d || !desc || !out) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
+    if (desc->byte_width == 0) return fail(MLV_ERROR_INVALID_ARG, "byte_width is 0");
+    MLV_TRY(set_device(d));
+    auto *b = new mlv_buffer_t();
+    b->device = d;
+    b->size = desc->byte_width;
+    b->bind = desc->bind_flags;
+    mlv_status st = dev_alloc((void **)&b->ptr, (desc->byte_width + 15) & ~15ull);
+    if (st != MLV_OK) {
+        delete b;
+        return st;
+    }
+    if (desc->bind_flags & MLV_BIND_CONSTANT_BUFFER) b->shadow.assign(desc->byte_width, 0);
+    if (init) {
+        cudaError_t e = cudaMemcpy(b->ptr, init, desc->byte_width, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            cudaFree(b->ptr);
+            delete b;
+            return fail(MLV_ERROR_DEVICE, cudaGetErrorString(e));
+        }
+        if (!b->shadow.empty()) memcpy(b->shadow.data(), init, desc->byte_width);
+    }
+    *out = b;
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_destroy_buffer(mlv_buffer b) {
+    if (!b) return fail(MLV_ERROR_INVALID_ARG, "buffer is NULL");
+    cudaSetDevice(b->device->ordinal);
+    if (b->device->immediate) cudaStreamSynchronize(b->device->immediate->stream);
+    cudaFree(b->ptr);
+    delete b;
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_create_texture2d(mlv_device d, const mlv_texture2d_desc *desc, const void *init,
+                                        uint32_t row_pitch, mlv_texture2d *out) {
+    if (!d || !desc || !out) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
+    uint32_t tb = texel_bytes(desc->format);
+    if (!tb) return fail(MLV_ERROR_INVALID_ARG, "unknown texture format");
+    if (desc->width == 0 || desc->height == 0 || desc->width > 16384 || desc->height > 16384)
+        return fail(MLV_ERROR_INVALID_ARG, "texture size must be 1..16384");
+    MLV_TRY(set_device(d));
+    auto *t = new mlv_texture2d_t();
+    t->device = d;
+    t->width = desc->width;
+    t->height = desc->height;
+    t->format = desc->format;
+    t->bind = desc->bind_flags;
+    t->texel_bytes = tb;
+    size_t bytes = (size_t)desc->width * desc->height * tb;
+    mlv_status st = dev_alloc((void **)&t->ptr, (bytes + 15) & ~(size_t)15);
+    if (st != MLV_OK) {
+        delete t;
+        return st;
+    }
+    if (desc->format == MLV_FORMAT_D32_FLOAT) {
+        t->tiles_x = (desc->width + kTile - 1) / kTile;
+        t->tiles_y = (desc->height + kTile - 1) / kTile;
+        size_t nt = (size_t)t->tiles_x * t->tiles_y;
+        st = dev_alloc((void **)&t->tile_min, nt * 4);
+        if (st == MLV_OK) st = dev_alloc((void **)&t->tile_max, nt * 4);
+        if (st != MLV_OK) {
+            cudaFree(t->ptr); cudaFree(t->tile_min);
+            delete t;
+            return st;
+        }
+        cudaMemset(t->tile_min, 0, nt * 4);
+        std::vector<float> ones(nt, 1.0f);
+        cudaMemcpy(t->tile_max, ones.data(), nt * 4, cudaMemcpyHostToDevice);
+    }
+    if (init) {
+        size_t row = (size_t)desc->width * tb;
+        cudaError_t e = cudaMemcpy2D(t->ptr, row, init, row_pitch ? row_pitch : row, row, desc->height,
+                                     cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            cudaFree(t->ptr);
+            delete t;
+            return fail(MLV_ERROR_DEVICE, cudaGetErrorString(e));
+        }
+    } else {
+        cudaMemset(t->ptr, 0, bytes);
+    }
+    *out = t;
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_destroy_texture2d(mlv_texture2d t) {
+    if (!t) return fail(MLV_ERROR_INVALID_ARG, "texture is NULL");
+    cudaSetDevice(t->device->ordinal);
+    if (t->device->immediate) cudaStreamSynchronize(t->device->immediate->stream);
+    cudaFree(t->ptr);
+    cudaFree(t->tile_min);
+    cudaFree(t->tile_max);
+    delete t;
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_buffer_device_pointer(mlv_buffer b, void **out) {
+    if (!b || !out) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
+    *out = b->ptr;
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_texture2d_device_pointer(mlv_texture2d t, void **out) {
+    if (!t || !out) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
+    *out = t->ptr;
+    return MLV_OK;
+}
+
+static mlv_status need_immediate(mlv_context c) {
+    if (!c) return fail(MLV_ERROR_INVALID_ARG, "context is NULL");
+    if (c->deferred) return fail(MLV_ERROR_INVALID_STATE, "this call needs the immediate context");
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_update_buffer(mlv_context c, mlv_buffer b, uint64_t offset, const void *data, uint64_t size) {
+    MLV_TRY(need_immediate(c));
+    if (!b || !data) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
+    if (offset + size > b->size) return fail(MLV_ERROR_INVALID_ARG, "update outside the buffer");
+    MLV_TRY(set_device(c->device));
+    MLV_TRY(sync_context(c));   // queued draws may still read the old contents
+    CUDA_TRY(cudaMemcpy(b->ptr + offset, data, size, cudaMemcpyHostToDevice));
+    if (!b->shadow.empty()) memcpy(b->shadow.data() + offset, data, size);
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_update_texture2d(mlv_context c, mlv_texture2d t, const void *data, uint32_t row_pitch) {
+    MLV_TRY(need_immediate(c));
+    if (!t || !data) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
+    MLV_TRY(set_device(c->device));
+    MLV_TRY(sync_context(c));
+    size_t row = (size_t)t->width * t->texel_bytes;
+    CUDA_TRY(cudaMemcpy2D(t->ptr, row, data, row_pitch ? row_pitch : row, row, t->height, cudaMemcpyHostToDevice));
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_read_texture2d(mlv_context c, mlv_texture2d t, void *dst, uint32_t row_pitch) {
+    MLV_TRY(need_immediate(c));
+    if (!t || !dst) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
+    MLV_TRY(set_device(c->device));
+    MLV_TRY(sync_context(c));
+    size_t row = (size_t)t->width * t->texel_bytes;
+    CUDA_TRY(cudaMemcpy2D(dst, row_pitch ? row_pitch : row, t->ptr, row, row, t->height, cudaMemcpyDeviceToHost));
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_ia_set_primitive_topology(mlv_context c, mlv_primitive_topology topo) {
+    if (!c) return fail(MLV_ERROR_INVALID_ARG, "context is NULL");
+    if (topo != MLV_PRIMITIVE_TOPOLOGY_TRIANGLELIST) return fail(MLV_ERROR_UNSUPPORTED, "only triangle lists");
+    c->st.topology = topo;
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_ia_set_index_buffer(mlv_context c, mlv_buffer b, mlv_format fmt, uint32_t offset) {
+    if (!c) return fail(MLV_ERROR_INVALID_ARG, "context is NULL");
+    if (b && fmt != MLV_FORMAT_R32_UINT) return fail(MLV_ERROR_UNSUPPORTED, "index buffers are 32-bit");
+    if (offset & 3) return fail(MLV_ERROR_INVALID_ARG, "index buffer offset must be a multiple of 4");
+    c->st.ib = b;
+    c->st.ib_offset = offset;
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_ia_set_vertex_buffers(mlv_context c, uint32_t start, uint32_t n, const mlv_buffer *bufs,
+                                             const uint32_t *strides, const uint32_t *offsets) {
+    if (!c) return fail(MLV_ERROR_INVALID_ARG, "context is NULL");
+    if (start != 0 || n > 1) return fail(MLV_ERROR_UNSUPPORTED, "one vertex buffer slot");
+    if (n == 0) return MLV_OK;
+    if (!bufs || !strides) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
+    if (bufs[0] && (strides[0] < 32 || (strides[0] & 3)))
+        return fail(MLV_ERROR_INVALID_ARG, "vertex stride must be >= 32 and a multiple of 4");
+    c->st.vb = bufs[0];
+    c->st.vb_stride = strides[0];
+    c->st.vb_offset = offsets ? offsets[0] : 0;
+    if (c->st.vb_offset & 3) return fail(MLV_ERROR_INVALID_ARG, "vertex buffer offset must be a multiple of 4");
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_vs_set_shader(mlv_context c, mlv_vertex_shader_id s) {
+    if (!c) return fail(MLV_ERROR_INVALID_ARG, "context is NULL");
+    if (s < MLV_VS_BASIC || s > MLV_VS_PASSTHROUGH_UV) return fail(MLV_ERROR_INVALID_ARG, "unknown vertex shader");
+    c->st.vs = s;
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_ps_set_shader(mlv_context c, mlv_pixel_shader_id s) {
+    if (!c) return fail(MLV_ERROR_INVALID_ARG, "context is NULL");
+    if (s < MLV_PS_BASIC || s > MLV_PS_COLOR_TIMES_TEXEL) return fail(MLV_ERROR_INVALID_ARG, "unknown pixel shader");
+    c->st.ps = s;
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_vs_set_constant_buffers(mlv_context c, uint32_t start, uint32_t n, const mlv_buffer *bufs) {
+    if (!c || (n && !bufs)) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
+    if (start + n > MLV_CONSTANT_BUFFER_SLOT_COUNT) return fail(MLV_ERROR_INVALID_ARG, "slot out of range");
+    for (uint32_t i = 0; i < n; ++i) c->st.vs_cb[start + i] = bufs[i];
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_vs_set_shader_resources(mlv_context c, uint32_t start, uint32_t n, const mlv_texture2d *t) {
+    if (!c || (n && !t)) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
+    if (start + n > MLV_SHADER_RESOURCE_SLOT_COUNT) return fail(MLV_ERROR_INVALID_ARG, "slot out of range");
+    for (uint32_t i = 0; i < n; ++i) c->st.vs_srv[start + i] = t[i];
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_ps_set_shader_resources(mlv_context c, uint32_t start, uint32_t n, const mlv_texture2d *t) {
+    if (!c || (n && !t)) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
+    if (start + n > MLV_SHADER_RESOURCE_SLOT_COUNT) return fail(MLV_ERROR_INVALID_ARG, "slot out of range");
+    for (uint32_t i = 0; i < n; ++i) c->st.ps_srv[start + i] = t[i];
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_rs_set_viewports(mlv_context c, uint32_t n, const mlv_viewport *vp) {
+    if (!c || (n && !vp)) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
+    if (n != 1) return fail(MLV_ERROR_UNSUPPORTED, "one viewport");
+    c->st.viewport = vp[0];
+    c->st.viewport_set = true;
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_rs_set_state(mlv_context c, const mlv_rasterizer_desc *d) {
+    if (!c) return fail(MLV_ERROR_INVALID_ARG, "context is NULL");
+    if (!d) { c->st.cull = 1; return MLV_OK; }
+    switch (d->cull_mode) {
+        case MLV_CULL_NONE: c->st.cull = 0; break;
+        case MLV_CULL_BACK: c->st.cull = 1; break;
+        case MLV_CULL_FRONT: c->st.cull = 2; break;
+        default: return fail(MLV_ERROR_INVALID_ARG, "unknown cull mode");
+    }
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_om_set_depth_stencil_state(mlv_context c, const mlv_depth_stencil_desc *d) {
+    if (!c) return fail(MLV_ERROR_INVALID_ARG, "context is NULL");
+    if (!d) { c->st.depth_less = 0; return MLV_OK; }
+    if (!d->depth_enable) return fail(MLV_ERROR_UNSUPPORTED, "depth testing cannot be disabled");
+    if (d->depth_func == MLV_COMPARISON_GREATER_EQUAL) c->st.depth_less = 0;
+    else if (d->depth_func == MLV_COMPARISON_LESS) c->st.depth_less = 1;
+    else return fail(MLV_ERROR_UNSUPPORTED, "depth function must be LESS or GREATER_EQUAL");
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_om_set_render_targets(mlv_context c, mlv_texture2d rt, mlv_texture2d ds) {
+    if (!c) return fail(MLV_ERROR_INVALID_ARG, "context is NULL");
+    if (rt && rt->format != MLV_FORMAT_R8G8B8A8_UNORM)
+        return fail(MLV_ERROR_INVALID_ARG, "render target must be R8G8B8A8_UNORM");
+    if (ds && ds->format != MLV_FORMAT_D32_FLOAT) return fail(MLV_ERROR_INVALID_ARG, "depth target must be D32_FLOAT");
+    if (rt && ds && (rt->width != ds->width || rt->height != ds->height))
+        return fail(MLV_ERROR_INVALID_ARG, "render target and depth target differ in size");
+    c->st.rtv = rt;
+    c->st.dsv = ds;
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_om_set_visibility_targets(mlv_context c, mlv_texture2d tri, mlv_texture2d draw,
+                                                 mlv_texture2d bary) {
+    if (!c) return fail(MLV_ERROR_INVALID_ARG, "context is NULL");
+    if (tri && tri->format != MLV_FORMAT_R32_UINT) return fail(MLV_ERROR_INVALID_ARG, "triangle-id target must be R32_UINT");
+    if (draw && draw->format != MLV_FORMAT_R32_UINT) return fail(MLV_ERROR_INVALID_ARG, "draw-id target must be R32_UINT");
+    if (bary && bary->format != MLV_FORMAT_R32G32_FLOAT)
+        return fail(MLV_ERROR_INVALID_ARG, "barycentric target must be R32G32_FLOAT");
+    c->st.vis_tri = tri;
+    c->st.vis_draw = draw;
+    c->st.vis_bary = bary;
+    return MLV_OK;
+}
+
+static uint32_t encode_clear(const float *c) {
+    auto tr = [](float x) -> uint32_t {
+        if (!(x > -9.2e18f && x < 9.2e18f)) return 0u;
+        return (uint32_t)(long long)x;
+    };
+    return (tr(c[3] * 255.f) << 24) + (tr(c[2] * 255.f) << 16) + (tr(c[1] * 255.f) << 8) + tr(c[0] * 255.f);
+}
+
+static bool draw_touches(const DrawCmd &d, mlv_texture2d t) {
+    if (d.rtv == t || d.dsv == t || d.vis_tri == t || d.vis_draw == t || d.vis_bary == t) return true;
+    return d.desc.vs_tex.data == t->ptr || d.desc.ps_tex.data == t->ptr;
+}
+
+static mlv_status submit_clear(mlv_context c, const ClearCmd &cl) {
+    if (c->deferred) {
+        // A clear joins the last segment (it runs before the segment's draws) unless one of those
+        // draws reads or writes the cleared texture; then it opens a new segment.
+        if (!c->recorded.empty()) {
+            Segment &last = c->recorded.back();
+            bool conflict = false;
+            for (const DrawCmd &d : last.draws) conflict = conflict || draw_touches(d, cl.target);
+            if (!conflict) {
+                last.clears.push_back(cl);
+                return MLV_OK;
+            }
+        }
+        Segment seg;
+        seg.clears.push_back(cl);
+        c->recorded.push_back(std::move(seg));
+        return MLV_OK;
+    }
+    Segment seg;
+    seg.clears.push_back(cl);
+    return submit_segment(c, std::move(seg));
+}
+
+MLV_API mlv_status mlv_clear_render_target_view(mlv_context c, mlv_texture2d rt, const float rgba[4]) {
+    if (!c || !rt || !rgba) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
+    if (rt->format != MLV_FORMAT_R8G8B8A8_UNORM) return fail(MLV_ERROR_INVALID_ARG, "not a colour target");
+    ClearCmd cl = {rt, 0, encode_clear(rgba), 0.f};
+    rt->draws_since_clear = 0;
+    return submit_clear(c, cl);
+}
+
+MLV_API mlv_status mlv_clear_depth_stencil_view(mlv_context c, mlv_texture2d ds, float depth) {
+    if (!c || !ds) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
+    if (ds->format != MLV_FORMAT_D32_FLOAT) return fail(MLV_ERROR_INVALID_ARG, "not a depth target");
+    ClearCmd cl = {ds, 1, 0u, depth};
+    return submit_clear(c, cl);
+}
+
+MLV_API mlv_status mlv_clear_texture_u32(mlv_context c, mlv_texture2d t, uint32_t value) {
+    if (!c || !t) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
+    ClearCmd cl = {t, 2, value, 0.f};
+    return submit_clear(c, cl);
+}
+
+static mlv_status build_draw(mlv_context c, uint32_t count, uint32_t start, int32_t base_vertex, bool indexed,
+                             DrawCmd &out) {
+    const PipelineState &s = c->st;
+    if (!s.rtv || !s.dsv) return fail(MLV_ERROR_INVALID_STATE, "render target and depth target must be bound");
+    if (!s.vb) return fail(MLV_ERROR_INVALID_STATE, "no vertex buffer bound");
+    if (indexed && !s.ib) return fail(MLV_ERROR_INVALID_STATE, "no index buffer bound");
+    if (!s.vs || !s.ps) return fail(MLV_ERROR_INVALID_STATE, "shaders not set");
+    if (!s.viewport_set) return fail(MLV_ERROR_INVALID_STATE, "no viewport set");
+    const mlv_viewport &vp = s.viewport;
+    if (!(vp.width >= 1.0f && vp.height >= 1.0f) || vp.width > (float)s.rtv->width ||
+        vp.height > (float)s.rtv->height || vp.top_left_x != 0.0f || vp.top_left_y != 0.0f)
+        return fail(MLV_ERROR_INVALID_STATE, "the viewport must start at (0,0) and fit in the render target");
+    DrawDesc &d = out.desc;
+    memset(&d, 0, sizeof(d));
+    d.vb = s.vb->ptr + s.vb_offset;
+    d.vb_stride = s.vb_stride;
+    uint64_t avail = s.vb->size > s.vb_offset ? s.vb->size - s.vb_offset : 0;
+    d.vertex_count = avail >= 32 ? (uint32_t)std::min<uint64_t>((avail - 32) / s.vb_stride + 1, 0xFFFFFFFFu) : 0;
+    if (indexed) {
+        uint64_t nidx = (s.ib->size - s.ib_offset) / 4;
+        if ((uint64_t)start + count > nidx) return fail(MLV_ERROR_INVALID_ARG, "draw reads past the index buffer");
+        d.ib = (const uint32_t *)(s.ib->ptr + s.ib_offset);
+    } else {
+        d.ib = nullptr;
+        base_vertex = 0;
+    }
+    d.start_index = start;
+    d.base_vertex = base_vertex;
+    d.tri_count = count / 3;
+    d.vs = s.vs;
+    d.ps = s.ps;
+    d.cull = s.cull;
+    d.depth_less = s.depth_less;
+    mlv_buffer cb = s.vs_cb[0];
+    if (s.vs == MLV_VS_BASIC || s.vs == MLV_VS_VERTEX_LIGHTING || s.vs == MLV_VS_FULLSCREEN) {
+        if (!cb || cb->shadow.size() < sizeof(d.cb))
+            return fail(MLV_ERROR_INVALID_STATE, "VS constant buffer 0 must hold a 192-byte PerFrameCB");
+    }
+    if (cb && !cb->shadow.empty()) memcpy(d.cb, cb->shadow.data(), std::min(sizeof(d.cb), cb->shadow.size()));
+    screen_from_ndc(vp, d.screen_from_ndc);
+    d.vp_w = (int32_t)vp.width;
+    d.vp_h = (int32_t)vp.height;
+    mlv_texture2d vt = s.vs_srv[0], pt = s.ps_srv[0];
+    auto is_float = [](mlv_texture2d t) {
+        return t && (t->format == MLV_FORMAT_R32G32B32A32_FLOAT || t->format == MLV_FORMAT_R16G16B16A16_FLOAT);
+    };
+    if (s.vs == MLV_VS_VERTEX_LIGHTING && !is_float(vt))
+        return fail(MLV_ERROR_INVALID_STATE, "vertex_lighting_vs needs a float texture in VS slot 0");
+    if (s.ps == MLV_PS_BASIC && !(pt && pt->format == MLV_FORMAT_R8G8B8A8_UNORM))
+        return fail(MLV_ERROR_INVALID_STATE, "basic_ps needs an R8G8B8A8 texture in PS slot 0");
+    if (s.ps == MLV_PS_ENV_LIGHTING && !is_float(pt))
+        return fail(MLV_ERROR_INVALID_STATE, "env_lighting_ps needs a float texture in PS slot 0");
+    if (s.ps == MLV_PS_COLOR_TIMES_TEXEL && !(pt && (is_float(pt) || pt->format == MLV_FORMAT_R8G8B8A8_UNORM)))
+        return fail(MLV_ERROR_INVALID_STATE, "COLOR_TIMES_TEXEL needs a texture in PS slot 0");
+    d.vs_tex = tex_desc(vt);
+    d.ps_tex = tex_desc(pt);
+    auto vis_ok = [&](mlv_texture2d t) { return !t || (t->width == s.rtv->width && t->height == s.rtv->height); };
+    if (!vis_ok(s.vis_tri) || !vis_ok(s.vis_draw) || !vis_ok(s.vis_bary))
+        return fail(MLV_ERROR_INVALID_STATE, "visibility targets must match the render target size");
+    d.draw_seq = s.rtv->draws_since_clear++;
+    out.rtv = s.rtv;
+    out.dsv = s.dsv;
+    out.vis_tri = s.vis_tri;
+    out.vis_draw = s.vis_draw;
+    out.vis_bary = s.vis_bary;
+    out.index_count = count;
+    return MLV_OK;
+}
+
+static mlv_status submit_draw(mlv_context c, DrawCmd &&dc) {
+    if (c->deferred) {
+        // a draw that samples a texture an earlier draw of the segment renders to (or renders to
+        // one an earlier draw samples) starts a new segment: a batch reads all inputs first
+        bool conflict = c->recorded.empty();
+        if (!conflict) {
+            for (const DrawCmd &d : c->recorded.back().draws) {
+                auto ptr_of = [](mlv_texture2d t) { return t ? (const void *)t->ptr : (const void *)1; };
+                if (d.desc.vs_tex.data == ptr_of(dc.rtv) || d.desc.ps_tex.data == ptr_of(dc.rtv) ||
+                    dc.desc.vs_tex.data == ptr_of(d.rtv) || dc.desc.ps_tex.data == ptr_of(d.rtv) ||
+                    dc.desc.vs_tex.data == ptr_of(d.dsv) || dc.desc.ps_tex.data == ptr_of(d.dsv))
+                    conflict = true;
+            }
+        }
+        if (conflict) c->recorded.emplace_back();
+        Segment &last = c->recorded.back();
+        last.draws.push_back(std::move(dc));
+        last.input_triangles += last.draws.back().desc.tri_count;
+        last.vertex_count += last.draws.back().index_count;
+        return MLV_OK;
+    }
+    Segment seg;
+    seg.input_triangles = dc.desc.tri_count;
+    seg.vertex_count = dc.index_count;
+    seg.draws.push_back(std::move(dc));
+    return submit_segment(c, std::move(seg));
+}
+
+MLV_API mlv_status mlv_draw_indexed(mlv_context c, uint32_t count, uint32_t start, int32_t base_vertex) {
+    if (!c) return fail(MLV_ERROR_INVALID_ARG, "context is NULL");
+    DrawCmd dc;
+    MLV_TRY(build_draw(c, count, start, base_vertex, true, dc));
+    return submit_draw(c, std::move(dc));
+}
+
+MLV_API mlv_status mlv_draw(mlv_context c, uint32_t count, uint32_t start) {
+    if (!c) return fail(MLV_ERROR_INVALID_ARG, "context is NULL");
+    DrawCmd dc;
+    MLV_TRY(build_draw(c, count, start, 0, false, dc));
+    return submit_draw(c, std::move(dc));
+}
+
+MLV_API mlv_status mlv_flush(mlv_context c) {
+    if (!c) return fail(MLV_ERROR_INVALID_ARG, "context is NULL");
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_finish(mlv_context c) {
+    MLV_TRY(need_immediate(c));
+    MLV_TRY(set_device(c->device));
+    return sync_context(c);
+}
+
+MLV_API mlv_status mlv_get_stream(mlv_context c, void **out) {
+    if (!c || !out) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
+    *out = c->deferred ? nullptr : (void *)c->stream;
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_finish_command_list(mlv_context c, mlv_command_list *out) {
+    if (!c || !out) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
+    if (!c->deferred) return fail(MLV_ERROR_INVALID_STATE, "command lists come from deferred contexts");
+    auto *l = new mlv_command_list_t();
+    l->device = c->device;
+    l->segments.swap(c->recorded);
+    *out = l;
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_destroy_command_list(mlv_command_list l) {
+    if (!l) return fail(MLV_ERROR_INVALID_ARG, "list is NULL");
+    cudaSetDevice(l->device->ordinal);
+    if (l->device->immediate) cudaStreamSynchronize(l->device->immediate->stream);
+    if (l->exec) cudaGraphExecDestroy(l->exec);
+    cudaFree(l->d_draws);
+    cudaFree(l->d_views);
+    delete l;
+    return MLV_OK;
+}
+
+// Builds the list's device descriptors, sizes the workspace for its largest segment and
+// records all of its kernels on the context stream (eagerly, or into a graph being captured).
+static mlv_status run_list(mlv_context_t *c, mlv_command_list l, uint32_t seq, bool upload) {
+    std::vector<Plan> plans(l->segments.size());
+    BatchSizes maxs;
+    size_t nd = 0, nv = 0;
+    for (size_t i = 0; i < l->segments.size(); ++i) {
+        MLV_TRY(plan_segment(l->segments[i], plans[i]));
+        const BatchSizes &s = plans[i].sizes;
+        maxs.tris = std::max(maxs.tris, s.tris);
+        maxs.records = std::max(maxs.records, s.records);
+        maxs.bins = std::max(maxs.bins, s.bins);
+        maxs.tiles = std::max(maxs.tiles, s.tiles);
+        maxs.draws = std::max(maxs.draws, s.draws);
+        maxs.views = std::max(maxs.views, s.views);
+        nd += plans[i].draws.size();
+        nv += plans[i].views.size();
+    }
+    if (!c->capturing_graph) MLV_TRY(ensure_workspace(c, maxs, false));
+    if (upload || !l->d_draws) {
+        if (nd > l->draws_total || !l->d_draws) {
+            cudaFree(l->d_draws);
+            l->d_draws = nullptr;
+            MLV_TRY(dev_alloc((void **)&l->d_draws, std::max<size_t>(nd, 1) * sizeof(DrawDesc)));
+            l->draws_total = nd;
+        }
+        if (nv > l->views_total || !l->d_views) {
+            cudaFree(l->d_views);
+            l->d_views = nullptr;
+            MLV_TRY(dev_alloc((void **)&l->d_views, std::max<size_t>(nv, 1) * sizeof(ViewDesc)));
+            l->views_total = nv;
+        }
+        l->draw_off.clear();
+        l->view_off.clear();
+        size_t od = 0, ov = 0;
+        for (auto &p : plans) {
+            l->draw_off.push_back(od);
+            l->view_off.push_back(ov);
+            if (!p.draws.empty())
+                CUDA_TRY(cudaMemcpy(l->d_draws + od, p.draws.data(), sizeof(DrawDesc) * p.draws.size(),
+                                    cudaMemcpyHostToDevice));
+            if (!p.views.empty())
+                CUDA_TRY(cudaMemcpy(l->d_views + ov, p.views.data(), sizeof(ViewDesc) * p.views.size(),
+                                    cudaMemcpyHostToDevice));
+            od += p.draws.size();
+            ov += p.views.size();
+        }
+    }
+    for (size_t i = 0; i < l->segments.size(); ++i) {
+        MLV_TRY(run_clears(c, l->segments[i]));
+        if (!plans[i].draws.empty())
+            MLV_TRY(launch_draws(c, plans[i], l->d_draws + l->draw_off[i], l->d_views + l->view_off[i], seq));
+        c->host_stats[0] += l->segments[i].vertex_count;
+        c->host_stats[1] += l->segments[i].input_triangles;
+        c->host_stats[2] += l->segments[i].draws.size();
+    }
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_execute_command_list(mlv_context c, mlv_command_list l) {
+    MLV_TRY(need_immediate(c));
+    if (!l) return fail(MLV_ERROR_INVALID_ARG, "list is NULL");
+    MLV_TRY(set_device(c->device));
+    const uint32_t seq = ++c->batch_seq;
+    c->last_single = false;
+    if (l->executions == 0 || c->profiling) {
+        // first execution runs eagerly and synchronises, so that the workspace is sized before
+        // the list is captured into a graph
+        MLV_TRY(run_list(c, l, seq, l->executions == 0));
+        c->pending.push_back({nullptr, nullptr, l, seq});
+        ++l->executions;
+        if (l->executions == 1) MLV_TRY(sync_context(c));
+        return MLV_OK;
+    }
+    if (!l->exec || l->exec_generation != c->ws.generation || l->exec_context != c) {
+        if (l->exec) cudaGraphExecDestroy(l->exec);
+        l->exec = nullptr;
+        cudaGraph_t g = nullptr;
+        uint64_t saved[8];
+        memcpy(saved, c->host_stats, sizeof(saved));
+        CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        c->capturing_graph = true;
+        mlv_status st = run_list(c, l, seq, false);
+        c->capturing_graph = false;
+        cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+        memcpy(c->host_stats, saved, sizeof(saved));
+        if (st != MLV_OK) {
+            if (g) cudaGraphDestroy(g);
+            return st;
+        }
+        if (e != cudaSuccess) return fail(MLV_ERROR_DEVICE, std::string("graph capture: ") + cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&l->exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return fail(MLV_ERROR_DEVICE, std::string("graph instantiate: ") + cudaGetErrorString(e));
+        l->exec_generation = c->ws.generation;
+        l->exec_context = c;
+    }
+    CUDA_TRY(cudaGraphLaunch(l->exec, c->stream));
+    for (const Segment &s : l->segments) {
+        c->host_stats[0] += s.vertex_count;
+        c->host_stats[1] += s.input_triangles;
+        c->host_stats[2] += s.draws.size();
+        c->host_stats[3] += s.draws.empty() ? 0 : 1;
+        c->host_stats[4] += s.clears.size() + (s.draws.empty() ? 0 : 4);
+    }
+    c->pending.push_back({nullptr, nullptr, l, seq});
+    if (c->pending.size() > 4096) MLV_TRY(sync_context(c));
+    ++l->executions;
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_get_stats(mlv_context c, mlv_stats *out) {
+    MLV_TRY(need_immediate(c));
+    if (!out) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
+    MLV_TRY(set_device(c->device));
+    MLV_TRY(sync_context(c));
+    MLV_TRY(ensure_fixed(c));
+    unsigned long long dev[kStatCount];
+    CUDA_TRY(cudaMemcpy(dev, c->ws.stats, sizeof(dev), cudaMemcpyDeviceToHost));
+    out->vertex_count = c->host_stats[0];
+    out->input_triangle_count = c->host_stats[1];
+    out->assembled_triangle_count = dev[kStatAssembled];
+    out->active_bin_count = dev[kStatActiveBins];
+    out->total_triangle_count_in_bins = dev[kStatBinEntries];
+    out->draw_count = c->host_stats[2];
+    out->batch_count = c->host_stats[3];
+    out->kernel_launches = c->host_stats[4];
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_reset_stats(mlv_context c) {
+    MLV_TRY(need_immediate(c));
+    MLV_TRY(set_device(c->device));
+    MLV_TRY(sync_context(c));
+    MLV_TRY(ensure_fixed(c));
+    CUDA_TRY(cudaMemset(c->ws.stats, 0, sizeof(unsigned long long) * kStatCount));
+    memset(c->host_stats, 0, sizeof(c->host_stats));
+    memset(c->stage_ms, 0, sizeof(c->stage_ms));
+    memset(c->stage_launches, 0, sizeof(c->stage_launches));
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_get_tuning(mlv_context c, mlv_tuning *out) {
+    if (!c || !out) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
+    *out = c->tuning;
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_set_tuning(mlv_context c, const mlv_tuning *t) {
+    if (!c || !t) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
+    if (t->tile_warps_per_block != 2 && t->tile_warps_per_block != 4 && t->tile_warps_per_block != 8)
+        return fail(MLV_ERROR_INVALID_ARG, "tile_warps_per_block must be 2, 4 or 8");
+    if (t->lanes_per_triangle != 1) return fail(MLV_ERROR_UNSUPPORTED, "lanes_per_triangle must be 1");
+    if (t->geometry_block != 128 && t->geometry_block != 256 && t->geometry_block != 512)
+        return fail(MLV_ERROR_INVALID_ARG, "geometry_block must be 128, 256 or 512");
+    if (t->big_triangle_tiles < 1) return fail(MLV_ERROR_INVALID_ARG, "big_triangle_tiles must be >= 1");
+    c->tuning = *t;
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_set_profiling(mlv_context c, int enable) {
+    MLV_TRY(need_immediate(c));
+    c->profiling = enable != 0;
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_get_stage_times(mlv_context c, double *ms, uint64_t *launches) {
+    MLV_TRY(need_immediate(c));
+    MLV_TRY(set_device(c->device));
+    MLV_TRY(sync_context(c));
+    for (int i = 0; i < MLV_STAGE_COUNT; ++i) {
+        if (ms) ms[i] = c->stage_ms[i];
+        if (launches) launches[i] = c->stage_launches[i];
+    }
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_set_debug_capture(mlv_context c, int enable) {
+    MLV_TRY(need_immediate(c));
+    MLV_TRY(set_device(c->device));
+    MLV_TRY(sync_context(c));
+    c->capture_infos = enable != 0;
+    if (c->capture_infos && c->ws.list && !c->ws.info_mask)
+        MLV_TRY(dev_alloc((void **)&c->ws.info_mask, (size_t)c->ws.list_cap * 8));
+    ++c->ws.generation;
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_get_tile_infos(mlv_context c, uint32_t *tile_index, uint32_t *tri_id, uint64_t *mask,
+                                      uint64_t capacity, uint64_t *out_count) {
+    MLV_TRY(need_immediate(c));
+    if (!out_count) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
+    MLV_TRY(set_device(c->device));
+    MLV_TRY(sync_context(c));
+    if (!c->capture_infos || !c->last_single || !c->ws.info_mask)
+        return fail(MLV_ERROR_INVALID_STATE, "capture was off or the last batch was not a single draw");
+    const uint32_t nb = c->last_total_bins;
+    std::vector<uint32_t> start(nb + 1);
+    CUDA_TRY(cudaMemcpy(start.data(), c->ws.bin_start, sizeof(uint32_t) * (nb + 1), cudaMemcpyDeviceToHost));
+    const uint32_t total = start[nb];
+    *out_count = total;
+    if (!tile_index || !tri_id || !mask) return MLV_OK;
+    if (capacity < total) return fail(MLV_ERROR_INVALID_ARG, "capacity too small");
+    std::vector<uint32_t> list(total);
+    std::vector<uint64_t> m(total);
+    uint32_t rb = 0;
+    if (total) {
+        CUDA_TRY(cudaMemcpy(list.data(), c->ws.list, sizeof(uint32_t) * total, cudaMemcpyDeviceToHost));
+        CUDA_TRY(cudaMemcpy(m.data(), c->ws.info_mask, sizeof(uint64_t) * total, cudaMemcpyDeviceToHost));
+    }
+    CUDA_TRY(cudaMemcpy(&rb, c->ws.draw_record_begin, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    uint64_t k = 0;
+    for (uint32_t b = 0; b < nb; ++b) {
+        std::vector<std::pair<uint32_t, uint64_t>> e;
+        for (uint32_t i = start[b]; i < start[b + 1]; ++i) e.push_back({list[i] - rb, m[i]});
+        std::sort(e.begin(), e.end());
+        for (auto &pr : e) {
+            tile_index[k] = b;
+            tri_id[k] = pr.first;
+            mask[k] = pr.second;
+            ++k;
+        }
+    }
+    return MLV_OK;
+}
+
+}  // extern "C"

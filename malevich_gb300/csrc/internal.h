@@ -1,0 +1,119 @@
+// Internal data layout shared by the host runtime (api.cu) and the kernels (kernels.cu).
+#pragma once
+#include <cstdint>
+#include <vector_types.h>
+
+namespace mlv {
+
+constexpr int kTile = 8;                 // 8x8 pixel tiles: the reference's bins (main.c:24-25)
+constexpr int kSubpix = 4;               // 28.4 fixed point (main.c:39)
+constexpr int kMaxClipVertices = 16;     // main.c:38
+constexpr int kMaxViewsPerBatch = 4096;
+
+// Error bits of the context's device status word.
+enum : uint32_t {
+    kErrLookbackTimeout = 1u << 0,
+    kErrRecordOverflow = 1u << 1,
+    kErrListOverflow = 1u << 2,
+    kErrBigOverflow = 1u << 3,
+    kErrBadIndex = 1u << 4,
+};
+
+struct TexDesc {
+    const void *data;
+    uint32_t width, height;
+    int32_t format;                      // 1 RGBA8, 2 RGBA16F, 3 RGBA32F
+    int32_t pad;
+};
+
+// One draw of a batch, as the kernels see it (the reference's Pipeline state at draw_indexed time).
+struct DrawDesc {
+    const uint8_t *vb;
+    const uint32_t *ib;                  // nullptr: implicit indices
+    uint32_t vb_stride, vertex_count;
+    uint32_t start_index;
+    int32_t base_vertex;
+    uint32_t tri_begin;                  // first input triangle of this draw in the batch
+    uint32_t tri_count;
+    int32_t vs, ps, cull, depth_less;    // cull: 0 none, 1 back (reference), 2 front
+    uint32_t view;                       // view (render target + depth) index in the batch
+    uint32_t draw_in_view;               // position among the view's draws in this batch
+    uint32_t draw_seq;                   // draw number since the render target's last clear
+    uint32_t pad0;
+    float cb[48];                        // PerFrameCB snapshot
+    float screen_from_ndc[16];           // main.c:825-830, computed on the host as the reference does
+    int32_t vp_w, vp_h;                  // (i32)viewport.width/height
+    uint32_t pad1[2];
+    TexDesc vs_tex, ps_tex;
+};
+
+struct ViewDesc {
+    uint32_t *color;
+    float *depth;
+    float *tile_min, *tile_max;          // hierarchical Z per 8x8 tile
+    uint32_t *vis_tri;                   // optional visibility outputs
+    uint32_t *vis_draw;
+    float *vis_bary;
+    uint32_t width, height, tiles_x, tiles_y;
+    uint32_t tile_base;                  // first tile of this view in the batch's tile space
+    uint32_t draw_begin, draw_count;     // the view's draws are contiguous in the draw array
+    uint32_t bin_base;                   // bin of (tile t, draw d) = bin_base + t * draw_count + d
+    uint32_t pad[2];
+};
+
+// Per assembled triangle, read by the tile kernel for every (tile, triangle) pair: 64 bytes.
+//   w0 = e0.a, e0.b, e0.c, e1.a      w1 = e1.b, e1.c, e2.a, e2.b
+//   w2 = e2.c, inv_area, zbound, z0  w3 = z1, z2, bbox min (x | y << 16), bbox max (x | y << 16)
+struct TriRaster {
+    int4 w[4];
+};
+
+// Per assembled triangle, read once per shaded pixel: 80 bytes.
+//   s0 = rw0, rw1, rw2, draw          s1..s3 = reg1 (xyzw) of vertices 0..2
+//   s4 = reg2.x of vertices 0..2, pad
+struct TriShade {
+    float4 s[5];
+};
+
+// Screen-space positions (reg0 after the viewport transform), for the differentiable path.
+struct TriGeom {
+    float x[3], y[3], z[3], w[3];
+};
+
+struct BatchParams {
+    const DrawDesc *draws;
+    const ViewDesc *views;
+    uint32_t num_draws, num_views;
+    uint32_t total_tris;                 // input triangles in the batch
+    uint32_t total_tiles;                // sum of views' tiles
+    uint32_t total_bins;                 // sum of views' tiles * draws
+    uint32_t record_capacity, list_capacity, big_capacity;
+    uint32_t big_tiles;                  // triangles spanning more tiles go to the big list
+    uint32_t batch_seq;
+    TriRaster *raster;
+    TriShade *shade;
+    TriGeom *geom;                       // nullptr unless the geometry is kept
+    uint32_t *draw_record_begin;         // first record of each draw
+    uint32_t *bin_count;                 // [total_bins], zero between batches
+    uint32_t *bin_start;                 // [total_bins + 1]
+    uint32_t *list;                      // [list_capacity] record ids, grouped by bin
+    uint32_t *big_list;                  // [big_capacity]
+    uint64_t *info_mask;                 // optional TileInfo capture, parallel to list
+    unsigned long long *scan_status;     // decoupled look-back of k_geometry: (epoch:30|flag:2) << 32 | value
+    unsigned long long *scan_status2;    // decoupled look-back of k_scan
+    uint32_t *counters;                  // see Counter
+    unsigned long long *stats;           // device statistics, see StatSlot
+    uint32_t *error;                     // [0] error bits, [1] first failing batch seq, [2..] need
+};
+
+enum Counter : int {
+    kCtrGeomTicket = 0, kCtrGeomDone, kCtrGeomEpoch, kCtrGeomTotal,
+    kCtrScanTicket, kCtrScanDone, kCtrScanEpoch,
+    kCtrBigCount, kCtrCount = 16
+};
+
+enum StatSlot : int {
+    kStatAssembled = 0, kStatActiveBins, kStatBinEntries, kStatCount = 8
+};
+
+}  // namespace mlv

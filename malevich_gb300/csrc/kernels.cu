@@ -1,0 +1,790 @@
+// Draw-path kernels for sm_103a.
+//
+// One batch (any number of draws over any number of render targets) runs as four kernels:
+//   k_geometry  IA + VS + primitive assembly/clip/setup + per-(tile, draw) bin counts
+//               (source/main.c:662-913 and the counting half of the binner, 924-936). One thread
+//               per input triangle; assembled triangles are written in the reference's serial
+//               order (input triangle, fan index) by a single-pass decoupled look-back scan.
+//   k_scan      exclusive scan of the bin counts (main.c:937-946), same look-back scheme.
+//   k_scatter   bin lists (main.c:950-962); the order inside a bin does not matter (see k_tile).
+//   k_tile      one warp per 8x8 tile: hierarchical Z, coverage, depth, pixel shader, output
+//               merger, write-back (main.c:983-1189, 577-603), for every draw of the batch that
+//               touches the tile, in draw order, with colour and depth held on-chip until one
+//               write-back.
+//
+// Why the order inside a bin does not matter: there is no blending (main.c:1180-1181) and pixel
+// shaders have no side effects, so after a draw a pixel holds the output of the *last* fragment
+// (in assembled order) whose depth is the maximum among the fragments that passed coverage, the
+// hierarchical-Z test and `z >= depth at draw start` (GREATER_EQUAL; for LESS, the *first*
+// fragment with the minimum depth). That is a max (min) over the 64-bit key (depth, order), which
+// the tile kernel computes with shared-memory atomics, then shades only the winner.
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "internal.h"
+#include "shade.cuh"
+
+namespace mlv {
+
+__constant__ float c_clip_planes[6][4];
+
+// ------------------------------------------------------------------ memory-order helpers
+
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release_u64(unsigned long long *p, unsigned long long v) {
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__device__ __forceinline__ uint32_t ld_volatile_u32(const uint32_t *p) {
+    return *(const volatile uint32_t *)p;
+}
+
+constexpr uint32_t kFlagAggregate = 1, kFlagInclusive = 2;
+constexpr uint32_t kSpinLimit = 1u << 22;   // bounded wait: about half a second with the backoff
+
+// Decoupled look-back (single thread). Publishes this block's aggregate, accumulates the
+// predecessors' values until an inclusive prefix is found, publishes the inclusive value and
+// returns the exclusive prefix. Every wait is bounded: on timeout the error bit is set and the
+// block still publishes, so that no successor waits on it.
+__device__ uint32_t lookback(unsigned long long *status, uint32_t bid, uint32_t epoch, uint32_t aggregate,
+                             uint32_t *error) {
+    const unsigned long long tag = (unsigned long long)(epoch & 0x3FFFFFFFu) << 34;
+    if (bid == 0) {
+        st_release_u64(status, tag | ((unsigned long long)kFlagInclusive << 32) | aggregate);
+        return 0;
+    }
+    st_release_u64(status + bid, tag | ((unsigned long long)kFlagAggregate << 32) | aggregate);
+    uint32_t prefix = 0;
+    int32_t j = (int32_t)bid - 1;
+    uint32_t spins = 0;
+    while (j >= 0) {
+        unsigned long long s = ld_acquire_u64(status + j);
+        uint32_t hi = (uint32_t)(s >> 32);
+        uint32_t flag = hi & 3u;
+        if ((hi >> 2) != (epoch & 0x3FFFFFFFu) || flag == 0) {
+            if (++spins > kSpinLimit) {
+                atomicOr(error, kErrLookbackTimeout);
+                break;
+            }
+            __nanosleep(64);
+            continue;
+        }
+        prefix += (uint32_t)s;
+        if (flag == kFlagInclusive) break;
+        --j;
+    }
+    st_release_u64(status + bid, tag | ((unsigned long long)kFlagInclusive << 32) | (prefix + aggregate));
+    return prefix;
+}
+
+template <int BLOCK>
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *s_warp, uint32_t &total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < BLOCK / 32 ? s_warp[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < BLOCK / 32) s_warp[lane] = w;
+    }
+    __syncthreads();
+    total = s_warp[BLOCK / 32 - 1];
+    uint32_t warp_prefix = warp ? s_warp[warp - 1] : 0;
+    return warp_prefix + x - v;
+}
+
+// ------------------------------------------------------------------ primitive setup
+
+// One clip-space vertex as the rest of the pipeline sees it: SV_POSITION + reg1.xyz + U + V.
+struct Vtx {
+    float v[9];
+};
+
+struct Setup {
+    int32_t e[9];           // edge0 a,b,c  edge1 a,b,c  edge2 a,b,c
+    float inv_area, zbound;
+    float ss[3][4];         // screen-space reg0 of the three vertices
+    float rw[3];
+    int32_t minx, miny, maxx, maxy;
+};
+
+// set_edge_function, main.c:563-575 (wrapping int32)
+__device__ __forceinline__ void set_edge(int32_t *e, int32_t area, int32_t x0, int32_t y0, int32_t x1, int32_t y1) {
+    uint32_t a = (uint32_t)y0 - (uint32_t)y1;
+    uint32_t b = (uint32_t)x1 - (uint32_t)x0;
+    if (area < 0) { a = 0u - a; b = 0u - b; }
+    uint32_t c = (0u - a) * (uint32_t)x0 - b * (uint32_t)y0;
+    e[0] = (int32_t)a; e[1] = (int32_t)b; e[2] = (int32_t)c;
+}
+
+// Projection, viewport, 28.4 snap, signed area, cull, edge functions, 1/w, depth bound and pixel
+// bounds for one (possibly clip-generated) triangle: main.c:798-904. Returns false when culled.
+__device__ __forceinline__ bool setup_triangle(const DrawDesc &d, const Vtx &v0, const Vtx &v1, const Vtx &v2,
+                                               Setup &s) {
+    const Vtx *tv[3] = {&v0, &v1, &v2};
+    const float *m = d.screen_from_ndc;
+    int32_t x[3], y[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        float rw = 1.0f / tv[k]->v[3];
+        float p0 = tv[k]->v[0] * rw, p1 = tv[k]->v[1] * rw, p2 = tv[k]->v[2] * rw, p3 = tv[k]->v[3] * rw;
+        s.rw[k] = rw;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) s.ss[k][r] = dot4_lr(m + 4 * r, p0, p1, p2, p3);
+        x[k] = snap28_4(s.ss[k][0]);
+        y[k] = snap28_4(s.ss[k][1]);
+    }
+    int32_t area = (int32_t)(((uint32_t)x[1] - (uint32_t)x[0]) * ((uint32_t)y[2] - (uint32_t)y[0]) -
+                             ((uint32_t)x[2] - (uint32_t)x[0]) * ((uint32_t)y[1] - (uint32_t)y[0]));
+    if (d.cull == 1 && area > 0) return false;
+    if (d.cull == 2 && area < 0) return false;
+    set_edge(s.e + 6, area, x[0], y[0], x[1], y[1]);
+    set_edge(s.e + 0, area, x[1], y[1], x[2], y[2]);
+    set_edge(s.e + 3, area, x[2], y[2], x[0], y[0]);
+    float af = (float)(area >> (kSubpix * 2));
+    if (af == 0.0f) af = 1.0f;
+    s.inv_area = fabsf(1.f / af);
+    if (d.depth_less)
+        s.zbound = fmin_ref(s.ss[0][2], fmin_ref(s.ss[1][2], s.ss[2][2]));
+    else
+        s.zbound = fmax_ref(s.ss[0][2], fmax_ref(s.ss[1][2], s.ss[2][2]));
+    int32_t mnx = min(x[0], min(x[1], x[2])) >> kSubpix, mny = min(y[0], min(y[1], y[2])) >> kSubpix;
+    int32_t mxx = max(x[0], max(x[1], x[2])) >> kSubpix, mxy = max(y[0], max(y[1], y[2])) >> kSubpix;
+    mnx = min(max(mnx, 0), d.vp_w - 1);
+    mny = min(max(mny, 0), d.vp_h - 1);
+    mxx = min(mxx + 1, d.vp_w - 1);
+    mxy = min(mxy + 1, d.vp_h - 1);
+    s.minx = mnx; s.miny = mny; s.maxx = mxx; s.maxy = mxy;
+    return true;
+}
+
+__device__ __forceinline__ void write_record(const BatchParams &bp, uint32_t rec, uint32_t draw, const Setup &s,
+                                             const Vtx &v0, const Vtx &v1, const Vtx &v2) {
+    int4 *r = bp.raster[rec].w;
+    r[0] = make_int4(s.e[0], s.e[1], s.e[2], s.e[3]);
+    r[1] = make_int4(s.e[4], s.e[5], s.e[6], s.e[7]);
+    r[2] = make_int4(s.e[8], __float_as_int(s.inv_area), __float_as_int(s.zbound), __float_as_int(s.ss[0][2]));
+    r[3] = make_int4(__float_as_int(s.ss[1][2]), __float_as_int(s.ss[2][2]),
+                     (s.minx & 0xFFFF) | (s.miny << 16), (s.maxx & 0xFFFF) | (s.maxy << 16));
+    float4 *h = bp.shade[rec].s;
+    h[0] = make_float4(s.rw[0], s.rw[1], s.rw[2], __uint_as_float(draw));
+    h[1] = make_float4(v0.v[4], v0.v[5], v0.v[6], v0.v[7]);
+    h[2] = make_float4(v1.v[4], v1.v[5], v1.v[6], v1.v[7]);
+    h[3] = make_float4(v2.v[4], v2.v[5], v2.v[6], v2.v[7]);
+    h[4] = make_float4(v0.v[8], v1.v[8], v2.v[8], 0.0f);
+    if (bp.geom) {
+        TriGeom &g = bp.geom[rec];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            g.x[k] = s.ss[k][0]; g.y[k] = s.ss[k][1]; g.z[k] = s.ss[k][2]; g.w[k] = s.ss[k][3];
+        }
+    }
+}
+
+// clip_by_plane, main.c:609-647 (Sutherland-Hodgman on one normalised plane, plane_d = 0)
+__device__ void clip_by_plane(Vtx *poly, Vtx *tmp, int &count, const float *n) {
+    int nv = count, out = 0;
+    if (nv <= 0) return;
+    float cd = dot4_lr(n, poly[0].v[0], poly[0].v[1], poly[0].v[2], poly[0].v[3]);
+    bool cin = cd > -0.0f;
+    for (int i = 0; i < nv; ++i) {
+        int next = (i + 1) % nv;
+        if (cin && out < kMaxClipVertices) tmp[out++] = poly[i];
+        const Vtx &pn = poly[next];
+        float nd = dot4_lr(n, pn.v[0], pn.v[1], pn.v[2], pn.v[3]);
+        bool nin = nd > -0.0f;
+        if (cin != nin && out < kMaxClipVertices) {
+            float t = (0.0f + cd) / (cd - nd);
+            float omt = 1.f - t;
+#pragma unroll
+            for (int c = 0; c < 9; ++c) tmp[out].v[c] = poly[i].v[c] * omt + pn.v[c] * t;
+            ++out;
+        }
+        cd = nd;
+        cin = nin;
+    }
+    count = out;
+    for (int i = 0; i < out; ++i) poly[i] = tmp[i];
+}
+
+__device__ __forceinline__ uint32_t find_draw(const BatchParams &bp, uint32_t tri) {
+    uint32_t lo = 0, hi = bp.num_draws;   // last draw with tri_begin <= tri
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&bp.draws[mid].tri_begin) <= tri) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ void fetch_vertex(const DrawDesc &d, uint32_t idx_pos, float *in, uint32_t *warn) {
+    int64_t idx = d.ib ? (int64_t)__ldg(d.ib + idx_pos) : (int64_t)idx_pos;
+    idx += d.base_vertex;
+    if (idx < 0 || idx >= (int64_t)d.vertex_count) {
+        atomicOr(warn, kErrBadIndex);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) in[k] = 0.0f;   // D3D11: out-of-range vertex fetch reads zeros
+        return;
+    }
+    const uint8_t *p = d.vb + (size_t)idx * d.vb_stride;
+    if ((((uintptr_t)p) & 15) == 0) {
+        float4 a = __ldg((const float4 *)p), b = __ldg((const float4 *)p + 1);
+        in[0] = a.x; in[1] = a.y; in[2] = a.z; in[3] = a.w; in[4] = b.x; in[5] = b.y; in[6] = b.z; in[7] = b.w;
+    } else {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) in[k] = __ldg((const float *)p + k);
+    }
+}
+
+__device__ __forceinline__ void tile_range(const ViewDesc &v, int32_t minx, int32_t miny, int32_t maxx, int32_t maxy,
+                                           int32_t &tx0, int32_t &ty0, int32_t &tx1, int32_t &ty1) {
+    // binner, main.c:927-928 (C division truncates toward zero)
+    tx0 = max(minx / kTile, 0);
+    ty0 = max(miny / kTile, 0);
+    tx1 = min(maxx / kTile, (int32_t)v.tiles_x - 1);
+    ty1 = min(maxy / kTile, (int32_t)v.tiles_y - 1);
+}
+
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_geometry(BatchParams bp) {
+    __shared__ uint32_t s_bid, s_epoch, s_prefix, s_total;
+    __shared__ uint32_t s_warp[BLOCK / 32];
+    __shared__ uint32_t s_nbig;
+    __shared__ uint32_t s_big[BLOCK];
+    if (threadIdx.x == 0) {
+        s_bid = atomicAdd(bp.counters + kCtrGeomTicket, 1u);
+        s_epoch = ld_volatile_u32(bp.counters + kCtrGeomEpoch);
+        s_nbig = 0;
+    }
+    __syncthreads();
+    const uint32_t bid = s_bid;
+    const uint32_t tri = bid * BLOCK + threadIdx.x;
+    const bool active = tri < bp.total_tris;
+
+    uint32_t draw = 0;
+    Vtx v[3];
+    Setup su;
+    int nout = 0;
+    bool clipped = false;
+    if (active) {
+        draw = find_draw(bp, tri);
+        const DrawDesc &d = bp.draws[draw];
+        const uint32_t local = tri - d.tri_begin;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            float in[8];
+            fetch_vertex(d, d.start_index + 3 * local + k, in, bp.error + 2);
+            run_vs(d.vs, in, d.cb, d.vs_tex, v[k].v);
+        }
+        const float *p0 = v[0].v, *p1 = v[1].v, *p2 = v[2].v;
+        // main.c:759-781
+        bool reject = p0[3] == 0 || p1[3] == 0 || p2[3] == 0;
+        reject = reject || (p0[0] < -p0[3] && p1[0] < -p1[3] && p2[0] < -p2[3]) ||
+                 (p0[0] > +p0[3] && p1[0] > +p1[3] && p2[0] > +p2[3]) ||
+                 (p0[1] < -p0[3] && p1[1] < -p1[3] && p2[1] < -p2[3]) ||
+                 (p0[1] > +p0[3] && p1[1] > +p1[3] && p2[1] > +p2[3]) ||
+                 (p0[2] < 0.f && p1[2] < 0.f && p2[2] < 0.f) ||
+                 (p0[2] > +p0[3] && p1[2] > +p1[3] && p2[2] > +p2[3]);
+        if (!reject) {
+            clipped = !((p0[0] >= -p0[3] && p1[0] >= -p1[3] && p2[0] >= -p2[3]) &&
+                        (p0[0] <= +p0[3] && p1[0] <= +p1[3] && p2[0] <= +p2[3]) &&
+                        (p0[1] >= -p0[3] && p1[1] >= -p1[3] && p2[1] >= -p2[3]) &&
+                        (p0[1] <= +p0[3] && p1[1] <= +p1[3] && p2[1] <= +p2[3]) &&
+                        (p0[2] >= 0.f && p1[2] >= 0.f && p2[2] >= 0.f) &&
+                        (p0[2] <= +p0[3] && p1[2] <= +p1[3] && p2[2] <= +p2[3]));
+            if (!clipped) {
+                nout = setup_triangle(d, v[0], v[1], v[2], su) ? 1 : 0;
+            } else {
+                Vtx poly[kMaxClipVertices], tmp[kMaxClipVertices];
+                poly[0] = v[0]; poly[1] = v[1]; poly[2] = v[2];
+                int count = 3;
+                for (int p = 0; p < 6; ++p) clip_by_plane(poly, tmp, count, c_clip_planes[p]);
+                for (int f = 1; f < count - 1; ++f) {
+                    Setup s2;
+                    if (setup_triangle(d, poly[0], poly[f], poly[f + 1], s2)) ++nout;
+                }
+            }
+        }
+    }
+
+    // order-preserving compaction: block scan + decoupled look-back
+    uint32_t total;
+    uint32_t excl = block_exclusive_scan<BLOCK>((uint32_t)nout, s_warp, total);
+    if (threadIdx.x == 0) {
+        unsigned long long *status = bp.scan_status;
+        s_prefix = lookback(status, bid, s_epoch, total, bp.error);
+        s_total = total;
+    }
+    __syncthreads();
+    const uint32_t base = s_prefix + excl;
+
+    if (active) {
+        const DrawDesc &d = bp.draws[draw];
+        if (tri == d.tri_begin) bp.draw_record_begin[draw] = base;
+    }
+
+    if (nout > 0) {
+        const DrawDesc &d = bp.draws[draw];
+        const ViewDesc &vw = bp.views[d.view];
+        const uint32_t bin_stride = vw.draw_count;
+        auto emit = [&](uint32_t rec, const Setup &s, const Vtx &a, const Vtx &b, const Vtx &c) {
+            if (rec >= bp.record_capacity) {
+                atomicOr(bp.error, kErrRecordOverflow);
+                atomicMin(bp.error + 1, bp.batch_seq);
+                return;
+            }
+            write_record(bp, rec, draw, s, a, b, c);
+            int32_t tx0, ty0, tx1, ty1;
+            tile_range(vw, s.minx, s.miny, s.maxx, s.maxy, tx0, ty0, tx1, ty1);
+            int32_t ntiles = (tx1 >= tx0 && ty1 >= ty0) ? (tx1 - tx0 + 1) * (ty1 - ty0 + 1) : 0;
+            if (ntiles > (int32_t)bp.big_tiles) {
+                // counted cooperatively by the block below; if the block's list is full (only
+                // possible with many clip-generated fans) this thread counts it itself
+                uint32_t slot = atomicAdd(&s_nbig, 1u);
+                if (slot < (uint32_t)BLOCK) {
+                    s_big[slot] = rec;
+                    return;
+                }
+            }
+            for (int32_t ty = ty0; ty <= ty1; ++ty)
+                for (int32_t tx = tx0; tx <= tx1; ++tx) {
+                    uint32_t bin = vw.bin_base + ((uint32_t)ty * vw.tiles_x + (uint32_t)tx) * bin_stride + d.draw_in_view;
+                    atomicAdd(bp.bin_count + bin, 1u);
+                }
+        };
+        if (!clipped) {
+            emit(base, su, v[0], v[1], v[2]);
+        } else {
+            Vtx poly[kMaxClipVertices], tmp[kMaxClipVertices];
+            poly[0] = v[0]; poly[1] = v[1]; poly[2] = v[2];
+            int count = 3;
+            for (int p = 0; p < 6; ++p) clip_by_plane(poly, tmp, count, c_clip_planes[p]);
+            uint32_t k = 0;
+            for (int f = 1; f < count - 1; ++f) {
+                Setup s2;
+                if (setup_triangle(d, poly[0], poly[f], poly[f + 1], s2)) {
+                    emit(base + k, s2, poly[0], poly[f], poly[f + 1]);
+                    ++k;
+                }
+            }
+        }
+    }
+    __syncthreads();
+
+    // triangles spanning many tiles: the whole block counts their tiles
+    const uint32_t nbig = min(s_nbig, (uint32_t)BLOCK);
+    for (uint32_t b = 0; b < nbig; ++b) {
+        const uint32_t rec = s_big[b];
+        const int4 w3 = bp.raster[rec].w[3];
+        const uint32_t dr = __float_as_uint(bp.shade[rec].s[0].w);
+        const DrawDesc &d = bp.draws[dr];
+        const ViewDesc &vw = bp.views[d.view];
+        int32_t minx = (int16_t)(w3.z & 0xFFFF), miny = w3.z >> 16, maxx = (int16_t)(w3.w & 0xFFFF), maxy = w3.w >> 16;
+        int32_t tx0, ty0, tx1, ty1;
+        tile_range(vw, minx, miny, maxx, maxy, tx0, ty0, tx1, ty1);
+        const int32_t nx = tx1 - tx0 + 1, n = nx * (ty1 - ty0 + 1);
+        for (int32_t i = threadIdx.x; i < n; i += BLOCK) {
+            uint32_t tx = tx0 + i % nx, ty = ty0 + i / nx;
+            uint32_t bin = vw.bin_base + (ty * vw.tiles_x + tx) * vw.draw_count + d.draw_in_view;
+            atomicAdd(bp.bin_count + bin, 1u);
+        }
+    }
+
+    // the last block resets the ticket and advances the epoch (graph-replay safe)
+    if (threadIdx.x == 0) {
+        if (bid == gridDim.x - 1) {
+            bp.counters[kCtrGeomTotal] = s_prefix + s_total;
+            atomicAdd(bp.stats + kStatAssembled, (unsigned long long)(s_prefix + s_total));
+        }
+        __threadfence();
+        uint32_t done = atomicAdd(bp.counters + kCtrGeomDone, 1u);
+        if (done == gridDim.x - 1) {
+            bp.counters[kCtrGeomTicket] = 0;
+            bp.counters[kCtrGeomDone] = 0;
+            bp.counters[kCtrGeomEpoch] = s_epoch + 1;
+            __threadfence();
+        }
+    }
+}
+
+// ------------------------------------------------------------------ bin scan
+
+constexpr int kScanBlock = 256, kScanItems = 8;
+
+__global__ void __launch_bounds__(kScanBlock) k_scan(BatchParams bp) {
+    __shared__ uint32_t s_bid, s_epoch, s_prefix;
+    __shared__ uint32_t s_warp[kScanBlock / 32];
+    if (ld_volatile_u32(bp.error)) return;   // uniform: set only by earlier kernels
+    if (threadIdx.x == 0) {
+        s_bid = atomicAdd(bp.counters + kCtrScanTicket, 1u);
+        s_epoch = ld_volatile_u32(bp.counters + kCtrScanEpoch);
+    }
+    __syncthreads();
+    const uint32_t bid = s_bid;
+    const uint32_t n = bp.total_bins;
+    const uint32_t base = bid * kScanBlock * kScanItems + threadIdx.x * kScanItems;
+    uint32_t vals[kScanItems];
+    uint32_t sum = 0, active = 0;
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) {
+        uint32_t idx = base + i;
+        vals[i] = idx < n ? bp.bin_count[idx] : 0u;
+        sum += vals[i];
+        active += vals[i] ? 1u : 0u;
+    }
+    uint32_t total;
+    uint32_t excl = block_exclusive_scan<kScanBlock>(sum, s_warp, total);
+    if (threadIdx.x == 0) s_prefix = lookback(bp.scan_status2, bid, s_epoch, total, bp.error);
+    __syncthreads();
+    uint32_t run = s_prefix + excl;
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) {
+        uint32_t idx = base + i;
+        if (idx < n) bp.bin_start[idx] = run;
+        run += vals[i];
+    }
+    // active-bin statistic (main.c:937-944)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) active += __shfl_xor_sync(0xFFFFFFFFu, active, o);
+    if ((threadIdx.x & 31) == 0 && active) atomicAdd(bp.stats + kStatActiveBins, (unsigned long long)active);
+    if (threadIdx.x == 0) {
+        if (bid == gridDim.x - 1) {
+            bp.bin_start[n] = s_prefix + total;
+            atomicAdd(bp.stats + kStatBinEntries, (unsigned long long)(s_prefix + total));
+        }
+        __threadfence();
+        uint32_t done = atomicAdd(bp.counters + kCtrScanDone, 1u);
+        if (done == gridDim.x - 1) {
+            bp.counters[kCtrScanTicket] = 0;
+            bp.counters[kCtrScanDone] = 0;
+            bp.counters[kCtrScanEpoch] = s_epoch + 1;
+            __threadfence();
+        }
+    }
+}
+
+// ------------------------------------------------------------------ bin scatter
+
+constexpr int kScatterBlock = 256;
+
+__global__ void __launch_bounds__(kScatterBlock) k_scatter(BatchParams bp) {
+    __shared__ uint32_t s_nbig;
+    __shared__ uint32_t s_big[kScatterBlock];
+    if (ld_volatile_u32(bp.error)) return;
+    const uint32_t total = bp.bin_start[bp.total_bins];
+    if (total > bp.list_capacity) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            atomicOr(bp.error, kErrListOverflow);
+            atomicMin(bp.error + 1, bp.batch_seq);
+            atomicMax(bp.error + 3, total);
+        }
+        return;
+    }
+    const uint32_t nrec = min(bp.counters[kCtrGeomTotal], bp.record_capacity);
+    for (uint32_t base = blockIdx.x * kScatterBlock; base < nrec; base += gridDim.x * kScatterBlock) {
+        if (threadIdx.x == 0) s_nbig = 0;
+        __syncthreads();
+        const uint32_t rec = base + threadIdx.x;
+        if (rec < nrec) {
+            const int4 w3 = bp.raster[rec].w[3];
+            const uint32_t dr = __float_as_uint(bp.shade[rec].s[0].w);
+            const DrawDesc &d = bp.draws[dr];
+            const ViewDesc &vw = bp.views[d.view];
+            int32_t minx = (int16_t)(w3.z & 0xFFFF), miny = w3.z >> 16, maxx = (int16_t)(w3.w & 0xFFFF), maxy = w3.w >> 16;
+            int32_t tx0, ty0, tx1, ty1;
+            tile_range(vw, minx, miny, maxx, maxy, tx0, ty0, tx1, ty1);
+            int32_t ntiles = (tx1 >= tx0 && ty1 >= ty0) ? (tx1 - tx0 + 1) * (ty1 - ty0 + 1) : 0;
+            if (ntiles > (int32_t)bp.big_tiles) {
+                s_big[atomicAdd(&s_nbig, 1u)] = rec;
+            } else {
+                for (int32_t ty = ty0; ty <= ty1; ++ty)
+                    for (int32_t tx = tx0; tx <= tx1; ++tx) {
+                        uint32_t bin = vw.bin_base + ((uint32_t)ty * vw.tiles_x + (uint32_t)tx) * vw.draw_count + d.draw_in_view;
+                        uint32_t pos = atomicSub(bp.bin_count + bin, 1u) - 1u;
+                        bp.list[bp.bin_start[bin] + pos] = rec;
+                    }
+            }
+        }
+        __syncthreads();
+        for (uint32_t b = 0; b < s_nbig; ++b) {
+            const uint32_t r = s_big[b];
+            const int4 w3 = bp.raster[r].w[3];
+            const uint32_t dr = __float_as_uint(bp.shade[r].s[0].w);
+            const DrawDesc &d = bp.draws[dr];
+            const ViewDesc &vw = bp.views[d.view];
+            int32_t minx = (int16_t)(w3.z & 0xFFFF), miny = w3.z >> 16, maxx = (int16_t)(w3.w & 0xFFFF), maxy = w3.w >> 16;
+            int32_t tx0, ty0, tx1, ty1;
+            tile_range(vw, minx, miny, maxx, maxy, tx0, ty0, tx1, ty1);
+            const int32_t nx = tx1 - tx0 + 1, n = nx * (ty1 - ty0 + 1);
+            for (int32_t i = threadIdx.x; i < n; i += kScatterBlock) {
+                uint32_t tx = tx0 + i % nx, ty = ty0 + i / nx;
+                uint32_t bin = vw.bin_base + (ty * vw.tiles_x + tx) * vw.draw_count + d.draw_in_view;
+                uint32_t pos = atomicSub(bp.bin_count + bin, 1u) - 1u;
+                bp.list[bp.bin_start[bin] + pos] = r;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------ tile kernel
+
+// Monotone map of a float depth to u32 (after folding -0 onto +0, which compares equal).
+__device__ __forceinline__ uint32_t depth_key(float z) {
+    uint32_t u = __float_as_uint(z);
+    if (u == 0x80000000u) u = 0;
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+__device__ __forceinline__ float depth_from_key(uint32_t k) {
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k);
+}
+
+__device__ __forceinline__ uint32_t find_view(const BatchParams &bp, uint32_t tile) {
+    uint32_t lo = 0, hi = bp.num_views;
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&bp.views[mid].tile_base) <= tile) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
+    __shared__ unsigned long long s_best[WARPS][64];
+    __shared__ float s_depth[WARPS][64];
+    if (ld_volatile_u32(bp.error)) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t gtile = blockIdx.x * WARPS + warp;
+    if (gtile >= bp.total_tiles) return;
+    const uint32_t vi = find_view(bp, gtile);
+    const ViewDesc &V = bp.views[vi];
+    const uint32_t t = gtile - V.tile_base;
+    const uint32_t tx = t % V.tiles_x, ty = t / V.tiles_x;
+    const uint32_t bin0 = V.bin_base + t * V.draw_count;
+    const uint32_t dc = V.draw_count;
+    if (bp.bin_start[bin0] == bp.bin_start[bin0 + dc]) return;   // no draw binned a triangle here
+
+    const int32_t x0 = (int32_t)tx * kTile, y0 = (int32_t)ty * kTile;
+    // lane owns pixels p0 = lane (rows 0-3) and p1 = lane + 32 (rows 4-7)
+    const int32_t px = x0 + (lane & 7), py0 = y0 + (lane >> 3), py1 = py0 + 4;
+    const bool valid0 = px < (int32_t)V.width && py0 < (int32_t)V.height;
+    const bool valid1 = px < (int32_t)V.width && py1 < (int32_t)V.height;
+    const size_t o0 = (size_t)py0 * V.width + px, o1 = (size_t)py1 * V.width + px;
+    float dcur0 = valid0 ? V.depth[o0] : 0.0f;
+    float dcur1 = valid1 ? V.depth[o1] : 0.0f;
+    uint32_t win0 = 0xFFFFFFFFu, win1 = 0xFFFFFFFFu;
+    s_depth[warp][lane] = dcur0;
+    s_depth[warp][lane + 32] = dcur1;
+    float hiz_min = V.tile_min[t], hiz_max = V.tile_max[t];
+    bool touched = false;
+
+    for (uint32_t dd = 0; dd < dc; ++dd) {
+        const uint32_t s = bp.bin_start[bin0 + dd], e = bp.bin_start[bin0 + dd + 1];
+        if (s == e) continue;
+        touched = true;
+        const DrawDesc &D = bp.draws[V.draw_begin + dd];
+        const bool less = D.depth_less != 0;
+        const unsigned long long sentinel = less ? ~0ull : 0ull;
+        s_best[warp][lane] = sentinel;
+        s_best[warp][lane + 32] = sentinel;
+        __syncwarp();
+        const float hiz = less ? hiz_max : hiz_min;
+        for (uint32_t i = s + lane; i < e; i += 32) {
+            const uint32_t rec = bp.list[i];
+            const int4 *R = bp.raster[rec].w;
+            const int4 w2 = R[2], w3 = R[3];
+            const float zb = __int_as_float(w2.z);
+            uint64_t mask = 0;
+            const bool rejected = less ? (zb > hiz) : (zb < hiz);   // main.c:1005-1010 (mirrored for LESS)
+            if (!rejected) {
+                const int4 w0 = R[0], w1 = R[1];
+                const uint32_t a0 = w0.x, b0 = w0.y, c0 = w0.z, a1 = w0.w, b1 = w1.x, c1 = w1.y, a2 = w1.z, b2 = w1.w,
+                               c2 = w2.x;
+                const float inv_area = __int_as_float(w2.y), z0 = __int_as_float(w2.w), z1 = __int_as_float(w3.x),
+                            z2 = __int_as_float(w3.y);
+                const float dz1 = z1 - z0, dz2 = z2 - z0;
+                int32_t bx0 = (int16_t)(w3.z & 0xFFFF), by0 = w3.z >> 16;
+                int32_t bx1 = (int16_t)(w3.w & 0xFFFF), by1 = w3.w >> 16;
+                bx0 = max(bx0, x0); by0 = max(by0, y0);
+                bx1 = min(bx1, x0 + kTile - 1); by1 = min(by1, y0 + kTile - 1);
+                for (int32_t y = by0; y <= by1; ++y) {
+                    // main.c:1015-1025: ((a*x)<<4) + ((b*y)<<4) + c, wrapping int32
+                    uint32_t E0 = ((a0 * (uint32_t)bx0) << kSubpix) + ((b0 * (uint32_t)y) << kSubpix) + c0;
+                    uint32_t E1 = ((a1 * (uint32_t)bx0) << kSubpix) + ((b1 * (uint32_t)y) << kSubpix) + c1;
+                    uint32_t E2 = ((a2 * (uint32_t)bx0) << kSubpix) + ((b2 * (uint32_t)y) << kSubpix) + c2;
+                    for (int32_t x = bx0; x <= bx1; ++x) {
+                        if ((int32_t)(E0 | E1 | E2) > 0) {   // main.c:1028
+                            const int p = (y - y0) * 8 + (x - x0);
+                            mask |= 1ull << p;
+                            // main.c:1092-1102 and 1131-1132 for reg0.z
+                            const float bb1 = (float)((int32_t)E1 >> (kSubpix * 2)) * inv_area;
+                            const float bb2 = (float)((int32_t)E2 >> (kSubpix * 2)) * inv_area;
+                            float z = z0 + dz1 * bb1;
+                            z = z + dz2 * bb2;
+                            const float dstart = s_depth[warp][p];
+                            const bool cand = less ? (z < dstart) : (z >= dstart);   // main.c:1164-1168
+                            if (cand) {
+                                const unsigned long long key = ((unsigned long long)depth_key(z) << 32) | rec;
+                                if (less) atomicMin(&s_best[warp][p], key);
+                                else atomicMax(&s_best[warp][p], key);
+                            }
+                        }
+                        E0 += a0 << kSubpix; E1 += a1 << kSubpix; E2 += a2 << kSubpix;
+                    }
+                }
+            }
+            if (bp.info_mask) bp.info_mask[i] = mask;
+        }
+        __syncwarp();
+        // fold this draw's winners into the running state; hierarchical Z update (write_tile, main.c:589-603)
+        const unsigned long long k0 = s_best[warp][lane], k1 = s_best[warp][lane + 32];
+        if (k0 != sentinel) { dcur0 = depth_from_key((uint32_t)(k0 >> 32)); win0 = (uint32_t)k0; }
+        if (k1 != sentinel) { dcur1 = depth_from_key((uint32_t)(k1 >> 32)); win1 = (uint32_t)k1; }
+        s_depth[warp][lane] = dcur0;
+        s_depth[warp][lane + 32] = dcur1;
+        float mn = 1.0f, mx = 0.0f;
+        if (valid0) { mn = fmin_ref(mn, dcur0); mx = fmax_ref(mx, dcur0); }
+        if (valid1) { mn = fmin_ref(mn, dcur1); mx = fmax_ref(mx, dcur1); }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            float a = __shfl_xor_sync(0xFFFFFFFFu, mn, o), b = __shfl_xor_sync(0xFFFFFFFFu, mx, o);
+            mn = fmin_ref(mn, a);
+            mx = fmax_ref(mx, b);
+        }
+        hiz_min = mn;
+        hiz_max = mx;
+        __syncwarp();
+    }
+    if (!touched) return;
+
+    // shade the final winners (one pixel-shader invocation per written pixel) and write back
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const uint32_t rec = h ? win1 : win0;
+        const bool valid = h ? valid1 : valid0;
+        if (rec == 0xFFFFFFFFu || !valid) continue;
+        const int32_t y = h ? py1 : py0;
+        const size_t o = h ? o1 : o0;
+        const int4 *R = bp.raster[rec].w;
+        const int4 w0 = R[0], w1 = R[1], w2 = R[2], w3 = R[3];
+        const float4 *S = bp.shade[rec].s;
+        const float4 s0 = S[0];
+        const uint32_t dr = __float_as_uint(s0.w);
+        const DrawDesc &D = bp.draws[dr];
+        const uint32_t E1 = (((uint32_t)w0.w * (uint32_t)px) << kSubpix) + (((uint32_t)w1.x * (uint32_t)y) << kSubpix) + (uint32_t)w1.y;
+        const uint32_t E2 = (((uint32_t)w1.z * (uint32_t)px) << kSubpix) + (((uint32_t)w1.w * (uint32_t)y) << kSubpix) + (uint32_t)w2.x;
+        const float inv_area = __int_as_float(w2.y);
+        const float b1 = (float)((int32_t)E1 >> (kSubpix * 2)) * inv_area;
+        const float b2 = (float)((int32_t)E2 >> (kSubpix * 2)) * inv_area;
+        const float z0 = __int_as_float(w2.w), z1 = __int_as_float(w3.x), z2 = __int_as_float(w3.y);
+        float z = z0 + (z1 - z0) * b1;
+        z = z + (z2 - z0) * b2;
+        // perspective correction, main.c:1106-1115
+        float den = (1.0f - (b1 + b2)) * s0.x;
+        den = den + b1 * s0.y;
+        den = den + b2 * s0.z;
+        den = 1.0f / den;
+        const float pb1 = (b1 * s0.y) * den;
+        const float pb2 = (b2 * s0.z) * den;
+        const float4 r0 = S[1], r1 = S[2], r2 = S[3], uv2 = S[4];
+        auto interp = [&](float v0, float v1, float v2) {
+            float tmp = v0 + (v1 - v0) * pb1;
+            return tmp + (v2 - v0) * pb2;
+        };
+        const float a0 = interp(r0.x, r1.x, r2.x), a1 = interp(r0.y, r1.y, r2.y), a2 = interp(r0.z, r1.z, r2.z);
+        const float u = interp(r0.w, r1.w, r2.w), v = interp(uv2.x, uv2.y, uv2.z);
+        const float3 c = run_ps(D.ps, a0, a1, a2, u, v, D.ps_tex);
+        V.color[o] = pack_color(c.x, c.y, c.z);
+        V.depth[o] = z;
+        if (V.vis_tri) V.vis_tri[o] = rec - bp.draw_record_begin[dr];
+        if (V.vis_draw) V.vis_draw[o] = D.draw_seq;
+        if (V.vis_bary) reinterpret_cast<float2 *>(V.vis_bary)[o] = make_float2(b1, b2);
+    }
+    if (lane == 0) {
+        V.tile_min[t] = hiz_min;
+        V.tile_max[t] = hiz_max;
+    }
+}
+
+// ------------------------------------------------------------------ clears
+
+__global__ void k_fill_u32(uint32_t *p, size_t n, uint32_t value, const uint32_t *error) {
+    if (error && ld_volatile_u32(error)) return;
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t n4 = n / 4;
+    const uint4 v4 = make_uint4(value, value, value, value);
+    if ((((uintptr_t)p) & 15) == 0) {
+        for (size_t k = i; k < n4; k += (size_t)gridDim.x * blockDim.x) reinterpret_cast<uint4 *>(p)[k] = v4;
+        for (size_t k = n4 * 4 + i; k < n; k += (size_t)gridDim.x * blockDim.x) p[k] = value;
+    } else {
+        for (size_t k = i; k < n; k += (size_t)gridDim.x * blockDim.x) p[k] = value;
+    }
+}
+
+// ------------------------------------------------------------------ host-side launchers
+
+void set_clip_planes(const float planes[6][4], cudaStream_t stream) {
+    cudaMemcpyToSymbolAsync(c_clip_planes, planes, sizeof(float) * 24, 0, cudaMemcpyHostToDevice, stream);
+}
+
+cudaError_t launch_fill_u32(uint32_t *p, size_t n, uint32_t value, const uint32_t *error, cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    int threads = 256;
+    size_t blocks = (n / 4 + threads - 1) / threads;
+    if (blocks < 1) blocks = 1;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    k_fill_u32<<<(unsigned)blocks, threads, 0, stream>>>(p, n, value, error);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_geometry(const BatchParams &bp, uint32_t block, cudaStream_t stream) {
+    if (bp.total_tris == 0) return cudaSuccess;
+    switch (block) {
+        case 128: k_geometry<128><<<(bp.total_tris + 127) / 128, 128, 0, stream>>>(bp); break;
+        case 512: k_geometry<512><<<(bp.total_tris + 511) / 512, 512, 0, stream>>>(bp); break;
+        default: k_geometry<256><<<(bp.total_tris + 255) / 256, 256, 0, stream>>>(bp); break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scan(const BatchParams &bp, cudaStream_t stream) {
+    const uint32_t per = kScanBlock * kScanItems;
+    const uint32_t blocks = (bp.total_bins + per - 1) / per;
+    k_scan<<<blocks ? blocks : 1, kScanBlock, 0, stream>>>(bp);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scatter(const BatchParams &bp, int num_sms, cudaStream_t stream) {
+    uint32_t blocks = (bp.total_tris + kScatterBlock - 1) / kScatterBlock;
+    uint32_t cap = (uint32_t)num_sms * 8;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    k_scatter<<<blocks, kScatterBlock, 0, stream>>>(bp);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tile(const BatchParams &bp, uint32_t warps, cudaStream_t stream) {
+    switch (warps) {
+        case 2: k_tile<2><<<(bp.total_tiles + 1) / 2, 64, 0, stream>>>(bp); break;
+        case 8: k_tile<8><<<(bp.total_tiles + 7) / 8, 256, 0, stream>>>(bp); break;
+        default: k_tile<4><<<(bp.total_tiles + 3) / 4, 128, 0, stream>>>(bp); break;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace mlv

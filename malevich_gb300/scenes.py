@@ -440,3 +440,55 @@ def small_scene(seed, width=64, height=64, vs=VS_BASIC, ps=PS_BASIC, n_objects=4
         draws.append(Draw(vs, ps, vb, ib, len(ib), cb=cb, vs_tex=vs_tex, ps_tex=ps_tex, viewport=vp,
                           depth_func=df))
     return Frame(width, height, draws, clear_color=REFERENCE_CLEAR_COLOR, clear_depth=cd)
+
+
+# ------------------------------------------------------------------ (de)serialisation
+
+def frame_to_arrays(frame, prefix="frame"):
+    """Flattens a Frame into a dict of numpy arrays (for .npz fixtures)."""
+    out = {prefix + "/size": np.array([frame.width, frame.height], np.int64),
+           prefix + "/ndraws": np.array([len(frame.draws)], np.int64)}
+    if frame.clear_color is not None:
+        out[prefix + "/clear_color"] = np.array(frame.clear_color, np.float32)
+    if frame.clear_depth is not None:
+        out[prefix + "/clear_depth"] = np.array([frame.clear_depth], np.float32)
+    for i, d in enumerate(frame.draws):
+        p = "%s/draw%d/" % (prefix, i)
+        out[p + "ints"] = np.array([d.vs, d.ps, d.index_count, d.cull, d.depth_func, d.start_index, d.base_vertex],
+                                   np.int64)
+        out[p + "vb"] = d.vb
+        if d.ib is not None:
+            out[p + "ib"] = d.ib
+        if d.cb is not None:
+            out[p + "cb"] = d.cb
+        out[p + "viewport"] = np.array(d.viewport, np.float32)
+        for name in ("vs_tex", "ps_tex"):
+            t = getattr(d, name)
+            if t is not None:
+                out[p + name] = t.data
+                out[p + name + "_fmt"] = np.array([t.format], np.int64)
+    return out
+
+
+def frame_from_arrays(z, prefix="frame"):
+    w, h = (int(v) for v in z[prefix + "/size"])
+    cc = tuple(float(v) for v in z[prefix + "/clear_color"]) if prefix + "/clear_color" in z else None
+    cd = float(z[prefix + "/clear_depth"][0]) if prefix + "/clear_depth" in z else None
+    fr = Frame(w, h, [], clear_color=cc, clear_depth=cd)
+    texcache = {}
+    for i in range(int(z[prefix + "/ndraws"][0])):
+        p = "%s/draw%d/" % (prefix, i)
+        vs, ps, n, cull, df, si, bv = (int(v) for v in z[p + "ints"])
+        texs = {}
+        for name in ("vs_tex", "ps_tex"):
+            if p + name in z:
+                data = z[p + name]
+                key = (data.shape, data.dtype.str, hash(data.tobytes()))
+                if key not in texcache:
+                    texcache[key] = Texture(data, int(z[p + name + "_fmt"][0]))
+                texs[name] = texcache[key]
+        fr.draws.append(Draw(vs, ps, z[p + "vb"], z[p + "ib"] if p + "ib" in z else None, n,
+                             cb=z[p + "cb"] if p + "cb" in z else None, vs_tex=texs.get("vs_tex"),
+                             ps_tex=texs.get("ps_tex"), viewport=tuple(float(v) for v in z[p + "viewport"]),
+                             cull=cull, depth_func=df, start_index=si, base_vertex=bv))
+    return fr

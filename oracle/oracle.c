@@ -389,16 +389,16 @@ static void push_tri(tri_buf *b, const tri_rec *r) {
 }
 
 /* primitive_assembly_stage body for one input triangle, main.c:753-907 */
-static void assemble(const orc_draw *d, const float vout[3][12], tri_buf *out) {
+static int assemble(const orc_draw *d, const float vout[3][12], tri_buf *out) {
     const float *p0 = vout[0], *p1 = vout[1], *p2 = vout[2];
-    if (p0[3] == 0 || p1[3] == 0 || p2[3] == 0) return;
+    if (p0[3] == 0 || p1[3] == 0 || p2[3] == 0) return 0;
     if ((p0[0] < -p0[3] && p1[0] < -p1[3] && p2[0] < -p2[3]) ||
         (p0[0] > +p0[3] && p1[0] > +p1[3] && p2[0] > +p2[3]) ||
         (p0[1] < -p0[3] && p1[1] < -p1[3] && p2[1] < -p2[3]) ||
         (p0[1] > +p0[3] && p1[1] > +p1[3] && p2[1] > +p2[3]) ||
         (p0[2] < 0.f && p1[2] < 0.f && p2[2] < 0.f) ||
         (p0[2] > +p0[3] && p1[2] > +p1[3] && p2[2] > +p2[3]))
-        return;
+        return 0;
     int clip = !((p0[0] >= -p0[3] && p1[0] >= -p1[3] && p2[0] >= -p2[3]) &&
                  (p0[0] <= +p0[3] && p1[0] <= +p1[3] && p2[0] <= +p2[3]) &&
                  (p0[1] >= -p0[3] && p1[1] >= -p1[3] && p2[1] >= -p2[3]) &&
@@ -460,6 +460,7 @@ static void assemble(const orc_draw *d, const float vout[3][12], tri_buf *out) {
         r.minx = minx; r.miny = miny; r.maxx = maxx; r.maxy = maxy;
         push_tri(out, &r);
     }
+    return clip;
 }
 
 static int vertex_fetch(const orc_draw *d, uint32_t idx_pos, float in[8]) {
@@ -504,7 +505,8 @@ int orc_draw_indexed(orc_target *t, const orc_draw *d, uint32_t draw_seq, orc_st
      * in the reference; chunk-local output keeps the serial (input triangle, fan) order */
     tri_buf *chunks = (tri_buf *)calloc(nchunks ? nchunks : 1, sizeof(tri_buf));
     int bad = 0;
-#pragma omp parallel for schedule(dynamic, 1) reduction(| : bad)
+    uint64_t nclipped = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(| : bad) reduction(+ : nclipped)
     for (uint32_t c = 0; c < nchunks; ++c) {
         uint32_t end = (c + 1) * CHUNK < ntri ? (c + 1) * CHUNK : ntri;
         for (uint32_t i = c * CHUNK; i < end; ++i) {
@@ -514,7 +516,7 @@ int orc_draw_indexed(orc_target *t, const orc_draw *d, uint32_t draw_seq, orc_st
                 orc_run_vs(d->vs, vin, d->cb, &d->vs_tex, vout[k]);
             }
             if (bad) break;
-            assemble(d, (const float(*)[12])vout, &chunks[c]);
+            nclipped += (uint64_t)assemble(d, (const float(*)[12])vout, &chunks[c]);
         }
     }
     if (bad) {
@@ -682,6 +684,7 @@ int orc_draw_indexed(orc_target *t, const orc_draw *d, uint32_t draw_seq, orc_st
         st->active_bin_count += active;
         st->total_triangle_count_in_bins += total;
         st->fragments_written += frags;
+        st->clipped_triangle_count += nclipped;
     }
     if (cap) {
         orc_capture_free(cap);

@@ -70,6 +70,7 @@ typedef struct orc_target {
 typedef struct orc_stats {
     uint64_t vertex_count, input_triangle_count, assembled_triangle_count;
     uint64_t active_bin_count, total_triangle_count_in_bins, fragments_written;
+    uint64_t clipped_triangle_count;  /* input triangles that went through the clipper */
 } orc_stats;
 
 /* Optional capture of one draw's intermediate results. Arrays are (re)allocated by the oracle

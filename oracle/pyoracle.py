@@ -46,7 +46,8 @@ class OrcTarget(ctypes.Structure):
 class OrcStats(ctypes.Structure):
     _fields_ = [("vertex_count", ctypes.c_uint64), ("input_triangle_count", ctypes.c_uint64),
                 ("assembled_triangle_count", ctypes.c_uint64), ("active_bin_count", ctypes.c_uint64),
-                ("total_triangle_count_in_bins", ctypes.c_uint64), ("fragments_written", ctypes.c_uint64)]
+                ("total_triangle_count_in_bins", ctypes.c_uint64), ("fragments_written", ctypes.c_uint64),
+                ("clipped_triangle_count", ctypes.c_uint64)]
 
 
 class OrcCapture(ctypes.Structure):
