@@ -1,0 +1,398 @@
+"""Benchmark of the Malevich draw path on GB300.
+
+Workload: the scene-scale frame (1920x1080 RGBA8 + D32, 12 draws, ~1.1M input triangles: a
+512x512-cell heightfield and 11 icospheres/boxes of 5k-60k triangles; vertex_lighting_vs +
+env_lighting_ps with a 2048x1024 RGBA16F radiance map and a 64x32 RGBA32F irradiance map), seeded
+synthetic data. One step renders the whole frame (clears + 12 draws) as one batched command list
+(a CUDA graph). The L2 cache is flushed between steps (a 256 MB write, outside the timed events).
+
+value     input triangles per second over the K timed steps (Mtri/s), inputs resident in HBM.
+e2e       the same frame through the C ABI from host buffers: every step uploads the vertex and
+          index buffers and both textures from pinned host memory and reads the colour target back.
+per_draw  the same frame drawn per draw on the immediate context (one launch sequence per draw).
+gpix_per_s fragments written (the oracle's count of covered, hierarchical-Z and depth-test passing
+          fragments in serial order) per second.
+roofline  the dominant kernel's algorithmic bytes per launch over its CUDA-event duration, against
+          the measured HBM copy bandwidth.
+cpu_baseline the oracle port of the reference's pipeline core on the host cores (all threads).
+
+--impl reference times the CPU implementation instead (the reference's own AVX2 core cannot build
+on an aarch64 host, so the oracle port stands in for it there) and prints its line.
+N > 1 (torchrun): every rank renders its own replica of the frame (replicas only: the path has no
+exchange step); value aggregates all ranks over the max-over-ranks time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Gpix/s & Mtri/s, batched vs per-draw on 1 GB300; fwd+bwd ms/view at FD tol"
+WORKLOAD = ("scene-scale frame 1920x1080 RGBA8+D32, 12 draws, ~1.1M input triangles (512x512-cell "
+            "heightfield + 11 icospheres/boxes of 5k-60k), vertex_lighting_vs + env_lighting_ps, "
+            "radiance 2048x1024 RGBA16F, irradiance 64x32 RGBA32F, reference depth mode")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--cpu-sample-frames", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary (profiles/), if present."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    v = d.get(kernel)
+    return None if v is None else float(v.get("bytes_per_launch", 0)) or None
+
+
+def cpu_baseline(frame, frames):
+    """The oracle port of the reference's pipeline core, all host threads, on `frames` frames."""
+    from oracle import pyoracle
+    lib = pyoracle.oracle_lib()
+    cores = os.cpu_count() or 1
+    lib.orc_set_threads(cores)
+    pyoracle.render_oracle(frame)   # warm-up (page-in, thread pool)
+    t0 = time.perf_counter()
+    out = None
+    for _ in range(frames):
+        out = pyoracle.render_oracle(frame)
+    dt = (time.perf_counter() - t0) / frames
+    return dt, cores, out["stats"]
+
+
+def algorithmic_bytes(frame, dev_stats, fragments):
+    """Algorithmic bytes of the two main kernels for one frame (measurement)."""
+    idx = sum(d.index_count for d in frame.draws) * 4
+    uniq = 0
+    for d in frame.draws:
+        uniq += len(np.unique(d.ib[:d.index_count])) if d.ib is not None else d.index_count
+    vtx = uniq * 32
+    assembled = dev_stats["assembled_triangle_count"]
+    entries = dev_stats["total_triangle_count_in_bins"]
+    geometry = idx + vtx + assembled * (64 + 80) + entries * 4
+    w, h = frame.width, frame.height
+    pixels = w * h
+    tex = 0
+    seen = set()
+    for d in frame.draws:
+        t = d.ps_tex
+        if t is not None and id(t.data) not in seen:
+            seen.add(id(t.data))
+            tex += t.data.nbytes
+    # tile kernel: every (tile, triangle) pair reads a list entry and a 64-byte raster record; the
+    # depth buffer is read once; colour and depth written once; one shading record (64 + 80 bytes)
+    # per written pixel; the radiance texture footprint counted once, capped at its size
+    tile = entries * (4 + 64) + pixels * 4 + pixels * 8 + min(fragments, pixels) * (64 + 80) + tex
+    return {"k_geometry": geometry, "k_tile": tile}
+
+
+def run_reference_arm(args, rank, world):
+    if rank != 0:
+        return 0
+    from malevich_gb300 import scenes
+    frame = scenes.config2_scene(seed=args.seed)
+    from oracle import pyoracle
+    lib = pyoracle.oracle_lib()
+    cores = os.cpu_count() or 1
+    lib.orc_set_threads(cores)
+    for _ in range(max(1, min(args.warmup, 1))):
+        pyoracle.render_oracle(frame)
+    times, stats = [], None
+    for _ in range(max(1, min(args.steps, 3))):
+        t0 = time.perf_counter()
+        stats = pyoracle.render_oracle(frame)["stats"]
+        times.append(time.perf_counter() - t0)
+    dt = statistics.median(times)
+    tris = frame.input_triangles
+    value = tris / dt / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Mtri/s", "n_gpus": world,
+        "steps": len(times), "warmup": 1, "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "input_triangles": tris, "resolution": [frame.width, frame.height],
+                   "draws": len(frame.draws)},
+        "gpix_per_s": round(stats["fragments_written"] / dt / 1e9, 6),
+        "cpu_baseline": {"value": round(value, 4), "unit": "Mtri/s", "cores": cores, "kind": "port",
+                         "sample": "%d full frames of the workload (median)" % len(times)},
+        "e2e": {"value": round(value, 4), "unit": "Mtri/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": ("the reference's own core is AVX2 C and does not build on this aarch64 host; the oracle "
+                 "port of it (oracle/oracle.c, OpenMP) runs instead"),
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_info()
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if args.impl == "gb300" else "gloo")
+    if args.impl == "reference":
+        rc = run_reference_arm(args, rank, world)
+        if dist:
+            dist.barrier()
+            dist.destroy_process_group()
+        return rc
+
+    import torch
+    from malevich_gb300 import api, build, scenes
+    build.build()
+    torch.cuda.set_device(local)
+    frame = scenes.config2_scene(seed=args.seed)
+    dev = api.Device(local)
+    ctx = dev.immediate
+    r = api.FrameRenderer(dev, frame)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.ExternalStream(ctx.stream())
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    # --- warm-up (first execution sizes the workspace and captures the graph)
+    for _ in range(max(args.warmup, 3)):
+        r.render_batched()
+    ctx.finish()
+    st0 = ctx.stats()
+
+    # --- timed: K batched frames, L2 flushed between them outside the events
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    wall0 = time.perf_counter()
+    for i in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(i)
+            evs[i][0].record(stream)
+        r.render_batched()
+        with torch.cuda.stream(stream):
+            evs[i][1].record(stream)
+    ctx.finish()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    barrier()
+    clk = clocks.stop()
+    st1 = ctx.stats()
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    ms = float(np.mean(step_ms))
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    launches = int(st1["kernel_launches"] - st0["kernel_launches"])
+    frame_stats = {k: (st1[k] - st0[k]) // args.steps for k in st1}
+    tris = frame.input_triangles
+    value = tris * world / (ms / 1e3) / 1e6
+
+    # --- per-draw (immediate context, one launch sequence per draw), same flushing
+    for _ in range(3):
+        r.render_per_draw()
+    ctx.finish()
+    pd = []
+    for i in range(args.steps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            flush.fill_(i)
+            a.record(stream)
+        r.render_per_draw()
+        with torch.cuda.stream(stream):
+            b.record(stream)
+        pd.append((a, b))
+    ctx.finish()
+    pd_ms = float(np.mean([a.elapsed_time(b) for a, b in pd]))
+
+    # --- per-kernel durations (stage events on the context stream), same frame, eager launches
+    ctx.set_profiling(True)
+    ctx.reset_stats()
+    for i in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(i)
+        ctx.finish()
+        r.render_batched()
+    stages = ctx.stage_times()
+    ctx.set_profiling(False)
+    stage_avg = {k: (v[0] / v[1] if v[1] else 0.0) for k, v in stages.items()}
+
+    # --- e2e through the C ABI from pinned host buffers
+    host_bufs = []
+    pinned = []
+
+    def pin(a):
+        t = torch.from_numpy(np.ascontiguousarray(a).view(np.uint8).reshape(-1)).pin_memory()
+        pinned.append(t)
+        return t.numpy()
+
+    for key, (buf, arr) in r._buffers.items():
+        if key[1] in (api.BIND_VERTEX_BUFFER, api.BIND_INDEX_BUFFER):
+            host_bufs.append((buf, pin(arr)))
+    host_tex = [(tex, pin(t.data)) for tex, t in r._textures.values()]
+    h2d = sum(a.nbytes for _, a in host_bufs) + sum(a.nbytes for _, a in host_tex)
+    rt = r.targets[0][0]
+    out_img = torch.empty((frame.height, frame.width), dtype=torch.int32).pin_memory().numpy().view(np.uint32)
+    d2h = out_img.nbytes
+    lib = api.load_library()
+    import ctypes
+
+    def e2e_step():
+        for buf, a in host_bufs:
+            ctx.lib.mlv_update_buffer(ctx.handle, buf.handle, 0, a.ctypes.data_as(ctypes.c_void_p), a.nbytes)
+        for tex, a in host_tex:
+            ctx.lib.mlv_update_texture2d(ctx.handle, tex.handle, a.ctypes.data_as(ctypes.c_void_p), 0)
+        r.render_batched()
+        ctx.lib.mlv_read_texture2d(ctx.handle, rt.handle, out_img.ctypes.data_as(ctypes.c_void_p), 0)
+
+    for _ in range(3):
+        e2e_step()
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+
+    result = None
+    if rank == 0:
+        # fragments written (Gpix/s numerator) and the CPU baseline come from the oracle
+        cpu = None
+        fragments = None
+        if not args.no_cpu_baseline:
+            dt, cores, ost = cpu_baseline(frame, args.cpu_sample_frames)
+            fragments = ost["fragments_written"]
+            cpu = {"value": round(tris / dt / 1e6, 4), "unit": "Mtri/s", "cores": cores, "kind": "port",
+                   "sample": "%d full frames of the workload" % args.cpu_sample_frames}
+        peak, peak_kind = measured_peaks()
+        ab = algorithmic_bytes(frame, frame_stats, fragments or frame.width * frame.height)
+        dominant = "k_tile" if stage_avg.get("tile", 0) >= stage_avg.get("geometry", 0) else "k_geometry"
+        dur_ms = stage_avg["tile" if dominant == "k_tile" else "geometry"]
+        achieved = ab[dominant] / (dur_ms / 1e3) / 1e9 if dur_ms else 0.0
+        result = {
+            "metric": METRIC, "value": round(value, 3), "unit": "Mtri/s", "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": round(ms, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "input_triangles": tris, "resolution": [frame.width, frame.height],
+                       "draws": len(frame.draws), "mode": "batched command list (CUDA graph)",
+                       "l2": "flushed between steps (256 MB write outside the timed events)",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "gpix_per_s": round(fragments / (ms / 1e3) / 1e9, 4) if fragments else None,
+            "per_draw": {"value": round(tris / (pd_ms / 1e3) / 1e6, 3), "unit": "Mtri/s", "ms_per_frame": round(pd_ms, 4),
+                         "batched_speedup": round(pd_ms / ms, 3)},
+            "e2e": {"value": round(tris * world / e2e_s / 1e6, 3), "unit": "Mtri/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_s * 1e3, 3)},
+            "roofline": {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 1), "peak": peak,
+                         "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                         "algorithmic_bytes": int(ab[dominant]), "duration_ms": round(dur_ms, 4),
+                         "traffic": ncu_traffic(dominant)},
+            "stage_ms": {k: round(v, 4) for k, v in stage_avg.items()},
+            "frame_stats": {k: int(v) for k, v in frame_stats.items()},
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "gpu_launches": launches,
+            "wall_s_timed": round(wall, 4),
+        }
+        print(json.dumps(result))
+    r.destroy()
+    dev.destroy()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -169,6 +169,11 @@ __device__ __forceinline__ bool setup_triangle(const DrawDesc &d, const Vtx &v0,
     mny = min(max(mny, 0), d.vp_h - 1);
     mxx = min(mxx + 1, d.vp_w - 1);
     mxy = min(mxy + 1, d.vp_h - 1);
+    // Every maximum <= -8 bins nowhere and covers no pixel (C division truncates -1..-7 to tile 0,
+    // main.c:928), so clamping it there changes nothing and keeps the bounds exact in the 16-bit
+    // fields of TriRaster, which the scatter kernel re-reads to find the same tiles.
+    mxx = max(mxx, -8);
+    mxy = max(mxy, -8);
     s.minx = mnx; s.miny = mny; s.maxx = mxx; s.maxy = mxy;
     return true;
 }

@@ -258,7 +258,7 @@ def heightfield(rng, cells, size, height, center=(0.0, 0.0, 0.0)):
     j, i = np.meshgrid(np.arange(cells), np.arange(cells), indexing="ij")
     a = (j * n + i).ravel()
     b, c, d = a + 1, a + n, a + n + 1
-    faces = np.stack([np.stack([a, d, b], 1), np.stack([a, c, d], 1)], 1).reshape(-1, 3)
+    faces = np.stack([np.stack([a, b, d], 1), np.stack([a, d, c], 1)], 1).reshape(-1, 3)
     return verts, faces.astype(np.int64)
 
 
