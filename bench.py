@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--cpu-sample-frames", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-once", action="store_true",
+                    help="render the frame once (batched, eager) and exit: a short launch sequence for ncu")
     return ap.parse_args()
 
 
@@ -231,6 +233,13 @@ def main():
     dev = api.Device(local)
     ctx = dev.immediate
     r = api.FrameRenderer(dev, frame)
+    if args.profile_once:
+        r.render_batched()
+        ctx.finish()
+        print(json.dumps({"profile_once": True, "stats": ctx.stats()}))
+        r.destroy()
+        dev.destroy()
+        return 0
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.int32, device="cuda")
     stream = torch.cuda.ExternalStream(ctx.stream())
 

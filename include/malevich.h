@@ -310,9 +310,10 @@ MLV_API mlv_status mlv_set_tuning(mlv_context context, const mlv_tuning *tuning)
 
 /* Per-stage device time (replaces the reference's Remotery CPU samples, main.c:663-1260).
  * When enabled, CUDA events bracket every stage on the context's stream; reading synchronises.
- * Stages: 0 clear, 1 geometry (IA+VS+PA+bin count), 2 bin scan, 3 bin scatter, 4 tile
- * (raster+PS+OM). Times in milliseconds, summed since the last reset. */
-#define MLV_STAGE_COUNT 5
+ * Stages: 0 clear, 1 geometry (IA + primitive assembly + bin count, and the vertex shader for
+ * draws shaded per index), 2 bin scan, 3 bin scatter, 4 tile (raster+PS+OM), 5 vertex shading
+ * (once per vertex). Times in milliseconds, summed since the last reset. */
+#define MLV_STAGE_COUNT 6
 MLV_API mlv_status mlv_set_profiling(mlv_context context, int enable);
 MLV_API mlv_status mlv_get_stage_times(mlv_context context, double *ms, uint64_t *launches);
 

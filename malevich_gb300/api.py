@@ -28,7 +28,7 @@ BIND_VERTEX_BUFFER, BIND_INDEX_BUFFER, BIND_CONSTANT_BUFFER, BIND_SHADER_RESOURC
 BIND_RENDER_TARGET, BIND_DEPTH_STENCIL, BIND_UNORDERED_ACCESS = 0x20, 0x40, 0x80
 CULL_NONE, CULL_FRONT, CULL_BACK = 1, 2, 3
 COMPARISON_LESS, COMPARISON_GREATER_EQUAL = 2, 7
-STAGES = ("clear", "geometry", "bin_scan", "bin_scatter", "tile")
+STAGES = ("clear", "geometry", "bin_scan", "bin_scatter", "tile", "vertex")
 
 # every function the header declares (tests check the library exports all of them)
 EXPORTS = [
@@ -327,10 +327,10 @@ class Context:
         _check(self.lib.mlv_set_profiling(self.handle, int(bool(enable))))
 
     def stage_times(self):
-        ms = (ctypes.c_double * 5)()
-        n = (ctypes.c_uint64 * 5)()
+        ms = (ctypes.c_double * len(STAGES))()
+        n = (ctypes.c_uint64 * len(STAGES))()
         _check(self.lib.mlv_get_stage_times(self.handle, ms, n))
-        return {STAGES[i]: (float(ms[i]), int(n[i])) for i in range(5)}
+        return {STAGES[i]: (float(ms[i]), int(n[i])) for i in range(len(STAGES))}
 
     def set_debug_capture(self, enable):
         _check(self.lib.mlv_set_debug_capture(self.handle, int(bool(enable))))

@@ -26,6 +26,7 @@
 namespace mlv {
 void set_clip_planes(const float planes[6][4], cudaStream_t stream);
 cudaError_t launch_fill_u32(uint32_t *p, size_t n, uint32_t value, const uint32_t *error, cudaStream_t stream);
+cudaError_t launch_vertex(const BatchParams &bp, cudaStream_t stream);
 cudaError_t launch_geometry(const BatchParams &bp, uint32_t block, cudaStream_t stream);
 cudaError_t launch_scan(const BatchParams &bp, cudaStream_t stream);
 cudaError_t launch_scatter(const BatchParams &bp, int num_sms, cudaStream_t stream);
@@ -160,6 +161,8 @@ struct Workspace {
     DrawDesc *d_draws = nullptr;
     ViewDesc *d_views = nullptr;
     uint32_t desc_draw_cap = 0, desc_view_cap = 0;
+    float4 *vs_out = nullptr;
+    uint32_t vs_cap = 0;
     uint64_t generation = 0;
 };
 
@@ -175,6 +178,7 @@ struct mlv_command_list_t {
     ViewDesc *d_views = nullptr;
     std::vector<size_t> draw_off, view_off;
     size_t draws_total = 0, views_total = 0;
+    uint64_t launches_per_execution = 0;
 };
 
 struct PendingJob {
@@ -288,7 +292,7 @@ static mlv_status ensure_fixed(mlv_context_t *c) {
 }
 
 struct BatchSizes {
-    uint64_t tris = 0, records = 0, bins = 0, tiles = 0, draws = 0, views = 0;
+    uint64_t tris = 0, records = 0, bins = 0, tiles = 0, draws = 0, views = 0, vertices = 0;
 };
 
 static mlv_status reset_scan_state(Workspace &w) {
@@ -359,6 +363,11 @@ static mlv_status ensure_workspace(mlv_context_t *c, const BatchSizes &s, bool k
         }
     }
     {
+        float4 *before = w.vs_out;
+        MLV_TRY(grow(&w.vs_out, w.vs_cap, s.vertices * 3, sizeof(float4)));
+        if (before != w.vs_out) changed = true;
+    }
+    {
         DrawDesc *b1 = w.d_draws;
         ViewDesc *b2 = w.d_views;
         MLV_TRY(grow(&w.d_draws, w.desc_draw_cap, s.draws));
@@ -392,7 +401,7 @@ static mlv_status plan_segment(const Segment &seg, Plan &p) {
         groups[g].second.push_back(i);
     }
     uint32_t tri = 0, tiles = 0;
-    uint64_t bins = 0, records = 0;
+    uint64_t bins = 0, records = 0, verts = 0;
     for (size_t g = 0; g < groups.size(); ++g) {
         const DrawCmd &first = seg.draws[groups[g].second[0]];
         ViewDesc v = {};
@@ -419,6 +428,13 @@ static mlv_status plan_segment(const Segment &seg, Plan &p) {
             d.draw_in_view = (uint32_t)k;
             d.tri_begin = tri;
             tri += d.tri_count;
+            // shade each vertex once when the draw references most of its buffer; a draw that
+            // touches a small part of a large buffer keeps per-index shading
+            d.vs_cached = (d.ib != nullptr && d.vertex_count > 0 && d.tri_count > 0 &&
+                           (uint64_t)d.vertex_count <= 2ull * 3ull * d.tri_count) ? 1u : 0u;
+            d.vs_base = (uint32_t)verts;
+            d.vs_count = d.vs_cached ? d.vertex_count : 0u;
+            verts += d.vs_count;
             records += (uint64_t)d.tri_count + std::max<uint64_t>(2ull * d.tri_count, 512);
             p.draws.push_back(d);
         }
@@ -426,8 +442,9 @@ static mlv_status plan_segment(const Segment &seg, Plan &p) {
         bins += (uint64_t)v.tiles_x * v.tiles_y * v.draw_count;
         p.views.push_back(v);
     }
-    if (bins > 0x7FFFFFFFull || tiles > 0x7FFFFFFFu)
-        return fail(MLV_ERROR_CAPACITY_EXCEEDED, "batch has too many bins");
+    if (bins > 0x7FFFFFFFull || tiles > 0x7FFFFFFFu || verts > 0x7FFFFFFFull / 3)
+        return fail(MLV_ERROR_CAPACITY_EXCEEDED, "batch has too many bins or vertices");
+    p.sizes.vertices = verts;
     p.sizes.tris = tri;
     p.sizes.records = records;
     p.sizes.bins = bins;
@@ -511,6 +528,8 @@ static mlv_status launch_draws(mlv_context_t *c, const Plan &p, DrawDesc *d_draw
     bp.big_capacity = 0;
     bp.big_tiles = c->tuning.big_triangle_tiles;
     bp.batch_seq = seq;
+    bp.total_vertices = (uint32_t)p.sizes.vertices;
+    bp.vs_out = w.vs_out;
     bp.raster = w.raster;
     bp.shade = w.shade;
     bp.geom = w.keep_geom ? w.geom : nullptr;
@@ -527,6 +546,12 @@ static mlv_status launch_draws(mlv_context_t *c, const Plan &p, DrawDesc *d_draw
     c->host_stats[3] += 1;
     if (bp.total_tris == 0) return MLV_OK;   // nothing to assemble: no kernel has work
     cudaEvent_t e;
+    if (bp.total_vertices) {
+        ev_begin(c, 5, &e);
+        CUDA_TRY(launch_vertex(bp, c->stream));
+        ev_end(c, e);
+        c->host_stats[4] += 1;
+    }
     ev_begin(c, 1, &e);
     CUDA_TRY(launch_geometry(bp, c->tuning.geometry_block, c->stream));
     ev_end(c, e);
@@ -703,7 +728,7 @@ static void free_workspace(Workspace &w) {
     cudaFree(w.raster); cudaFree(w.shade); cudaFree(w.geom); cudaFree(w.draw_record_begin);
     cudaFree(w.bin_count); cudaFree(w.bin_start); cudaFree(w.list); cudaFree(w.info_mask);
     cudaFree(w.scan_status); cudaFree(w.scan_status2); cudaFree(w.counters); cudaFree(w.stats);
-    cudaFree(w.error); cudaFree(w.d_draws); cudaFree(w.d_views);
+    cudaFree(w.error); cudaFree(w.d_draws); cudaFree(w.d_views); cudaFree(w.vs_out);
     w = Workspace();
 }
 
@@ -1240,6 +1265,7 @@ static mlv_status run_list(mlv_context_t *c, mlv_command_list l, uint32_t seq, b
         maxs.tiles = std::max(maxs.tiles, s.tiles);
         maxs.draws = std::max(maxs.draws, s.draws);
         maxs.views = std::max(maxs.views, s.views);
+        maxs.vertices = std::max(maxs.vertices, s.vertices);
         nd += plans[i].draws.size();
         nv += plans[i].views.size();
     }
@@ -1310,6 +1336,7 @@ MLV_API mlv_status mlv_execute_command_list(mlv_context c, mlv_command_list l) {
         mlv_status st = run_list(c, l, seq, false);
         c->capturing_graph = false;
         cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+        l->launches_per_execution = c->host_stats[4] - saved[4];
         memcpy(c->host_stats, saved, sizeof(saved));
         if (st != MLV_OK) {
             if (g) cudaGraphDestroy(g);
@@ -1328,8 +1355,8 @@ MLV_API mlv_status mlv_execute_command_list(mlv_context c, mlv_command_list l) {
         c->host_stats[1] += s.input_triangles;
         c->host_stats[2] += s.draws.size();
         c->host_stats[3] += s.draws.empty() ? 0 : 1;
-        c->host_stats[4] += s.clears.size() + (s.draws.empty() ? 0 : 4);
     }
+    c->host_stats[4] += l->launches_per_execution;
     c->pending.push_back({nullptr, nullptr, l, seq});
     if (c->pending.size() > 4096) MLV_TRY(sync_context(c));
     ++l->executions;

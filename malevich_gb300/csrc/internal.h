@@ -39,11 +39,11 @@ struct DrawDesc {
     uint32_t view;                       // view (render target + depth) index in the batch
     uint32_t draw_in_view;               // position among the view's draws in this batch
     uint32_t draw_seq;                   // draw number since the render target's last clear
-    uint32_t pad0;
+    uint32_t vs_cached;                  // 1: vertices were shaded once by k_vertex into vs_out
     float cb[48];                        // PerFrameCB snapshot
     float screen_from_ndc[16];           // main.c:825-830, computed on the host as the reference does
     int32_t vp_w, vp_h;                  // (i32)viewport.width/height
-    uint32_t pad1[2];
+    uint32_t vs_base, vs_count;          // this draw's range in vs_out (count 0 when not cached)
     TexDesc vs_tex, ps_tex;
 };
 
@@ -90,6 +90,8 @@ struct BatchParams {
     uint32_t record_capacity, list_capacity, big_capacity;
     uint32_t big_tiles;                  // triangles spanning more tiles go to the big list
     uint32_t batch_seq;
+    uint32_t total_vertices;             // sum of vs_count
+    float4 *vs_out;                      // 3 float4 per shaded vertex: SV_POSITION, reg1, (reg2.x, 0, 0, 0)
     TriRaster *raster;
     TriShade *shade;
     TriGeom *geom;                       // nullptr unless the geometry is kept

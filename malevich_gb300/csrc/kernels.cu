@@ -47,38 +47,54 @@ __device__ __forceinline__ uint32_t ld_volatile_u32(const uint32_t *p) {
 constexpr uint32_t kFlagAggregate = 1, kFlagInclusive = 2;
 constexpr uint32_t kSpinLimit = 1u << 22;   // bounded wait: about half a second with the backoff
 
-// Decoupled look-back (single thread). Publishes this block's aggregate, accumulates the
-// predecessors' values until an inclusive prefix is found, publishes the inclusive value and
-// returns the exclusive prefix. Every wait is bounded: on timeout the error bit is set and the
-// block still publishes, so that no successor waits on it.
-__device__ uint32_t lookback(unsigned long long *status, uint32_t bid, uint32_t epoch, uint32_t aggregate,
-                             uint32_t *error) {
-    const unsigned long long tag = (unsigned long long)(epoch & 0x3FFFFFFFu) << 34;
+// Decoupled look-back, run by one full warp. Publishes this block's aggregate, then inspects the
+// 32 closest predecessors at once: if every one up to the nearest inclusive prefix is ready, their
+// values are summed with one warp reduction; otherwise the window is re-read. Without an
+// inclusive prefix in the window, the 32 aggregates are added and the window moves back. Every
+// wait is bounded: on timeout the error bit is set and the block still publishes, so no successor
+// waits on it. Returns the exclusive prefix in every lane.
+__device__ uint32_t lookback_warp(unsigned long long *status, uint32_t bid, uint32_t epoch, uint32_t aggregate,
+                                  uint32_t *error) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t ep = epoch & 0x3FFFFFFFu;
+    const unsigned long long tag = (unsigned long long)ep << 34;
     if (bid == 0) {
-        st_release_u64(status, tag | ((unsigned long long)kFlagInclusive << 32) | aggregate);
+        if (lane == 0) st_release_u64(status, tag | ((unsigned long long)kFlagInclusive << 32) | aggregate);
         return 0;
     }
-    st_release_u64(status + bid, tag | ((unsigned long long)kFlagAggregate << 32) | aggregate);
+    if (lane == 0) st_release_u64(status + bid, tag | ((unsigned long long)kFlagAggregate << 32) | aggregate);
     uint32_t prefix = 0;
-    int32_t j = (int32_t)bid - 1;
+    int32_t top = (int32_t)bid - 1;
     uint32_t spins = 0;
-    while (j >= 0) {
-        unsigned long long s = ld_acquire_u64(status + j);
-        uint32_t hi = (uint32_t)(s >> 32);
-        uint32_t flag = hi & 3u;
-        if ((hi >> 2) != (epoch & 0x3FFFFFFFu) || flag == 0) {
+    while (true) {
+        const int32_t j = top - (int32_t)lane;
+        uint32_t flag = kFlagInclusive, val = 0;   // before block 0: an inclusive zero ends the walk
+        if (j >= 0) {
+            const unsigned long long sv = ld_acquire_u64(status + j);
+            const uint32_t hi = (uint32_t)(sv >> 32);
+            flag = ((hi >> 2) == ep) ? (hi & 3u) : 0u;
+            val = (uint32_t)sv;
+        }
+        const uint32_t incl = __ballot_sync(0xFFFFFFFFu, flag == kFlagInclusive);
+        const uint32_t waiting = __ballot_sync(0xFFFFFFFFu, flag == 0);
+        const int first = incl ? __ffs(incl) - 1 : 32;
+        const uint32_t need = first >= 31 ? 0xFFFFFFFFu : ((2u << first) - 1u);
+        if (waiting & need) {
             if (++spins > kSpinLimit) {
-                atomicOr(error, kErrLookbackTimeout);
+                if (lane == 0) atomicOr(error, kErrLookbackTimeout);
                 break;
             }
-            __nanosleep(64);
+            __nanosleep(32);
             continue;
         }
-        prefix += (uint32_t)s;
-        if (flag == kFlagInclusive) break;
-        --j;
+        uint32_t c = ((int)lane <= first) ? val : 0u;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xFFFFFFFFu, c, o);
+        prefix += c;
+        if (first < 32) break;
+        top -= 32;
     }
-    st_release_u64(status + bid, tag | ((unsigned long long)kFlagInclusive << 32) | (prefix + aggregate));
+    if (lane == 0) st_release_u64(status + bid, tag | ((unsigned long long)kFlagInclusive << 32) | (prefix + aggregate));
     return prefix;
 }
 
@@ -264,6 +280,63 @@ __device__ __forceinline__ void tile_range(const ViewDesc &v, int32_t minx, int3
     ty1 = min(maxy / kTile, (int32_t)v.tiles_y - 1);
 }
 
+// ------------------------------------------------------------------ unique-vertex shading
+
+// The reference shades one vertex per index (main.c:673, "no post-transform cache"). A vertex
+// shader is a pure function of its input, so shading every vertex of the buffer once gives
+// bit-identical outputs; k_geometry then gathers them by index.
+constexpr int kVertexBlock = 256;
+
+__device__ __forceinline__ uint32_t find_vertex_draw(const BatchParams &bp, uint32_t v) {
+    uint32_t lo = 0, hi = bp.num_draws;   // last draw with vs_base <= v
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&bp.draws[mid].vs_base) <= v) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(kVertexBlock) k_vertex(BatchParams bp) {
+    const uint32_t v = blockIdx.x * kVertexBlock + threadIdx.x;
+    if (v >= bp.total_vertices) return;
+    const DrawDesc &d = bp.draws[find_vertex_draw(bp, v)];
+    const uint32_t local = v - d.vs_base;
+    const uint8_t *p = d.vb + (size_t)local * d.vb_stride;
+    float in[8];
+    if ((((uintptr_t)p) & 15) == 0) {
+        float4 a = __ldg((const float4 *)p), b = __ldg((const float4 *)p + 1);
+        in[0] = a.x; in[1] = a.y; in[2] = a.z; in[3] = a.w; in[4] = b.x; in[5] = b.y; in[6] = b.z; in[7] = b.w;
+    } else {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) in[k] = __ldg((const float *)p + k);
+    }
+    float o[9];
+    run_vs(d.vs, in, d.cb, d.vs_tex, o);
+    float4 *out = bp.vs_out + 3 * (size_t)v;
+    out[0] = make_float4(o[0], o[1], o[2], o[3]);
+    out[1] = make_float4(o[4], o[5], o[6], o[7]);
+    out[2] = make_float4(o[8], 0.0f, 0.0f, 0.0f);
+}
+
+// Vertex k of a triangle: from the shaded-vertex buffer, or shaded here (per-index path, and for
+// out-of-range indices, which read zeros as in Direct3D 11).
+__device__ __forceinline__ void triangle_vertex(const BatchParams &bp, const DrawDesc &d, uint32_t idx_pos, float *o) {
+    if (d.vs_cached) {
+        int64_t idx = d.ib ? (int64_t)__ldg(d.ib + idx_pos) : (int64_t)idx_pos;
+        idx += d.base_vertex;
+        if (idx >= 0 && idx < (int64_t)d.vertex_count) {
+            const float4 *src = bp.vs_out + 3 * ((size_t)d.vs_base + (size_t)idx);
+            const float4 a = __ldg(src), b = __ldg(src + 1), c = __ldg(src + 2);
+            o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+            o[4] = b.x; o[5] = b.y; o[6] = b.z; o[7] = b.w; o[8] = c.x;
+            return;
+        }
+    }
+    float in[8];
+    fetch_vertex(d, idx_pos, in, bp.error + 2);
+    run_vs(d.vs, in, d.cb, d.vs_tex, o);
+}
+
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK) k_geometry(BatchParams bp) {
     __shared__ uint32_t s_bid, s_epoch, s_prefix, s_total;
@@ -290,11 +363,7 @@ __global__ void __launch_bounds__(BLOCK) k_geometry(BatchParams bp) {
         const DrawDesc &d = bp.draws[draw];
         const uint32_t local = tri - d.tri_begin;
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            float in[8];
-            fetch_vertex(d, d.start_index + 3 * local + k, in, bp.error + 2);
-            run_vs(d.vs, in, d.cb, d.vs_tex, v[k].v);
-        }
+        for (int k = 0; k < 3; ++k) triangle_vertex(bp, d, d.start_index + 3 * local + k, v[k].v);
         const float *p0 = v[0].v, *p1 = v[1].v, *p2 = v[2].v;
         // main.c:759-781
         bool reject = p0[3] == 0 || p1[3] == 0 || p2[3] == 0;
@@ -329,10 +398,12 @@ __global__ void __launch_bounds__(BLOCK) k_geometry(BatchParams bp) {
     // order-preserving compaction: block scan + decoupled look-back
     uint32_t total;
     uint32_t excl = block_exclusive_scan<BLOCK>((uint32_t)nout, s_warp, total);
-    if (threadIdx.x == 0) {
-        unsigned long long *status = bp.scan_status;
-        s_prefix = lookback(status, bid, s_epoch, total, bp.error);
-        s_total = total;
+    if (threadIdx.x < 32) {
+        const uint32_t p = lookback_warp(bp.scan_status, bid, s_epoch, total, bp.error);
+        if (threadIdx.x == 0) {
+            s_prefix = p;
+            s_total = total;
+        }
     }
     __syncthreads();
     const uint32_t base = s_prefix + excl;
@@ -453,7 +524,10 @@ __global__ void __launch_bounds__(kScanBlock) k_scan(BatchParams bp) {
     }
     uint32_t total;
     uint32_t excl = block_exclusive_scan<kScanBlock>(sum, s_warp, total);
-    if (threadIdx.x == 0) s_prefix = lookback(bp.scan_status2, bid, s_epoch, total, bp.error);
+    if (threadIdx.x < 32) {
+        const uint32_t p = lookback_warp(bp.scan_status2, bid, s_epoch, total, bp.error);
+        if (threadIdx.x == 0) s_prefix = p;
+    }
     __syncthreads();
     uint32_t run = s_prefix + excl;
 #pragma unroll
@@ -582,7 +656,10 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
     const uint32_t tx = t % V.tiles_x, ty = t / V.tiles_x;
     const uint32_t bin0 = V.bin_base + t * V.draw_count;
     const uint32_t dc = V.draw_count;
-    if (bp.bin_start[bin0] == bp.bin_start[bin0 + dc]) return;   // no draw binned a triangle here
+    // the bin boundaries of this tile's draws, one per lane (lane d holds bin_start[bin0 + d])
+    const uint32_t my_start = lane <= dc ? __ldg(bp.bin_start + bin0 + lane) : 0u;
+    const uint32_t last = dc < 32 ? __shfl_sync(0xFFFFFFFFu, my_start, dc) : __ldg(bp.bin_start + bin0 + dc);
+    if (__shfl_sync(0xFFFFFFFFu, my_start, 0) == last) return;   // no draw binned a triangle here
 
     const int32_t x0 = (int32_t)tx * kTile, y0 = (int32_t)ty * kTile;
     // lane owns pixels p0 = lane (rows 0-3) and p1 = lane + 32 (rows 4-7)
@@ -599,7 +676,14 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
     bool touched = false;
 
     for (uint32_t dd = 0; dd < dc; ++dd) {
-        const uint32_t s = bp.bin_start[bin0 + dd], e = bp.bin_start[bin0 + dd + 1];
+        uint32_t s, e;
+        if (dd + 1 < 32) {
+            s = __shfl_sync(0xFFFFFFFFu, my_start, dd);
+            e = __shfl_sync(0xFFFFFFFFu, my_start, dd + 1);
+        } else {
+            s = __ldg(bp.bin_start + bin0 + dd);
+            e = __ldg(bp.bin_start + bin0 + dd + 1);
+        }
         if (s == e) continue;
         touched = true;
         const DrawDesc &D = bp.draws[V.draw_begin + dd];
@@ -754,6 +838,12 @@ cudaError_t launch_fill_u32(uint32_t *p, size_t n, uint32_t value, const uint32_
     if (blocks < 1) blocks = 1;
     if (blocks > 152 * 16) blocks = 152 * 16;
     k_fill_u32<<<(unsigned)blocks, threads, 0, stream>>>(p, n, value, error);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_vertex(const BatchParams &bp, cudaStream_t stream) {
+    if (bp.total_vertices == 0) return cudaSuccess;
+    k_vertex<<<(bp.total_vertices + kVertexBlock - 1) / kVertexBlock, kVertexBlock, 0, stream>>>(bp);
     return cudaGetLastError();
 }
 
