@@ -29,6 +29,7 @@ cudaError_t launch_fill_u32(uint32_t *p, size_t n, uint32_t value, const uint32_
 cudaError_t launch_vertex(const BatchParams &bp, cudaStream_t stream);
 cudaError_t launch_geometry(const BatchParams &bp, uint32_t block, cudaStream_t stream);
 cudaError_t launch_scan(const BatchParams &bp, cudaStream_t stream);
+cudaError_t launch_rank(const BatchParams &bp, cudaStream_t stream);
 cudaError_t launch_scatter(const BatchParams &bp, int num_sms, cudaStream_t stream);
 cudaError_t launch_tile(const BatchParams &bp, uint32_t warps, cudaStream_t stream);
 }  // namespace mlv
@@ -144,10 +145,12 @@ struct Workspace {
     TriRaster *raster = nullptr;
     TriShade *shade = nullptr;
     TriGeom *geom = nullptr;
-    uint32_t record_cap = 0;
+    uint32_t record_cap = 0;          // slots: input triangles + clip-fan overflow
+    uint32_t overflow_cap = 0;        // overflow slots the last sizing reserved
     bool keep_geom = false;
-    uint32_t *draw_record_begin = nullptr;
-    uint32_t draw_cap = 0;
+    uint16_t *tri_info = nullptr;
+    uint32_t *rank = nullptr;
+    uint32_t tri_cap = 0;
     uint32_t *bin_count = nullptr, *bin_start = nullptr;
     uint32_t bin_cap = 0;
     uint32_t *list = nullptr;
@@ -211,7 +214,7 @@ struct mlv_context_t {
     // last single-draw segment, for mlv_get_tile_infos
     bool last_single = false;
     uint32_t last_total_bins = 0, last_tiles_x = 0, last_draw_count = 0;
-    uint32_t last_records = 0;
+    uint32_t last_tris = 0;
 };
 
 // ------------------------------------------------------------------ small helpers
@@ -269,7 +272,7 @@ static TexDesc tex_desc(mlv_texture2d t) {
 // ------------------------------------------------------------------ workspace
 
 // error words: [0] error bits, [1] first failing batch number (min), [2] warnings, [3] bin
-// entries a list overflow needed
+// entries a list overflow needed, [4] clip-fan slots a record overflow needed
 static mlv_status reset_error_words(Workspace &w) {
     const uint32_t init[8] = {0, 0xFFFFFFFFu, 0, 0, 0, 0, 0, 0};
     CUDA_TRY(cudaMemcpy(w.error, init, sizeof(init), cudaMemcpyHostToDevice));
@@ -292,7 +295,7 @@ static mlv_status ensure_fixed(mlv_context_t *c) {
 }
 
 struct BatchSizes {
-    uint64_t tris = 0, records = 0, bins = 0, tiles = 0, draws = 0, views = 0, vertices = 0;
+    uint64_t tris = 0, overflow = 0, bins = 0, tiles = 0, draws = 0, views = 0, vertices = 0;
 };
 
 static mlv_status reset_scan_state(Workspace &w) {
@@ -307,10 +310,11 @@ static mlv_status ensure_workspace(mlv_context_t *c, const BatchSizes &s, bool k
     Workspace &w = c->ws;
     MLV_TRY(ensure_fixed(c));
     bool changed = false;
-    if (s.records > w.record_cap || !w.raster || (keep_geom && !w.geom)) {
-        uint64_t n = std::max<uint64_t>(s.records, (uint64_t)w.record_cap + w.record_cap / 2);
+    const uint64_t slots = s.tris + std::max<uint64_t>(s.overflow, w.overflow_cap);
+    if (slots > w.record_cap || !w.raster || (keep_geom && !w.geom)) {
+        uint64_t n = std::max<uint64_t>(slots, (uint64_t)w.record_cap + w.record_cap / 2);
         n = std::max<uint64_t>(n, 4096);
-        if (n > 0x7FFFFFFFull) return fail(MLV_ERROR_CAPACITY_EXCEEDED, "more than 2^31 assembled triangles");
+        if (n > 0x7FFFFFFFull) return fail(MLV_ERROR_CAPACITY_EXCEEDED, "more than 2^31 triangle slots");
         cudaFree(w.raster); cudaFree(w.shade); cudaFree(w.geom);
         w.raster = nullptr; w.shade = nullptr; w.geom = nullptr;
         MLV_TRY(dev_alloc((void **)&w.raster, n * sizeof(TriRaster)));
@@ -320,10 +324,19 @@ static mlv_status ensure_workspace(mlv_context_t *c, const BatchSizes &s, bool k
         w.record_cap = (uint32_t)n;
         changed = true;
     }
+    w.overflow_cap = std::max<uint32_t>(w.overflow_cap, (uint32_t)std::min<uint64_t>(s.overflow, 0x7FFFFFFFull));
     {
-        uint32_t *before = w.draw_record_begin;
-        MLV_TRY(grow(&w.draw_record_begin, w.draw_cap, s.draws));
-        if (before != w.draw_record_begin) changed = true;
+        uint16_t *before = w.tri_info;
+        uint32_t cap = w.tri_cap;
+        MLV_TRY(grow(&w.tri_info, cap, s.tris + 1, sizeof(uint16_t)));
+        if (before != w.tri_info) {
+            cudaFree(w.rank);
+            w.rank = nullptr;
+            uint32_t cap2 = 0;
+            MLV_TRY(grow(&w.rank, cap2, cap, sizeof(uint32_t)));
+            changed = true;
+        }
+        w.tri_cap = cap;
     }
     {
         uint32_t *before = w.bin_count;
@@ -339,7 +352,7 @@ static mlv_status ensure_workspace(mlv_context_t *c, const BatchSizes &s, bool k
         w.bin_cap = cap;
     }
     {
-        uint64_t want = std::max<uint64_t>(s.records * 2, 1u << 16);
+        uint64_t want = std::max<uint64_t>(s.tris * 2, 1u << 16);
         uint32_t *before = w.list;
         if (want > w.list_cap || !w.list) {
             uint32_t cap = w.list_cap;
@@ -355,7 +368,7 @@ static mlv_status ensure_workspace(mlv_context_t *c, const BatchSizes &s, bool k
     }
     {
         unsigned long long *b1 = w.scan_status, *b2 = w.scan_status2;
-        MLV_TRY(grow(&w.scan_status, w.status_cap, s.tris / 128 + 2, sizeof(unsigned long long)));
+        MLV_TRY(grow(&w.scan_status, w.status_cap, s.tris / 2048 + 2, sizeof(unsigned long long)));
         MLV_TRY(grow(&w.scan_status2, w.status2_cap, s.bins / 2048 + 2, sizeof(unsigned long long)));
         if (b1 != w.scan_status || b2 != w.scan_status2) {
             MLV_TRY(reset_scan_state(w));
@@ -401,7 +414,7 @@ static mlv_status plan_segment(const Segment &seg, Plan &p) {
         groups[g].second.push_back(i);
     }
     uint32_t tri = 0, tiles = 0;
-    uint64_t bins = 0, records = 0, verts = 0;
+    uint64_t bins = 0, verts = 0;
     for (size_t g = 0; g < groups.size(); ++g) {
         const DrawCmd &first = seg.draws[groups[g].second[0]];
         ViewDesc v = {};
@@ -435,7 +448,6 @@ static mlv_status plan_segment(const Segment &seg, Plan &p) {
             d.vs_base = (uint32_t)verts;
             d.vs_count = d.vs_cached ? d.vertex_count : 0u;
             verts += d.vs_count;
-            records += (uint64_t)d.tri_count + std::max<uint64_t>(2ull * d.tri_count, 512);
             p.draws.push_back(d);
         }
         tiles += v.tiles_x * v.tiles_y;
@@ -446,7 +458,9 @@ static mlv_status plan_segment(const Segment &seg, Plan &p) {
         return fail(MLV_ERROR_CAPACITY_EXCEEDED, "batch has too many bins or vertices");
     p.sizes.vertices = verts;
     p.sizes.tris = tri;
-    p.sizes.records = records;
+    // clip fans beyond the slots of their input triangles; clipping is rare, and an overflow is
+    // detected, regrown and re-run
+    p.sizes.overflow = std::max<uint64_t>(4096, (uint64_t)tri / 8);
     p.sizes.bins = bins;
     p.sizes.tiles = tiles;
     p.sizes.draws = p.draws.size();
@@ -523,9 +537,8 @@ static mlv_status launch_draws(mlv_context_t *c, const Plan &p, DrawDesc *d_draw
     bp.total_tris = (uint32_t)p.sizes.tris;
     bp.total_tiles = (uint32_t)p.sizes.tiles;
     bp.total_bins = (uint32_t)p.sizes.bins;
-    bp.record_capacity = w.record_cap;
+    bp.overflow_capacity = w.record_cap - bp.total_tris;
     bp.list_capacity = w.list_cap;
-    bp.big_capacity = 0;
     bp.big_tiles = c->tuning.big_triangle_tiles;
     bp.batch_seq = seq;
     bp.total_vertices = (uint32_t)p.sizes.vertices;
@@ -533,7 +546,11 @@ static mlv_status launch_draws(mlv_context_t *c, const Plan &p, DrawDesc *d_draw
     bp.raster = w.raster;
     bp.shade = w.shade;
     bp.geom = w.keep_geom ? w.geom : nullptr;
-    bp.draw_record_begin = w.draw_record_begin;
+    bp.tri_info = w.tri_info;
+    bool want_rank = c->capture_infos;
+    for (const ViewDesc &v : p.views) want_rank = want_rank || v.vis_tri != nullptr;
+    bp.want_rank = want_rank ? 1u : 0u;
+    bp.rank = want_rank ? w.rank : nullptr;
     bp.bin_count = w.bin_count;
     bp.bin_start = w.bin_start;
     bp.list = w.list;
@@ -552,9 +569,15 @@ static mlv_status launch_draws(mlv_context_t *c, const Plan &p, DrawDesc *d_draw
         ev_end(c, e);
         c->host_stats[4] += 1;
     }
+    // the clip-fan slot counter starts at zero for every batch
+    CUDA_TRY(cudaMemsetAsync(w.counters + kCtrOverflow, 0, sizeof(uint32_t), c->stream));
     ev_begin(c, 1, &e);
     CUDA_TRY(launch_geometry(bp, c->tuning.geometry_block, c->stream));
     ev_end(c, e);
+    if (bp.want_rank) {
+        CUDA_TRY(launch_rank(bp, c->stream));
+        c->host_stats[4] += 1;
+    }
     ev_begin(c, 2, &e);
     CUDA_TRY(launch_scan(bp, c->stream));
     ev_end(c, e);
@@ -587,6 +610,7 @@ static mlv_status execute_segment_eager(mlv_context_t *c, const Segment &seg, ui
         c->last_total_bins = (uint32_t)p.sizes.bins;
         c->last_tiles_x = p.views[0].tiles_x;
         c->last_draw_count = 1;
+        c->last_tris = (uint32_t)p.sizes.tris;
     }
     return MLV_OK;
 }
@@ -620,12 +644,14 @@ static mlv_status check_and_recover(mlv_context_t *c) {
             return fail(MLV_ERROR_TIMEOUT, "a bounded device-side wait gave up (decoupled look-back)");
         }
         // regrow: records from the device's assembled count, list from the reported entry count
-        const uint32_t need_records = c->h_error[8 + kCtrGeomTotal];
         const uint32_t need_list = c->h_error[3];
+        const uint32_t need_fans = c->h_error[4];
         Workspace &w = c->ws;
-        if ((err & kErrRecordOverflow) && need_records >= w.record_cap) {
+        if (err & kErrRecordOverflow) {
+            // the clip-fan region must hold `need_fans` slots beyond the input triangles
             BatchSizes s;
-            s.records = (uint64_t)need_records + need_records / 4 + 1024;
+            s.overflow = (uint64_t)need_fans + need_fans / 2 + 4096;
+            s.tris = w.tri_cap ? w.tri_cap - 1 : 0;
             MLV_TRY(ensure_workspace(c, s, false));
         }
         if ((err & kErrListOverflow) && need_list > w.list_cap) {
@@ -725,7 +751,7 @@ MLV_API mlv_status mlv_create_device(int ordinal, mlv_device *out) {
 }
 
 static void free_workspace(Workspace &w) {
-    cudaFree(w.raster); cudaFree(w.shade); cudaFree(w.geom); cudaFree(w.draw_record_begin);
+    cudaFree(w.raster); cudaFree(w.shade); cudaFree(w.geom); cudaFree(w.tri_info); cudaFree(w.rank);
     cudaFree(w.bin_count); cudaFree(w.bin_start); cudaFree(w.list); cudaFree(w.info_mask);
     cudaFree(w.scan_status); cudaFree(w.scan_status2); cudaFree(w.counters); cudaFree(w.stats);
     cudaFree(w.error); cudaFree(w.d_draws); cudaFree(w.d_views); cudaFree(w.vs_out);
@@ -1260,7 +1286,7 @@ static mlv_status run_list(mlv_context_t *c, mlv_command_list l, uint32_t seq, b
         MLV_TRY(plan_segment(l->segments[i], plans[i]));
         const BatchSizes &s = plans[i].sizes;
         maxs.tris = std::max(maxs.tris, s.tris);
-        maxs.records = std::max(maxs.records, s.records);
+        maxs.overflow = std::max(maxs.overflow, s.overflow);
         maxs.bins = std::max(maxs.bins, s.bins);
         maxs.tiles = std::max(maxs.tiles, s.tiles);
         maxs.draws = std::max(maxs.draws, s.draws);
@@ -1457,16 +1483,28 @@ MLV_API mlv_status mlv_get_tile_infos(mlv_context c, uint32_t *tile_index, uint3
     if (capacity < total) return fail(MLV_ERROR_INVALID_ARG, "capacity too small");
     std::vector<uint32_t> list(total);
     std::vector<uint64_t> m(total);
-    uint32_t rb = 0;
+    const uint32_t nt = c->last_tris;
+    std::vector<uint16_t> info(nt + 1);
+    std::vector<uint32_t> rank(nt + 1);
     if (total) {
         CUDA_TRY(cudaMemcpy(list.data(), c->ws.list, sizeof(uint32_t) * total, cudaMemcpyDeviceToHost));
         CUDA_TRY(cudaMemcpy(m.data(), c->ws.info_mask, sizeof(uint64_t) * total, cudaMemcpyDeviceToHost));
     }
-    CUDA_TRY(cudaMemcpy(&rb, c->ws.draw_record_begin, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    if (nt) {
+        CUDA_TRY(cudaMemcpy(info.data(), c->ws.tri_info, sizeof(uint16_t) * nt, cudaMemcpyDeviceToHost));
+        CUDA_TRY(cudaMemcpy(rank.data(), c->ws.rank, sizeof(uint32_t) * nt, cudaMemcpyDeviceToHost));
+    }
+    // key (g << 3 | c) -> the reference's triangle id: assembled triangles before g, plus the
+    // emitted fans of g before fan c - 1
+    auto tri_of = [&](uint32_t key) {
+        const uint32_t g = key >> 3, cf = key & 7u;
+        const uint32_t fm = info[g] & 0xFFu;
+        return rank[g] + (cf ? (uint32_t)__builtin_popcount(fm & ((1u << (cf - 1)) - 1u)) : 0u);
+    };
     uint64_t k = 0;
     for (uint32_t b = 0; b < nb; ++b) {
         std::vector<std::pair<uint32_t, uint64_t>> e;
-        for (uint32_t i = start[b]; i < start[b + 1]; ++i) e.push_back({list[i] - rb, m[i]});
+        for (uint32_t i = start[b]; i < start[b + 1]; ++i) e.push_back({tri_of(list[i]), m[i]});
         std::sort(e.begin(), e.end());
         for (auto &pr : e) {
             tile_index[k] = b;

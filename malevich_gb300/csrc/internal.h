@@ -80,6 +80,12 @@ struct TriGeom {
     float x[3], y[3], z[3], w[3];
 };
 
+// Assembled triangles live in slots indexed by their input triangle g (draw-major across the
+// batch): an unclipped triangle's record is slot g; the clip-fan triangles of a clipped input
+// triangle live in an overflow region at slot total_tris + base + f (raw fan index f), with base
+// stored in slot g. The 32-bit key (g << 3) | c, c = 0 for an unclipped triangle and f + 1 for
+// fan f, orders triangles exactly as the reference's serial primitive assembly does
+// (input triangle, then fan; main.c:751,797), with no compaction pass.
 struct BatchParams {
     const DrawDesc *draws;
     const ViewDesc *views;
@@ -87,31 +93,34 @@ struct BatchParams {
     uint32_t total_tris;                 // input triangles in the batch
     uint32_t total_tiles;                // sum of views' tiles
     uint32_t total_bins;                 // sum of views' tiles * draws
-    uint32_t record_capacity, list_capacity, big_capacity;
-    uint32_t big_tiles;                  // triangles spanning more tiles go to the big list
+    uint32_t overflow_capacity;          // clip-fan slots after the total_tris primary slots
+    uint32_t list_capacity;
+    uint32_t big_tiles;                  // triangles spanning more tiles are binned by a whole block
     uint32_t batch_seq;
     uint32_t total_vertices;             // sum of vs_count
+    uint32_t want_rank;                  // 1: compute assembled-triangle ranks (visibility, capture)
     float4 *vs_out;                      // 3 float4 per shaded vertex: SV_POSITION, reg1, (reg2.x, 0, 0, 0)
-    TriRaster *raster;
+    TriRaster *raster;                   // [total_tris + overflow_capacity]
     TriShade *shade;
     TriGeom *geom;                       // nullptr unless the geometry is kept
-    uint32_t *draw_record_begin;         // first record of each draw
+    uint16_t *tri_info;                  // [total_tris]: emitted-fan mask | clipped << 8
+    uint32_t *rank;                      // [total_tris]: assembled triangles before g (exclusive)
     uint32_t *bin_count;                 // [total_bins], zero between batches
     uint32_t *bin_start;                 // [total_bins + 1]
-    uint32_t *list;                      // [list_capacity] record ids, grouped by bin
-    uint32_t *big_list;                  // [big_capacity]
+    uint32_t *list;                      // [list_capacity] triangle keys, grouped by bin
     uint64_t *info_mask;                 // optional TileInfo capture, parallel to list
-    unsigned long long *scan_status;     // decoupled look-back of k_geometry: (epoch:30|flag:2) << 32 | value
+    unsigned long long *scan_status;     // decoupled look-back of k_rank: (epoch:30|flag:2) << 32 | value
     unsigned long long *scan_status2;    // decoupled look-back of k_scan
     uint32_t *counters;                  // see Counter
     unsigned long long *stats;           // device statistics, see StatSlot
-    uint32_t *error;                     // [0] error bits, [1] first failing batch seq, [2..] need
+    uint32_t *error;                     // [0] error bits, [1] first failing batch, [2] warnings,
+                                         // [3] bin entries needed, [4] clip-fan slots needed
 };
 
 enum Counter : int {
-    kCtrGeomTicket = 0, kCtrGeomDone, kCtrGeomEpoch, kCtrGeomTotal,
+    kCtrRankTicket = 0, kCtrRankDone, kCtrRankEpoch, kCtrOverflow,
     kCtrScanTicket, kCtrScanDone, kCtrScanEpoch,
-    kCtrBigCount, kCtrCount = 16
+    kCtrCount = 16
 };
 
 enum StatSlot : int {

@@ -1,11 +1,16 @@
 // Draw-path kernels for sm_103a.
 //
-// One batch (any number of draws over any number of render targets) runs as four kernels:
-//   k_geometry  IA + VS + primitive assembly/clip/setup + per-(tile, draw) bin counts
-//               (source/main.c:662-913 and the counting half of the binner, 924-936). One thread
-//               per input triangle; assembled triangles are written in the reference's serial
-//               order (input triangle, fan index) by a single-pass decoupled look-back scan.
-//   k_scan      exclusive scan of the bin counts (main.c:937-946), same look-back scheme.
+// One batch (any number of draws over any number of render targets) runs as:
+//   k_vertex    the vertex shader, once per vertex of each draw's buffer (main.c:698-734 shades
+//               once per index; the shader is pure, so the outputs are identical).
+//   k_geometry  IA + primitive assembly/clip/setup + per-(tile, draw) bin counts
+//               (main.c:662-913 and the counting half of the binner, 924-936). One thread per input
+//               triangle; records go to slots indexed by input triangle (see BatchParams), so the
+//               reference's serial order is the slot order and no compaction is needed.
+//   k_rank      only when visibility or TileInfo outputs are requested: the reference's compact
+//               triangle index (its `out_triangle_index`, main.c:873-875), by an exclusive scan of
+//               the per-input-triangle output counts.
+//   k_scan      exclusive scan of the bin counts (main.c:937-946).
 //   k_scatter   bin lists (main.c:950-962); the order inside a bin does not matter (see k_tile).
 //   k_tile      one warp per 8x8 tile: hierarchical Z, coverage, depth, pixel shader, output
 //               merger, write-back (main.c:983-1189, 577-603), for every draw of the batch that
@@ -195,7 +200,7 @@ __device__ __forceinline__ bool setup_triangle(const DrawDesc &d, const Vtx &v0,
 }
 
 __device__ __forceinline__ void write_record(const BatchParams &bp, uint32_t rec, uint32_t draw, const Setup &s,
-                                             const Vtx &v0, const Vtx &v1, const Vtx &v2) {
+                                             const Vtx &v0, const Vtx &v1, const Vtx &v2, uint32_t extra = 0) {
     int4 *r = bp.raster[rec].w;
     r[0] = make_int4(s.e[0], s.e[1], s.e[2], s.e[3]);
     r[1] = make_int4(s.e[4], s.e[5], s.e[6], s.e[7]);
@@ -207,7 +212,7 @@ __device__ __forceinline__ void write_record(const BatchParams &bp, uint32_t rec
     h[1] = make_float4(v0.v[4], v0.v[5], v0.v[6], v0.v[7]);
     h[2] = make_float4(v1.v[4], v1.v[5], v1.v[6], v1.v[7]);
     h[3] = make_float4(v2.v[4], v2.v[5], v2.v[6], v2.v[7]);
-    h[4] = make_float4(v0.v[8], v1.v[8], v2.v[8], 0.0f);
+    h[4] = make_float4(v0.v[8], v1.v[8], v2.v[8], __uint_as_float(extra));
     if (bp.geom) {
         TriGeom &g = bp.geom[rec];
 #pragma unroll
@@ -337,31 +342,36 @@ __device__ __forceinline__ void triangle_vertex(const BatchParams &bp, const Dra
     run_vs(d.vs, in, d.cb, d.vs_tex, o);
 }
 
+// Slot of the record a triangle key names (see BatchParams).
+__device__ __forceinline__ uint32_t record_of(const BatchParams &bp, uint32_t key) {
+    const uint32_t g = key >> 3, c = key & 7u;
+    if (c == 0) return g;
+    return bp.total_tris + (uint32_t)__ldg(&bp.raster[g].w[0].x) + (c - 1);
+}
+
+__device__ __forceinline__ void count_tiles(const BatchParams &bp, const DrawDesc &d, const ViewDesc &vw,
+                                            int32_t tx0, int32_t ty0, int32_t tx1, int32_t ty1) {
+    for (int32_t ty = ty0; ty <= ty1; ++ty)
+        for (int32_t tx = tx0; tx <= tx1; ++tx) {
+            uint32_t bin = vw.bin_base + ((uint32_t)ty * vw.tiles_x + (uint32_t)tx) * vw.draw_count + d.draw_in_view;
+            atomicAdd(bp.bin_count + bin, 1u);
+        }
+}
+
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK) k_geometry(BatchParams bp) {
-    __shared__ uint32_t s_bid, s_epoch, s_prefix, s_total;
-    __shared__ uint32_t s_warp[BLOCK / 32];
     __shared__ uint32_t s_nbig;
     __shared__ uint32_t s_big[BLOCK];
-    if (threadIdx.x == 0) {
-        s_bid = atomicAdd(bp.counters + kCtrGeomTicket, 1u);
-        s_epoch = ld_volatile_u32(bp.counters + kCtrGeomEpoch);
-        s_nbig = 0;
-    }
+    if (threadIdx.x == 0) s_nbig = 0;
     __syncthreads();
-    const uint32_t bid = s_bid;
-    const uint32_t tri = bid * BLOCK + threadIdx.x;
-    const bool active = tri < bp.total_tris;
-
-    uint32_t draw = 0;
-    Vtx v[3];
-    Setup su;
-    int nout = 0;
-    bool clipped = false;
-    if (active) {
-        draw = find_draw(bp, tri);
+    const uint32_t g = blockIdx.x * BLOCK + threadIdx.x;
+    uint32_t mask = 0;
+    if (g < bp.total_tris) {
+        const uint32_t draw = find_draw(bp, g);
         const DrawDesc &d = bp.draws[draw];
-        const uint32_t local = tri - d.tri_begin;
+        const ViewDesc &vw = bp.views[d.view];
+        const uint32_t local = g - d.tri_begin;
+        Vtx v[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) triangle_vertex(bp, d, d.start_index + 3 * local + k, v[k].v);
         const float *p0 = v[0].v, *p1 = v[1].v, *p2 = v[2].v;
@@ -373,6 +383,22 @@ __global__ void __launch_bounds__(BLOCK) k_geometry(BatchParams bp) {
                  (p0[1] > +p0[3] && p1[1] > +p1[3] && p2[1] > +p2[3]) ||
                  (p0[2] < 0.f && p1[2] < 0.f && p2[2] < 0.f) ||
                  (p0[2] > +p0[3] && p1[2] > +p1[3] && p2[2] > +p2[3]);
+        bool clipped = false;
+        auto bin_record = [&](uint32_t slot, const Setup &su) {
+            int32_t tx0, ty0, tx1, ty1;
+            tile_range(vw, su.minx, su.miny, su.maxx, su.maxy, tx0, ty0, tx1, ty1);
+            int32_t ntiles = (tx1 >= tx0 && ty1 >= ty0) ? (tx1 - tx0 + 1) * (ty1 - ty0 + 1) : 0;
+            if (ntiles > (int32_t)bp.big_tiles) {
+                // counted cooperatively by the whole block below; if the block's list is full (only
+                // possible with many clip fans) this thread counts the tiles itself
+                uint32_t slot_i = atomicAdd(&s_nbig, 1u);
+                if (slot_i < (uint32_t)BLOCK) {
+                    s_big[slot_i] = slot;
+                    return;
+                }
+            }
+            count_tiles(bp, d, vw, tx0, ty0, tx1, ty1);
+        };
         if (!reject) {
             clipped = !((p0[0] >= -p0[3] && p1[0] >= -p1[3] && p2[0] >= -p2[3]) &&
                         (p0[0] <= +p0[3] && p1[0] <= +p1[3] && p2[0] <= +p2[3]) &&
@@ -381,84 +407,46 @@ __global__ void __launch_bounds__(BLOCK) k_geometry(BatchParams bp) {
                         (p0[2] >= 0.f && p1[2] >= 0.f && p2[2] >= 0.f) &&
                         (p0[2] <= +p0[3] && p1[2] <= +p1[3] && p2[2] <= +p2[3]));
             if (!clipped) {
-                nout = setup_triangle(d, v[0], v[1], v[2], su) ? 1 : 0;
+                Setup su;
+                if (setup_triangle(d, v[0], v[1], v[2], su)) {
+                    write_record(bp, g, draw, su, v[0], v[1], v[2]);
+                    mask = 1;
+                    bin_record(g, su);
+                }
             } else {
                 Vtx poly[kMaxClipVertices], tmp[kMaxClipVertices];
                 poly[0] = v[0]; poly[1] = v[1]; poly[2] = v[2];
                 int count = 3;
                 for (int p = 0; p < 6; ++p) clip_by_plane(poly, tmp, count, c_clip_planes[p]);
-                for (int f = 1; f < count - 1; ++f) {
-                    Setup s2;
-                    if (setup_triangle(d, poly[0], poly[f], poly[f + 1], s2)) ++nout;
+                const int nf = count - 2;
+                if (nf > 0) {
+                    const uint32_t base = atomicAdd(bp.counters + kCtrOverflow, (uint32_t)nf);
+                    if (base + (uint32_t)nf > bp.overflow_capacity) {
+                        atomicOr(bp.error, kErrRecordOverflow);
+                        atomicMin(bp.error + 1, bp.batch_seq);
+                        atomicMax(bp.error + 4, base + (uint32_t)nf);
+                    } else {
+                        bp.raster[g].w[0].x = (int)base;   // slot g holds the fans' base
+                        for (int f = 0; f < nf && f < 7; ++f) {
+                            Setup su;
+                            if (setup_triangle(d, poly[0], poly[f + 1], poly[f + 2], su)) {
+                                const uint32_t slot = bp.total_tris + base + (uint32_t)f;
+                                write_record(bp, slot, draw, su, poly[0], poly[f + 1], poly[f + 2]);
+                                mask |= 1u << f;
+                                bin_record(slot, su);
+                            }
+                        }
+                    }
                 }
             }
         }
+        bp.tri_info[g] = (uint16_t)(mask | (clipped ? 0x100u : 0u));
     }
-
-    // order-preserving compaction: block scan + decoupled look-back
-    uint32_t total;
-    uint32_t excl = block_exclusive_scan<BLOCK>((uint32_t)nout, s_warp, total);
-    if (threadIdx.x < 32) {
-        const uint32_t p = lookback_warp(bp.scan_status, bid, s_epoch, total, bp.error);
-        if (threadIdx.x == 0) {
-            s_prefix = p;
-            s_total = total;
-        }
-    }
-    __syncthreads();
-    const uint32_t base = s_prefix + excl;
-
-    if (active) {
-        const DrawDesc &d = bp.draws[draw];
-        if (tri == d.tri_begin) bp.draw_record_begin[draw] = base;
-    }
-
-    if (nout > 0) {
-        const DrawDesc &d = bp.draws[draw];
-        const ViewDesc &vw = bp.views[d.view];
-        const uint32_t bin_stride = vw.draw_count;
-        auto emit = [&](uint32_t rec, const Setup &s, const Vtx &a, const Vtx &b, const Vtx &c) {
-            if (rec >= bp.record_capacity) {
-                atomicOr(bp.error, kErrRecordOverflow);
-                atomicMin(bp.error + 1, bp.batch_seq);
-                return;
-            }
-            write_record(bp, rec, draw, s, a, b, c);
-            int32_t tx0, ty0, tx1, ty1;
-            tile_range(vw, s.minx, s.miny, s.maxx, s.maxy, tx0, ty0, tx1, ty1);
-            int32_t ntiles = (tx1 >= tx0 && ty1 >= ty0) ? (tx1 - tx0 + 1) * (ty1 - ty0 + 1) : 0;
-            if (ntiles > (int32_t)bp.big_tiles) {
-                // counted cooperatively by the block below; if the block's list is full (only
-                // possible with many clip-generated fans) this thread counts it itself
-                uint32_t slot = atomicAdd(&s_nbig, 1u);
-                if (slot < (uint32_t)BLOCK) {
-                    s_big[slot] = rec;
-                    return;
-                }
-            }
-            for (int32_t ty = ty0; ty <= ty1; ++ty)
-                for (int32_t tx = tx0; tx <= tx1; ++tx) {
-                    uint32_t bin = vw.bin_base + ((uint32_t)ty * vw.tiles_x + (uint32_t)tx) * bin_stride + d.draw_in_view;
-                    atomicAdd(bp.bin_count + bin, 1u);
-                }
-        };
-        if (!clipped) {
-            emit(base, su, v[0], v[1], v[2]);
-        } else {
-            Vtx poly[kMaxClipVertices], tmp[kMaxClipVertices];
-            poly[0] = v[0]; poly[1] = v[1]; poly[2] = v[2];
-            int count = 3;
-            for (int p = 0; p < 6; ++p) clip_by_plane(poly, tmp, count, c_clip_planes[p]);
-            uint32_t k = 0;
-            for (int f = 1; f < count - 1; ++f) {
-                Setup s2;
-                if (setup_triangle(d, poly[0], poly[f], poly[f + 1], s2)) {
-                    emit(base + k, s2, poly[0], poly[f], poly[f + 1]);
-                    ++k;
-                }
-            }
-        }
-    }
+    // assembled-triangle statistic (main.c:1238)
+    uint32_t n = __popc(mask);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xFFFFFFFFu, n, o);
+    if ((threadIdx.x & 31) == 0 && n) atomicAdd(bp.stats + kStatAssembled, (unsigned long long)n);
     __syncthreads();
 
     // triangles spanning many tiles: the whole block counts their tiles
@@ -472,26 +460,61 @@ __global__ void __launch_bounds__(BLOCK) k_geometry(BatchParams bp) {
         int32_t minx = (int16_t)(w3.z & 0xFFFF), miny = w3.z >> 16, maxx = (int16_t)(w3.w & 0xFFFF), maxy = w3.w >> 16;
         int32_t tx0, ty0, tx1, ty1;
         tile_range(vw, minx, miny, maxx, maxy, tx0, ty0, tx1, ty1);
-        const int32_t nx = tx1 - tx0 + 1, n = nx * (ty1 - ty0 + 1);
-        for (int32_t i = threadIdx.x; i < n; i += BLOCK) {
+        const int32_t nx = tx1 - tx0 + 1, nt = nx * (ty1 - ty0 + 1);
+        for (int32_t i = threadIdx.x; i < nt; i += BLOCK) {
             uint32_t tx = tx0 + i % nx, ty = ty0 + i / nx;
             uint32_t bin = vw.bin_base + (ty * vw.tiles_x + tx) * vw.draw_count + d.draw_in_view;
             atomicAdd(bp.bin_count + bin, 1u);
         }
     }
+}
 
-    // the last block resets the ticket and advances the epoch (graph-replay safe)
+// ------------------------------------------------------------------ assembled-triangle ranks
+
+constexpr int kRankBlock = 256, kRankItems = 8;
+
+// rank[g] = number of triangles input triangles 0..g-1 of the batch assembled (exclusive scan of
+// the popcount of tri_info's fan masks), same decoupled look-back as k_scan.
+__global__ void __launch_bounds__(kRankBlock) k_rank(BatchParams bp) {
+    __shared__ uint32_t s_bid, s_epoch, s_prefix;
+    __shared__ uint32_t s_warp[kRankBlock / 32];
     if (threadIdx.x == 0) {
-        if (bid == gridDim.x - 1) {
-            bp.counters[kCtrGeomTotal] = s_prefix + s_total;
-            atomicAdd(bp.stats + kStatAssembled, (unsigned long long)(s_prefix + s_total));
-        }
+        s_bid = atomicAdd(bp.counters + kCtrRankTicket, 1u);
+        s_epoch = ld_volatile_u32(bp.counters + kCtrRankEpoch);
+    }
+    __syncthreads();
+    const uint32_t bid = s_bid;
+    const uint32_t n = bp.total_tris;
+    const uint32_t base = bid * kRankBlock * kRankItems + threadIdx.x * kRankItems;
+    uint32_t vals[kRankItems];
+    uint32_t sum = 0;
+#pragma unroll
+    for (int i = 0; i < kRankItems; ++i) {
+        uint32_t idx = base + i;
+        vals[i] = idx < n ? (uint32_t)__popc(bp.tri_info[idx] & 0xFFu) : 0u;
+        sum += vals[i];
+    }
+    uint32_t total;
+    uint32_t excl = block_exclusive_scan<kRankBlock>(sum, s_warp, total);
+    if (threadIdx.x < 32) {
+        const uint32_t p = lookback_warp(bp.scan_status, bid, s_epoch, total, bp.error);
+        if (threadIdx.x == 0) s_prefix = p;
+    }
+    __syncthreads();
+    uint32_t run = s_prefix + excl;
+#pragma unroll
+    for (int i = 0; i < kRankItems; ++i) {
+        uint32_t idx = base + i;
+        if (idx < n) bp.rank[idx] = run;
+        run += vals[i];
+    }
+    if (threadIdx.x == 0) {
         __threadfence();
-        uint32_t done = atomicAdd(bp.counters + kCtrGeomDone, 1u);
+        uint32_t done = atomicAdd(bp.counters + kCtrRankDone, 1u);
         if (done == gridDim.x - 1) {
-            bp.counters[kCtrGeomTicket] = 0;
-            bp.counters[kCtrGeomDone] = 0;
-            bp.counters[kCtrGeomEpoch] = s_epoch + 1;
+            bp.counters[kCtrRankTicket] = 0;
+            bp.counters[kCtrRankDone] = 0;
+            bp.counters[kCtrRankEpoch] = s_epoch + 1;
             __threadfence();
         }
     }
@@ -560,9 +583,41 @@ __global__ void __launch_bounds__(kScanBlock) k_scan(BatchParams bp) {
 
 constexpr int kScatterBlock = 256;
 
+__device__ __forceinline__ void scatter_tiles(const BatchParams &bp, uint32_t key, uint32_t rec, int32_t first,
+                                              int32_t stride) {
+    const int4 w3 = __ldg(&bp.raster[rec].w[3]);
+    const uint32_t dr = __float_as_uint(__ldg(&bp.shade[rec].s[0].w));
+    const DrawDesc &d = bp.draws[dr];
+    const ViewDesc &vw = bp.views[d.view];
+    int32_t minx = (int16_t)(w3.z & 0xFFFF), miny = w3.z >> 16, maxx = (int16_t)(w3.w & 0xFFFF), maxy = w3.w >> 16;
+    int32_t tx0, ty0, tx1, ty1;
+    tile_range(vw, minx, miny, maxx, maxy, tx0, ty0, tx1, ty1);
+    const int32_t nx = tx1 - tx0 + 1;
+    const int32_t nt = (tx1 >= tx0 && ty1 >= ty0) ? nx * (ty1 - ty0 + 1) : 0;
+    for (int32_t i = first; i < nt; i += stride) {
+        uint32_t tx = tx0 + i % nx, ty = ty0 + i / nx;
+        uint32_t bin = vw.bin_base + (ty * vw.tiles_x + tx) * vw.draw_count + d.draw_in_view;
+        uint32_t pos = atomicSub(bp.bin_count + bin, 1u) - 1u;
+        bp.list[bp.bin_start[bin] + pos] = key;
+    }
+}
+
+__device__ __forceinline__ int32_t tile_count_of(const BatchParams &bp, uint32_t rec) {
+    const int4 w3 = __ldg(&bp.raster[rec].w[3]);
+    const uint32_t dr = __float_as_uint(__ldg(&bp.shade[rec].s[0].w));
+    const ViewDesc &vw = bp.views[bp.draws[dr].view];
+    int32_t minx = (int16_t)(w3.z & 0xFFFF), miny = w3.z >> 16, maxx = (int16_t)(w3.w & 0xFFFF), maxy = w3.w >> 16;
+    int32_t tx0, ty0, tx1, ty1;
+    tile_range(vw, minx, miny, maxx, maxy, tx0, ty0, tx1, ty1);
+    return (tx1 >= tx0 && ty1 >= ty0) ? (tx1 - tx0 + 1) * (ty1 - ty0 + 1) : 0;
+}
+
+// One thread per input triangle: every assembled triangle it produced goes to the lists of the
+// tiles its bounds cover (main.c:950-962). Triangles over more than big_tiles tiles are
+// scattered by the whole block, as k_geometry counted them.
 __global__ void __launch_bounds__(kScatterBlock) k_scatter(BatchParams bp) {
     __shared__ uint32_t s_nbig;
-    __shared__ uint32_t s_big[kScatterBlock];
+    __shared__ uint32_t s_big[kScatterBlock * 2];
     if (ld_volatile_u32(bp.error)) return;
     const uint32_t total = bp.bin_start[bp.total_bins];
     if (total > bp.list_capacity) {
@@ -573,48 +628,35 @@ __global__ void __launch_bounds__(kScatterBlock) k_scatter(BatchParams bp) {
         }
         return;
     }
-    const uint32_t nrec = min(bp.counters[kCtrGeomTotal], bp.record_capacity);
-    for (uint32_t base = blockIdx.x * kScatterBlock; base < nrec; base += gridDim.x * kScatterBlock) {
+    for (uint32_t base = blockIdx.x * kScatterBlock; base < bp.total_tris; base += gridDim.x * kScatterBlock) {
         if (threadIdx.x == 0) s_nbig = 0;
         __syncthreads();
-        const uint32_t rec = base + threadIdx.x;
-        if (rec < nrec) {
-            const int4 w3 = bp.raster[rec].w[3];
-            const uint32_t dr = __float_as_uint(bp.shade[rec].s[0].w);
-            const DrawDesc &d = bp.draws[dr];
-            const ViewDesc &vw = bp.views[d.view];
-            int32_t minx = (int16_t)(w3.z & 0xFFFF), miny = w3.z >> 16, maxx = (int16_t)(w3.w & 0xFFFF), maxy = w3.w >> 16;
-            int32_t tx0, ty0, tx1, ty1;
-            tile_range(vw, minx, miny, maxx, maxy, tx0, ty0, tx1, ty1);
-            int32_t ntiles = (tx1 >= tx0 && ty1 >= ty0) ? (tx1 - tx0 + 1) * (ty1 - ty0 + 1) : 0;
-            if (ntiles > (int32_t)bp.big_tiles) {
-                s_big[atomicAdd(&s_nbig, 1u)] = rec;
-            } else {
-                for (int32_t ty = ty0; ty <= ty1; ++ty)
-                    for (int32_t tx = tx0; tx <= tx1; ++tx) {
-                        uint32_t bin = vw.bin_base + ((uint32_t)ty * vw.tiles_x + (uint32_t)tx) * vw.draw_count + d.draw_in_view;
-                        uint32_t pos = atomicSub(bp.bin_count + bin, 1u) - 1u;
-                        bp.list[bp.bin_start[bin] + pos] = rec;
+        const uint32_t g = base + threadIdx.x;
+        if (g < bp.total_tris) {
+            const uint32_t info = bp.tri_info[g];
+            uint32_t m = info & 0xFFu;
+            const bool clipped = (info & 0x100u) != 0;
+            const uint32_t fan_base = (clipped && m) ? (uint32_t)__ldg(&bp.raster[g].w[0].x) : 0u;
+            while (m) {
+                const uint32_t f = __ffs(m) - 1;
+                m &= m - 1;
+                const uint32_t key = (g << 3) | (clipped ? f + 1 : 0u);
+                const uint32_t rec = clipped ? bp.total_tris + fan_base + f : g;
+                if (tile_count_of(bp, rec) > (int32_t)bp.big_tiles) {
+                    uint32_t slot = atomicAdd(&s_nbig, 1u);
+                    if (slot < 2u * kScatterBlock) {
+                        s_big[slot] = key;   // scattered by the whole block below
+                        continue;
                     }
+                }
+                scatter_tiles(bp, key, rec, 0, 1);
             }
         }
         __syncthreads();
-        for (uint32_t b = 0; b < s_nbig; ++b) {
-            const uint32_t r = s_big[b];
-            const int4 w3 = bp.raster[r].w[3];
-            const uint32_t dr = __float_as_uint(bp.shade[r].s[0].w);
-            const DrawDesc &d = bp.draws[dr];
-            const ViewDesc &vw = bp.views[d.view];
-            int32_t minx = (int16_t)(w3.z & 0xFFFF), miny = w3.z >> 16, maxx = (int16_t)(w3.w & 0xFFFF), maxy = w3.w >> 16;
-            int32_t tx0, ty0, tx1, ty1;
-            tile_range(vw, minx, miny, maxx, maxy, tx0, ty0, tx1, ty1);
-            const int32_t nx = tx1 - tx0 + 1, n = nx * (ty1 - ty0 + 1);
-            for (int32_t i = threadIdx.x; i < n; i += kScatterBlock) {
-                uint32_t tx = tx0 + i % nx, ty = ty0 + i / nx;
-                uint32_t bin = vw.bin_base + (ty * vw.tiles_x + tx) * vw.draw_count + d.draw_in_view;
-                uint32_t pos = atomicSub(bp.bin_count + bin, 1u) - 1u;
-                bp.list[bp.bin_start[bin] + pos] = r;
-            }
+        const uint32_t nbig = min(s_nbig, 2u * kScatterBlock);
+        for (uint32_t b = 0; b < nbig; ++b) {
+            const uint32_t key = s_big[b];
+            scatter_tiles(bp, key, record_of(bp, key), threadIdx.x, kScatterBlock);
         }
         __syncthreads();
     }
@@ -642,10 +684,42 @@ __device__ __forceinline__ uint32_t find_view(const BatchParams &bp, uint32_t ti
     return lo;
 }
 
+// Position of the k-th (0-based) set bit of m, k < popc(m).
+__device__ __forceinline__ uint32_t nth_set_bit(uint32_t m, uint32_t k) {
+    uint32_t pos = 0;
+#pragma unroll
+    for (uint32_t step = 16; step; step >>= 1) {
+        const uint32_t c = __popc(m & ((1u << step) - 1u));
+        if (k >= c) {
+            k -= c;
+            m >>= step;
+            pos += step;
+        }
+    }
+    return pos;
+}
+
+// Per-triangle parameters staged in shared memory for the work-expansion loop (17 words per
+// triangle, an odd stride, so lanes reading different triangles hit different banks).
+constexpr int kStage = 17;
+enum : int {
+    kSE0 = 0, kSE1, kSE2,          // edge values at the clipped bounding box's first pixel
+    kSA0, kSA1, kSA2,              // x steps (a << 4)
+    kSB0, kSB1, kSB2,              // y steps (b << 4)
+    kSInvArea, kSZ0, kSDz1, kSDz2, // barycentric scale and depth plane
+    kSOrigin,                      // box origin in the tile: x | y << 8
+    kSWidth,                       // box width | reciprocal << 8 (row = local * recip >> 16)
+    kSKey,                         // triangle key
+    kSPad
+};
+
 template <int WARPS>
 __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
     __shared__ unsigned long long s_best[WARPS][64];
     __shared__ float s_depth[WARPS][64];
+    __shared__ uint32_t s_stage[WARPS][32 * kStage];
+    __shared__ uint32_t s_pref[WARPS][32];
+    __shared__ unsigned long long s_mask[WARPS][32];
     if (ld_volatile_u32(bp.error)) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t gtile = blockIdx.x * WARPS + warp;
@@ -673,7 +747,9 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
     s_depth[warp][lane] = dcur0;
     s_depth[warp][lane + 32] = dcur1;
     float hiz_min = V.tile_min[t], hiz_max = V.tile_max[t];
-    bool touched = false;
+    uint32_t *stage = s_stage[warp];
+    uint32_t *pref = s_pref[warp];
+    const bool capture = bp.info_mask != nullptr;
 
     for (uint32_t dd = 0; dd < dc; ++dd) {
         uint32_t s, e;
@@ -685,61 +761,96 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
             e = __ldg(bp.bin_start + bin0 + dd + 1);
         }
         if (s == e) continue;
-        touched = true;
         const DrawDesc &D = bp.draws[V.draw_begin + dd];
         const bool less = D.depth_less != 0;
         const unsigned long long sentinel = less ? ~0ull : 0ull;
         s_best[warp][lane] = sentinel;
         s_best[warp][lane + 32] = sentinel;
-        __syncwarp();
         const float hiz = less ? hiz_max : hiz_min;
-        for (uint32_t i = s + lane; i < e; i += 32) {
-            const uint32_t rec = bp.list[i];
-            const int4 *R = bp.raster[rec].w;
-            const int4 w2 = R[2], w3 = R[3];
-            const float zb = __int_as_float(w2.z);
-            uint64_t mask = 0;
-            const bool rejected = less ? (zb > hiz) : (zb < hiz);   // main.c:1005-1010 (mirrored for LESS)
-            if (!rejected) {
-                const int4 w0 = R[0], w1 = R[1];
-                const uint32_t a0 = w0.x, b0 = w0.y, c0 = w0.z, a1 = w0.w, b1 = w1.x, c1 = w1.y, a2 = w1.z, b2 = w1.w,
-                               c2 = w2.x;
-                const float inv_area = __int_as_float(w2.y), z0 = __int_as_float(w2.w), z1 = __int_as_float(w3.x),
-                            z2 = __int_as_float(w3.y);
-                const float dz1 = z1 - z0, dz2 = z2 - z0;
+        for (uint32_t chunk = s; chunk < e; chunk += 32) {
+            const uint32_t i = chunk + lane;
+            uint32_t cnt = 0;
+            if (i < e) {
+                const uint32_t key = bp.list[i];
+                const uint32_t rec = record_of(bp, key);
+                const int4 *R = bp.raster[rec].w;
+                const int4 w2 = R[2], w3 = R[3];
+                const float zb = __int_as_float(w2.z);
+                const bool rejected = less ? (zb > hiz) : (zb < hiz);   // main.c:1005-1010 (mirrored for LESS)
                 int32_t bx0 = (int16_t)(w3.z & 0xFFFF), by0 = w3.z >> 16;
                 int32_t bx1 = (int16_t)(w3.w & 0xFFFF), by1 = w3.w >> 16;
                 bx0 = max(bx0, x0); by0 = max(by0, y0);
                 bx1 = min(bx1, x0 + kTile - 1); by1 = min(by1, y0 + kTile - 1);
-                for (int32_t y = by0; y <= by1; ++y) {
+                if (!rejected && bx1 >= bx0 && by1 >= by0) {
+                    const int4 w0 = R[0], w1 = R[1];
+                    const uint32_t a0 = w0.x, b0 = w0.y, c0 = w0.z, a1 = w0.w, b1 = w1.x, c1 = w1.y, a2 = w1.z,
+                                   b2 = w1.w, c2 = w2.x;
+                    const uint32_t w = (uint32_t)(bx1 - bx0 + 1), h = (uint32_t)(by1 - by0 + 1);
+                    cnt = w * h;
+                    uint32_t *st = stage + lane * kStage;
                     // main.c:1015-1025: ((a*x)<<4) + ((b*y)<<4) + c, wrapping int32
-                    uint32_t E0 = ((a0 * (uint32_t)bx0) << kSubpix) + ((b0 * (uint32_t)y) << kSubpix) + c0;
-                    uint32_t E1 = ((a1 * (uint32_t)bx0) << kSubpix) + ((b1 * (uint32_t)y) << kSubpix) + c1;
-                    uint32_t E2 = ((a2 * (uint32_t)bx0) << kSubpix) + ((b2 * (uint32_t)y) << kSubpix) + c2;
-                    for (int32_t x = bx0; x <= bx1; ++x) {
-                        if ((int32_t)(E0 | E1 | E2) > 0) {   // main.c:1028
-                            const int p = (y - y0) * 8 + (x - x0);
-                            mask |= 1ull << p;
-                            // main.c:1092-1102 and 1131-1132 for reg0.z
-                            const float bb1 = (float)((int32_t)E1 >> (kSubpix * 2)) * inv_area;
-                            const float bb2 = (float)((int32_t)E2 >> (kSubpix * 2)) * inv_area;
-                            float z = z0 + dz1 * bb1;
-                            z = z + dz2 * bb2;
-                            const float dstart = s_depth[warp][p];
-                            const bool cand = less ? (z < dstart) : (z >= dstart);   // main.c:1164-1168
-                            if (cand) {
-                                const unsigned long long key = ((unsigned long long)depth_key(z) << 32) | rec;
-                                if (less) atomicMin(&s_best[warp][p], key);
-                                else atomicMax(&s_best[warp][p], key);
-                            }
-                        }
-                        E0 += a0 << kSubpix; E1 += a1 << kSubpix; E2 += a2 << kSubpix;
+                    st[kSE0] = ((a0 * (uint32_t)bx0) << kSubpix) + ((b0 * (uint32_t)by0) << kSubpix) + c0;
+                    st[kSE1] = ((a1 * (uint32_t)bx0) << kSubpix) + ((b1 * (uint32_t)by0) << kSubpix) + c1;
+                    st[kSE2] = ((a2 * (uint32_t)bx0) << kSubpix) + ((b2 * (uint32_t)by0) << kSubpix) + c2;
+                    st[kSA0] = a0 << kSubpix; st[kSA1] = a1 << kSubpix; st[kSA2] = a2 << kSubpix;
+                    st[kSB0] = b0 << kSubpix; st[kSB1] = b1 << kSubpix; st[kSB2] = b2 << kSubpix;
+                    const float z0 = __int_as_float(w2.w);
+                    st[kSInvArea] = (uint32_t)w2.y;
+                    st[kSZ0] = (uint32_t)w2.w;
+                    st[kSDz1] = __float_as_uint(__int_as_float(w3.x) - z0);
+                    st[kSDz2] = __float_as_uint(__int_as_float(w3.y) - z0);
+                    st[kSOrigin] = (uint32_t)(bx0 - x0) | ((uint32_t)(by0 - y0) << 8);
+                    st[kSWidth] = w | (((65536u + w - 1) / w) << 8);
+                    st[kSKey] = key;
+                }
+            }
+            if (capture) s_mask[warp][lane] = 0;
+            // exclusive offsets of the (triangle, pixel) work items
+            uint32_t incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            pref[lane] = incl;
+            const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+            __syncwarp();
+            for (uint32_t item = lane; item < total; item += 32) {
+                uint32_t j = 0;   // triangle of this item: number of prefixes <= item
+#pragma unroll
+                for (uint32_t step = 16; step; step >>= 1)
+                    if (pref[j + step - 1] <= item) j += step;
+                const uint32_t *st = stage + j * kStage;
+                const uint32_t local = item - (j ? pref[j - 1] : 0u);
+                const uint32_t wr = st[kSWidth];
+                const uint32_t row = (local * (wr >> 8)) >> 16;
+                const uint32_t col = local - row * (wr & 0xFFu);
+                const uint32_t E0 = st[kSE0] + col * st[kSA0] + row * st[kSB0];
+                const uint32_t E1 = st[kSE1] + col * st[kSA1] + row * st[kSB1];
+                const uint32_t E2 = st[kSE2] + col * st[kSA2] + row * st[kSB2];
+                if ((int32_t)(E0 | E1 | E2) > 0) {   // main.c:1028
+                    const uint32_t org = st[kSOrigin];
+                    const int p = (int)(((org >> 8) + row) * 8 + (org & 0xFFu) + col);
+                    if (capture) atomicOr(&s_mask[warp][j], 1ull << p);
+                    // main.c:1092-1102 and 1131-1132 for reg0.z
+                    const float inv_area = __uint_as_float(st[kSInvArea]);
+                    const float bb1 = (float)((int32_t)E1 >> (kSubpix * 2)) * inv_area;
+                    const float bb2 = (float)((int32_t)E2 >> (kSubpix * 2)) * inv_area;
+                    float z = __uint_as_float(st[kSZ0]) + __uint_as_float(st[kSDz1]) * bb1;
+                    z = z + __uint_as_float(st[kSDz2]) * bb2;
+                    const float dstart = s_depth[warp][p];
+                    const bool cand = less ? (z < dstart) : (z >= dstart);   // main.c:1164-1168
+                    if (cand) {
+                        const unsigned long long k = ((unsigned long long)depth_key(z) << 32) | st[kSKey];
+                        if (less) atomicMin(&s_best[warp][p], k);
+                        else atomicMax(&s_best[warp][p], k);
                     }
                 }
             }
-            if (bp.info_mask) bp.info_mask[i] = mask;
+            __syncwarp();
+            if (capture && i < e) bp.info_mask[i] = cnt ? s_mask[warp][lane] : 0ull;
+            __syncwarp();
         }
-        __syncwarp();
         // fold this draw's winners into the running state; hierarchical Z update (write_tile, main.c:589-603)
         const unsigned long long k0 = s_best[warp][lane], k1 = s_best[warp][lane + 32];
         if (k0 != sentinel) { dcur0 = depth_from_key((uint32_t)(k0 >> 32)); win0 = (uint32_t)k0; }
@@ -759,24 +870,31 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
         hiz_max = mx;
         __syncwarp();
     }
-    if (!touched) return;
 
-    // shade the final winners (one pixel-shader invocation per written pixel) and write back
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        const uint32_t rec = h ? win1 : win0;
-        const bool valid = h ? valid1 : valid0;
-        if (rec == 0xFFFFFFFFu || !valid) continue;
-        const int32_t y = h ? py1 : py0;
-        const size_t o = h ? o1 : o0;
+    // shade the final winners, one pixel-shader invocation per written pixel, compacted over the
+    // warp so that a partly covered tile needs one pass
+    const uint32_t m0 = __ballot_sync(0xFFFFFFFFu, win0 != 0xFFFFFFFFu && valid0);
+    const uint32_t m1 = __ballot_sync(0xFFFFFFFFu, win1 != 0xFFFFFFFFu && valid1);
+    const uint32_t n0 = __popc(m0), n = n0 + __popc(m1);
+    for (uint32_t q0 = 0; q0 < n; q0 += 32) {
+        const uint32_t q = q0 + lane;
+        const uint32_t half = q < n0 ? 0u : 1u;
+        uint32_t src = 0;
+        if (q < n) src = nth_set_bit(half ? m1 : m0, half ? q - n0 : q);
+        const uint32_t wa = __shfl_sync(0xFFFFFFFFu, win0, src), wb = __shfl_sync(0xFFFFFFFFu, win1, src);
+        if (q >= n) continue;
+        const uint32_t key = half ? wb : wa;
+        const int32_t x = x0 + (int32_t)(src & 7), y = y0 + (int32_t)(src >> 3) + (half ? 4 : 0);
+        const size_t o = (size_t)y * V.width + x;
+        const uint32_t rec = record_of(bp, key);
         const int4 *R = bp.raster[rec].w;
         const int4 w0 = R[0], w1 = R[1], w2 = R[2], w3 = R[3];
         const float4 *S = bp.shade[rec].s;
         const float4 s0 = S[0];
         const uint32_t dr = __float_as_uint(s0.w);
         const DrawDesc &D = bp.draws[dr];
-        const uint32_t E1 = (((uint32_t)w0.w * (uint32_t)px) << kSubpix) + (((uint32_t)w1.x * (uint32_t)y) << kSubpix) + (uint32_t)w1.y;
-        const uint32_t E2 = (((uint32_t)w1.z * (uint32_t)px) << kSubpix) + (((uint32_t)w1.w * (uint32_t)y) << kSubpix) + (uint32_t)w2.x;
+        const uint32_t E1 = (((uint32_t)w0.w * (uint32_t)x) << kSubpix) + (((uint32_t)w1.x * (uint32_t)y) << kSubpix) + (uint32_t)w1.y;
+        const uint32_t E2 = (((uint32_t)w1.z * (uint32_t)x) << kSubpix) + (((uint32_t)w1.w * (uint32_t)y) << kSubpix) + (uint32_t)w2.x;
         const float inv_area = __int_as_float(w2.y);
         const float b1 = (float)((int32_t)E1 >> (kSubpix * 2)) * inv_area;
         const float b2 = (float)((int32_t)E2 >> (kSubpix * 2)) * inv_area;
@@ -800,7 +918,13 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
         const float3 c = run_ps(D.ps, a0, a1, a2, u, v, D.ps_tex);
         V.color[o] = pack_color(c.x, c.y, c.z);
         V.depth[o] = z;
-        if (V.vis_tri) V.vis_tri[o] = rec - bp.draw_record_begin[dr];
+        if (V.vis_tri && bp.rank) {
+            // the reference's triangle id: its index among the draw's assembled triangles
+            const uint32_t g = key >> 3, cf = key & 7u;
+            const uint32_t fmask = bp.tri_info[g] & 0xFFu;
+            const uint32_t below = cf ? (uint32_t)__popc(fmask & ((1u << (cf - 1)) - 1u)) : 0u;
+            V.vis_tri[o] = bp.rank[g] - bp.rank[D.tri_begin] + below;
+        }
         if (V.vis_draw) V.vis_draw[o] = D.draw_seq;
         if (V.vis_bary) reinterpret_cast<float2 *>(V.vis_bary)[o] = make_float2(b1, b2);
     }
@@ -854,6 +978,13 @@ cudaError_t launch_geometry(const BatchParams &bp, uint32_t block, cudaStream_t 
         case 512: k_geometry<512><<<(bp.total_tris + 511) / 512, 512, 0, stream>>>(bp); break;
         default: k_geometry<256><<<(bp.total_tris + 255) / 256, 256, 0, stream>>>(bp); break;
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rank(const BatchParams &bp, cudaStream_t stream) {
+    const uint32_t per = kRankBlock * kRankItems;
+    const uint32_t blocks = (bp.total_tris + per - 1) / per;
+    k_rank<<<blocks ? blocks : 1, kRankBlock, 0, stream>>>(bp);
     return cudaGetLastError();
 }
 
