@@ -299,10 +299,15 @@ MLV_API mlv_status mlv_reset_stats(mlv_context context);
 /* Launch-shape knobs of the tile kernel, picked by the autotuner (malevich_gb300/autotune.py).
  * The hierarchical-Z tile stays 8x8 pixels: it is observable (main.c:1005-1010). */
 typedef struct mlv_tuning {
-    uint32_t tile_warps_per_block;    /* warps per CTA of the tile kernel, 1..16 */
-    uint32_t lanes_per_triangle;      /* lanes that share one triangle's pixels: 1, 2, 4, 8, 16 or 32 */
+    uint32_t tile_warps_per_block;    /* warps per CTA of the tile kernel: 2, 4 or 8 */
+    uint32_t lanes_per_triangle;      /* reserved, must be 1 (the tile kernel balances pixels itself) */
     uint32_t big_triangle_tiles;      /* triangles spanning more tiles are binned cooperatively */
     uint32_t geometry_block;          /* threads per CTA of the geometry kernel: 128, 256 or 512 */
+    /* First sizes of the two buffers only the device can size (0 = automatic). When a batch needs
+     * more, its render-target writes are skipped on the device and the next synchronisation
+     * regrows the buffer and re-runs the batch, so these only trade memory for a re-run. */
+    uint32_t initial_bin_entries;
+    uint32_t initial_clip_fan_slots;
 } mlv_tuning;
 
 MLV_API mlv_status mlv_get_tuning(mlv_context context, mlv_tuning *out_tuning);

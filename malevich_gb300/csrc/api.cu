@@ -198,7 +198,7 @@ struct mlv_context_t {
     PipelineState st;
     std::vector<Segment> recorded;     // deferred contexts
     Workspace ws;
-    mlv_tuning tuning = {4, 1, 16, 256};
+    mlv_tuning tuning = {4, 1, 16, 256, 0, 0};
     uint64_t host_stats[8] = {};       // vertex_count, input triangles, draws, batches, launches
     bool profiling = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pool;
@@ -352,7 +352,8 @@ static mlv_status ensure_workspace(mlv_context_t *c, const BatchSizes &s, bool k
         w.bin_cap = cap;
     }
     {
-        uint64_t want = std::max<uint64_t>(s.tris * 2, 1u << 16);
+        uint64_t want = c->tuning.initial_bin_entries ? c->tuning.initial_bin_entries
+                                                      : std::max<uint64_t>(s.tris * 3, 1u << 20);
         uint32_t *before = w.list;
         if (want > w.list_cap || !w.list) {
             uint32_t cap = w.list_cap;
@@ -399,7 +400,7 @@ struct Plan {
     BatchSizes sizes;
 };
 
-static mlv_status plan_segment(const Segment &seg, Plan &p) {
+static mlv_status plan_segment(const Segment &seg, Plan &p, uint32_t fan_slots_hint = 0) {
     p.draws.clear();
     p.views.clear();
     p.sizes = BatchSizes();
@@ -461,6 +462,7 @@ static mlv_status plan_segment(const Segment &seg, Plan &p) {
     // clip fans beyond the slots of their input triangles; clipping is rare, and an overflow is
     // detected, regrown and re-run
     p.sizes.overflow = std::max<uint64_t>(4096, (uint64_t)tri / 8);
+    if (fan_slots_hint) p.sizes.overflow = fan_slots_hint;
     p.sizes.bins = bins;
     p.sizes.tiles = tiles;
     p.sizes.draws = p.draws.size();
@@ -591,20 +593,22 @@ static mlv_status launch_draws(mlv_context_t *c, const Plan &p, DrawDesc *d_draw
     return MLV_OK;
 }
 
-static mlv_status execute_segment_eager(mlv_context_t *c, const Segment &seg, uint32_t seq) {
+static mlv_status execute_segment_eager(mlv_context_t *c, const Segment &seg, uint32_t seq, bool rerun = false) {
     MLV_TRY(run_clears(c, seg));
     if (seg.draws.empty()) return MLV_OK;
     Plan p;
-    MLV_TRY(plan_segment(seg, p));
+    MLV_TRY(plan_segment(seg, p, c->tuning.initial_clip_fan_slots));
     MLV_TRY(ensure_workspace(c, p.sizes, false));
     CUDA_TRY(cudaMemcpyAsync(c->ws.d_draws, p.draws.data(), sizeof(DrawDesc) * p.draws.size(),
                              cudaMemcpyHostToDevice, c->stream));
     CUDA_TRY(cudaMemcpyAsync(c->ws.d_views, p.views.data(), sizeof(ViewDesc) * p.views.size(),
                              cudaMemcpyHostToDevice, c->stream));
     MLV_TRY(launch_draws(c, p, c->ws.d_draws, c->ws.d_views, seq));
-    c->host_stats[0] += seg.vertex_count;
-    c->host_stats[1] += seg.input_triangles;
-    c->host_stats[2] += seg.draws.size();
+    if (!rerun) {
+        c->host_stats[0] += seg.vertex_count;
+        c->host_stats[1] += seg.input_triangles;
+        c->host_stats[2] += seg.draws.size();
+    }
     c->last_single = seg.draws.size() == 1;
     if (c->last_single) {
         c->last_total_bins = (uint32_t)p.sizes.bins;
@@ -663,7 +667,9 @@ static mlv_status check_and_recover(mlv_context_t *c) {
             if (c->capture_infos) MLV_TRY(dev_alloc((void **)&w.info_mask, (size_t)w.list_cap * 8));
             ++w.generation;
         }
-        // reset the device state the skipped kernels left behind
+        // reset the device state the skipped kernels left behind (and the failed batches' staged
+        // statistics, which the re-run stages again)
+        CUDA_TRY(cudaMemset(w.stats, 0, sizeof(unsigned long long) * kStatTotal));
         CUDA_TRY(cudaMemset(w.bin_count, 0, sizeof(uint32_t) * w.bin_cap));
         MLV_TRY(reset_scan_state(w));
         MLV_TRY(reset_error_words(w));
@@ -675,10 +681,11 @@ static mlv_status check_and_recover(mlv_context_t *c) {
         for (const PendingJob &j : jobs) {
             if (j.seq < failed) continue;
             if (j.segment) {
-                MLV_TRY(execute_segment_eager(c, *j.segment, j.seq));
+                MLV_TRY(execute_segment_eager(c, *j.segment, j.seq, true));
             } else {
-                for (const Segment &s : j.list->segments) MLV_TRY(execute_segment_eager(c, s, j.seq));
+                for (const Segment &s : j.list->segments) MLV_TRY(execute_segment_eager(c, s, j.seq, true));
             }
+            c->pending.push_back(j);
         }
         CUDA_TRY(cudaStreamSynchronize(c->stream));
     }
@@ -1283,7 +1290,7 @@ static mlv_status run_list(mlv_context_t *c, mlv_command_list l, uint32_t seq, b
     BatchSizes maxs;
     size_t nd = 0, nv = 0;
     for (size_t i = 0; i < l->segments.size(); ++i) {
-        MLV_TRY(plan_segment(l->segments[i], plans[i]));
+        MLV_TRY(plan_segment(l->segments[i], plans[i], c->tuning.initial_clip_fan_slots));
         const BatchSizes &s = plans[i].sizes;
         maxs.tris = std::max(maxs.tris, s.tris);
         maxs.overflow = std::max(maxs.overflow, s.overflow);
@@ -1399,9 +1406,9 @@ MLV_API mlv_status mlv_get_stats(mlv_context c, mlv_stats *out) {
     CUDA_TRY(cudaMemcpy(dev, c->ws.stats, sizeof(dev), cudaMemcpyDeviceToHost));
     out->vertex_count = c->host_stats[0];
     out->input_triangle_count = c->host_stats[1];
-    out->assembled_triangle_count = dev[kStatAssembled];
-    out->active_bin_count = dev[kStatActiveBins];
-    out->total_triangle_count_in_bins = dev[kStatBinEntries];
+    out->assembled_triangle_count = dev[kStatTotal + kStatAssembled];
+    out->active_bin_count = dev[kStatTotal + kStatActiveBins];
+    out->total_triangle_count_in_bins = dev[kStatTotal + kStatBinEntries];
     out->draw_count = c->host_stats[2];
     out->batch_count = c->host_stats[3];
     out->kernel_launches = c->host_stats[4];

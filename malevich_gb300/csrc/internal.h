@@ -123,8 +123,11 @@ enum Counter : int {
     kCtrCount = 16
 };
 
+// Statistics are staged per batch (slots kStat*) and added to the totals (kStat* + kStatTotal)
+// by the tile kernel, which runs only for batches that completed; a batch that is re-run after
+// an overflow is therefore counted once.
 enum StatSlot : int {
-    kStatAssembled = 0, kStatActiveBins, kStatBinEntries, kStatCount = 8
+    kStatAssembled = 0, kStatActiveBins, kStatBinEntries, kStatTotal = 4, kStatCount = 8
 };
 
 }  // namespace mlv

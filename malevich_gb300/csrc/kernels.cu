@@ -721,6 +721,13 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
     __shared__ uint32_t s_pref[WARPS][32];
     __shared__ unsigned long long s_mask[WARPS][32];
     if (ld_volatile_u32(bp.error)) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        // commit the batch's staged statistics (k_geometry and k_scan finished before this kernel)
+        for (int k = 0; k < 3; ++k) {
+            bp.stats[kStatTotal + k] += bp.stats[k];
+            bp.stats[k] = 0;
+        }
+    }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t gtile = blockIdx.x * WARPS + warp;
     if (gtile >= bp.total_tiles) return;

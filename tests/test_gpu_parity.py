@@ -200,3 +200,19 @@ def test_gpu_status_codes(device):
     finally:
         rt.destroy()
         ds.destroy()
+
+
+def test_gpu_workspace_overflow_is_regrown_and_rerun():
+    """Tiny first buffers: batches overflow, skip their writes, and are re-run after regrowing;
+    the image and the statistics come out as if nothing happened."""
+    from malevich_gb300 import build
+    build.build()
+    dev = api.Device(0)
+    try:
+        dev.immediate.set_tuning(initial_bin_entries=64, initial_clip_fan_slots=1)
+        fr = scenes.small_scene(3, 64, 64, n_objects=4, inside=True)
+        fr.draws += scenes.small_scene(4, 64, 64, n_objects=3).draws
+        got = render_gpu(dev, fr)
+        check_against_oracle(got, pyoracle.render_oracle(fr))
+    finally:
+        dev.destroy()
