@@ -147,18 +147,21 @@ def cpu_baseline(frame, frames):
     return dt, cores, out["stats"]
 
 
-def algorithmic_bytes(frame, dev_stats, fragments):
-    """Algorithmic bytes of the two main kernels for one frame (measurement)."""
+def algorithmic_bytes(frame, dev_stats, written_pixels):
+    """Algorithmic DRAM bytes of one launch of the two main kernels: every datum the kernel must
+    touch counted once (re-reads that caches serve are not algorithmic)."""
     idx = sum(d.index_count for d in frame.draws) * 4
     uniq = 0
     for d in frame.draws:
         uniq += len(np.unique(d.ib[:d.index_count])) if d.ib is not None else d.index_count
-    vtx = uniq * 32
     assembled = dev_stats["assembled_triangle_count"]
     entries = dev_stats["total_triangle_count_in_bins"]
-    geometry = idx + vtx + assembled * (64 + 80) + entries * 4
+    tris = frame.input_triangles
+    # k_geometry: indices, the shaded vertices (48 B each, once), the per-input-triangle info word,
+    # the assembled triangles' records (64 B raster + 80 B shading) and one bin count per entry
+    geometry = idx + uniq * 48 + tris * 2 + assembled * (64 + 80) + entries * 4
     w, h = frame.width, frame.height
-    pixels = w * h
+    bins = w * h // 64 * len(frame.draws)
     tex = 0
     seen = set()
     for d in frame.draws:
@@ -166,10 +169,11 @@ def algorithmic_bytes(frame, dev_stats, fragments):
         if t is not None and id(t.data) not in seen:
             seen.add(id(t.data))
             tex += t.data.nbytes
-    # tile kernel: every (tile, triangle) pair reads a list entry and a 64-byte raster record; the
-    # depth buffer is read once; colour and depth written once; one shading record (64 + 80 bytes)
-    # per written pixel; the radiance texture footprint counted once, capped at its size
-    tile = entries * (4 + 64) + pixels * 4 + pixels * 8 + min(fragments, pixels) * (64 + 80) + tex
+    # k_tile: bin bounds, list entries, each assembled triangle's records once, the depth buffer
+    # read once, colour + depth written for every written pixel, the sampled texture once (capped
+    # at the footprint of 4 taps per written pixel)
+    tex = min(tex, written_pixels * 4 * 8)
+    tile = bins * 4 + entries * 4 + assembled * (64 + 80) + w * h * 4 + written_pixels * 8 + tex
     return {"k_geometry": geometry, "k_tile": tile}
 
 
@@ -284,6 +288,9 @@ def main():
     tris = frame.input_triangles
     value = tris * world / (ms / 1e3) / 1e6
 
+    img = r.read(0)["depth"]
+    r_img_written = int(np.count_nonzero(img != np.float32(frame.clear_depth)))
+
     # --- per-draw (immediate context, one launch sequence per draw), same flushing
     for _ in range(3):
         r.render_per_draw()
@@ -360,13 +367,14 @@ def main():
         # fragments written (Gpix/s numerator) and the CPU baseline come from the oracle
         cpu = None
         fragments = None
+        written_px = int((r_img_written) if r_img_written is not None else frame.width * frame.height)
         if not args.no_cpu_baseline:
             dt, cores, ost = cpu_baseline(frame, args.cpu_sample_frames)
             fragments = ost["fragments_written"]
             cpu = {"value": round(tris / dt / 1e6, 4), "unit": "Mtri/s", "cores": cores, "kind": "port",
                    "sample": "%d full frames of the workload" % args.cpu_sample_frames}
         peak, peak_kind = measured_peaks()
-        ab = algorithmic_bytes(frame, frame_stats, fragments or frame.width * frame.height)
+        ab = algorithmic_bytes(frame, frame_stats, written_px)
         dominant = "k_tile" if stage_avg.get("tile", 0) >= stage_avg.get("geometry", 0) else "k_geometry"
         dur_ms = stage_avg["tile" if dominant == "k_tile" else "geometry"]
         achieved = ab[dominant] / (dur_ms / 1e3) / 1e9 if dur_ms else 0.0

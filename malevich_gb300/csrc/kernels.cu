@@ -522,7 +522,7 @@ __global__ void __launch_bounds__(kRankBlock) k_rank(BatchParams bp) {
 
 // ------------------------------------------------------------------ bin scan
 
-constexpr int kScanBlock = 256, kScanItems = 8;
+constexpr int kScanBlock = 512, kScanItems = 16;   // 8192 bins per block: few look-back windows
 
 __global__ void __launch_bounds__(kScanBlock) k_scan(BatchParams bp) {
     __shared__ uint32_t s_bid, s_epoch, s_prefix;
