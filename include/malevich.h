@@ -329,6 +329,66 @@ MLV_API mlv_status mlv_set_debug_capture(mlv_context context, int enable);
 MLV_API mlv_status mlv_get_tile_infos(mlv_context context, uint32_t *tile_index, uint32_t *triangle_id,
                                       uint64_t *mask, uint64_t capacity, uint64_t *out_count);
 
+
+/* ------------------------------------------------------------------ allocation-free draw
+ * No counterpart in the reference: it is an addition for callers that cannot call cudaMalloc -
+ * a host application that owns all device memory through its own allocator, a render loop whose
+ * rule is no allocation after start-up, or code issuing work while another component of the
+ * process captures a CUDA graph, where an allocation would be captured or refused. The call draws
+ * one indexed (or, with index_buffer NULL, non-indexed) draw into caller-owned device memory with
+ * the same kernels and results as mlv_draw_indexed. Its scratch (triangle records, bins, lists,
+ * counters) is one static device array of MLV_NOALLOC_SCRATCH_BYTES that every GPU which loads
+ * this library holds until the process exits; the call allocates nothing.
+ *  - Limits: MLV_NOALLOC_MAX_TRIANGLES input triangles, MLV_NOALLOC_MAX_TILES 8x8 tiles in the
+ *    render target (1024x1024 pixels), MLV_NOALLOC_MAX_CLIP_FANS clip-generated triangles and
+ *    MLV_NOALLOC_MAX_BIN_ENTRIES (tile, triangle) pairs. Larger sizes are rejected with
+ *    MLV_ERROR_CAPACITY_EXCEEDED (the last two are only known on the device: the call then
+ *    returns that status and leaves the render target unwritten). Vertex buffers of more than
+ *    MLV_NOALLOC_MAX_VERTICES vertices are shaded per index instead of once per vertex.
+ *  - The first call on a device, with that device current, looks up the array's device address
+ *    and loads constants; make that first call before any stream capture.
+ *  - Every call shares the array and resets what must start at zero; calls that overlap on the
+ *    GPU (on different streams, or from several threads) race on it and must not be issued.
+ *  - The call waits for its stream before it returns, to report device-side overflows.
+ *  - tile_min/tile_max are the depth target's hierarchical-Z state (float per 8x8 tile); pass
+ *    MLV_NOALLOC_RESET_HIERARCHICAL_Z on the first draw after clearing the depth target. */
+#define MLV_NOALLOC_MAX_TRIANGLES 32768u
+#define MLV_NOALLOC_MAX_VERTICES 32768u
+#define MLV_NOALLOC_MAX_TILES 16384u
+#define MLV_NOALLOC_MAX_CLIP_FANS 8192u
+#define MLV_NOALLOC_MAX_BIN_ENTRIES 131072u
+#define MLV_NOALLOC_SCRATCH_BYTES 8194560u
+#define MLV_NOALLOC_RESET_HIERARCHICAL_Z 0x1u
+
+typedef struct mlv_noalloc_texture {
+    const void *data;            /* device pointer, rows tightly packed */
+    uint32_t width, height;
+    mlv_format format;           /* R8G8B8A8_UNORM, R16G16B16A16_FLOAT or R32G32B32A32_FLOAT */
+} mlv_noalloc_texture;
+
+typedef struct mlv_noalloc_draw {
+    const void *vertex_buffer;   /* device pointer */
+    uint32_t vertex_stride, vertex_count;
+    const uint32_t *index_buffer;/* device pointer, or NULL for implicit indices */
+    uint32_t index_count, start_index;
+    int32_t base_vertex;
+    mlv_vertex_shader_id vs;
+    mlv_pixel_shader_id ps;
+    const float *per_frame_cb;   /* host pointer to 48 floats (mlv_per_frame_cb), or NULL */
+    mlv_noalloc_texture vs_texture, ps_texture;
+    mlv_viewport viewport;
+    mlv_cull_mode cull_mode;
+    mlv_comparison_func depth_func;
+    uint32_t *color;             /* device pointer, width*height render-target texels */
+    float *depth;                /* device pointer, width*height */
+    float *tile_min, *tile_max;  /* device pointers, ceil(width/8)*ceil(height/8) each */
+    uint32_t width, height;
+    uint32_t flags;              /* MLV_NOALLOC_RESET_HIERARCHICAL_Z */
+} mlv_noalloc_draw;
+
+/* cuda_stream: a cudaStream_t (NULL: the default stream). */
+MLV_API mlv_status mlv_draw_indexed_noalloc(const mlv_noalloc_draw *draw, void *cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -44,6 +44,7 @@ EXPORTS = [
     "mlv_finish", "mlv_finish_command_list", "mlv_execute_command_list", "mlv_destroy_command_list",
     "mlv_get_stream", "mlv_get_stats", "mlv_reset_stats", "mlv_get_tuning", "mlv_set_tuning",
     "mlv_set_profiling", "mlv_get_stage_times", "mlv_set_debug_capture", "mlv_get_tile_infos",
+    "mlv_draw_indexed_noalloc",
 ]
 
 
@@ -154,6 +155,7 @@ def load_library(path=LIB_PATH):
     lib.mlv_get_stage_times.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_uint64)]
     lib.mlv_set_debug_capture.argtypes = [vp, ctypes.c_int]
     lib.mlv_get_tile_infos.argtypes = [vp, vp, vp, vp, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]
+    lib.mlv_draw_indexed_noalloc.argtypes = [vp, vp]
     _lib = lib
     return lib
 

@@ -45,6 +45,10 @@ static mlv_status fail(mlv_status st, const std::string &msg) {
     return st;
 }
 
+namespace mlv {
+void set_last_error(const std::string &msg) { g_last_error = msg; }
+}  // namespace mlv
+
 #define CUDA_TRY(expr)                                                                               \
     do {                                                                                             \
         cudaError_t _e = (expr);                                                                     \
