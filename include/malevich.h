@@ -357,7 +357,7 @@ MLV_API mlv_status mlv_get_tile_infos(mlv_context context, uint32_t *tile_index,
 #define MLV_NOALLOC_MAX_TILES 16384u
 #define MLV_NOALLOC_MAX_CLIP_FANS 8192u
 #define MLV_NOALLOC_MAX_BIN_ENTRIES 131072u
-#define MLV_NOALLOC_SCRATCH_BYTES 8194560u
+#define MLV_NOALLOC_SCRATCH_BYTES 9505280u
 #define MLV_NOALLOC_RESET_HIERARCHICAL_Z 0x1u
 
 typedef struct mlv_noalloc_texture {

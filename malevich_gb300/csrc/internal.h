@@ -80,6 +80,13 @@ struct TriGeom {
     float x[3], y[3], z[3], w[3];
 };
 
+// One assembled triangle's share of the binner's scatter (main.c:950-962): its key and the bins of
+// its tile rectangle, bin(x, y) = first_bin + y * row_stride + x * col_stride.
+struct BinJob {
+    uint32_t key, first_bin, nx, ny;
+    uint32_t col_stride, row_stride, pad0, pad1;
+};
+
 // Assembled triangles live in slots indexed by their input triangle g (draw-major across the
 // batch): an unclipped triangle's record is slot g; the clip-fan triangles of a clipped input
 // triangle live in an overflow region at slot total_tris + base + f (raw fan index f), with base
@@ -104,6 +111,7 @@ struct BatchParams {
     TriShade *shade;
     TriGeom *geom;                       // nullptr unless the geometry is kept
     uint16_t *tri_info;                  // [total_tris]: emitted-fan mask | clipped << 8
+    BinJob *jobs;                        // [total_tris + overflow_capacity], kCtrEmitted of them written
     uint32_t *rank;                      // [total_tris]: assembled triangles before g (exclusive)
     uint32_t *bin_count;                 // [total_bins], zero between batches
     uint32_t *bin_start;                 // [total_bins + 1]
@@ -118,10 +126,12 @@ struct BatchParams {
 };
 
 enum Counter : int {
-    kCtrRankTicket = 0, kCtrRankDone, kCtrRankEpoch, kCtrOverflow,
+    kCtrRankTicket = 0, kCtrRankDone, kCtrRankEpoch,
+    kCtrOverflow, kCtrEmitted,           // per-batch: clip-fan slots used, bin jobs written
     kCtrScanTicket, kCtrScanDone, kCtrScanEpoch,
     kCtrCount = 16
 };
+
 
 // Statistics are staged per batch (slots kStat*) and added to the totals (kStat* + kStatTotal)
 // by the tile kernel, which runs only for batches that completed; a batch that is re-run after

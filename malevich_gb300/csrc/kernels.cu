@@ -358,12 +358,16 @@ __device__ __forceinline__ void count_tiles(const BatchParams &bp, const DrawDes
         }
 }
 
+// A warp's triangles that span more than big_tiles tiles: at most 32 lanes x 7 clip fans.
+constexpr int kWarpQueue = 32 * 7;
+
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK) k_geometry(BatchParams bp) {
-    __shared__ uint32_t s_nbig;
-    __shared__ uint32_t s_big[BLOCK];
-    if (threadIdx.x == 0) s_nbig = 0;
-    __syncthreads();
+    __shared__ uint32_t s_q[BLOCK / 32][kWarpQueue];   // job slots
+    __shared__ uint32_t s_qn[BLOCK / 32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) s_qn[warp] = 0;
+    __syncwarp();
     const uint32_t g = blockIdx.x * BLOCK + threadIdx.x;
     uint32_t mask = 0;
     if (g < bp.total_tris) {
@@ -384,20 +388,29 @@ __global__ void __launch_bounds__(BLOCK) k_geometry(BatchParams bp) {
                  (p0[2] < 0.f && p1[2] < 0.f && p2[2] < 0.f) ||
                  (p0[2] > +p0[3] && p1[2] > +p1[3] && p2[2] > +p2[3]);
         bool clipped = false;
-        auto bin_record = [&](uint32_t slot, const Setup &su) {
+        // counts the bins of one emitted triangle and records its bin job for k_scatter
+        auto bin_record = [&](uint32_t key, const Setup &su) {
             int32_t tx0, ty0, tx1, ty1;
             tile_range(vw, su.minx, su.miny, su.maxx, su.maxy, tx0, ty0, tx1, ty1);
-            int32_t ntiles = (tx1 >= tx0 && ty1 >= ty0) ? (tx1 - tx0 + 1) * (ty1 - ty0 + 1) : 0;
-            if (ntiles > (int32_t)bp.big_tiles) {
-                // counted cooperatively by the whole block below; if the block's list is full (only
-                // possible with many clip fans) this thread counts the tiles itself
-                uint32_t slot_i = atomicAdd(&s_nbig, 1u);
-                if (slot_i < (uint32_t)BLOCK) {
-                    s_big[slot_i] = slot;
-                    return;
-                }
+            BinJob job;
+            job.key = key;
+            job.nx = tx1 >= tx0 ? (uint32_t)(tx1 - tx0 + 1) : 0u;
+            job.ny = ty1 >= ty0 ? (uint32_t)(ty1 - ty0 + 1) : 0u;
+            job.col_stride = vw.draw_count;
+            job.row_stride = vw.tiles_x * vw.draw_count;
+            job.first_bin = vw.bin_base + ((uint32_t)max(ty0, 0) * vw.tiles_x + (uint32_t)max(tx0, 0)) * vw.draw_count +
+                            d.draw_in_view;
+            job.pad0 = job.pad1 = 0;
+            if (job.nx == 0 || job.ny == 0) return;
+            const uint32_t slot = atomicAdd(bp.counters + kCtrEmitted, 1u);
+            bp.jobs[slot] = job;
+            if (job.nx * job.ny > bp.big_tiles) {
+                s_q[warp][atomicAdd(&s_qn[warp], 1u)] = slot;   // counted by the whole warp below
+                return;
             }
-            count_tiles(bp, d, vw, tx0, ty0, tx1, ty1);
+            for (uint32_t y = 0; y < job.ny; ++y)
+                for (uint32_t x = 0; x < job.nx; ++x)
+                    atomicAdd(bp.bin_count + job.first_bin + y * job.row_stride + x * job.col_stride, 1u);
         };
         if (!reject) {
             clipped = !((p0[0] >= -p0[3] && p1[0] >= -p1[3] && p2[0] >= -p2[3]) &&
@@ -411,7 +424,7 @@ __global__ void __launch_bounds__(BLOCK) k_geometry(BatchParams bp) {
                 if (setup_triangle(d, v[0], v[1], v[2], su)) {
                     write_record(bp, g, draw, su, v[0], v[1], v[2]);
                     mask = 1;
-                    bin_record(g, su);
+                    bin_record(g << 3, su);
                 }
             } else {
                 Vtx poly[kMaxClipVertices], tmp[kMaxClipVertices];
@@ -433,7 +446,7 @@ __global__ void __launch_bounds__(BLOCK) k_geometry(BatchParams bp) {
                                 const uint32_t slot = bp.total_tris + base + (uint32_t)f;
                                 write_record(bp, slot, draw, su, poly[0], poly[f + 1], poly[f + 2]);
                                 mask |= 1u << f;
-                                bin_record(slot, su);
+                                bin_record((g << 3) | (uint32_t)(f + 1), su);
                             }
                         }
                     }
@@ -446,25 +459,16 @@ __global__ void __launch_bounds__(BLOCK) k_geometry(BatchParams bp) {
     uint32_t n = __popc(mask);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xFFFFFFFFu, n, o);
-    if ((threadIdx.x & 31) == 0 && n) atomicAdd(bp.stats + kStatAssembled, (unsigned long long)n);
-    __syncthreads();
-
-    // triangles spanning many tiles: the whole block counts their tiles
-    const uint32_t nbig = min(s_nbig, (uint32_t)BLOCK);
-    for (uint32_t b = 0; b < nbig; ++b) {
-        const uint32_t rec = s_big[b];
-        const int4 w3 = bp.raster[rec].w[3];
-        const uint32_t dr = __float_as_uint(bp.shade[rec].s[0].w);
-        const DrawDesc &d = bp.draws[dr];
-        const ViewDesc &vw = bp.views[d.view];
-        int32_t minx = (int16_t)(w3.z & 0xFFFF), miny = w3.z >> 16, maxx = (int16_t)(w3.w & 0xFFFF), maxy = w3.w >> 16;
-        int32_t tx0, ty0, tx1, ty1;
-        tile_range(vw, minx, miny, maxx, maxy, tx0, ty0, tx1, ty1);
-        const int32_t nx = tx1 - tx0 + 1, nt = nx * (ty1 - ty0 + 1);
-        for (int32_t i = threadIdx.x; i < nt; i += BLOCK) {
-            uint32_t tx = tx0 + i % nx, ty = ty0 + i / nx;
-            uint32_t bin = vw.bin_base + (ty * vw.tiles_x + tx) * vw.draw_count + d.draw_in_view;
-            atomicAdd(bp.bin_count + bin, 1u);
+    if (lane == 0 && n) atomicAdd(bp.stats + kStatAssembled, (unsigned long long)n);
+    // triangles spanning many tiles: the warp counts their tiles together
+    __syncwarp();
+    const uint32_t nq = s_qn[warp];
+    for (uint32_t b = 0; b < nq; ++b) {
+        const BinJob job = bp.jobs[s_q[warp][b]];
+        const uint32_t nt = job.nx * job.ny;
+        for (uint32_t i = lane; i < nt; i += 32) {
+            const uint32_t y = i / job.nx, x = i - y * job.nx;
+            atomicAdd(bp.bin_count + job.first_bin + y * job.row_stride + x * job.col_stride, 1u);
         }
     }
 }
@@ -583,41 +587,11 @@ __global__ void __launch_bounds__(kScanBlock) k_scan(BatchParams bp) {
 
 constexpr int kScatterBlock = 256;
 
-__device__ __forceinline__ void scatter_tiles(const BatchParams &bp, uint32_t key, uint32_t rec, int32_t first,
-                                              int32_t stride) {
-    const int4 w3 = __ldg(&bp.raster[rec].w[3]);
-    const uint32_t dr = __float_as_uint(__ldg(&bp.shade[rec].s[0].w));
-    const DrawDesc &d = bp.draws[dr];
-    const ViewDesc &vw = bp.views[d.view];
-    int32_t minx = (int16_t)(w3.z & 0xFFFF), miny = w3.z >> 16, maxx = (int16_t)(w3.w & 0xFFFF), maxy = w3.w >> 16;
-    int32_t tx0, ty0, tx1, ty1;
-    tile_range(vw, minx, miny, maxx, maxy, tx0, ty0, tx1, ty1);
-    const int32_t nx = tx1 - tx0 + 1;
-    const int32_t nt = (tx1 >= tx0 && ty1 >= ty0) ? nx * (ty1 - ty0 + 1) : 0;
-    for (int32_t i = first; i < nt; i += stride) {
-        uint32_t tx = tx0 + i % nx, ty = ty0 + i / nx;
-        uint32_t bin = vw.bin_base + (ty * vw.tiles_x + tx) * vw.draw_count + d.draw_in_view;
-        uint32_t pos = atomicSub(bp.bin_count + bin, 1u) - 1u;
-        bp.list[bp.bin_start[bin] + pos] = key;
-    }
-}
-
-__device__ __forceinline__ int32_t tile_count_of(const BatchParams &bp, uint32_t rec) {
-    const int4 w3 = __ldg(&bp.raster[rec].w[3]);
-    const uint32_t dr = __float_as_uint(__ldg(&bp.shade[rec].s[0].w));
-    const ViewDesc &vw = bp.views[bp.draws[dr].view];
-    int32_t minx = (int16_t)(w3.z & 0xFFFF), miny = w3.z >> 16, maxx = (int16_t)(w3.w & 0xFFFF), maxy = w3.w >> 16;
-    int32_t tx0, ty0, tx1, ty1;
-    tile_range(vw, minx, miny, maxx, maxy, tx0, ty0, tx1, ty1);
-    return (tx1 >= tx0 && ty1 >= ty0) ? (tx1 - tx0 + 1) * (ty1 - ty0 + 1) : 0;
-}
-
-// One thread per input triangle: every assembled triangle it produced goes to the lists of the
-// tiles its bounds cover (main.c:950-962). Triangles over more than big_tiles tiles are
-// scattered by the whole block, as k_geometry counted them.
+// One thread per bin job (an emitted triangle): its key goes to the list of every bin of its tile
+// rectangle (main.c:950-962). Jobs over more than big_tiles bins are spread over the warp.
 __global__ void __launch_bounds__(kScatterBlock) k_scatter(BatchParams bp) {
-    __shared__ uint32_t s_nbig;
-    __shared__ uint32_t s_big[kScatterBlock * 2];
+    __shared__ BinJob s_q[kScatterBlock / 32][32];
+    __shared__ uint32_t s_qn[kScatterBlock / 32];
     if (ld_volatile_u32(bp.error)) return;
     const uint32_t total = bp.bin_start[bp.total_bins];
     if (total > bp.list_capacity) {
@@ -628,37 +602,40 @@ __global__ void __launch_bounds__(kScatterBlock) k_scatter(BatchParams bp) {
         }
         return;
     }
-    for (uint32_t base = blockIdx.x * kScatterBlock; base < bp.total_tris; base += gridDim.x * kScatterBlock) {
-        if (threadIdx.x == 0) s_nbig = 0;
-        __syncthreads();
-        const uint32_t g = base + threadIdx.x;
-        if (g < bp.total_tris) {
-            const uint32_t info = bp.tri_info[g];
-            uint32_t m = info & 0xFFu;
-            const bool clipped = (info & 0x100u) != 0;
-            const uint32_t fan_base = (clipped && m) ? (uint32_t)__ldg(&bp.raster[g].w[0].x) : 0u;
-            while (m) {
-                const uint32_t f = __ffs(m) - 1;
-                m &= m - 1;
-                const uint32_t key = (g << 3) | (clipped ? f + 1 : 0u);
-                const uint32_t rec = clipped ? bp.total_tris + fan_base + f : g;
-                if (tile_count_of(bp, rec) > (int32_t)bp.big_tiles) {
-                    uint32_t slot = atomicAdd(&s_nbig, 1u);
-                    if (slot < 2u * kScatterBlock) {
-                        s_big[slot] = key;   // scattered by the whole block below
-                        continue;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t njobs = ld_volatile_u32(bp.counters + kCtrEmitted);
+    for (uint32_t base = blockIdx.x * kScatterBlock; base < njobs; base += gridDim.x * kScatterBlock) {
+        if (lane == 0) s_qn[warp] = 0;
+        __syncwarp();
+        const uint32_t i = base + threadIdx.x;
+        if (i < njobs) {
+            const uint4 *jp = reinterpret_cast<const uint4 *>(bp.jobs + i);
+            const uint4 j0 = jp[0], j1 = jp[1];
+            BinJob job = {j0.x, j0.y, j0.z, j0.w, j1.x, j1.y, 0u, 0u};
+            if (job.nx * job.ny > bp.big_tiles) {
+                s_q[warp][atomicAdd(&s_qn[warp], 1u)] = job;
+            } else {
+                for (uint32_t y = 0; y < job.ny; ++y)
+                    for (uint32_t x = 0; x < job.nx; ++x) {
+                        const uint32_t bin = job.first_bin + y * job.row_stride + x * job.col_stride;
+                        const uint32_t pos = atomicSub(bp.bin_count + bin, 1u) - 1u;
+                        bp.list[bp.bin_start[bin] + pos] = job.key;
                     }
-                }
-                scatter_tiles(bp, key, rec, 0, 1);
             }
         }
-        __syncthreads();
-        const uint32_t nbig = min(s_nbig, 2u * kScatterBlock);
-        for (uint32_t b = 0; b < nbig; ++b) {
-            const uint32_t key = s_big[b];
-            scatter_tiles(bp, key, record_of(bp, key), threadIdx.x, kScatterBlock);
+        __syncwarp();
+        const uint32_t nq = s_qn[warp];
+        for (uint32_t b = 0; b < nq; ++b) {
+            const BinJob job = s_q[warp][b];
+            const uint32_t nt = job.nx * job.ny;
+            for (uint32_t t = lane; t < nt; t += 32) {
+                const uint32_t y = t / job.nx, x = t - y * job.nx;
+                const uint32_t bin = job.first_bin + y * job.row_stride + x * job.col_stride;
+                const uint32_t pos = atomicSub(bp.bin_count + bin, 1u) - 1u;
+                bp.list[bp.bin_start[bin] + pos] = job.key;
+            }
         }
-        __syncthreads();
+        __syncwarp();
     }
 }
 
@@ -1003,6 +980,7 @@ cudaError_t launch_scan(const BatchParams &bp, cudaStream_t stream) {
 }
 
 cudaError_t launch_scatter(const BatchParams &bp, int num_sms, cudaStream_t stream) {
+    // the job count is only known on the device: a grid of up to 8 blocks per SM strides over it
     uint32_t blocks = (bp.total_tris + kScatterBlock - 1) / kScatterBlock;
     uint32_t cap = (uint32_t)num_sms * 8;
     if (blocks > cap) blocks = cap;
