@@ -376,7 +376,7 @@ static mlv_status ensure_workspace(mlv_context_t *c, const BatchSizes &s, bool k
     {
         unsigned long long *b1 = w.scan_status, *b2 = w.scan_status2;
         MLV_TRY(grow(&w.scan_status, w.status_cap, s.tris / 2048 + 2, sizeof(unsigned long long)));
-        MLV_TRY(grow(&w.scan_status2, w.status2_cap, s.bins / 8192 + 2, sizeof(unsigned long long)));
+        MLV_TRY(grow(&w.scan_status2, w.status2_cap, s.bins / 4096 + 2, sizeof(unsigned long long)));
         if (b1 != w.scan_status || b2 != w.scan_status2) {
             MLV_TRY(reset_scan_state(w));
             changed = true;

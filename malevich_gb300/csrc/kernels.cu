@@ -362,7 +362,7 @@ __device__ __forceinline__ void count_tiles(const BatchParams &bp, const DrawDes
 constexpr int kWarpQueue = 32 * 7;
 
 template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK) k_geometry(BatchParams bp) {
+__global__ void __launch_bounds__(BLOCK, 2048 / BLOCK / 2) k_geometry(BatchParams bp) {
     __shared__ uint32_t s_q[BLOCK / 32][kWarpQueue];   // job slots
     __shared__ uint32_t s_qn[BLOCK / 32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -526,7 +526,7 @@ __global__ void __launch_bounds__(kRankBlock) k_rank(BatchParams bp) {
 
 // ------------------------------------------------------------------ bin scan
 
-constexpr int kScanBlock = 512, kScanItems = 16;   // 8192 bins per block: few look-back windows
+constexpr int kScanBlock = 256, kScanItems = 16;   // 4096 bins per block, read as 4 x uint4 per thread
 
 __global__ void __launch_bounds__(kScanBlock) k_scan(BatchParams bp) {
     __shared__ uint32_t s_bid, s_epoch, s_prefix;
@@ -542,10 +542,19 @@ __global__ void __launch_bounds__(kScanBlock) k_scan(BatchParams bp) {
     const uint32_t base = bid * kScanBlock * kScanItems + threadIdx.x * kScanItems;
     uint32_t vals[kScanItems];
     uint32_t sum = 0, active = 0;
+    if (base + kScanItems <= n) {
+        // bin_count is 16-byte aligned (cudaMalloc) and base is a multiple of 16
+#pragma unroll
+        for (int q = 0; q < kScanItems / 4; ++q) {
+            const uint4 v4 = reinterpret_cast<const uint4 *>(bp.bin_count + base)[q];
+            vals[4 * q] = v4.x; vals[4 * q + 1] = v4.y; vals[4 * q + 2] = v4.z; vals[4 * q + 3] = v4.w;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < kScanItems; ++i) vals[i] = base + i < n ? bp.bin_count[base + i] : 0u;
+    }
 #pragma unroll
     for (int i = 0; i < kScanItems; ++i) {
-        uint32_t idx = base + i;
-        vals[i] = idx < n ? bp.bin_count[idx] : 0u;
         sum += vals[i];
         active += vals[i] ? 1u : 0u;
     }
@@ -557,11 +566,21 @@ __global__ void __launch_bounds__(kScanBlock) k_scan(BatchParams bp) {
     }
     __syncthreads();
     uint32_t run = s_prefix + excl;
+    uint32_t outv[kScanItems];
 #pragma unroll
     for (int i = 0; i < kScanItems; ++i) {
-        uint32_t idx = base + i;
-        if (idx < n) bp.bin_start[idx] = run;
+        outv[i] = run;
         run += vals[i];
+    }
+    if (base + kScanItems <= n) {
+#pragma unroll
+        for (int q = 0; q < kScanItems / 4; ++q)
+            reinterpret_cast<uint4 *>(bp.bin_start + base)[q] =
+                make_uint4(outv[4 * q], outv[4 * q + 1], outv[4 * q + 2], outv[4 * q + 3]);
+    } else {
+#pragma unroll
+        for (int i = 0; i < kScanItems; ++i)
+            if (base + i < n) bp.bin_start[base + i] = outv[i];
     }
     // active-bin statistic (main.c:937-944)
 #pragma unroll
@@ -615,12 +634,27 @@ __global__ void __launch_bounds__(kScatterBlock) k_scatter(BatchParams bp) {
             if (job.nx * job.ny > bp.big_tiles) {
                 s_q[warp][atomicAdd(&s_qn[warp], 1u)] = job;
             } else {
-                for (uint32_t y = 0; y < job.ny; ++y)
-                    for (uint32_t x = 0; x < job.nx; ++x) {
-                        const uint32_t bin = job.first_bin + y * job.row_stride + x * job.col_stride;
-                        const uint32_t pos = atomicSub(bp.bin_count + bin, 1u) - 1u;
-                        bp.list[bp.bin_start[bin] + pos] = job.key;
+                // up to 4 bins at a time: the atomics and bin_start loads are independent, so they
+                // are all in flight together instead of one round trip after another
+                const uint32_t nt = job.nx * job.ny;
+                for (uint32_t t0 = 0; t0 < nt; t0 += 4) {
+                    uint32_t bin[4], pos[4], st[4];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const uint32_t t = t0 + k;
+                        const uint32_t y = t / job.nx, x = t - y * job.nx;
+                        bin[k] = job.first_bin + y * job.row_stride + x * job.col_stride;
                     }
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        if (t0 + k < nt) {
+                            pos[k] = atomicSub(bp.bin_count + bin[k], 1u) - 1u;
+                            st[k] = __ldg(bp.bin_start + bin[k]);
+                        }
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        if (t0 + k < nt) bp.list[st[k] + pos[k]] = job.key;
+                }
             }
         }
         __syncwarp();

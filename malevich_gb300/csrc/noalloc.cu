@@ -48,7 +48,7 @@ constexpr size_t kOffCounters = align256(kOffView + sizeof(ViewDesc));
 constexpr size_t kOffStats = align256(kOffCounters + sizeof(uint32_t) * kCtrCount);
 constexpr size_t kOffError = align256(kOffStats + sizeof(unsigned long long) * kStatCount);
 constexpr size_t kOffStatus = align256(kOffError + sizeof(uint32_t) * 8);
-constexpr size_t kStatusWords = kMaxTiles / 8192 + 2;
+constexpr size_t kStatusWords = kMaxTiles / 4096 + 2;
 constexpr size_t kOffBinCount = align256(kOffStatus + sizeof(unsigned long long) * kStatusWords);
 constexpr size_t kOffBinStart = align256(kOffBinCount + sizeof(uint32_t) * (kMaxTiles + 1));
 constexpr size_t kOffTriInfo = align256(kOffBinStart + sizeof(uint32_t) * (kMaxTiles + 1));
