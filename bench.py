@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--cpu-sample-frames", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-diff", action="store_true", help="skip the differentiable sections")
+    ap.add_argument("--diff-steps", type=int, default=100)
     ap.add_argument("--profile-once", action="store_true",
                     help="render the frame once (batched, eager) and exit: a short launch sequence for ncu")
     return ap.parse_args()
@@ -175,6 +177,115 @@ def algorithmic_bytes(frame, dev_stats, written_pixels):
     tex = min(tex, written_pixels * 4 * 8)
     tile = bins * 4 + entries * 4 + assembled * (64 + 80) + w * h * 4 + written_pixels * 8 + tex
     return {"k_geometry": geometry, "k_tile": tile}
+
+
+def run_diff_sections(dev, args):
+    """The differentiable configurations through the C ABI (no autograd): (4) forward + backward
+    time per view for 16 views at 512x512 of a 50k-triangle sphere; (5) an Adam loop over 256 views
+    at 256x256 of a 200k-triangle heightfield with a 2048x2048 RGBA32F texture initialised to 0.5,
+    fitting texture and vertex colours to a target rendered from a noise texture and colours."""
+    import ctypes
+    import torch
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from diffrender import DiffScene, gather_primitive_ids, visibility
+    from malevich_gb300 import api, scenes
+    lib = api.load_library()
+    stream = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    out = {}
+
+    # --- configuration 4: forward + backward per view
+    sc = scenes.diff_scene(seed=4)
+    prims = visibility(dev, sc)
+    ds = DiffScene(sc, prims)
+    col = torch.from_numpy(sc["col"]).cuda()
+    tex = torch.from_numpy(sc["tex"]).cuda()
+    pos = torch.from_numpy(sc["pos"]).cuda()
+    image = torch.empty((ds.views, ds.height, ds.width, 3), device="cuda")
+    target = torch.rand_like(image)
+    g_col, g_tex, g_pos = torch.zeros_like(col), torch.zeros_like(tex), torch.zeros_like(pos)
+
+    def fwd_bwd():
+        d = ds.desc(col, tex, pos, image=image)
+        lib.mlv_diff_forward(ctypes.byref(d), sp)
+        gi = 2.0 * (image - target) * ds.mask
+        d = ds.desc(col, tex, pos, grad_image=gi, g_col=g_col, g_tex=g_tex, g_pos=g_pos)
+        lib.mlv_diff_backward(ctypes.byref(d), sp)
+
+    for _ in range(3):
+        fwd_bwd()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    n = 20
+    for _ in range(n):
+        fwd_bwd()
+    b.record(stream)
+    torch.cuda.synchronize()
+    out["config4"] = {"views": ds.views, "resolution": [ds.width, ds.height], "triangles": ds.n_tris,
+                      "fwd_bwd_ms_per_view": round(a.elapsed_time(b) / n / ds.views, 5),
+                      "gradient_check": "tests/test_gpu_adjoint.py: 1e-4 relative vs the FP64 oracle adjoint"}
+    del ds, image, target, g_col, g_tex, g_pos
+
+    # --- configuration 5: batched + differentiable optimisation loop
+    torch.cuda.synchronize()
+    free0, total = torch.cuda.mem_get_info()
+    sc = scenes.diff_scene(seed=5, n_views=256, size=256, tex_size=2048, heightfield_cells=316)
+    rng = np.random.default_rng(55)
+    tex_true = torch.from_numpy(rng.random(sc["tex"].shape).astype(np.float32)).cuda()
+    col_true = torch.from_numpy(sc["col"]).cuda()
+    frames = scenes.diff_frames(sc)
+    vr = api.FrameRenderer(dev, frames, primitive_ids=True)
+    vr.render_batched()                      # sizes the workspace, captures the graph
+    prims = np.stack([vr.read(i)["vis_prim"] for i in range(len(frames))])
+    ds = DiffScene(sc, prims)
+    pos = torch.from_numpy(sc["pos"]).cuda()
+    target = torch.empty((ds.views, ds.height, ds.width, 3), device="cuda")
+    d = ds.desc(col_true, tex_true, pos, image=target)
+    lib.mlv_diff_forward(ctypes.byref(d), sp)
+    tex = torch.full_like(tex_true, 0.5).requires_grad_()
+    col = torch.full_like(col_true, 0.5).requires_grad_()
+    opt = torch.optim.Adam([tex, col], lr=1e-2)
+    image = torch.empty_like(target)
+
+    def step():
+        vr.render_batched()                  # visibility of all 256 views: one graph launch
+        dev.immediate.finish()
+        gather_primitive_ids(vr, ds.prim)
+        d = ds.desc(col, tex, pos, image=image)
+        lib.mlv_diff_forward(ctypes.byref(d), sp)
+        gi = 2.0 * (image - target) * ds.mask
+        tex.grad = torch.zeros_like(tex)
+        col.grad = torch.zeros_like(col)
+        d = ds.desc(col, tex, pos, grad_image=gi, g_col=col.grad, g_tex=tex.grad)
+        lib.mlv_diff_backward(ctypes.byref(d), sp)
+        opt.step()
+
+    t0 = time.perf_counter()
+    for _ in range(args.diff_steps):
+        step()
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / args.diff_steps
+    free1, _ = torch.cuda.mem_get_info()
+    with torch.no_grad():
+        seen = torch.zeros(tex.shape[:2], dtype=torch.bool, device="cuda")
+        gi = torch.ones_like(image) * ds.mask
+        gt = torch.zeros_like(tex)
+        d = ds.desc(col, tex, pos, grad_image=gi, g_tex=gt)
+        lib.mlv_diff_backward(ctypes.byref(d), sp)
+        seen = gt[..., 0] != 0
+        err = (tex - tex_true)[..., :3][seen]
+        rmse = float(torch.sqrt((err ** 2).mean()).item()) if err.numel() else None
+        err0 = (0.5 - tex_true)[..., :3][seen]
+        rmse0 = float(torch.sqrt((err0 ** 2).mean()).item()) if err0.numel() else None
+    out["config5"] = {"views": ds.views, "resolution": [ds.width, ds.height], "triangles": ds.n_tris,
+                      "texture": [2048, 2048], "adam_steps": args.diff_steps, "lr": 1e-2,
+                      "ms_per_step": round(dt * 1e3, 3),
+                      "peak_hbm_gb": round((total - min(free0, free1)) / 1e9, 2),
+                      "texture_rmse_start": rmse0, "texture_rmse_final": rmse,
+                      "step": "visibility (batched command list, CUDA graph) + mlv_diff_forward + "
+                              "mlv_diff_backward + torch Adam"}
+    vr.destroy()
+    return out
 
 
 def run_reference_arm(args, rank, world):
@@ -362,6 +473,12 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
 
+    diff = None
+    if not args.no_diff:
+        r.destroy()
+        r = None
+        diff = run_diff_sections(dev, args)
+
     result = None
     if rank == 0:
         # fragments written (Gpix/s numerator) and the CPU baseline come from the oracle
@@ -399,11 +516,13 @@ def main():
             "frame_stats": {k: int(v) for k, v in frame_stats.items()},
             "cpu_baseline": cpu,
             "clocks": clk,
+            "differentiable": diff,
             "gpu_launches": launches,
             "wall_s_timed": round(wall, 4),
         }
         print(json.dumps(result))
-    r.destroy()
+    if r is not None:
+        r.destroy()
     dev.destroy()
     if dist:
         dist.barrier()

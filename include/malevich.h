@@ -330,6 +330,40 @@ MLV_API mlv_status mlv_get_tile_infos(mlv_context context, uint32_t *tile_index,
                                       uint64_t *mask, uint64_t capacity, uint64_t *out_count);
 
 
+/* ------------------------------------------------------------------ differentiable shading (new)
+ * No reference counterpart: the reference's quantised barycentrics (main.c:1092-1102) have zero
+ * gradient almost everywhere. These calls shade under a fixed visibility - the per-pixel input
+ * triangle written by the rasteriser through mlv_om_set_primitive_id_target - with continuous
+ * barycentrics at the reference's sample point (the pixel corner), for MLV_VS_PASSTHROUGH_UV-style
+ * vertices: screen positions x, y in [0,1] (X = W x, Y = H (1 - y), w = 1), a colour and a UV per
+ * vertex, and the pixel shader colour * bilinear(RGBA32F texture, uv).xyz.
+ * mlv_diff_forward writes the image and the per-pixel barycentrics (the checkpoint);
+ * mlv_diff_backward reads the checkpoint and grad_image = dL/dimage, recomputes the interpolation
+ * and ADDS dL/dcolors, dL/dtexture (scattered through the bilinear weights) and dL/dpositions (the
+ * barycentric terms, visibility fixed) into the gradient arrays it is given (any may be NULL).
+ * All pointers are device memory; both calls are asynchronous on `cuda_stream`. */
+typedef struct mlv_diff_desc {
+    uint32_t n_verts, n_tris;
+    const uint32_t *index_buffer;     /* 3 * n_tris */
+    const float *colors;              /* 3 * n_verts */
+    const float *uvs;                 /* 2 * n_verts */
+    const float *texture;             /* tex_height * tex_width * 4 */
+    uint32_t tex_width, tex_height;
+    uint32_t num_views, width, height;
+    const float *positions;           /* num_views * n_verts * 2 */
+    const uint32_t *primitive_ids;    /* num_views * height * width; 0xFFFFFFFF: background */
+    float *barycentrics;              /* num_views * height * width * 2 (written by the forward) */
+    float *image;                     /* num_views * height * width * 3 (forward output) */
+    const float *grad_image;          /* num_views * height * width * 3 (backward input) */
+    float *grad_colors, *grad_texture, *grad_positions;
+} mlv_diff_desc;
+
+MLV_API mlv_status mlv_diff_forward(const mlv_diff_desc *desc, void *cuda_stream);
+MLV_API mlv_status mlv_diff_backward(const mlv_diff_desc *desc, void *cuda_stream);
+/* The visibility for the differentiable path: for every written pixel, the index (within its
+ * draw) of the input triangle that wrote it (Direct3D's SV_PrimitiveID); R32_UINT, or NULL. */
+MLV_API mlv_status mlv_om_set_primitive_id_target(mlv_context context, mlv_texture2d primitive_id);
+
 /* ------------------------------------------------------------------ allocation-free draw
  * No counterpart in the reference: it is an addition for callers that cannot call cudaMalloc -
  * a host application that owns all device memory through its own allocator, a render loop whose

@@ -44,7 +44,7 @@ EXPORTS = [
     "mlv_finish", "mlv_finish_command_list", "mlv_execute_command_list", "mlv_destroy_command_list",
     "mlv_get_stream", "mlv_get_stats", "mlv_reset_stats", "mlv_get_tuning", "mlv_set_tuning",
     "mlv_set_profiling", "mlv_get_stage_times", "mlv_set_debug_capture", "mlv_get_tile_infos",
-    "mlv_draw_indexed_noalloc",
+    "mlv_draw_indexed_noalloc", "mlv_diff_forward", "mlv_diff_backward", "mlv_om_set_primitive_id_target",
 ]
 
 
@@ -156,6 +156,9 @@ def load_library(path=LIB_PATH):
     lib.mlv_set_debug_capture.argtypes = [vp, ctypes.c_int]
     lib.mlv_get_tile_infos.argtypes = [vp, vp, vp, vp, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]
     lib.mlv_draw_indexed_noalloc.argtypes = [vp, vp]
+    lib.mlv_diff_forward.argtypes = [vp, vp]
+    lib.mlv_diff_backward.argtypes = [vp, vp]
+    lib.mlv_om_set_primitive_id_target.argtypes = [vp, vp]
     _lib = lib
     return lib
 
@@ -262,6 +265,9 @@ class Context:
     def om_set_visibility_targets(self, tri=None, draw=None, bary=None):
         h = lambda t: t.handle if t else None
         _check(self.lib.mlv_om_set_visibility_targets(self.handle, h(tri), h(draw), h(bary)))
+
+    def om_set_primitive_id_target(self, tex):
+        _check(self.lib.mlv_om_set_primitive_id_target(self.handle, tex.handle if tex else None))
 
     def clear_render_target(self, rt, rgba):
         _check(self.lib.mlv_clear_render_target_view(self.handle, rt.handle, (ctypes.c_float * 4)(*rgba)))
@@ -395,11 +401,12 @@ class FrameRenderer:
     """Uploads a Frame's (or several Frames') resources once and renders them through the C ABI,
     either per draw on the immediate context or as one command list (batched)."""
 
-    def __init__(self, device, frames, visibility=False):
+    def __init__(self, device, frames, visibility=False, primitive_ids=False):
         self.device = device
         self.frames = frames if isinstance(frames, (list, tuple)) else [frames]
         self._buffers, self._textures = {}, {}
         self.targets = []
+        self.prim_targets = []
         for fr in self.frames:
             rt = Texture2D(device, fr.width, fr.height, FORMAT_R8G8B8A8_UNORM, bind=BIND_RENDER_TARGET)
             ds = Texture2D(device, fr.width, fr.height, FORMAT_D32_FLOAT, bind=BIND_DEPTH_STENCIL)
@@ -409,6 +416,8 @@ class FrameRenderer:
                        Texture2D(device, fr.width, fr.height, FORMAT_R32_UINT, bind=BIND_UNORDERED_ACCESS),
                        Texture2D(device, fr.width, fr.height, FORMAT_R32G32_FLOAT, bind=BIND_UNORDERED_ACCESS))
             self.targets.append((rt, ds, vis))
+            self.prim_targets.append(Texture2D(device, fr.width, fr.height, FORMAT_R32_UINT,
+                                               bind=BIND_UNORDERED_ACCESS) if primitive_ids else None)
             for d in fr.draws:
                 self._buffer(d.vb, BIND_VERTEX_BUFFER)
                 if d.ib is not None:
@@ -432,7 +441,7 @@ class FrameRenderer:
             self._textures[key] = (Texture2D(self.device, t.width, t.height, _FMT[t.format], data=t.data), t)
         return self._textures[key][0]
 
-    def _issue(self, ctx, fr, targets):
+    def _issue(self, ctx, fr, targets, prim=None):
         rt, ds, vis = targets
         if fr.clear_color is not None:
             ctx.clear_render_target(rt, fr.clear_color)
@@ -442,8 +451,11 @@ class FrameRenderer:
             ctx.clear_u32(vis[0], 0xFFFFFFFF)
             ctx.clear_u32(vis[1], 0xFFFFFFFF)
             ctx.clear_u32(vis[2], 0)
+        if prim is not None:
+            ctx.clear_u32(prim, 0xFFFFFFFF)
         ctx.om_set_render_targets(rt, ds)
         ctx.om_set_visibility_targets(*(vis if vis is not None else (None, None, None)))
+        ctx.om_set_primitive_id_target(prim)
         for d in fr.draws:
             ctx.ia_set_vertex_buffer(self._buffer(d.vb, BIND_VERTEX_BUFFER), d.vb_stride)
             ctx.ia_set_index_buffer(self._buffer(d.ib, BIND_INDEX_BUFFER) if d.ib is not None else None)
@@ -463,15 +475,15 @@ class FrameRenderer:
     def render_per_draw(self):
         """Immediate context: one launch sequence per draw (the reference's draw_indexed loop)."""
         ctx = self.device.immediate
-        for fr, tg in zip(self.frames, self.targets):
-            self._issue(ctx, fr, tg)
+        for fr, tg, pr in zip(self.frames, self.targets, self.prim_targets):
+            self._issue(ctx, fr, tg, pr)
 
     def record(self):
         """Records every frame into one deferred context and returns the command list."""
         if self.command_list is None:
             dctx = self.device.create_deferred_context()
-            for fr, tg in zip(self.frames, self.targets):
-                self._issue(dctx, fr, tg)
+            for fr, tg, pr in zip(self.frames, self.targets, self.prim_targets):
+                self._issue(dctx, fr, tg, pr)
             self.command_list = dctx.finish_command_list()
             dctx.destroy()
         return self.command_list
@@ -488,6 +500,8 @@ class FrameRenderer:
             out["vis_tri"] = ctx.read_texture(vis[0])
             out["vis_draw"] = ctx.read_texture(vis[1])
             out["vis_bary"] = ctx.read_texture(vis[2])
+        if self.prim_targets[index] is not None:
+            out["vis_prim"] = ctx.read_texture(self.prim_targets[index])
         return out
 
     def destroy(self):
@@ -502,3 +516,6 @@ class FrameRenderer:
             ds.destroy()
             for v in vis or ():
                 v.destroy()
+        for p in self.prim_targets:
+            if p is not None:
+                p.destroy()

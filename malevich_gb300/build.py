@@ -14,7 +14,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmalevich_gb300.so")
-SOURCES = ["kernels.cu", "api.cu", "noalloc.cu"]
+SOURCES = ["kernels.cu", "api.cu", "noalloc.cu", "adjoint.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-prec-div=true", "-prec-sqrt=true", "-std=c++17",
          "-Xcompiler", "-fPIC,-fvisibility=hidden", "-I", CSRC, "-I", os.path.join(ROOT, "include")]

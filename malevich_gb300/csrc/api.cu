@@ -121,13 +121,13 @@ struct PipelineState {
     int cull = 1;          // internal: 0 none, 1 back, 2 front
     int depth_less = 0;
     mlv_texture2d rtv = nullptr, dsv = nullptr;
-    mlv_texture2d vis_tri = nullptr, vis_draw = nullptr, vis_bary = nullptr;
+    mlv_texture2d vis_tri = nullptr, vis_draw = nullptr, vis_bary = nullptr, vis_prim = nullptr;
     mlv_primitive_topology topology = MLV_PRIMITIVE_TOPOLOGY_TRIANGLELIST;
 };
 
 struct DrawCmd {
     DrawDesc desc;                 // view / draw_in_view / tri_begin filled by the planner
-    mlv_texture2d rtv, dsv, vis_tri, vis_draw, vis_bary;
+    mlv_texture2d rtv, dsv, vis_tri, vis_draw, vis_bary, vis_prim;
     uint32_t index_count;
 };
 
@@ -433,6 +433,7 @@ static mlv_status plan_segment(const Segment &seg, Plan &p, uint32_t fan_slots_h
         v.vis_tri = first.vis_tri ? (uint32_t *)first.vis_tri->ptr : nullptr;
         v.vis_draw = first.vis_draw ? (uint32_t *)first.vis_draw->ptr : nullptr;
         v.vis_bary = first.vis_bary ? (float *)first.vis_bary->ptr : nullptr;
+        v.vis_prim = first.vis_prim ? (uint32_t *)first.vis_prim->ptr : nullptr;
         v.width = rt->width;
         v.height = rt->height;
         v.tiles_x = ds->tiles_x;
@@ -1071,6 +1072,14 @@ MLV_API mlv_status mlv_om_set_render_targets(mlv_context c, mlv_texture2d rt, ml
     return MLV_OK;
 }
 
+MLV_API mlv_status mlv_om_set_primitive_id_target(mlv_context c, mlv_texture2d prim) {
+    if (!c) return fail(MLV_ERROR_INVALID_ARG, "context is NULL");
+    if (prim && prim->format != MLV_FORMAT_R32_UINT)
+        return fail(MLV_ERROR_INVALID_ARG, "primitive-id target must be R32_UINT");
+    c->st.vis_prim = prim;
+    return MLV_OK;
+}
+
 MLV_API mlv_status mlv_om_set_visibility_targets(mlv_context c, mlv_texture2d tri, mlv_texture2d draw,
                                                  mlv_texture2d bary) {
     if (!c) return fail(MLV_ERROR_INVALID_ARG, "context is NULL");
@@ -1093,7 +1102,8 @@ static uint32_t encode_clear(const float *c) {
 }
 
 static bool draw_touches(const DrawCmd &d, mlv_texture2d t) {
-    if (d.rtv == t || d.dsv == t || d.vis_tri == t || d.vis_draw == t || d.vis_bary == t) return true;
+    if (d.rtv == t || d.dsv == t || d.vis_tri == t || d.vis_draw == t || d.vis_bary == t || d.vis_prim == t)
+        return true;
     return d.desc.vs_tex.data == t->ptr || d.desc.ps_tex.data == t->ptr;
 }
 
@@ -1198,7 +1208,7 @@ static mlv_status build_draw(mlv_context c, uint32_t count, uint32_t start, int3
     d.vs_tex = tex_desc(vt);
     d.ps_tex = tex_desc(pt);
     auto vis_ok = [&](mlv_texture2d t) { return !t || (t->width == s.rtv->width && t->height == s.rtv->height); };
-    if (!vis_ok(s.vis_tri) || !vis_ok(s.vis_draw) || !vis_ok(s.vis_bary))
+    if (!vis_ok(s.vis_tri) || !vis_ok(s.vis_draw) || !vis_ok(s.vis_bary) || !vis_ok(s.vis_prim))
         return fail(MLV_ERROR_INVALID_STATE, "visibility targets must match the render target size");
     d.draw_seq = s.rtv->draws_since_clear++;
     out.rtv = s.rtv;
@@ -1206,6 +1216,7 @@ static mlv_status build_draw(mlv_context c, uint32_t count, uint32_t start, int3
     out.vis_tri = s.vis_tri;
     out.vis_draw = s.vis_draw;
     out.vis_bary = s.vis_bary;
+    out.vis_prim = s.vis_prim;
     out.index_count = count;
     return MLV_OK;
 }

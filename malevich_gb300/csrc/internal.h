@@ -54,11 +54,12 @@ struct ViewDesc {
     uint32_t *vis_tri;                   // optional visibility outputs
     uint32_t *vis_draw;
     float *vis_bary;
+    uint32_t *vis_prim;                  // input triangle index within its draw (differentiable path)
     uint32_t width, height, tiles_x, tiles_y;
     uint32_t tile_base;                  // first tile of this view in the batch's tile space
     uint32_t draw_begin, draw_count;     // the view's draws are contiguous in the draw array
     uint32_t bin_base;                   // bin of (tile t, draw d) = bin_base + t * draw_count + d
-    uint32_t pad[2];
+    uint32_t pad[4];
 };
 
 // Per assembled triangle, read by the tile kernel for every (tile, triangle) pair: 64 bytes.

@@ -944,6 +944,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
             V.vis_tri[o] = bp.rank[g] - bp.rank[D.tri_begin] + below;
         }
         if (V.vis_draw) V.vis_draw[o] = D.draw_seq;
+        if (V.vis_prim) V.vis_prim[o] = (key >> 3) - D.tri_begin;
         if (V.vis_bary) reinterpret_cast<float2 *>(V.vis_bary)[o] = make_float2(b1, b2);
     }
     if (lane == 0) {

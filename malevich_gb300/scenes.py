@@ -492,3 +492,61 @@ def frame_from_arrays(z, prefix="frame"):
                              ps_tex=texs.get("ps_tex"), viewport=tuple(float(v) for v in z[p + "viewport"]),
                              cull=cull, depth_func=df, start_index=si, base_vertex=bv))
     return fr
+
+
+# ------------------------------------------------------------------ differentiable scenes
+
+def diff_scene(seed=4, n_views=16, size=512, freq=50, tex_size=1024, heightfield_cells=None):
+    """The differentiable configuration: a geodesic sphere of 20*freq^2 triangles (freq 50: 50,000)
+    or, with heightfield_cells, a heightfield of 2*cells^2 triangles; per-vertex colours U(0,1),
+    UVs, an RGBA32F texture U(0,1); per view a seeded rotation and perspective projection into the
+    passthrough screen space [0,1]^2 (x, y) with depth z in (0,1). Returns a dict of arrays."""
+    rng = np.random.default_rng(seed)
+    if heightfield_cells:
+        v, faces = heightfield(rng, heightfield_cells, 2.0, 0.4)
+        P = v[:, 0:3].astype(np.float64)
+        uv = v[:, 6:8].astype(np.float32)
+    else:
+        dirs, faces = geodesic_sphere(freq)
+        P = dirs
+        uv = sphere_vertices(dirs, np.ones(len(dirs)))[:, 6:8]
+    n = len(P)
+    col = rng.random((n, 3)).astype(np.float32)
+    tex = rng.random((tex_size, tex_size, 4)).astype(np.float32)
+    pos = np.zeros((n_views, n, 2), np.float32)
+    z = np.zeros((n_views, n), np.float32)
+    for k in range(n_views):
+        q = rng.standard_normal(4)
+        q /= np.linalg.norm(q)
+        a, b, c, d = q
+        R = np.array([[a * a + b * b - c * c - d * d, 2 * (b * c - a * d), 2 * (b * d + a * c)],
+                      [2 * (b * c + a * d), a * a - b * b + c * c - d * d, 2 * (c * d - a * b)],
+                      [2 * (b * d - a * c), 2 * (c * d + a * b), a * a - b * b - c * c + d * d]])
+        Q = P @ R.T
+        dist = 3.0 if not heightfield_cells else 3.2
+        depth = Q[:, 2] + dist
+        f = 1.0 / np.tan(np.radians(50.0) / 2)
+        pos[k, :, 0] = 0.5 + 0.5 * f * Q[:, 0] / depth
+        pos[k, :, 1] = 0.5 + 0.5 * f * Q[:, 1] / depth
+        z[k] = (depth / (dist + 2.0)).astype(np.float32)
+    return {"ib": faces.astype(np.uint32), "col": col, "uv": uv.astype(np.float32), "tex": tex, "pos": pos, "z": z,
+            "width": size, "height": size}
+
+
+def diff_frames(scene, pos=None, col=None, uv=None):
+    """One frame per view drawing the scene with MLV_VS_PASSTHROUGH_UV + COLOR_TIMES_TEXEL (depth LESS
+    cleared to 1, no culling): the exact rasteriser's visibility for the differentiable path."""
+    pos = scene["pos"] if pos is None else pos
+    col = scene["col"] if col is None else col
+    uv = scene["uv"] if uv is None else uv
+    tex = Texture(scene["tex"], FMT_RGBA32F)
+    ib = pad_indices(scene["ib"])
+    n_tris = len(scene["ib"])
+    frames = []
+    for k in range(pos.shape[0]):
+        vb = np.concatenate([pos[k], scene["z"][k][:, None], col, uv], axis=1).astype(np.float32)
+        d = Draw(VS_PASSTHROUGH_UV, PS_COLOR_TIMES_TEXEL, vb, ib, 3 * n_tris, ps_tex=tex,
+                 viewport=(0.0, 0.0, float(scene["width"]), float(scene["height"]), 0.0, 1.0),
+                 cull=CULL_NONE, depth_func=DEPTH_LESS)
+        frames.append(Frame(scene["width"], scene["height"], [d], clear_color=(0.0, 0.0, 0.0, 0.0), clear_depth=1.0))
+    return frames

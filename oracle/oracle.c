@@ -17,6 +17,7 @@
 typedef struct vtx { float r[3][4]; } vtx;   /* 3 output registers of a vertex (main.c:117-119) */
 
 typedef struct tri_rec {                       /* Triangle + Setup (main.c:121-139) */
+    uint32_t input;                            /* input triangle index within the draw */
     int32_t e[3][3];                           /* edge functions a, b, c */
     float rw[3], inv_area, zbound;
     int32_t minx, miny, maxx, maxy;
@@ -314,6 +315,7 @@ void orc_clear_color(orc_target *t, const float rgba[4]) {
     for (size_t i = 0; i < n; ++i) t->color[i] = v;
     if (t->vis_tri) for (size_t i = 0; i < n; ++i) t->vis_tri[i] = 0xFFFFFFFFu;
     if (t->vis_draw) for (size_t i = 0; i < n; ++i) t->vis_draw[i] = 0xFFFFFFFFu;
+    if (t->vis_prim) for (size_t i = 0; i < n; ++i) t->vis_prim[i] = 0xFFFFFFFFu;
     if (t->vis_bary) for (size_t i = 0; i < 2 * n; ++i) t->vis_bary[i] = 0.f;
 }
 
@@ -389,7 +391,7 @@ static void push_tri(tri_buf *b, const tri_rec *r) {
 }
 
 /* primitive_assembly_stage body for one input triangle, main.c:753-907 */
-static int assemble(const orc_draw *d, const float vout[3][12], tri_buf *out) {
+static int assemble(const orc_draw *d, const float vout[3][12], uint32_t input, tri_buf *out) {
     const float *p0 = vout[0], *p1 = vout[1], *p2 = vout[2];
     if (p0[3] == 0 || p1[3] == 0 || p2[3] == 0) return 0;
     if ((p0[0] < -p0[3] && p1[0] < -p1[3] && p2[0] < -p2[3]) ||
@@ -434,6 +436,7 @@ static int assemble(const orc_draw *d, const float vout[3][12], tri_buf *out) {
         if (d->cull == ORC_CULL_BACK && area > 0) continue;
         if (d->cull == ORC_CULL_FRONT && area < 0) continue;
         tri_rec r;
+        r.input = input;
         set_edge(r.e[2], area, x[0], y[0], x[1], y[1]);
         set_edge(r.e[0], area, x[1], y[1], x[2], y[2]);
         set_edge(r.e[1], area, x[2], y[2], x[0], y[0]);
@@ -516,7 +519,7 @@ int orc_draw_indexed(orc_target *t, const orc_draw *d, uint32_t draw_seq, orc_st
                 orc_run_vs(d->vs, vin, d->cb, &d->vs_tex, vout[k]);
             }
             if (bad) break;
-            nclipped += (uint64_t)assemble(d, (const float(*)[12])vout, &chunks[c]);
+            nclipped += (uint64_t)assemble(d, (const float(*)[12])vout, i, &chunks[c]);
         }
     }
     if (bad) {
@@ -588,7 +591,7 @@ int orc_draw_indexed(orc_target *t, const orc_draw *d, uint32_t draw_seq, orc_st
     for (size_t k = 0; k < active; ++k) {
         const uint32_t b = active_list[k];
         const int32_t x0 = (int32_t)(b % (uint32_t)tx) * TILE, y0 = (int32_t)(b / (uint32_t)tx) * TILE;
-        uint32_t tcol[64], ttri[64], tdraw[64];
+        uint32_t tcol[64], ttri[64], tdraw[64], tprim[64];
         float tdep[64], tbary[128];
         uint8_t valid[64];
         for (int j = 0; j < 8; ++j)
@@ -601,6 +604,7 @@ int orc_draw_indexed(orc_target *t, const orc_draw *d, uint32_t draw_seq, orc_st
                 tdep[p] = valid[p] ? t->depth[o] : 0.f;
                 if (t->vis_tri) ttri[p] = valid[p] ? t->vis_tri[o] : 0;
                 if (t->vis_draw) tdraw[p] = valid[p] ? t->vis_draw[o] : 0;
+                if (t->vis_prim) tprim[p] = valid[p] ? t->vis_prim[o] : 0;
                 if (t->vis_bary) { tbary[2 * p] = valid[p] ? t->vis_bary[2 * o] : 0; tbary[2 * p + 1] = valid[p] ? t->vis_bary[2 * o + 1] : 0; }
             }
         const float hiz = less ? t->tile_max[b] : t->tile_min[b];
@@ -655,6 +659,7 @@ int orc_draw_indexed(orc_target *t, const orc_draw *d, uint32_t draw_seq, orc_st
                 tdep[p] = z;
                 ttri[p] = ids[q];
                 tdraw[p] = draw_seq;
+                tprim[p] = r->input;
                 tbary[2 * p] = b1; tbary[2 * p + 1] = b2;
                 ++frags;
             }
@@ -669,6 +674,7 @@ int orc_draw_indexed(orc_target *t, const orc_draw *d, uint32_t draw_seq, orc_st
                 t->depth[o] = tdep[p];
                 if (t->vis_tri) t->vis_tri[o] = ttri[p];
                 if (t->vis_draw) t->vis_draw[o] = tdraw[p];
+                if (t->vis_prim) t->vis_prim[o] = tprim[p];
                 if (t->vis_bary) { t->vis_bary[2 * o] = tbary[2 * p]; t->vis_bary[2 * o + 1] = tbary[2 * p + 1]; }
                 mnz = mn(mnz, tdep[p]);
                 mxz = mx(mxz, tdep[p]);

@@ -65,6 +65,7 @@ typedef struct orc_target {
     uint32_t *vis_tri;           /* optional: assembled triangle index of the last writer */
     uint32_t *vis_draw;          /* optional: draw sequence number of the last writer */
     float *vis_bary;             /* optional: 2 floats per pixel, quantised (b1, b2) */
+    uint32_t *vis_prim;          /* optional: input triangle index (within its draw) of the last writer */
 } orc_target;
 
 typedef struct orc_stats {
@@ -97,6 +98,30 @@ void orc_clear_depth(orc_target *t, float depth);
 int orc_draw_indexed(orc_target *t, const orc_draw *d, uint32_t draw_seq, orc_stats *stats,
                      orc_capture *cap);
 void orc_capture_free(orc_capture *cap);
+
+/* Differentiable shading model in FP64 (oracle_adjoint.c): vertex colour times a bilinear RGBA32F
+ * texel, continuous barycentrics at the pixel corner under fixed visibility (prim). */
+typedef struct orc_diff_scene {
+    uint32_t n_verts, n_tris;
+    const uint32_t *ib;          /* 3 * n_tris */
+    const double *col;           /* 3 * n_verts */
+    const double *uv;            /* 2 * n_verts */
+    const double *tex;           /* th * tw * 4 */
+    uint32_t tw, th;
+} orc_diff_scene;
+
+typedef struct orc_diff_view {
+    uint32_t width, height;
+    const double *pos;           /* 2 * n_verts: passthrough x, y in [0,1] */
+    const uint32_t *prim;        /* width * height: input triangle or 0xFFFFFFFF */
+    const double *target;        /* width * height * 3 */
+    const int32_t *cells;        /* optional frozen bilinear cells (s0, t0) per pixel */
+} orc_diff_view;
+
+double orc_diff_loss(const orc_diff_scene *s, const orc_diff_view *views, uint32_t nviews, double *image);
+void orc_diff_cells(const orc_diff_scene *s, const orc_diff_view *v, int32_t *cells);
+void orc_diff_grad(const orc_diff_scene *s, const orc_diff_view *views, uint32_t nviews, double *g_col,
+                   double *g_tex, double *g_pos);
 
 /* Building blocks exposed for the known-answer tests. */
 uint32_t orc_encode_clear_color(const float rgba[4]);

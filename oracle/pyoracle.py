@@ -40,7 +40,8 @@ class OrcDraw(ctypes.Structure):
 class OrcTarget(ctypes.Structure):
     _fields_ = [("color", ctypes.c_void_p), ("depth", ctypes.c_void_p), ("width", ctypes.c_uint32),
                 ("height", ctypes.c_uint32), ("tile_min", ctypes.c_void_p), ("tile_max", ctypes.c_void_p),
-                ("vis_tri", ctypes.c_void_p), ("vis_draw", ctypes.c_void_p), ("vis_bary", ctypes.c_void_p)]
+                ("vis_tri", ctypes.c_void_p), ("vis_draw", ctypes.c_void_p), ("vis_bary", ctypes.c_void_p),
+                ("vis_prim", ctypes.c_void_p)]
 
 
 class OrcStats(ctypes.Structure):
@@ -140,12 +141,13 @@ def render_oracle(frame, capture=False, threads=None):
     vis_tri = np.full((h, w), 0xFFFFFFFF, np.uint32)
     vis_draw = np.full((h, w), 0xFFFFFFFF, np.uint32)
     vis_bary = np.zeros((h, w, 2), np.float32)
+    vis_prim = np.full((h, w), 0xFFFFFFFF, np.uint32)
     if frame.initial_color is not None:
         color[...] = frame.initial_color
     if frame.initial_depth is not None:
         depth[...] = frame.initial_depth
     tgt = OrcTarget(_ptr(color), _ptr(depth), w, h, _ptr(tile_min), _ptr(tile_max), _ptr(vis_tri),
-                    _ptr(vis_draw), _ptr(vis_bary))
+                    _ptr(vis_draw), _ptr(vis_bary), _ptr(vis_prim))
     if frame.clear_color is not None:
         lib.orc_clear_color(ctypes.byref(tgt), (ctypes.c_float * 4)(*frame.clear_color))
     if frame.clear_depth is not None:
@@ -165,7 +167,7 @@ def render_oracle(frame, capture=False, threads=None):
             lib.orc_capture_free(ctypes.byref(cap))
     return {
         "color": color, "depth": depth, "vis_tri": vis_tri, "vis_draw": vis_draw, "vis_bary": vis_bary,
-        "tile_min": tile_min, "tile_max": tile_max,
+        "vis_prim": vis_prim, "tile_min": tile_min, "tile_max": tile_max,
         "stats": {k: int(getattr(stats, k)) for k, _ in OrcStats._fields_},
         "captures": caps,
     }
@@ -313,3 +315,72 @@ def render_reference(frame, capture=False, threads=1):
                   "active_bin_count": st[3], "total_triangle_count_in_bins": st[4]},
         "captures": caps,
     }
+
+
+# ------------------------------------------------------------------ differentiable model (FP64)
+
+class OrcDiffScene(ctypes.Structure):
+    _fields_ = [("n_verts", ctypes.c_uint32), ("n_tris", ctypes.c_uint32), ("ib", ctypes.c_void_p),
+                ("col", ctypes.c_void_p), ("uv", ctypes.c_void_p), ("tex", ctypes.c_void_p),
+                ("tw", ctypes.c_uint32), ("th", ctypes.c_uint32)]
+
+
+class OrcDiffView(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("pos", ctypes.c_void_p),
+                ("prim", ctypes.c_void_p), ("target", ctypes.c_void_p), ("cells", ctypes.c_void_p)]
+
+
+class DiffModel:
+    """FP64 differentiable shading (oracle_adjoint.c) over fixed visibility: loss, image, adjoint."""
+
+    def __init__(self, ib, col, uv, tex, views):
+        """ib (T,3) uint32; col (N,3); uv (N,2); tex (th,tw,4); views: list of dicts with keys
+        width, height, pos (N,2), prim (H,W) uint32, target (H,W,3)."""
+        self.lib = oracle_lib()
+        self.lib.orc_diff_loss.restype = ctypes.c_double
+        self.lib.orc_diff_loss.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p]
+        self.lib.orc_diff_grad.argtypes = [ctypes.c_void_p] * 2 + [ctypes.c_uint32] + [ctypes.c_void_p] * 3
+        self.lib.orc_diff_cells.argtypes = [ctypes.c_void_p] * 3
+        self.ib = np.ascontiguousarray(ib, np.uint32)
+        self.col = np.ascontiguousarray(col, np.float64)
+        self.uv = np.ascontiguousarray(uv, np.float64)
+        self.tex = np.ascontiguousarray(tex, np.float64)
+        self.views = [dict(v) for v in views]
+        for v in self.views:
+            v["pos"] = np.ascontiguousarray(v["pos"], np.float64)
+            v["prim"] = np.ascontiguousarray(v["prim"], np.uint32)
+            v["target"] = np.ascontiguousarray(v["target"], np.float64)
+            v["cells"] = None
+
+    def _structs(self):
+        sc = OrcDiffScene(len(self.col), len(self.ib), _ptr(self.ib), _ptr(self.col), _ptr(self.uv), _ptr(self.tex),
+                          self.tex.shape[1], self.tex.shape[0])
+        arr = (OrcDiffView * len(self.views))()
+        for i, v in enumerate(self.views):
+            arr[i] = OrcDiffView(v["width"], v["height"], _ptr(v["pos"]), _ptr(v["prim"]), _ptr(v["target"]),
+                                 _ptr(v["cells"]) if v["cells"] is not None else None)
+        return sc, arr
+
+    def freeze_cells(self):
+        """Holds each pixel's bilinear cell fixed (the loss becomes smooth in the positions)."""
+        sc, arr = self._structs()
+        for i, v in enumerate(self.views):
+            cells = np.zeros((v["height"], v["width"], 2), np.int32)
+            self.lib.orc_diff_cells(ctypes.byref(sc), ctypes.byref(arr[i]), _ptr(cells))
+            v["cells"] = cells
+
+    def loss(self, image=False):
+        sc, arr = self._structs()
+        img = None
+        if image:
+            img = np.zeros((len(self.views), self.views[0]["height"], self.views[0]["width"], 3), np.float64)
+        val = self.lib.orc_diff_loss(ctypes.byref(sc), arr, len(self.views), _ptr(img) if img is not None else None)
+        return (val, img) if image else val
+
+    def grad(self):
+        sc, arr = self._structs()
+        g_col = np.zeros_like(self.col)
+        g_tex = np.zeros_like(self.tex)
+        g_pos = np.zeros((len(self.views),) + self.col.shape[:1] + (2,), np.float64)
+        self.lib.orc_diff_grad(ctypes.byref(sc), arr, len(self.views), _ptr(g_col), _ptr(g_tex), _ptr(g_pos))
+        return g_col, g_tex, g_pos

@@ -1,0 +1,106 @@
+"""Test harness for the differentiable path: a torch.autograd.Function over the C ABI's
+mlv_diff_forward / mlv_diff_backward, and the visibility pass through the exact rasteriser.
+Used by the tests and by bench.py's differentiable sections only; the product is the C ABI."""
+import ctypes
+
+import numpy as np
+import torch
+
+from malevich_gb300 import api, scenes
+
+
+class DiffDesc(ctypes.Structure):
+    _fields_ = [("n_verts", ctypes.c_uint32), ("n_tris", ctypes.c_uint32), ("index_buffer", ctypes.c_void_p),
+                ("colors", ctypes.c_void_p), ("uvs", ctypes.c_void_p), ("texture", ctypes.c_void_p),
+                ("tex_width", ctypes.c_uint32), ("tex_height", ctypes.c_uint32), ("num_views", ctypes.c_uint32),
+                ("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("positions", ctypes.c_void_p),
+                ("primitive_ids", ctypes.c_void_p), ("barycentrics", ctypes.c_void_p), ("image", ctypes.c_void_p),
+                ("grad_image", ctypes.c_void_p), ("grad_colors", ctypes.c_void_p), ("grad_texture", ctypes.c_void_p),
+                ("grad_positions", ctypes.c_void_p)]
+
+
+def _p(t):
+    return t.data_ptr() if t is not None else None
+
+
+def visibility(device, scene, pos=None):
+    """Per-view primitive ids (the input triangle each pixel shows) from the exact rasteriser,
+    all views in one batched command list."""
+    frames = scenes.diff_frames(scene, pos=pos)
+    r = api.FrameRenderer(device, frames, primitive_ids=True)
+    r.render_batched()
+    prims = np.stack([r.read(i)["vis_prim"] for i in range(len(frames))])
+    r.destroy()
+    return prims
+
+
+class _DeviceArray:
+    """A tightly packed device texture exposed through __cuda_array_interface__ (no copy)."""
+
+    def __init__(self, ptr, shape, typestr):
+        self.__cuda_array_interface__ = {"shape": shape, "typestr": typestr, "data": (ptr, False), "version": 2}
+
+
+def gather_primitive_ids(renderer, out):
+    """Copies every view's primitive-id target of a FrameRenderer into out[views, H, W] (int32),
+    on torch's current stream, after the renderer's context has finished."""
+    for i, t in enumerate(renderer.prim_targets):
+        fr = renderer.frames[i]
+        out[i].copy_(torch.as_tensor(_DeviceArray(t.device_pointer(), (fr.height, fr.width), "<i4"), device="cuda"))
+    return out
+
+
+class DiffScene:
+    """Device-side topology, UVs, visibility and the checkpoint (barycentric) buffer."""
+
+    def __init__(self, scene, prims):
+        dev = "cuda"
+        self.ib = torch.from_numpy(np.ascontiguousarray(scene["ib"]).view(np.int32)).to(dev)
+        self.uv = torch.from_numpy(np.ascontiguousarray(scene["uv"], np.float32)).to(dev)
+        self.prim = torch.from_numpy(np.ascontiguousarray(prims).view(np.int32)).to(dev)
+        self.views, self.height, self.width = prims.shape
+        self.n_verts = scene["col"].shape[0]
+        self.n_tris = scene["ib"].shape[0]
+        self.bary = torch.zeros((self.views, self.height, self.width, 2), dtype=torch.float32, device=dev)
+        self.mask = (self.prim != -1).unsqueeze(-1).float()
+
+    def desc(self, col, tex, pos, image=None, grad_image=None, g_col=None, g_tex=None, g_pos=None):
+        return DiffDesc(self.n_verts, self.n_tris, _p(self.ib), _p(col), _p(self.uv), _p(tex), tex.shape[1],
+                        tex.shape[0], self.views, self.width, self.height, _p(pos), _p(self.prim), _p(self.bary),
+                        _p(image), _p(grad_image), _p(g_col), _p(g_tex), _p(g_pos))
+
+
+class DiffRender(torch.autograd.Function):
+    """image = render(colors, texture, positions) under the scene's fixed visibility."""
+
+    @staticmethod
+    def forward(ctx, col, tex, pos, scene):
+        lib = api.load_library()
+        col, tex, pos = col.contiguous(), tex.contiguous(), pos.contiguous()
+        image = torch.empty((scene.views, scene.height, scene.width, 3), dtype=torch.float32, device=col.device)
+        d = scene.desc(col, tex, pos, image=image)
+        st = lib.mlv_diff_forward(ctypes.byref(d), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+        if st != 0:
+            raise api.MalevichError(st, lib.mlv_get_last_error_string().decode())
+        ctx.scene = scene
+        ctx.save_for_backward(col, tex, pos)
+        return image
+
+    @staticmethod
+    def backward(ctx, grad_image):
+        lib = api.load_library()
+        col, tex, pos = ctx.saved_tensors
+        scene = ctx.scene
+        g_col = torch.zeros_like(col) if ctx.needs_input_grad[0] else None
+        g_tex = torch.zeros_like(tex) if ctx.needs_input_grad[1] else None
+        g_pos = torch.zeros_like(pos) if ctx.needs_input_grad[2] else None
+        gi = grad_image.contiguous()
+        d = scene.desc(col, tex, pos, grad_image=gi, g_col=g_col, g_tex=g_tex, g_pos=g_pos)
+        st = lib.mlv_diff_backward(ctypes.byref(d), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+        if st != 0:
+            raise api.MalevichError(st, lib.mlv_get_last_error_string().decode())
+        return g_col, g_tex, g_pos, None
+
+
+def l2_loss(image, target, scene):
+    return (((image - target) * scene.mask) ** 2).sum()
