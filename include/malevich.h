@@ -337,11 +337,16 @@ MLV_API mlv_status mlv_get_tile_infos(mlv_context context, uint32_t *tile_index,
  * barycentrics at the reference's sample point (the pixel corner), for MLV_VS_PASSTHROUGH_UV-style
  * vertices: screen positions x, y in [0,1] (X = W x, Y = H (1 - y), w = 1), a colour and a UV per
  * vertex, and the pixel shader colour * bilinear(RGBA32F texture, uv).xyz.
+ * A covered pixel whose continuous barycentrics are not all >= -1/8 is dropped (shades to 0, no
+ * gradient): the 28.4 snap moves a vertex by at most 1/32 pixel, so only corners the snap pulled
+ * into slivers under 1/4 pixel high are dropped, where the barycentrics extrapolate without bound.
  * mlv_diff_forward writes the image and the per-pixel barycentrics (the checkpoint);
  * mlv_diff_backward reads the checkpoint and grad_image = dL/dimage, recomputes the interpolation
  * and ADDS dL/dcolors, dL/dtexture (scattered through the bilinear weights) and dL/dpositions (the
  * barycentric terms, visibility fixed) into the gradient arrays it is given (any may be NULL).
- * All pointers are device memory; both calls are asynchronous on `cuda_stream`. */
+ * All pointers are device memory (positions, uvs, barycentrics 8-byte aligned, texture 16-byte);
+ * both calls are asynchronous on `cuda_stream`; the backward needs the checkpoint of a forward
+ * with the same positions. */
 typedef struct mlv_diff_desc {
     uint32_t n_verts, n_tris;
     const uint32_t *index_buffer;     /* 3 * n_tris */
@@ -352,7 +357,8 @@ typedef struct mlv_diff_desc {
     uint32_t num_views, width, height;
     const float *positions;           /* num_views * n_verts * 2 */
     const uint32_t *primitive_ids;    /* num_views * height * width; 0xFFFFFFFF: background */
-    float *barycentrics;              /* num_views * height * width * 2 (written by the forward) */
+    float *barycentrics;              /* num_views * height * width * 2 (written by the forward;
+                                         (-1, -1) marks a dropped pixel) */
     float *image;                     /* num_views * height * width * 3 (forward output) */
     const float *grad_image;          /* num_views * height * width * 3 (backward input) */
     float *grad_colors, *grad_texture, *grad_positions;

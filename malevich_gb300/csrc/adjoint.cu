@@ -29,10 +29,6 @@ namespace {
 
 constexpr int kDiffBlock = 256;
 
-struct Texel4 {
-    float v[3];
-};
-
 __device__ __forceinline__ int32_t clampi(int32_t x, int32_t hi) { return x < 0 ? 0 : (x > hi ? hi : x); }
 
 __device__ __forceinline__ float3 texel(const float *tex, uint32_t tw, uint32_t th, int32_t i, int32_t j) {
@@ -49,37 +45,104 @@ struct PixelEval {
     uint32_t vi[3];
 };
 
-// Interpolation and texture filtering for one covered pixel from its barycentrics.
-__device__ __forceinline__ void shade(const mlv_diff_desc &d, float l1, float l2, uint32_t tri, PixelEval &e) {
+// a d - b c with Kahan's FMA algorithm (error within 2 ulp; Jeannerod, Louvet and Muller, "Further
+// analysis of Kahan's algorithm for the accurate computation of 2x2 determinants", Math. Comp. 2013).
+__device__ __forceinline__ float det2(float a, float b, float c, float d) {
+    const float w = b * c;
+    const float e = fmaf(-b, c, w);
+    const float f = fmaf(a, d, -w);
+    return f + e;
+}
+
+// The differentiable coverage: a pixel the rasteriser gave to a triangle counts when its corner's
+// continuous barycentrics are all >= -1/8. The 28.4 snap moves a vertex by at most 1/32 pixel, so
+// every covered corner of a triangle whose heights exceed 1/4 pixel passes; the corners it drops
+// are those the snap pulled into slivers, where the continuous barycentrics extrapolate without
+// bound. A dropped pixel shades to 0 and its checkpoint holds kDropped.
+constexpr float kMinBarycentric = -0.125f;
+constexpr float kDropped = -1.0f;
+
+// The triangle relative to the pixel corner p = (x, y), in screen space X = W px, Y = H (1 - py):
+// a, b, c = v0 - p, v1 - p, v2 - p (one rounding each: fmaf of the exact product and the exact
+// integer offset), the edges e1 = v1 - v0, e2 = v2 - v0 from coordinate differences, and twice the
+// signed area A = cross(e1, e2).
+struct CornerGeom {
+    float ax, ay, bx, by, cx, cy;
+    float e1x, e1y, e2x, e2y, A;
+};
+
+__device__ __forceinline__ void corner_geometry(const float *pos, const uint32_t vi[3], float W, float H, float x,
+                                                float y, CornerGeom &g) {
+    const float2 p0 = __ldg(reinterpret_cast<const float2 *>(pos) + vi[0]);
+    const float2 p1 = __ldg(reinterpret_cast<const float2 *>(pos) + vi[1]);
+    const float2 p2 = __ldg(reinterpret_cast<const float2 *>(pos) + vi[2]);
+    const float hy = H - y;
+    g.ax = fmaf(W, p0.x, -x);
+    g.ay = fmaf(-H, p0.y, hy);
+    g.bx = fmaf(W, p1.x, -x);
+    g.by = fmaf(-H, p1.y, hy);
+    g.cx = fmaf(W, p2.x, -x);
+    g.cy = fmaf(-H, p2.y, hy);
+    g.e1x = W * (p1.x - p0.x);
+    g.e1y = H * (p0.y - p1.y);
+    g.e2x = W * (p2.x - p0.x);
+    g.e2y = H * (p0.y - p2.y);
+    g.A = det2(g.e1x, g.e2x, g.e1y, g.e2y);
+}
+
+__device__ __forceinline__ void load_triangle(const mlv_diff_desc &d, uint32_t tri, uint32_t vi[3]) {
+    vi[0] = __ldg(d.index_buffer + 3 * (size_t)tri);
+    vi[1] = __ldg(d.index_buffer + 3 * (size_t)tri + 1);
+    vi[2] = __ldg(d.index_buffer + 3 * (size_t)tri + 2);
+}
+
+// Interpolation and texture filtering for one covered pixel from its barycentrics. The texel
+// coordinates s = tw u - 1/2, t = th (1 - v) - 1/2 are formed as (vertex 0's coordinate, split
+// exactly into an integer and a fraction) + (the barycentric deltas), so the bilinear fractions
+// keep full single precision whatever the texture size.
+__device__ __forceinline__ void shade(const mlv_diff_desc &d, float l1, float l2, const uint32_t vi[3], PixelEval &e) {
     e.l1 = l1;
     e.l2 = l2;
     e.l0 = 1.0f - l1 - l2;
-    const float l[3] = {e.l0, e.l1, e.l2};
-    float u = 0.f, v = 0.f;
+    e.vi[0] = vi[0];
+    e.vi[1] = vi[1];
+    e.vi[2] = vi[2];
+    const float2 uv0 = __ldg(reinterpret_cast<const float2 *>(d.uvs) + vi[0]);
+    const float2 uv1 = __ldg(reinterpret_cast<const float2 *>(d.uvs) + vi[1]);
+    const float2 uv2 = __ldg(reinterpret_cast<const float2 *>(d.uvs) + vi[2]);
+    const float l[3] = {e.l0, l1, l2};
     e.col = make_float3(0.f, 0.f, 0.f);
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        const uint32_t q = __ldg(d.index_buffer + 3 * (size_t)tri + k);
-        e.vi[k] = q;
-        e.col.x += l[k] * __ldg(d.colors + 3 * (size_t)q);
-        e.col.y += l[k] * __ldg(d.colors + 3 * (size_t)q + 1);
-        e.col.z += l[k] * __ldg(d.colors + 3 * (size_t)q + 2);
-        u += l[k] * __ldg(d.uvs + 2 * (size_t)q);
-        v += l[k] * __ldg(d.uvs + 2 * (size_t)q + 1);
+        const float *c = d.colors + 3 * (size_t)vi[k];
+        e.col.x += l[k] * __ldg(c);
+        e.col.y += l[k] * __ldg(c + 1);
+        e.col.z += l[k] * __ldg(c + 2);
     }
-    const float sf = (float)d.tex_width * u - 0.5f, tf = (float)d.tex_height * (1.0f - v) - 0.5f;
-    e.s0 = (int32_t)floorf(sf);
-    e.t0 = (int32_t)floorf(tf);
-    e.fs = sf - (float)e.s0;
-    e.ft = tf - (float)e.t0;
+    const float tw = (float)d.tex_width, th = (float)d.tex_height;
+    // s at vertex 0: tw u0 = ps + pse exactly; ps - 1/2 is exact below 2^22
+    const float ps = tw * uv0.x, pse = fmaf(tw, uv0.x, -ps);
+    const float bs = ps - 0.5f, fbs = floorf(bs);
+    // t at vertex 0: (th - 1/2) - th v0, with th v0 = q + qe exactly and the difference by two-sum
+    const float q = th * uv0.y, qe = fmaf(th, uv0.y, -q);
+    const float a = th - 0.5f, r = a - q, rb = r - a;
+    const float re = (a - (r - rb)) + (-q - rb);
+    const float fbt = floorf(r);
+    const float rs = ((bs - fbs) + pse) + (l1 * (tw * (uv1.x - uv0.x)) + l2 * (tw * (uv2.x - uv0.x)));
+    const float rt = ((r - fbt) + (re - qe)) - (l1 * (th * (uv1.y - uv0.y)) + l2 * (th * (uv2.y - uv0.y)));
+    const float frs = floorf(rs), frt = floorf(rt);
+    e.s0 = (int32_t)fbs + (int32_t)frs;
+    e.t0 = (int32_t)fbt + (int32_t)frt;
+    e.fs = rs - frs;
+    e.ft = rt - frt;
     const float3 t00 = texel(d.texture, d.tex_width, d.tex_height, e.s0, e.t0);
     const float3 t10 = texel(d.texture, d.tex_width, d.tex_height, e.s0 + 1, e.t0);
     const float3 t01 = texel(d.texture, d.tex_width, d.tex_height, e.s0, e.t0 + 1);
     const float3 t11 = texel(d.texture, d.tex_width, d.tex_height, e.s0 + 1, e.t0 + 1);
-    const float a = 1.f - e.fs, b = 1.f - e.ft;
-    e.tex.x = b * (a * t00.x + e.fs * t10.x) + e.ft * (a * t01.x + e.fs * t11.x);
-    e.tex.y = b * (a * t00.y + e.fs * t10.y) + e.ft * (a * t01.y + e.fs * t11.y);
-    e.tex.z = b * (a * t00.z + e.fs * t10.z) + e.ft * (a * t01.z + e.fs * t11.z);
+    const float oa = 1.f - e.fs, ob = 1.f - e.ft;
+    e.tex.x = ob * (oa * t00.x + e.fs * t10.x) + e.ft * (oa * t01.x + e.fs * t11.x);
+    e.tex.y = ob * (oa * t00.y + e.fs * t10.y) + e.ft * (oa * t01.y + e.fs * t11.y);
+    e.tex.z = ob * (oa * t00.z + e.fs * t10.z) + e.ft * (oa * t01.z + e.fs * t11.z);
 }
 
 __global__ void __launch_bounds__(kDiffBlock) k_diff_forward(mlv_diff_desc d) {
@@ -92,24 +155,23 @@ __global__ void __launch_bounds__(kDiffBlock) k_diff_forward(mlv_diff_desc d) {
     float3 out = make_float3(0.f, 0.f, 0.f);
     float2 bary = make_float2(0.f, 0.f);
     if (tri != 0xFFFFFFFFu && tri < d.n_tris) {
-        const float W = (float)d.width, H = (float)d.height;
-        const float x = (float)(p % d.width), y = (float)(p / d.width);
-        const float *pos = d.positions + (size_t)view * d.n_verts * 2;
-        float X[3], Y[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            const uint32_t q = __ldg(d.index_buffer + 3 * (size_t)tri + k);
-            X[k] = W * __ldg(pos + 2 * (size_t)q);
-            Y[k] = H * (1.0f - __ldg(pos + 2 * (size_t)q + 1));
-        }
-        const float A = (X[1] - X[0]) * (Y[2] - Y[0]) - (X[2] - X[0]) * (Y[1] - Y[0]);
-        if (A != 0.0f) {
-            const float l1 = ((X[2] - x) * (Y[0] - y) - (Y[2] - y) * (X[0] - x)) / A;
-            const float l2 = ((X[0] - x) * (Y[1] - y) - (Y[0] - y) * (X[1] - x)) / A;
-            PixelEval e;
-            shade(d, l1, l2, tri, e);
-            out = make_float3(e.col.x * e.tex.x, e.col.y * e.tex.y, e.col.z * e.tex.z);
-            bary = make_float2(l1, l2);
+        uint32_t vi[3];
+        load_triangle(d, tri, vi);
+        CornerGeom g;
+        corner_geometry(d.positions + (size_t)view * d.n_verts * 2, vi, (float)d.width, (float)d.height,
+                        (float)(p % d.width), (float)(p / d.width), g);
+        bary = make_float2(kDropped, kDropped);
+        if (g.A != 0.0f) {
+            // lambda_k = cross(v_{k+1} - p, v_{k+2} - p) / A
+            const float l1 = det2(g.cx, g.cy, g.ax, g.ay) / g.A;
+            const float l2 = det2(g.ax, g.ay, g.bx, g.by) / g.A;
+            const float l0 = 1.0f - l1 - l2;
+            if (l0 >= kMinBarycentric && l1 >= kMinBarycentric && l2 >= kMinBarycentric) {
+                PixelEval e;
+                shade(d, l1, l2, vi, e);
+                out = make_float3(e.col.x * e.tex.x, e.col.y * e.tex.y, e.col.z * e.tex.z);
+                bary = make_float2(l1, l2);
+            }
         }
     }
     d.image[3 * i] = out.x;
@@ -127,8 +189,11 @@ __global__ void __launch_bounds__(kDiffBlock) k_diff_backward(mlv_diff_desc d) {
     const uint32_t view = (uint32_t)(i / npix);
     const uint32_t p = (uint32_t)(i - (size_t)view * npix);
     const float2 bary = reinterpret_cast<const float2 *>(d.barycentrics)[i];
+    if (bary.x < kMinBarycentric) return;  // dropped by the differentiable coverage
+    uint32_t vi[3];
+    load_triangle(d, tri, vi);
     PixelEval e;
-    shade(d, bary.x, bary.y, tri, e);
+    shade(d, bary.x, bary.y, vi, e);
     const float3 dout = make_float3(d.grad_image[3 * i], d.grad_image[3 * i + 1], d.grad_image[3 * i + 2]);
     const float3 dcol = make_float3(dout.x * e.tex.x, dout.y * e.tex.y, dout.z * e.tex.z);
     const float3 dtex = make_float3(dout.x * e.col.x, dout.y * e.col.y, dout.z * e.col.z);
@@ -168,35 +233,31 @@ __global__ void __launch_bounds__(kDiffBlock) k_diff_backward(mlv_diff_desc d) {
                           dtex.y * (((1.f - e.fs) * t01.y + e.fs * t11.y) - ((1.f - e.fs) * t00.y + e.fs * t10.y)) +
                           dtex.z * (((1.f - e.fs) * t01.z + e.fs * t11.z) - ((1.f - e.fs) * t00.z + e.fs * t10.z));
         const float du = dfs * (float)d.tex_width, dv = -dft * (float)d.tex_height;
+        // G_k = dL/dlambda_k, taken relative to G_0 (the barycentric derivatives sum to zero)
+        const float2 uv0 = __ldg(reinterpret_cast<const float2 *>(d.uvs) + e.vi[0]);
+        const float *c0 = d.colors + 3 * (size_t)e.vi[0];
         float G[3];
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            const uint32_t q = e.vi[k];
-            G[k] = du * __ldg(d.uvs + 2 * (size_t)q) + dv * __ldg(d.uvs + 2 * (size_t)q + 1) +
-                   dcol.x * __ldg(d.colors + 3 * (size_t)q) + dcol.y * __ldg(d.colors + 3 * (size_t)q + 1) +
-                   dcol.z * __ldg(d.colors + 3 * (size_t)q + 2);
+        for (int k = 1; k < 3; ++k) {
+            const float2 uvk = __ldg(reinterpret_cast<const float2 *>(d.uvs) + e.vi[k]);
+            const float *ck = d.colors + 3 * (size_t)e.vi[k];
+            G[k] = du * (uvk.x - uv0.x) + dv * (uvk.y - uv0.y) + dcol.x * (__ldg(ck) - __ldg(c0)) +
+                   dcol.y * (__ldg(ck + 1) - __ldg(c0 + 1)) + dcol.z * (__ldg(ck + 2) - __ldg(c0 + 2));
         }
         const float W = (float)d.width, H = (float)d.height;
-        const float x = (float)(p % d.width), y = (float)(p / d.width);
-        const float *pos = d.positions + (size_t)view * d.n_verts * 2;
-        float X[3], Y[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            X[k] = W * __ldg(pos + 2 * (size_t)e.vi[k]);
-            Y[k] = H * (1.0f - __ldg(pos + 2 * (size_t)e.vi[k] + 1));
-        }
-        const float A = (X[1] - X[0]) * (Y[2] - Y[0]) - (X[2] - X[0]) * (Y[1] - Y[0]);
-        if (A == 0.0f) return;
-        const float rA = 1.0f / A;
-        const float S = G[0] * l[0] + G[1] * l[1] + G[2] * l[2];
-        // d lambda_k / d v_j from the numerators cross(v_{k+1} - p, v_{k+2} - p), minus S dA/dv_j
+        CornerGeom g;
+        corner_geometry(d.positions + (size_t)view * d.n_verts * 2, e.vi, W, H, (float)(p % d.width),
+                        (float)(p / d.width), g);
+        const float rA = 1.0f / g.A;
+        const float S = G[1] * e.l1 + G[2] * e.l2;
+        // sum_k G_k d lambda_k / d v_j = (sum_k G_k d n_k / d v_j - S dA / d v_j) / A, n_k the numerators
         float gX[3], gY[3];
-        gX[0] = (G[1] * (-(Y[2] - y)) + G[2] * (Y[1] - y) - S * (-(Y[2] - Y[0]) + (Y[1] - Y[0]))) * rA;
-        gY[0] = (G[1] * (X[2] - x) + G[2] * (-(X[1] - x)) - S * ((X[2] - X[0]) - (X[1] - X[0]))) * rA;
-        gX[1] = (G[0] * (Y[2] - y) + G[2] * (-(Y[0] - y)) - S * (Y[2] - Y[0])) * rA;
-        gY[1] = (G[0] * (-(X[2] - x)) + G[2] * (X[0] - x) - S * (-(X[2] - X[0]))) * rA;
-        gX[2] = (G[0] * (-(Y[1] - y)) + G[1] * (Y[0] - y) - S * (-(Y[1] - Y[0]))) * rA;
-        gY[2] = (G[0] * (X[1] - x) + G[1] * (-(X[0] - x)) - S * (X[1] - X[0])) * rA;
+        gX[0] = (G[2] * g.by - G[1] * g.cy - S * (g.e1y - g.e2y)) * rA;
+        gY[0] = (G[1] * g.cx - G[2] * g.bx - S * (g.e2x - g.e1x)) * rA;
+        gX[1] = (-G[2] * g.ay - S * g.e2y) * rA;
+        gY[1] = (G[2] * g.ax + S * g.e2x) * rA;
+        gX[2] = (G[1] * g.ay + S * g.e1y) * rA;
+        gY[2] = (-G[1] * g.ax - S * g.e1x) * rA;
         float *gp = d.grad_positions + (size_t)view * d.n_verts * 2;
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
@@ -222,6 +283,11 @@ mlv_status check_desc(const mlv_diff_desc *d, bool backward) {
     }
     if (backward && !d->grad_image) {
         set_last_error("the backward needs grad_image");
+        return MLV_ERROR_INVALID_ARG;
+    }
+    if (((uintptr_t)d->positions | (uintptr_t)d->uvs | (uintptr_t)d->barycentrics) & 7u ||
+        (uintptr_t)d->texture & 15u) {
+        set_last_error("positions, uvs and barycentrics need 8-byte alignment, texture 16-byte");
         return MLV_ERROR_INVALID_ARG;
     }
     if ((uint64_t)d->width * d->height * d->num_views > 0xFFFFFFFFull * kDiffBlock) {

@@ -498,8 +498,8 @@ def frame_from_arrays(z, prefix="frame"):
 
 def diff_scene(seed=4, n_views=16, size=512, freq=50, tex_size=1024, heightfield_cells=None):
     """The differentiable configuration: a geodesic sphere of 20*freq^2 triangles (freq 50: 50,000)
-    or, with heightfield_cells, a heightfield of 2*cells^2 triangles; per-vertex colours U(0,1),
-    UVs, an RGBA32F texture U(0,1); per view a seeded rotation and perspective projection into the
+    with planar UVs (0.5 + 0.5 (x, y)) or, with heightfield_cells, a heightfield of 2*cells^2
+    triangles with its grid UVs; per-vertex colours U(0,1), an RGBA32F texture U(0,1); per view a seeded rotation and perspective projection into the
     passthrough screen space [0,1]^2 (x, y) with depth z in (0,1). Returns a dict of arrays."""
     rng = np.random.default_rng(seed)
     if heightfield_cells:
@@ -509,7 +509,10 @@ def diff_scene(seed=4, n_views=16, size=512, freq=50, tex_size=1024, heightfield
     else:
         dirs, faces = geodesic_sphere(freq)
         P = dirs
-        uv = sphere_vertices(dirs, np.ones(len(dirs)))[:, 6:8]
+        # a seam-free planar map: the spherical map's seam triangles interpolate across the whole
+        # texture (and its poles leave u undefined), which makes their texel lookups, and any
+        # gradient through them, ill-conditioned in single precision
+        uv = 0.5 + 0.5 * dirs[:, 0:2]
     n = len(P)
     col = rng.random((n, 3)).astype(np.float32)
     tex = rng.random((tex_size, tex_size, 4)).astype(np.float32)

@@ -120,6 +120,8 @@ typedef struct orc_diff_view {
 
 double orc_diff_loss(const orc_diff_scene *s, const orc_diff_view *views, uint32_t nviews, double *image);
 void orc_diff_cells(const orc_diff_scene *s, const orc_diff_view *v, int32_t *cells);
+/* The same cells chosen with the GPU kernels' single-precision operation sequence. */
+void orc_diff_cells_f32(const orc_diff_scene *s, const orc_diff_view *v, int32_t *cells);
 void orc_diff_grad(const orc_diff_scene *s, const orc_diff_view *views, uint32_t nviews, double *g_col,
                    double *g_tex, double *g_pos);
 

@@ -19,6 +19,12 @@
 
 #include "oracle.h"
 
+/* The differentiable coverage (malevich_gb300/csrc/adjoint.cu): a covered pixel counts when its
+ * corner's continuous barycentrics are all >= -1/8; a frozen cell of CELL_DROPPED marks a pixel
+ * the rule (evaluated in single precision) dropped. */
+#define MIN_BARYCENTRIC (-0.125)
+#define CELL_DROPPED INT32_MIN
+
 typedef struct {
     double l[3];           /* barycentrics */
     double col[3], tex[3]; /* interpolated colour, filtered texel */
@@ -35,7 +41,7 @@ static inline double tex_at(const orc_diff_scene *s, int32_t i, int32_t j, int c
     return s->tex[((size_t)j * s->tw + (size_t)i) * 4 + c];
 }
 
-/* Evaluates one covered pixel; returns 0 if the triangle is degenerate. */
+/* Evaluates one covered pixel; returns 0 if the differentiable coverage drops it. */
 static int eval_pixel(const orc_diff_scene *s, const orc_diff_view *v, uint32_t px, uint32_t py, uint32_t t,
                       const int32_t *cell, pix_state *ps) {
     const double W = (double)v->width, H = (double)v->height;
@@ -46,6 +52,7 @@ static int eval_pixel(const orc_diff_scene *s, const orc_diff_view *v, uint32_t 
         ps->Y[k] = H * (1.0 - v->pos[2 * (size_t)vi + 1]);
     }
     const double x = (double)px, y = (double)py;
+    if (cell && cell[0] == CELL_DROPPED) return 0;
     ps->A = (ps->X[1] - ps->X[0]) * (ps->Y[2] - ps->Y[0]) - (ps->X[2] - ps->X[0]) * (ps->Y[1] - ps->Y[0]);
     if (ps->A == 0.0) return 0;
     /* lambda_k = cross(v_{k+1} - p, v_{k+2} - p) / A */
@@ -53,6 +60,7 @@ static int eval_pixel(const orc_diff_scene *s, const orc_diff_view *v, uint32_t 
         int a = (k + 1) % 3, b = (k + 2) % 3;
         ps->l[k] = ((ps->X[a] - x) * (ps->Y[b] - y) - (ps->Y[a] - y) * (ps->X[b] - x)) / ps->A;
     }
+    if (!cell && (ps->l[0] < MIN_BARYCENTRIC || ps->l[1] < MIN_BARYCENTRIC || ps->l[2] < MIN_BARYCENTRIC)) return 0;
     double u = 0, vv = 0;
     for (int c = 0; c < 3; ++c) ps->col[c] = 0;
     for (int k = 0; k < 3; ++k) {
@@ -83,9 +91,9 @@ double orc_diff_loss(const orc_diff_scene *s, const orc_diff_view *views, uint32
                 const uint32_t t = v->prim[p];
                 if (t == 0xFFFFFFFFu) continue;
                 pix_state ps;
-                if (!eval_pixel(s, v, px, py, t, v->cells ? v->cells + 2 * p : NULL, &ps)) continue;
+                const int in = eval_pixel(s, v, px, py, t, v->cells ? v->cells + 2 * p : NULL, &ps);
                 for (int c = 0; c < 3; ++c) {
-                    double o = ps.col[c] * ps.tex[c];
+                    double o = in ? ps.col[c] * ps.tex[c] : 0.0; /* a dropped pixel shades to 0 */
                     if (image) image[((size_t)vi * v->width * v->height + p) * 3 + c] = o;
                     double d = o - v->target[p * 3 + c];
                     loss += d * d;
@@ -102,9 +110,74 @@ void orc_diff_cells(const orc_diff_scene *s, const orc_diff_view *v, int32_t *ce
             pix_state ps;
             cells[2 * p] = cells[2 * p + 1] = 0;
             if (v->prim[p] == 0xFFFFFFFFu) continue;
-            if (!eval_pixel(s, v, px, py, v->prim[p], NULL, &ps)) continue;
+            if (!eval_pixel(s, v, px, py, v->prim[p], NULL, &ps)) {
+                cells[2 * p] = cells[2 * p + 1] = CELL_DROPPED;
+                continue;
+            }
             cells[2 * p] = ps.s0;
             cells[2 * p + 1] = ps.t0;
+        }
+}
+
+/* a d - b c by Kahan's FMA algorithm, as the GPU kernels compute it (Jeannerod, Louvet and Muller,
+ * Math. Comp. 2013). */
+static inline float det2f(float a, float b, float c, float d) {
+    const float w = b * c;
+    const float e = fmaf(-b, c, w);
+    const float f = fmaf(a, d, -w);
+    return f + e;
+}
+
+/* The bilinear cell each pixel falls in, and the differentiable coverage, computed with the GPU
+ * kernels' single-precision operation sequence (malevich_gb300/csrc/adjoint.cu: corner_geometry,
+ * the barycentric division and shade's exact split of the texel coordinate). The cell is a discrete choice: the loss is
+ * continuous across cell boundaries but its derivative in the positions jumps there, so the FP64
+ * adjoint is compared with the GPU under the GPU's own cells. Compiled with -ffp-contract=off so
+ * every operation rounds like the kernel's (built with --fmad=false; fmaf where it calls fmaf). */
+void orc_diff_cells_f32(const orc_diff_scene *s, const orc_diff_view *v, int32_t *cells) {
+    const float W = (float)v->width, H = (float)v->height;
+    const float tw = (float)s->tw, th = (float)s->th;
+    for (uint32_t py = 0; py < v->height; ++py)
+        for (uint32_t px = 0; px < v->width; ++px) {
+            const size_t p = (size_t)py * v->width + px;
+            const uint32_t t = v->prim[p];
+            cells[2 * p] = cells[2 * p + 1] = 0;
+            if (t == 0xFFFFFFFFu) continue;
+            uint32_t vi[3];
+            float ppx[3], ppy[3];
+            for (int k = 0; k < 3; ++k) {
+                vi[k] = s->ib[3 * (size_t)t + k];
+                ppx[k] = (float)v->pos[2 * (size_t)vi[k]];
+                ppy[k] = (float)v->pos[2 * (size_t)vi[k] + 1];
+            }
+            const float x = (float)px, y = (float)py, hy = H - y;
+            const float ax = fmaf(W, ppx[0], -x), ay = fmaf(-H, ppy[0], hy);
+            const float bx = fmaf(W, ppx[1], -x), by = fmaf(-H, ppy[1], hy);
+            const float cx = fmaf(W, ppx[2], -x), cy = fmaf(-H, ppy[2], hy);
+            const float e1x = W * (ppx[1] - ppx[0]), e1y = H * (ppy[0] - ppy[1]);
+            const float e2x = W * (ppx[2] - ppx[0]), e2y = H * (ppy[0] - ppy[2]);
+            const float A = det2f(e1x, e2x, e1y, e2y);
+            cells[2 * p] = cells[2 * p + 1] = CELL_DROPPED;
+            if (A == 0.0f) continue;
+            const float l1 = det2f(cx, cy, ax, ay) / A;
+            const float l2 = det2f(ax, ay, bx, by) / A;
+            const float l0 = 1.0f - l1 - l2;
+            if (l0 < -0.125f || l1 < -0.125f || l2 < -0.125f) continue;
+            float u[3], w[3];
+            for (int k = 0; k < 3; ++k) {
+                u[k] = (float)s->uv[2 * (size_t)vi[k]];
+                w[k] = (float)s->uv[2 * (size_t)vi[k] + 1];
+            }
+            const float ps = tw * u[0], pse = fmaf(tw, u[0], -ps);
+            const float bs = ps - 0.5f, fbs = floorf(bs);
+            const float q = th * w[0], qe = fmaf(th, w[0], -q);
+            const float a = th - 0.5f, r = a - q, rb = r - a;
+            const float re = (a - (r - rb)) + (-q - rb);
+            const float fbt = floorf(r);
+            const float rs = ((bs - fbs) + pse) + (l1 * (tw * (u[1] - u[0])) + l2 * (tw * (u[2] - u[0])));
+            const float rt = ((r - fbt) + (re - qe)) - (l1 * (th * (w[1] - w[0])) + l2 * (th * (w[2] - w[0])));
+            cells[2 * p] = (int32_t)fbs + (int32_t)floorf(rs);
+            cells[2 * p + 1] = (int32_t)fbt + (int32_t)floorf(rt);
         }
 }
 

@@ -341,6 +341,7 @@ class DiffModel:
         self.lib.orc_diff_loss.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p]
         self.lib.orc_diff_grad.argtypes = [ctypes.c_void_p] * 2 + [ctypes.c_uint32] + [ctypes.c_void_p] * 3
         self.lib.orc_diff_cells.argtypes = [ctypes.c_void_p] * 3
+        self.lib.orc_diff_cells_f32.argtypes = [ctypes.c_void_p] * 3
         self.ib = np.ascontiguousarray(ib, np.uint32)
         self.col = np.ascontiguousarray(col, np.float64)
         self.uv = np.ascontiguousarray(uv, np.float64)
@@ -361,12 +362,14 @@ class DiffModel:
                                  _ptr(v["cells"]) if v["cells"] is not None else None)
         return sc, arr
 
-    def freeze_cells(self):
-        """Holds each pixel's bilinear cell fixed (the loss becomes smooth in the positions)."""
+    def freeze_cells(self, rule="f64"):
+        """Holds each pixel's bilinear cell fixed (the loss becomes smooth in the positions).
+        rule "f64" picks the cells in FP64; "f32" with the GPU kernels' single-precision sequence."""
+        fn = {"f64": self.lib.orc_diff_cells, "f32": self.lib.orc_diff_cells_f32}[rule]
         sc, arr = self._structs()
         for i, v in enumerate(self.views):
             cells = np.zeros((v["height"], v["width"], 2), np.int32)
-            self.lib.orc_diff_cells(ctypes.byref(sc), ctypes.byref(arr[i]), _ptr(cells))
+            fn(ctypes.byref(sc), ctypes.byref(arr[i]), _ptr(cells))
             v["cells"] = cells
 
     def loss(self, image=False):

@@ -58,12 +58,16 @@ def test_forward_and_adjoint_match_fp64_oracle(setup):
     views = [dict(width=sc["width"], height=sc["height"], pos=sc["pos"][k], prim=setup["prims"][k], target=target[k])
              for k in range(sc["pos"].shape[0])]
     model = pyoracle.DiffModel(sc["ib"], sc["col"], sc["uv"], sc["tex"], views)
+    # bilinear cells as the GPU's single-precision arithmetic picks them: the position derivative
+    # jumps at cell boundaries, so both sides must differentiate inside the same cell
+    model.freeze_cells(rule="f32")
     ref_loss, ref_img = model.loss(image=True)
-    assert rel_err(image.detach().cpu().numpy(), ref_img) <= 1e-5
-    assert abs(loss.item() - ref_loss) / ref_loss <= 1e-4
     g_col, g_tex, g_pos = model.grad()
-    errs = {"colors": rel_err(col.grad.cpu().numpy(), g_col), "texels": rel_err(tex.grad.cpu().numpy(), g_tex),
+    errs = {"image": rel_err(image.detach().cpu().numpy(), ref_img),
+            "loss": abs(loss.item() - ref_loss) / ref_loss,
+            "colors": rel_err(col.grad.cpu().numpy(), g_col), "texels": rel_err(tex.grad.cpu().numpy(), g_tex),
             "positions": rel_err(pos.grad.cpu().numpy(), g_pos)}
+    print("relative errors vs FP64:", errs)
     assert max(errs.values()) <= REL_TOL, errs
 
 
