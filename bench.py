@@ -54,6 +54,9 @@ def parse():
     ap.add_argument("--diff-steps", type=int, default=100)
     ap.add_argument("--profile-once", action="store_true",
                     help="render the frame once (batched, eager) and exit: a short launch sequence for ncu")
+    ap.add_argument("--profile-diff-views", type=int, default=0,
+                    help="run the differentiable loop's visibility pass, forward and adjoint once over this "
+                         "many views of its 256x256 heightfield workload and exit (a short sequence for ncu)")
     return ap.parse_args()
 
 
@@ -187,7 +190,7 @@ def run_diff_sections(dev, args):
     import ctypes
     import torch
     sys.path.insert(0, os.path.join(ROOT, "tests"))
-    from diffrender import DiffScene, gather_primitive_ids, visibility
+    from diffrender import DiffScene, visibility
     from malevich_gb300 import api, scenes
     lib = api.load_library()
     stream = torch.cuda.current_stream()
@@ -226,66 +229,136 @@ def run_diff_sections(dev, args):
                       "gradient_check": "tests/test_gpu_adjoint.py: 1e-4 relative vs the FP64 oracle adjoint"}
     del ds, image, target, g_col, g_tex, g_pos
 
-    # --- configuration 5: batched + differentiable optimisation loop
+    # --- configuration 5: batched + differentiable optimisation loop. Everything runs on the
+    # immediate context's stream: the visibility command list (one graph launch for all views,
+    # null pixel shader, primitive ids written straight into one [views][H][W] array), the
+    # forward, the loss gradient, the adjoint and Adam.
     torch.cuda.synchronize()
     free0, total = torch.cuda.mem_get_info()
     sc = scenes.diff_scene(seed=5, n_views=256, size=256, tex_size=2048, heightfield_cells=316)
     rng = np.random.default_rng(55)
-    tex_true = torch.from_numpy(rng.random(sc["tex"].shape).astype(np.float32)).cuda()
-    col_true = torch.from_numpy(sc["col"]).cuda()
-    frames = scenes.diff_frames(sc)
-    vr = api.FrameRenderer(dev, frames, primitive_ids=True)
-    vr.render_batched()                      # sizes the workspace, captures the graph
-    prims = np.stack([vr.read(i)["vis_prim"] for i in range(len(frames))])
-    ds = DiffScene(sc, prims)
-    pos = torch.from_numpy(sc["pos"]).cuda()
-    target = torch.empty((ds.views, ds.height, ds.width, 3), device="cuda")
-    d = ds.desc(col_true, tex_true, pos, image=target)
-    lib.mlv_diff_forward(ctypes.byref(d), sp)
-    tex = torch.full_like(tex_true, 0.5).requires_grad_()
-    col = torch.full_like(col_true, 0.5).requires_grad_()
-    opt = torch.optim.Adam([tex, col], lr=1e-2)
-    image = torch.empty_like(target)
-
-    def step():
-        vr.render_batched()                  # visibility of all 256 views: one graph launch
-        dev.immediate.finish()
-        gather_primitive_ids(vr, ds.prim)
-        d = ds.desc(col, tex, pos, image=image)
-        lib.mlv_diff_forward(ctypes.byref(d), sp)
-        gi = 2.0 * (image - target) * ds.mask
+    ctx = dev.immediate
+    cstream = torch.cuda.ExternalStream(ctx.stream())
+    csp = ctypes.c_void_p(ctx.stream())
+    with torch.cuda.stream(cstream):
+        tex_true = torch.from_numpy(rng.random(sc["tex"].shape).astype(np.float32)).cuda()
+        col_true = torch.from_numpy(sc["col"]).cuda()
+        V, S = sc["pos"].shape[0], sc["width"]
+        prim = torch.empty((V, S, S), dtype=torch.int32, device="cuda")
+        frames = scenes.diff_frames(sc, shade=False)
+        vr = api.FrameRenderer(dev, frames, primitive_id_memory=[prim[i].data_ptr() for i in range(V)])
+        vr.render_batched()                  # sizes the workspace, captures the graph
+        ds = DiffScene(sc, prim)
+        pos = torch.from_numpy(sc["pos"]).cuda()
+        target = torch.empty((ds.views, ds.height, ds.width, 3), device="cuda")
+        d = ds.desc(col_true, tex_true, pos, image=target)
+        lib.mlv_diff_forward(ctypes.byref(d), csp)
+        tex = torch.full_like(tex_true, 0.5).requires_grad_()
+        col = torch.full_like(col_true, 0.5).requires_grad_()
         tex.grad = torch.zeros_like(tex)
         col.grad = torch.zeros_like(col)
-        d = ds.desc(col, tex, pos, grad_image=gi, g_col=col.grad, g_tex=tex.grad)
-        lib.mlv_diff_backward(ctypes.byref(d), sp)
-        opt.step()
+        opt = torch.optim.Adam([tex, col], lr=1e-2, fused=True)
+        image = torch.empty_like(target)
+        gi = torch.empty_like(target)
+        d_fwd = ds.desc(col, tex, pos, image=image)
+        d_bwd = ds.desc(col, tex, pos, grad_image=gi, g_col=col.grad, g_tex=tex.grad)
+        phases = ("visibility", "forward", "loss_grad", "adjoint", "adam")
+        ev = [[torch.cuda.Event(enable_timing=True) for _ in range(len(phases) + 1)] for _ in range(args.diff_steps)]
 
-    t0 = time.perf_counter()
-    for _ in range(args.diff_steps):
-        step()
-    torch.cuda.synchronize()
-    dt = (time.perf_counter() - t0) / args.diff_steps
-    free1, _ = torch.cuda.mem_get_info()
-    with torch.no_grad():
-        seen = torch.zeros(tex.shape[:2], dtype=torch.bool, device="cuda")
-        gi = torch.ones_like(image) * ds.mask
-        gt = torch.zeros_like(tex)
-        d = ds.desc(col, tex, pos, grad_image=gi, g_tex=gt)
-        lib.mlv_diff_backward(ctypes.byref(d), sp)
-        seen = gt[..., 0] != 0
-        err = (tex - tex_true)[..., :3][seen]
-        rmse = float(torch.sqrt((err ** 2).mean()).item()) if err.numel() else None
-        err0 = (0.5 - tex_true)[..., :3][seen]
-        rmse0 = float(torch.sqrt((err0 ** 2).mean()).item()) if err0.numel() else None
+        def step(e=None):
+            rec = (lambda k: e[k].record(cstream)) if e else (lambda k: None)
+            rec(0)
+            vr.render_batched()              # visibility of all views: one graph launch
+            rec(1)
+            lib.mlv_diff_forward(ctypes.byref(d_fwd), csp)
+            rec(2)
+            torch.sub(image, target, out=gi).mul_(2.0)
+            tex.grad.zero_()
+            col.grad.zero_()
+            rec(3)
+            lib.mlv_diff_backward(ctypes.byref(d_bwd), csp)
+            rec(4)
+            opt.step()
+            rec(5)
+
+        for _ in range(3):
+            step()
+        # reset the optimiser and parameters after the warm-up so the timed run is the full fit
+        tex.data.fill_(0.5)
+        col.data.fill_(0.5)
+        opt = torch.optim.Adam([tex, col], lr=1e-2, fused=True)
+        cstream.synchronize()
+        free_mid, _ = torch.cuda.mem_get_info()
+        t0 = time.perf_counter()
+        for i in range(args.diff_steps):
+            step(ev[i])
+        cstream.synchronize()
+        dt = (time.perf_counter() - t0) / args.diff_steps
+        phase_ms = {p: round(float(np.mean([ev[i][k].elapsed_time(ev[i][k + 1]) for i in range(args.diff_steps)])), 4)
+                    for k, p in enumerate(phases)}
+        dev_ms = float(np.mean([ev[i][0].elapsed_time(ev[i][-1]) for i in range(args.diff_steps)]))
+        free1, _ = torch.cuda.mem_get_info()
+        # per-stage times of the visibility pass (one eager, profiled execution)
+        ctx.set_profiling(True)
+        ctx.reset_stats()
+        vr.render_batched()
+        vis_stages = {k: round(v[0], 4) for k, v in ctx.stage_times().items()}
+        vis_stats = {k: int(v) for k, v in ctx.stats().items()}
+        ctx.set_profiling(False)
+        with torch.no_grad():
+            gt = torch.zeros_like(tex)
+            d = ds.desc(col, tex, pos, grad_image=torch.ones_like(image), g_tex=gt)
+            lib.mlv_diff_backward(ctypes.byref(d), csp)
+            seen = gt[..., 0] != 0
+            err = (tex - tex_true)[..., :3][seen]
+            rmse = float(torch.sqrt((err ** 2).mean()).item()) if err.numel() else None
+            err0 = (0.5 - tex_true)[..., :3][seen]
+            rmse0 = float(torch.sqrt((err0 ** 2).mean()).item()) if err0.numel() else None
+            lossv = float(((image - target) ** 2).sum().item())
     out["config5"] = {"views": ds.views, "resolution": [ds.width, ds.height], "triangles": ds.n_tris,
                       "texture": [2048, 2048], "adam_steps": args.diff_steps, "lr": 1e-2,
-                      "ms_per_step": round(dt * 1e3, 3),
-                      "peak_hbm_gb": round((total - min(free0, free1)) / 1e9, 2),
-                      "texture_rmse_start": rmse0, "texture_rmse_final": rmse,
-                      "step": "visibility (batched command list, CUDA graph) + mlv_diff_forward + "
-                              "mlv_diff_backward + torch Adam"}
+                      "ms_per_step": round(dt * 1e3, 3), "device_ms_per_step": round(dev_ms, 3),
+                      "phase_ms": phase_ms, "visibility_stage_ms": vis_stages, "visibility_stats": vis_stats,
+                      "hbm_footprint_gb": round((free0 - min(free_mid, free1)) / 1e9, 2),
+                      "hbm_device_used_gb": round((total - min(free_mid, free1)) / 1e9, 2),
+                      "texture_rmse_start": rmse0, "texture_rmse_final": rmse, "final_loss": lossv,
+                      "texels_seen": int(seen.sum().item()),
+                      "step": "visibility (batched command list, one CUDA graph launch, null pixel shader) + "
+                              "mlv_diff_forward + loss gradient + mlv_diff_backward + torch Adam"}
     vr.destroy()
     return out
+
+
+def profile_diff(dev, views):
+    """One visibility pass (eager), forward and adjoint over `views` views of the differentiable
+    loop's workload (256x256, 200k-triangle heightfield, 2048x2048 texture)."""
+    import ctypes
+    import torch
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from diffrender import DiffScene
+    from malevich_gb300 import api, scenes
+    lib = api.load_library()
+    sc = scenes.diff_scene(seed=5, n_views=views, size=256, tex_size=2048, heightfield_cells=316)
+    ctx = dev.immediate
+    cstream = torch.cuda.ExternalStream(ctx.stream())
+    csp = ctypes.c_void_p(ctx.stream())
+    with torch.cuda.stream(cstream):
+        prim = torch.empty((views, 256, 256), dtype=torch.int32, device="cuda")
+        vr = api.FrameRenderer(dev, scenes.diff_frames(sc, shade=False),
+                               primitive_id_memory=[prim[i].data_ptr() for i in range(views)])
+        vr.render_batched()
+        ds = DiffScene(sc, prim)
+        col = torch.from_numpy(sc["col"]).cuda()
+        tex = torch.from_numpy(sc["tex"]).cuda()
+        pos = torch.from_numpy(sc["pos"]).cuda()
+        image = torch.empty((views, 256, 256, 3), device="cuda")
+        lib.mlv_diff_forward(ctypes.byref(ds.desc(col, tex, pos, image=image)), csp)
+        g_col, g_tex = torch.zeros_like(col), torch.zeros_like(tex)
+        lib.mlv_diff_backward(ctypes.byref(ds.desc(col, tex, pos, grad_image=image, g_col=g_col, g_tex=g_tex)), csp)
+    cstream.synchronize()
+    st = ctx.stats()
+    vr.destroy()
+    return {"views": views, "stats": st}
 
 
 def run_reference_arm(args, rank, world):
@@ -344,9 +417,13 @@ def main():
     from malevich_gb300 import api, build, scenes
     build.build()
     torch.cuda.set_device(local)
-    frame = scenes.config2_scene(seed=args.seed)
     dev = api.Device(local)
     ctx = dev.immediate
+    if args.profile_diff_views:
+        print(json.dumps({"profile_diff": profile_diff(dev, args.profile_diff_views)}))
+        dev.destroy()
+        return 0
+    frame = scenes.config2_scene(seed=args.seed)
     r = api.FrameRenderer(dev, frame)
     if args.profile_once:
         r.render_batched()

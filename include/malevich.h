@@ -139,7 +139,9 @@ typedef enum mlv_pixel_shader_id {
     MLV_PS_BASIC = 1,            /* basic_ps.c:16-29 (PS SRV 0: RGBA8) */
     MLV_PS_PASSTHROUGH = 2,      /* passthrough_ps.c:13-22 */
     MLV_PS_ENV_LIGHTING = 3,     /* env_lighting_ps.c:13-26 (PS SRV 0: float lat-long map) */
-    MLV_PS_COLOR_TIMES_TEXEL = 4 /* new: COLOR * bilinear(SRV 0, UV).xyz */
+    MLV_PS_COLOR_TIMES_TEXEL = 4, /* new: COLOR * bilinear(SRV 0, UV).xyz */
+    MLV_PS_NONE = 5               /* new: no pixel shader (Direct3D 11's null PS): depth and the
+                                     visibility targets are written, the render target is not */
 } mlv_pixel_shader_id;
 
 /* Vs_Input of basic_vs / vertex_lighting_vs (basic_vs.c:3-7): 32 bytes */
@@ -194,6 +196,11 @@ MLV_API mlv_status mlv_destroy_buffer(mlv_buffer buffer);
 MLV_API mlv_status mlv_create_texture2d(mlv_device device, const mlv_texture2d_desc *desc, const void *init_data,
                                         uint32_t row_pitch, mlv_texture2d *out_texture);
 MLV_API mlv_status mlv_destroy_texture2d(mlv_texture2d texture);
+/* New: a texture placed on caller-owned device memory (tightly packed rows, 16-byte aligned,
+ * width * height * texel bytes long), left uninitialised and not freed by mlv_destroy_texture2d;
+ * e.g. the per-view primitive-id targets of a batch laid out as one [views][height][width] array. */
+MLV_API mlv_status mlv_create_texture2d_on_memory(mlv_device device, const mlv_texture2d_desc *desc,
+                                                  void *device_memory, mlv_texture2d *out_texture);
 /* Raw device addresses for zero-copy interop (e.g. wrapping a render target as a tensor). */
 MLV_API mlv_status mlv_buffer_device_pointer(mlv_buffer buffer, void **out_ptr);
 MLV_API mlv_status mlv_texture2d_device_pointer(mlv_texture2d texture, void **out_ptr);

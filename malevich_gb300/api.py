@@ -34,7 +34,7 @@ STAGES = ("clear", "geometry", "bin_scan", "bin_scatter", "tile", "vertex")
 EXPORTS = [
     "mlv_get_last_error_string", "mlv_get_abi_version", "mlv_create_device", "mlv_destroy_device",
     "mlv_get_immediate_context", "mlv_create_deferred_context", "mlv_destroy_context", "mlv_create_buffer",
-    "mlv_destroy_buffer", "mlv_create_texture2d", "mlv_destroy_texture2d", "mlv_buffer_device_pointer",
+    "mlv_destroy_buffer", "mlv_create_texture2d", "mlv_create_texture2d_on_memory", "mlv_destroy_texture2d", "mlv_buffer_device_pointer",
     "mlv_texture2d_device_pointer", "mlv_update_buffer", "mlv_update_texture2d", "mlv_read_texture2d",
     "mlv_ia_set_primitive_topology", "mlv_ia_set_index_buffer", "mlv_ia_set_vertex_buffers",
     "mlv_vs_set_shader", "mlv_vs_set_constant_buffers", "mlv_vs_set_shader_resources", "mlv_ps_set_shader",
@@ -117,6 +117,7 @@ def load_library(path=LIB_PATH):
     lib.mlv_create_buffer.argtypes = [vp, ctypes.POINTER(BufferDesc), vp, ctypes.POINTER(vp)]
     lib.mlv_destroy_buffer.argtypes = [vp]
     lib.mlv_create_texture2d.argtypes = [vp, ctypes.POINTER(Texture2DDesc), vp, ctypes.c_uint32, ctypes.POINTER(vp)]
+    lib.mlv_create_texture2d_on_memory.argtypes = [vp, ctypes.POINTER(Texture2DDesc), vp, ctypes.POINTER(vp)]
     lib.mlv_destroy_texture2d.argtypes = [vp]
     lib.mlv_buffer_device_pointer.argtypes = [vp, ctypes.POINTER(vp)]
     lib.mlv_texture2d_device_pointer.argtypes = [vp, ctypes.POINTER(vp)]
@@ -195,12 +196,17 @@ class Buffer:
 
 
 class Texture2D:
-    def __init__(self, device, width, height, fmt, data=None, bind=BIND_SHADER_RESOURCE):
+    def __init__(self, device, width, height, fmt, data=None, bind=BIND_SHADER_RESOURCE, device_memory=None):
+        """device_memory: place the texture on that caller-owned device address instead."""
         lib = load_library()
         arr = None if data is None else np.ascontiguousarray(data)
         h = ctypes.c_void_p()
-        _check(lib.mlv_create_texture2d(device.handle, ctypes.byref(Texture2DDesc(width, height, fmt, bind)),
-                                        _ptr(arr) if arr is not None else None, 0, ctypes.byref(h)))
+        desc = Texture2DDesc(width, height, fmt, bind)
+        if device_memory is not None:
+            _check(lib.mlv_create_texture2d_on_memory(device.handle, ctypes.byref(desc), device_memory, ctypes.byref(h)))
+        else:
+            _check(lib.mlv_create_texture2d(device.handle, ctypes.byref(desc), _ptr(arr) if arr is not None else None,
+                                            0, ctypes.byref(h)))
         self.handle, self.width, self.height, self.format, self.device = h, width, height, fmt, device
 
     def destroy(self):
@@ -401,7 +407,9 @@ class FrameRenderer:
     """Uploads a Frame's (or several Frames') resources once and renders them through the C ABI,
     either per draw on the immediate context or as one command list (batched)."""
 
-    def __init__(self, device, frames, visibility=False, primitive_ids=False):
+    def __init__(self, device, frames, visibility=False, primitive_ids=False, primitive_id_memory=None):
+        """primitive_id_memory: one device address per frame on which to place its primitive-id
+        target (e.g. the slices of a [frames][height][width] int32 tensor)."""
         self.device = device
         self.frames = frames if isinstance(frames, (list, tuple)) else [frames]
         self._buffers, self._textures = {}, {}
@@ -416,8 +424,9 @@ class FrameRenderer:
                        Texture2D(device, fr.width, fr.height, FORMAT_R32_UINT, bind=BIND_UNORDERED_ACCESS),
                        Texture2D(device, fr.width, fr.height, FORMAT_R32G32_FLOAT, bind=BIND_UNORDERED_ACCESS))
             self.targets.append((rt, ds, vis))
-            self.prim_targets.append(Texture2D(device, fr.width, fr.height, FORMAT_R32_UINT,
-                                               bind=BIND_UNORDERED_ACCESS) if primitive_ids else None)
+            mem = primitive_id_memory[len(self.prim_targets)] if primitive_id_memory is not None else None
+            self.prim_targets.append(Texture2D(device, fr.width, fr.height, FORMAT_R32_UINT, bind=BIND_UNORDERED_ACCESS,
+                                               device_memory=mem) if primitive_ids or mem else None)
             for d in fr.draws:
                 self._buffer(d.vb, BIND_VERTEX_BUFFER)
                 if d.ib is not None:

@@ -18,6 +18,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <unordered_set>
 #include <vector>
 
 #include "../../include/malevich.h"
@@ -26,6 +27,8 @@
 namespace mlv {
 void set_clip_planes(const float planes[6][4], cudaStream_t stream);
 cudaError_t launch_fill_u32(uint32_t *p, size_t n, uint32_t value, const uint32_t *error, cudaStream_t stream);
+cudaError_t launch_fill_many(const FillJob *d_jobs, uint32_t njobs, uint32_t nchunks, const uint32_t *error,
+                             cudaStream_t stream);
 cudaError_t launch_vertex(const BatchParams &bp, cudaStream_t stream);
 cudaError_t launch_geometry(const BatchParams &bp, uint32_t block, cudaStream_t stream);
 cudaError_t launch_scan(const BatchParams &bp, cudaStream_t stream);
@@ -93,6 +96,7 @@ struct mlv_texture2d_t {
     float *tile_min = nullptr, *tile_max = nullptr;   // hierarchical Z (depth textures)
     uint32_t tiles_x = 0, tiles_y = 0;
     uint32_t draws_since_clear = 0;                    // render targets: numbers draws for visibility
+    bool owns_memory = true;                           // false: placed on caller memory
 };
 
 static uint32_t texel_bytes(mlv_format f) {
@@ -169,6 +173,8 @@ struct Workspace {
     DrawDesc *d_draws = nullptr;
     ViewDesc *d_views = nullptr;
     uint32_t desc_draw_cap = 0, desc_view_cap = 0;
+    FillJob *d_fills = nullptr;
+    uint32_t fill_cap = 0;
     float4 *vs_out = nullptr;
     uint32_t vs_cap = 0;
     uint64_t generation = 0;
@@ -184,8 +190,9 @@ struct mlv_command_list_t {
     int executions = 0;
     DrawDesc *d_draws = nullptr;   // per-segment descriptor copies owned by the list
     ViewDesc *d_views = nullptr;
-    std::vector<size_t> draw_off, view_off;
-    size_t draws_total = 0, views_total = 0;
+    FillJob *d_fills = nullptr;    // per-segment batched clears
+    std::vector<size_t> draw_off, view_off, fill_off;
+    size_t draws_total = 0, views_total = 0, fills_total = 0;
     uint64_t launches_per_execution = 0;
 };
 
@@ -511,27 +518,61 @@ static void collect_events(mlv_context_t *c) {
     c->ev_next = 0;
 }
 
-static mlv_status run_clears(mlv_context_t *c, const Segment &seg) {
-    for (const ClearCmd &cl : seg.clears) {
-        cudaEvent_t e;
-        ev_begin(c, 0, &e);
+// The fills of a segment's clears, one job per written array (a depth clear also resets the
+// target's tile minima to 0, main.c:1212-1214, and the tile maxima that depth LESS uses to 1).
+// A target cleared twice keeps its last clear, so the jobs write disjoint memory.
+static uint32_t build_fills(const Segment &seg, std::vector<FillJob> &jobs) {
+    jobs.clear();
+    std::unordered_set<mlv_texture2d> seen;
+    for (auto it = seg.clears.rbegin(); it != seg.clears.rend(); ++it) {
+        const ClearCmd &cl = *it;
         mlv_texture2d t = cl.target;
-        size_t n = (size_t)t->width * t->height * (t->texel_bytes / 4);
+        if (!seen.insert(t).second) continue;
         uint32_t value = cl.value;
         if (cl.kind == 1) memcpy(&value, &cl.depth, 4);
-        CUDA_TRY(launch_fill_u32((uint32_t *)t->ptr, n, value, c->ws.error, c->stream));
+        jobs.push_back({(uint32_t *)t->ptr, (uint64_t)t->width * t->height * (t->texel_bytes / 4), value, 0});
         if (cl.kind == 1) {
-            // clear_depth_stencil_view resets the tile minima to 0 (main.c:1212-1214); the tile
-            // maxima that depth LESS uses start at 1
-            size_t nt = (size_t)t->tiles_x * t->tiles_y;
-            CUDA_TRY(launch_fill_u32((uint32_t *)t->tile_min, nt, 0u, c->ws.error, c->stream));
-            CUDA_TRY(launch_fill_u32((uint32_t *)t->tile_max, nt, 0x3F800000u, c->ws.error, c->stream));
-            c->host_stats[4] += 2;
+            const uint64_t nt = (uint64_t)t->tiles_x * t->tiles_y;
+            jobs.push_back({(uint32_t *)t->tile_min, nt, 0u, 0});
+            jobs.push_back({(uint32_t *)t->tile_max, nt, 0x3F800000u, 0});
         }
-        c->host_stats[4] += 1;
-        ev_end(c, e);
     }
+    uint32_t chunks = 0;
+    for (FillJob &j : jobs) {
+        j.chunk_begin = chunks;
+        chunks += (uint32_t)((j.n + kFillChunk - 1) / kFillChunk);
+    }
+    return chunks;
+}
+
+// Runs a segment's clears: one batched fill from `d_jobs` (device copies of `jobs`) when given,
+// else through the workspace's fill buffer, or directly when there is a single array.
+static mlv_status run_fills(mlv_context_t *c, const std::vector<FillJob> &jobs, uint32_t chunks,
+                            const FillJob *d_jobs) {
+    if (jobs.empty()) return MLV_OK;
+    cudaEvent_t e;
+    ev_begin(c, 0, &e);
+    if (!d_jobs && jobs.size() == 1) {
+        CUDA_TRY(launch_fill_u32(jobs[0].p, jobs[0].n, jobs[0].value, c->ws.error, c->stream));
+    } else {
+        if (!d_jobs) {
+            Workspace &w = c->ws;
+            MLV_TRY(grow(&w.d_fills, w.fill_cap, jobs.size()));
+            CUDA_TRY(cudaMemcpyAsync(w.d_fills, jobs.data(), sizeof(FillJob) * jobs.size(), cudaMemcpyHostToDevice,
+                                     c->stream));
+            d_jobs = w.d_fills;
+        }
+        CUDA_TRY(launch_fill_many(d_jobs, (uint32_t)jobs.size(), chunks, c->ws.error, c->stream));
+    }
+    c->host_stats[4] += 1;
+    ev_end(c, e);
     return MLV_OK;
+}
+
+static mlv_status run_clears(mlv_context_t *c, const Segment &seg) {
+    std::vector<FillJob> jobs;
+    const uint32_t chunks = build_fills(seg, jobs);
+    return run_fills(c, jobs, chunks, nullptr);
 }
 
 // Launches the kernels of one segment's draws. `d_draws`/`d_views` hold the plan's descriptors
@@ -769,7 +810,7 @@ static void free_workspace(Workspace &w) {
     cudaFree(w.raster); cudaFree(w.shade); cudaFree(w.geom); cudaFree(w.jobs); cudaFree(w.tri_info); cudaFree(w.rank);
     cudaFree(w.bin_count); cudaFree(w.bin_start); cudaFree(w.list); cudaFree(w.info_mask);
     cudaFree(w.scan_status); cudaFree(w.scan_status2); cudaFree(w.counters); cudaFree(w.stats);
-    cudaFree(w.error); cudaFree(w.d_draws); cudaFree(w.d_views); cudaFree(w.vs_out);
+    cudaFree(w.error); cudaFree(w.d_draws); cudaFree(w.d_views); cudaFree(w.d_fills); cudaFree(w.vs_out);
     w = Workspace();
 }
 
@@ -852,8 +893,8 @@ MLV_API mlv_status mlv_destroy_buffer(mlv_buffer b) {
     return MLV_OK;
 }
 
-MLV_API mlv_status mlv_create_texture2d(mlv_device d, const mlv_texture2d_desc *desc, const void *init,
-                                        uint32_t row_pitch, mlv_texture2d *out) {
+static mlv_status create_texture2d(mlv_device d, const mlv_texture2d_desc *desc, const void *init,
+                                   uint32_t row_pitch, void *placed, mlv_texture2d *out) {
     if (!d || !desc || !out) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
     uint32_t tb = texel_bytes(desc->format);
     if (!tb) return fail(MLV_ERROR_INVALID_ARG, "unknown texture format");
@@ -868,11 +909,20 @@ MLV_API mlv_status mlv_create_texture2d(mlv_device d, const mlv_texture2d_desc *
     t->bind = desc->bind_flags;
     t->texel_bytes = tb;
     size_t bytes = (size_t)desc->width * desc->height * tb;
-    mlv_status st = dev_alloc((void **)&t->ptr, (bytes + 15) & ~(size_t)15);
+    mlv_status st = MLV_OK;
+    if (placed) {
+        t->ptr = (uint8_t *)placed;
+        t->owns_memory = false;
+    } else {
+        st = dev_alloc((void **)&t->ptr, (bytes + 15) & ~(size_t)15);
+    }
     if (st != MLV_OK) {
         delete t;
         return st;
     }
+    auto free_own = [&]() {
+        if (t->owns_memory) cudaFree(t->ptr);
+    };
     if (desc->format == MLV_FORMAT_D32_FLOAT) {
         t->tiles_x = (desc->width + kTile - 1) / kTile;
         t->tiles_y = (desc->height + kTile - 1) / kTile;
@@ -880,7 +930,8 @@ MLV_API mlv_status mlv_create_texture2d(mlv_device d, const mlv_texture2d_desc *
         st = dev_alloc((void **)&t->tile_min, nt * 4);
         if (st == MLV_OK) st = dev_alloc((void **)&t->tile_max, nt * 4);
         if (st != MLV_OK) {
-            cudaFree(t->ptr); cudaFree(t->tile_min);
+            free_own();
+            cudaFree(t->tile_min);
             delete t;
             return st;
         }
@@ -893,22 +944,36 @@ MLV_API mlv_status mlv_create_texture2d(mlv_device d, const mlv_texture2d_desc *
         cudaError_t e = cudaMemcpy2D(t->ptr, row, init, row_pitch ? row_pitch : row, row, desc->height,
                                      cudaMemcpyHostToDevice);
         if (e != cudaSuccess) {
-            cudaFree(t->ptr);
+            free_own();
+            cudaFree(t->tile_min);
+            cudaFree(t->tile_max);
             delete t;
             return fail(MLV_ERROR_DEVICE, cudaGetErrorString(e));
         }
-    } else {
+    } else if (!placed) {
         cudaMemset(t->ptr, 0, bytes);
     }
     *out = t;
     return MLV_OK;
 }
 
+MLV_API mlv_status mlv_create_texture2d(mlv_device d, const mlv_texture2d_desc *desc, const void *init,
+                                        uint32_t row_pitch, mlv_texture2d *out) {
+    return create_texture2d(d, desc, init, row_pitch, nullptr, out);
+}
+
+MLV_API mlv_status mlv_create_texture2d_on_memory(mlv_device d, const mlv_texture2d_desc *desc, void *device_memory,
+                                                  mlv_texture2d *out) {
+    if (!device_memory) return fail(MLV_ERROR_INVALID_ARG, "device_memory is NULL");
+    if ((uintptr_t)device_memory & 15u) return fail(MLV_ERROR_INVALID_ARG, "device_memory must be 16-byte aligned");
+    return create_texture2d(d, desc, nullptr, 0, device_memory, out);
+}
+
 MLV_API mlv_status mlv_destroy_texture2d(mlv_texture2d t) {
     if (!t) return fail(MLV_ERROR_INVALID_ARG, "texture is NULL");
     cudaSetDevice(t->device->ordinal);
     if (t->device->immediate) cudaStreamSynchronize(t->device->immediate->stream);
-    cudaFree(t->ptr);
+    if (t->owns_memory) cudaFree(t->ptr);
     cudaFree(t->tile_min);
     cudaFree(t->tile_max);
     delete t;
@@ -1004,7 +1069,7 @@ MLV_API mlv_status mlv_vs_set_shader(mlv_context c, mlv_vertex_shader_id s) {
 
 MLV_API mlv_status mlv_ps_set_shader(mlv_context c, mlv_pixel_shader_id s) {
     if (!c) return fail(MLV_ERROR_INVALID_ARG, "context is NULL");
-    if (s < MLV_PS_BASIC || s > MLV_PS_COLOR_TIMES_TEXEL) return fail(MLV_ERROR_INVALID_ARG, "unknown pixel shader");
+    if (s < MLV_PS_BASIC || s > MLV_PS_NONE) return fail(MLV_ERROR_INVALID_ARG, "unknown pixel shader");
     c->st.ps = s;
     return MLV_OK;
 }
@@ -1297,6 +1362,7 @@ MLV_API mlv_status mlv_destroy_command_list(mlv_command_list l) {
     if (l->exec) cudaGraphExecDestroy(l->exec);
     cudaFree(l->d_draws);
     cudaFree(l->d_views);
+    cudaFree(l->d_fills);
     delete l;
     return MLV_OK;
 }
@@ -1321,6 +1387,29 @@ static mlv_status run_list(mlv_context_t *c, mlv_command_list l, uint32_t seq, b
         nv += plans[i].views.size();
     }
     if (!c->capturing_graph) MLV_TRY(ensure_workspace(c, maxs, false));
+    std::vector<std::vector<FillJob>> fills(l->segments.size());
+    std::vector<uint32_t> fill_chunks(l->segments.size());
+    size_t nf = 0;
+    for (size_t i = 0; i < l->segments.size(); ++i) {
+        fill_chunks[i] = build_fills(l->segments[i], fills[i]);
+        nf += fills[i].size();
+    }
+    if (upload || !l->d_fills) {
+        if (nf > l->fills_total || !l->d_fills) {
+            cudaFree(l->d_fills);
+            l->d_fills = nullptr;
+            MLV_TRY(dev_alloc((void **)&l->d_fills, std::max<size_t>(nf, 1) * sizeof(FillJob)));
+            l->fills_total = nf;
+        }
+        l->fill_off.clear();
+        size_t of = 0;
+        for (auto &f : fills) {
+            l->fill_off.push_back(of);
+            if (!f.empty())
+                CUDA_TRY(cudaMemcpy(l->d_fills + of, f.data(), sizeof(FillJob) * f.size(), cudaMemcpyHostToDevice));
+            of += f.size();
+        }
+    }
     if (upload || !l->d_draws) {
         if (nd > l->draws_total || !l->d_draws) {
             cudaFree(l->d_draws);
@@ -1351,7 +1440,7 @@ static mlv_status run_list(mlv_context_t *c, mlv_command_list l, uint32_t seq, b
         }
     }
     for (size_t i = 0; i < l->segments.size(); ++i) {
-        MLV_TRY(run_clears(c, l->segments[i]));
+        MLV_TRY(run_fills(c, fills[i], fill_chunks[i], l->d_fills + l->fill_off[i]));
         if (!plans[i].draws.empty())
             MLV_TRY(launch_draws(c, plans[i], l->d_draws + l->draw_off[i], l->d_views + l->view_off[i], seq));
         c->host_stats[0] += l->segments[i].vertex_count;

@@ -7,6 +7,7 @@ namespace mlv {
 
 constexpr int kTile = 8;                 // 8x8 pixel tiles: the reference's bins (main.c:24-25)
 constexpr int kSubpix = 4;               // 28.4 fixed point (main.c:39)
+constexpr int kPsNone = 5;               // MLV_PS_NONE: depth and visibility only
 constexpr int kMaxClipVertices = 16;     // main.c:38
 constexpr int kMaxViewsPerBatch = 4096;
 
@@ -80,6 +81,15 @@ struct TriShade {
 struct TriGeom {
     float x[3], y[3], z[3], w[3];
 };
+
+// One fill of a batched clear: n 32-bit words at p set to value; chunk_begin is the exclusive prefix
+// of the jobs' chunk counts (kFillChunk words each), by which a block finds its job.
+struct FillJob {
+    uint32_t *p;
+    uint64_t n;
+    uint32_t value, chunk_begin;
+};
+constexpr uint32_t kFillChunk = 8192;
 
 // One assembled triangle's share of the binner's scatter (main.c:950-962): its key and the bins of
 // its tile rectangle, bin(x, y) = first_bin + y * row_stride + x * col_stride.

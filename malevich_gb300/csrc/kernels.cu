@@ -199,20 +199,15 @@ __device__ __forceinline__ bool setup_triangle(const DrawDesc &d, const Vtx &v0,
     return true;
 }
 
-__device__ __forceinline__ void write_record(const BatchParams &bp, uint32_t rec, uint32_t draw, const Setup &s,
-                                             const Vtx &v0, const Vtx &v1, const Vtx &v2, uint32_t extra = 0) {
+__device__ __forceinline__ void write_record(const BatchParams &bp, uint32_t rec, uint32_t draw, int ps,
+                                             const Setup &s, const Vtx &v0, const Vtx &v1, const Vtx &v2,
+                                             uint32_t extra = 0) {
     int4 *r = bp.raster[rec].w;
     r[0] = make_int4(s.e[0], s.e[1], s.e[2], s.e[3]);
     r[1] = make_int4(s.e[4], s.e[5], s.e[6], s.e[7]);
     r[2] = make_int4(s.e[8], __float_as_int(s.inv_area), __float_as_int(s.zbound), __float_as_int(s.ss[0][2]));
     r[3] = make_int4(__float_as_int(s.ss[1][2]), __float_as_int(s.ss[2][2]),
                      (s.minx & 0xFFFF) | (s.miny << 16), (s.maxx & 0xFFFF) | (s.maxy << 16));
-    float4 *h = bp.shade[rec].s;
-    h[0] = make_float4(s.rw[0], s.rw[1], s.rw[2], __uint_as_float(draw));
-    h[1] = make_float4(v0.v[4], v0.v[5], v0.v[6], v0.v[7]);
-    h[2] = make_float4(v1.v[4], v1.v[5], v1.v[6], v1.v[7]);
-    h[3] = make_float4(v2.v[4], v2.v[5], v2.v[6], v2.v[7]);
-    h[4] = make_float4(v0.v[8], v1.v[8], v2.v[8], __uint_as_float(extra));
     if (bp.geom) {
         TriGeom &g = bp.geom[rec];
 #pragma unroll
@@ -220,6 +215,13 @@ __device__ __forceinline__ void write_record(const BatchParams &bp, uint32_t rec
             g.x[k] = s.ss[k][0]; g.y[k] = s.ss[k][1]; g.z[k] = s.ss[k][2]; g.w[k] = s.ss[k][3];
         }
     }
+    float4 *h = bp.shade[rec].s;
+    h[0] = make_float4(s.rw[0], s.rw[1], s.rw[2], __uint_as_float(draw));
+    if (ps == kPsNone) return;   // a null pixel shader reads no attributes
+    h[1] = make_float4(v0.v[4], v0.v[5], v0.v[6], v0.v[7]);
+    h[2] = make_float4(v1.v[4], v1.v[5], v1.v[6], v1.v[7]);
+    h[3] = make_float4(v2.v[4], v2.v[5], v2.v[6], v2.v[7]);
+    h[4] = make_float4(v0.v[8], v1.v[8], v2.v[8], __uint_as_float(extra));
 }
 
 // clip_by_plane, main.c:609-647 (Sutherland-Hodgman on one normalised plane, plane_d = 0)
@@ -370,6 +372,8 @@ __global__ void __launch_bounds__(BLOCK, 2048 / BLOCK / 2) k_geometry(BatchParam
     __syncwarp();
     const uint32_t g = blockIdx.x * BLOCK + threadIdx.x;
     uint32_t mask = 0;
+    BinJob own;                 // the job of an unclipped triangle, given its slot warp-wide below
+    bool have_own = false;
     if (g < bp.total_tris) {
         const uint32_t draw = find_draw(bp, g);
         const DrawDesc &d = bp.draws[draw];
@@ -388,11 +392,10 @@ __global__ void __launch_bounds__(BLOCK, 2048 / BLOCK / 2) k_geometry(BatchParam
                  (p0[2] < 0.f && p1[2] < 0.f && p2[2] < 0.f) ||
                  (p0[2] > +p0[3] && p1[2] > +p1[3] && p2[2] > +p2[3]);
         bool clipped = false;
-        // counts the bins of one emitted triangle and records its bin job for k_scatter
-        auto bin_record = [&](uint32_t key, const Setup &su) {
+        // the bin job of one emitted triangle; false when it touches no tile
+        auto make_job = [&](uint32_t key, const Setup &su, BinJob &job) {
             int32_t tx0, ty0, tx1, ty1;
             tile_range(vw, su.minx, su.miny, su.maxx, su.maxy, tx0, ty0, tx1, ty1);
-            BinJob job;
             job.key = key;
             job.nx = tx1 >= tx0 ? (uint32_t)(tx1 - tx0 + 1) : 0u;
             job.ny = ty1 >= ty0 ? (uint32_t)(ty1 - ty0 + 1) : 0u;
@@ -401,7 +404,12 @@ __global__ void __launch_bounds__(BLOCK, 2048 / BLOCK / 2) k_geometry(BatchParam
             job.first_bin = vw.bin_base + ((uint32_t)max(ty0, 0) * vw.tiles_x + (uint32_t)max(tx0, 0)) * vw.draw_count +
                             d.draw_in_view;
             job.pad0 = job.pad1 = 0;
-            if (job.nx == 0 || job.ny == 0) return;
+            return job.nx != 0 && job.ny != 0;
+        };
+        // clip-fan triangles: counts the bins and records the job for k_scatter one by one
+        auto bin_record = [&](uint32_t key, const Setup &su) {
+            BinJob job;
+            if (!make_job(key, su, job)) return;
             const uint32_t slot = atomicAdd(bp.counters + kCtrEmitted, 1u);
             bp.jobs[slot] = job;
             if (job.nx * job.ny > bp.big_tiles) {
@@ -422,9 +430,9 @@ __global__ void __launch_bounds__(BLOCK, 2048 / BLOCK / 2) k_geometry(BatchParam
             if (!clipped) {
                 Setup su;
                 if (setup_triangle(d, v[0], v[1], v[2], su)) {
-                    write_record(bp, g, draw, su, v[0], v[1], v[2]);
+                    write_record(bp, g, draw, d.ps, su, v[0], v[1], v[2]);
                     mask = 1;
-                    bin_record(g << 3, su);
+                    have_own = make_job(g << 3, su, own);
                 }
             } else {
                 Vtx poly[kMaxClipVertices], tmp[kMaxClipVertices];
@@ -444,7 +452,7 @@ __global__ void __launch_bounds__(BLOCK, 2048 / BLOCK / 2) k_geometry(BatchParam
                             Setup su;
                             if (setup_triangle(d, poly[0], poly[f + 1], poly[f + 2], su)) {
                                 const uint32_t slot = bp.total_tris + base + (uint32_t)f;
-                                write_record(bp, slot, draw, su, poly[0], poly[f + 1], poly[f + 2]);
+                                write_record(bp, slot, draw, d.ps, su, poly[0], poly[f + 1], poly[f + 2]);
                                 mask |= 1u << f;
                                 bin_record((g << 3) | (uint32_t)(f + 1), su);
                             }
@@ -455,6 +463,30 @@ __global__ void __launch_bounds__(BLOCK, 2048 / BLOCK / 2) k_geometry(BatchParam
         }
         bp.tri_info[g] = (uint16_t)(mask | (clipped ? 0x100u : 0u));
     }
+    // job slots of the unclipped triangles: one counter update per warp
+    const uint32_t want = __ballot_sync(0xFFFFFFFFu, have_own);
+    uint32_t slot0 = 0;
+    if (lane == 0 && want) slot0 = atomicAdd(bp.counters + kCtrEmitted, (uint32_t)__popc(want));
+    slot0 = __shfl_sync(0xFFFFFFFFu, slot0, 0);
+    uint32_t single_bin = 0xFFFFFFFFu;   // the bin of a one-tile triangle, counted per warp below
+    if (have_own) {
+        const uint32_t slot = slot0 + (uint32_t)__popc(want & ((1u << lane) - 1u));
+        bp.jobs[slot] = own;
+        const uint32_t nt = own.nx * own.ny;
+        if (nt == 1) {
+            single_bin = own.first_bin;
+        } else if (nt > bp.big_tiles) {
+            s_q[warp][atomicAdd(&s_qn[warp], 1u)] = slot;   // counted by the whole warp below
+        } else {
+            for (uint32_t y = 0; y < own.ny; ++y)
+                for (uint32_t x = 0; x < own.nx; ++x)
+                    atomicAdd(bp.bin_count + own.first_bin + y * own.row_stride + x * own.col_stride, 1u);
+        }
+    }
+    // neighbouring triangles of a mesh mostly share their tile: one update per distinct bin
+    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, single_bin);
+    if (single_bin != 0xFFFFFFFFu && lane == __ffs(peers) - 1)
+        atomicAdd(bp.bin_count + single_bin, (uint32_t)__popc(peers));
     // assembled-triangle statistic (main.c:1238)
     uint32_t n = __popc(mask);
 #pragma unroll
@@ -919,22 +951,24 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
         const float z0 = __int_as_float(w2.w), z1 = __int_as_float(w3.x), z2 = __int_as_float(w3.y);
         float z = z0 + (z1 - z0) * b1;
         z = z + (z2 - z0) * b2;
-        // perspective correction, main.c:1106-1115
-        float den = (1.0f - (b1 + b2)) * s0.x;
-        den = den + b1 * s0.y;
-        den = den + b2 * s0.z;
-        den = 1.0f / den;
-        const float pb1 = (b1 * s0.y) * den;
-        const float pb2 = (b2 * s0.z) * den;
-        const float4 r0 = S[1], r1 = S[2], r2 = S[3], uv2 = S[4];
-        auto interp = [&](float v0, float v1, float v2) {
-            float tmp = v0 + (v1 - v0) * pb1;
-            return tmp + (v2 - v0) * pb2;
-        };
-        const float a0 = interp(r0.x, r1.x, r2.x), a1 = interp(r0.y, r1.y, r2.y), a2 = interp(r0.z, r1.z, r2.z);
-        const float u = interp(r0.w, r1.w, r2.w), v = interp(uv2.x, uv2.y, uv2.z);
-        const float3 c = run_ps(D.ps, a0, a1, a2, u, v, D.ps_tex);
-        V.color[o] = pack_color(c.x, c.y, c.z);
+        if (D.ps != kPsNone) {
+            // perspective correction, main.c:1106-1115
+            float den = (1.0f - (b1 + b2)) * s0.x;
+            den = den + b1 * s0.y;
+            den = den + b2 * s0.z;
+            den = 1.0f / den;
+            const float pb1 = (b1 * s0.y) * den;
+            const float pb2 = (b2 * s0.z) * den;
+            const float4 r0 = S[1], r1 = S[2], r2 = S[3], uv2 = S[4];
+            auto interp = [&](float v0, float v1, float v2) {
+                float tmp = v0 + (v1 - v0) * pb1;
+                return tmp + (v2 - v0) * pb2;
+            };
+            const float a0 = interp(r0.x, r1.x, r2.x), a1 = interp(r0.y, r1.y, r2.y), a2 = interp(r0.z, r1.z, r2.z);
+            const float u = interp(r0.w, r1.w, r2.w), v = interp(uv2.x, uv2.y, uv2.z);
+            const float3 c = run_ps(D.ps, a0, a1, a2, u, v, D.ps_tex);
+            V.color[o] = pack_color(c.x, c.y, c.z);
+        }
         V.depth[o] = z;
         if (V.vis_tri && bp.rank) {
             // the reference's triangle id: its index among the draw's assembled triangles
@@ -968,7 +1002,44 @@ __global__ void k_fill_u32(uint32_t *p, size_t n, uint32_t value, const uint32_t
     }
 }
 
+// All clears of a segment in one launch: each block fills whole chunks of kFillChunk words,
+// finding its job by binary search over chunk_begin. The jobs write disjoint memory (a segment's
+// clears are de-duplicated per target on the host, keeping the last).
+constexpr int kFillBlock = 256;
+
+__global__ void __launch_bounds__(kFillBlock) k_fill_many(const FillJob *jobs, uint32_t njobs, uint32_t nchunks,
+                                                          const uint32_t *error) {
+    if (error && ld_volatile_u32(error)) return;
+    for (uint32_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        uint32_t lo = 0, hi = njobs;   // last job with chunk_begin <= c
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (__ldg(&jobs[mid].chunk_begin) <= c) lo = mid; else hi = mid;
+        }
+        const FillJob j = jobs[lo];
+        const uint64_t begin = (uint64_t)(c - j.chunk_begin) * kFillChunk;
+        const uint64_t end = min(begin + kFillChunk, j.n);
+        uint32_t *p = j.p + begin;
+        const uint32_t cnt = (uint32_t)(end - begin);
+        if ((((uintptr_t)p) & 15) == 0) {
+            const uint4 v4 = make_uint4(j.value, j.value, j.value, j.value);
+            for (uint32_t k = threadIdx.x; k < cnt / 4; k += kFillBlock) reinterpret_cast<uint4 *>(p)[k] = v4;
+            for (uint32_t k = (cnt & ~3u) + threadIdx.x; k < cnt; k += kFillBlock) p[k] = j.value;
+        } else {
+            for (uint32_t k = threadIdx.x; k < cnt; k += kFillBlock) p[k] = j.value;
+        }
+    }
+}
+
 // ------------------------------------------------------------------ host-side launchers
+
+cudaError_t launch_fill_many(const FillJob *d_jobs, uint32_t njobs, uint32_t nchunks, const uint32_t *error,
+                             cudaStream_t stream) {
+    if (njobs == 0 || nchunks == 0) return cudaSuccess;
+    const uint32_t blocks = nchunks < 152u * 8u ? nchunks : 152u * 8u;
+    k_fill_many<<<blocks, kFillBlock, 0, stream>>>(d_jobs, njobs, nchunks, error);
+    return cudaGetLastError();
+}
 
 void set_clip_planes(const float planes[6][4], cudaStream_t stream) {
     cudaMemcpyToSymbolAsync(c_clip_planes, planes, sizeof(float) * 24, 0, cudaMemcpyHostToDevice, stream);

@@ -20,7 +20,7 @@ import numpy as np
 
 # shader ids (same numbering as include/malevich.h)
 VS_BASIC, VS_VERTEX_LIGHTING, VS_PASSTHROUGH, VS_FULLSCREEN, VS_PASSTHROUGH_UV = 1, 2, 3, 4, 5
-PS_BASIC, PS_PASSTHROUGH, PS_ENV_LIGHTING, PS_COLOR_TIMES_TEXEL = 1, 2, 3, 4
+PS_BASIC, PS_PASSTHROUGH, PS_ENV_LIGHTING, PS_COLOR_TIMES_TEXEL, PS_NONE = 1, 2, 3, 4, 5
 FMT_RGBA8, FMT_RGBA16F, FMT_RGBA32F = 1, 2, 3
 CULL_NONE, CULL_BACK, CULL_FRONT = 0, 1, 2
 DEPTH_GREATER_EQUAL, DEPTH_LESS = 0, 1
@@ -536,9 +536,10 @@ def diff_scene(seed=4, n_views=16, size=512, freq=50, tex_size=1024, heightfield
             "width": size, "height": size}
 
 
-def diff_frames(scene, pos=None, col=None, uv=None):
+def diff_frames(scene, pos=None, col=None, uv=None, shade=True):
     """One frame per view drawing the scene with MLV_VS_PASSTHROUGH_UV + COLOR_TIMES_TEXEL (depth LESS
-    cleared to 1, no culling): the exact rasteriser's visibility for the differentiable path."""
+    cleared to 1, no culling): the exact rasteriser's visibility for the differentiable path.
+    shade=False: the null pixel shader and no colour clear (depth and visibility only)."""
     pos = scene["pos"] if pos is None else pos
     col = scene["col"] if col is None else col
     uv = scene["uv"] if uv is None else uv
@@ -548,8 +549,10 @@ def diff_frames(scene, pos=None, col=None, uv=None):
     frames = []
     for k in range(pos.shape[0]):
         vb = np.concatenate([pos[k], scene["z"][k][:, None], col, uv], axis=1).astype(np.float32)
-        d = Draw(VS_PASSTHROUGH_UV, PS_COLOR_TIMES_TEXEL, vb, ib, 3 * n_tris, ps_tex=tex,
+        d = Draw(VS_PASSTHROUGH_UV, PS_COLOR_TIMES_TEXEL if shade else PS_NONE, vb, ib, 3 * n_tris,
+                 ps_tex=tex if shade else None,
                  viewport=(0.0, 0.0, float(scene["width"]), float(scene["height"]), 0.0, 1.0),
                  cull=CULL_NONE, depth_func=DEPTH_LESS)
-        frames.append(Frame(scene["width"], scene["height"], [d], clear_color=(0.0, 0.0, 0.0, 0.0), clear_depth=1.0))
+        frames.append(Frame(scene["width"], scene["height"], [d], clear_color=(0.0, 0.0, 0.0, 0.0) if shade else None,
+                            clear_depth=1.0))
     return frames

@@ -485,7 +485,7 @@ static int texture_ok(const orc_texture *t, int want_float, int any) {
 
 static int validate(const orc_draw *d) {
     if (d->vs < ORC_VS_BASIC || d->vs > ORC_VS_PASSTHROUGH_UV) return -1;
-    if (d->ps < ORC_PS_BASIC || d->ps > ORC_PS_COLOR_TIMES_TEXEL) return -1;
+    if (d->ps < ORC_PS_BASIC || d->ps > ORC_PS_NONE) return -1;
     if (d->vb_stride < 32 || !d->vb) return -1;
     if ((d->vs == ORC_VS_BASIC || d->vs == ORC_VS_VERTEX_LIGHTING || d->vs == ORC_VS_FULLSCREEN) && !d->cb)
         return -1;
@@ -653,9 +653,11 @@ int orc_draw_indexed(orc_target *t, const orc_draw *d, uint32_t draw_seq, orc_st
                 float z = at[2];
                 int pass = less ? (z < tdep[p]) : (z >= tdep[p]);
                 if (!pass) continue;
-                float col[3];
-                orc_run_ps(d->ps, at, &d->ps_tex, col);
-                tcol[p] = pack_color(col);
+                if (d->ps != ORC_PS_NONE) { /* a null pixel shader leaves the colour */
+                    float col[3];
+                    orc_run_ps(d->ps, at, &d->ps_tex, col);
+                    tcol[p] = pack_color(col);
+                }
                 tdep[p] = z;
                 ttri[p] = ids[q];
                 tdraw[p] = draw_seq;

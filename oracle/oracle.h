@@ -33,7 +33,7 @@ extern "C" {
 enum { ORC_FMT_RGBA8 = 1, ORC_FMT_RGBA16F = 2, ORC_FMT_RGBA32F = 3 };
 enum { ORC_VS_BASIC = 1, ORC_VS_VERTEX_LIGHTING = 2, ORC_VS_PASSTHROUGH = 3, ORC_VS_FULLSCREEN = 4,
        ORC_VS_PASSTHROUGH_UV = 5 };
-enum { ORC_PS_BASIC = 1, ORC_PS_PASSTHROUGH = 2, ORC_PS_ENV_LIGHTING = 3, ORC_PS_COLOR_TIMES_TEXEL = 4 };
+enum { ORC_PS_BASIC = 1, ORC_PS_PASSTHROUGH = 2, ORC_PS_ENV_LIGHTING = 3, ORC_PS_COLOR_TIMES_TEXEL = 4, ORC_PS_NONE = 5 };
 enum { ORC_CULL_NONE = 0, ORC_CULL_BACK = 1, ORC_CULL_FRONT = 2 };
 enum { ORC_DEPTH_GREATER_EQUAL = 0, ORC_DEPTH_LESS = 1 };
 

@@ -25,8 +25,8 @@ def _p(t):
 
 def visibility(device, scene, pos=None):
     """Per-view primitive ids (the input triangle each pixel shows) from the exact rasteriser,
-    all views in one batched command list."""
-    frames = scenes.diff_frames(scene, pos=pos)
+    all views in one batched command list, with the null pixel shader."""
+    frames = scenes.diff_frames(scene, pos=pos, shade=False)
     r = api.FrameRenderer(device, frames, primitive_ids=True)
     r.render_batched()
     prims = np.stack([r.read(i)["vis_prim"] for i in range(len(frames))])
@@ -34,30 +34,18 @@ def visibility(device, scene, pos=None):
     return prims
 
 
-class _DeviceArray:
-    """A tightly packed device texture exposed through __cuda_array_interface__ (no copy)."""
-
-    def __init__(self, ptr, shape, typestr):
-        self.__cuda_array_interface__ = {"shape": shape, "typestr": typestr, "data": (ptr, False), "version": 2}
-
-
-def gather_primitive_ids(renderer, out):
-    """Copies every view's primitive-id target of a FrameRenderer into out[views, H, W] (int32),
-    on torch's current stream, after the renderer's context has finished."""
-    for i, t in enumerate(renderer.prim_targets):
-        fr = renderer.frames[i]
-        out[i].copy_(torch.as_tensor(_DeviceArray(t.device_pointer(), (fr.height, fr.width), "<i4"), device="cuda"))
-    return out
-
-
 class DiffScene:
     """Device-side topology, UVs, visibility and the checkpoint (barycentric) buffer."""
 
     def __init__(self, scene, prims):
+        """prims: per-view primitive ids, a numpy array or an int32 device tensor used in place."""
         dev = "cuda"
         self.ib = torch.from_numpy(np.ascontiguousarray(scene["ib"]).view(np.int32)).to(dev)
         self.uv = torch.from_numpy(np.ascontiguousarray(scene["uv"], np.float32)).to(dev)
-        self.prim = torch.from_numpy(np.ascontiguousarray(prims).view(np.int32)).to(dev)
+        if isinstance(prims, torch.Tensor):
+            self.prim = prims
+        else:
+            self.prim = torch.from_numpy(np.ascontiguousarray(prims).view(np.int32)).to(dev)
         self.views, self.height, self.width = prims.shape
         self.n_verts = scene["col"].shape[0]
         self.n_tris = scene["ib"].shape[0]

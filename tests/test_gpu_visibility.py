@@ -1,0 +1,70 @@
+"""The visibility pass of the differentiable path through the C ABI: the null pixel shader
+(MLV_PS_NONE, depth and visibility only) and primitive-id targets placed on caller memory
+(mlv_create_texture2d_on_memory), against the shaded pass and the oracle."""
+import numpy as np
+import pytest
+
+from malevich_gb300 import api, scenes
+from oracle import pyoracle
+
+pytestmark = pytest.mark.gpu
+
+
+def small_diff_scene():
+    return scenes.diff_scene(seed=9, n_views=4, size=96, freq=12, tex_size=64)
+
+
+def test_null_pixel_shader_keeps_colour_and_matches_depth_and_ids(device):
+    sc = small_diff_scene()
+    shaded = scenes.diff_frames(sc)
+    bare = scenes.diff_frames(sc, shade=False)
+    r1 = api.FrameRenderer(device, shaded, visibility=True, primitive_ids=True)
+    r1.render_batched()
+    r2 = api.FrameRenderer(device, bare, visibility=True, primitive_ids=True)
+    ctx = device.immediate
+    for rt, _, _ in r2.targets:
+        ctx.clear_render_target(rt, (0.25, 0.5, 0.75, 1.0))
+    r2.render_batched()
+    import ctypes
+    sentinel = np.uint32(pyoracle.oracle_lib().orc_encode_clear_color((ctypes.c_float * 4)(0.25, 0.5, 0.75, 1.0)))
+    for k in range(len(shaded)):
+        a, b = r1.read(k), r2.read(k)
+        for key in ("depth", "vis_tri", "vis_draw", "vis_bary", "vis_prim"):
+            assert np.array_equal(a[key].view(np.uint32), b[key].view(np.uint32)), key
+        assert np.all(b["color"] == sentinel)
+        o = pyoracle.render_oracle(bare[k])
+        assert np.array_equal(b["vis_prim"], o["vis_prim"])
+        assert np.array_equal(b["depth"].view(np.uint32), o["depth"].view(np.uint32))
+    r1.destroy()
+    r2.destroy()
+
+
+def test_primitive_ids_placed_on_caller_memory(device):
+    import torch
+    sc = small_diff_scene()
+    frames = scenes.diff_frames(sc, shade=False)
+    n, s = len(frames), sc["width"]
+    prim = torch.full((n, s, s), 7, dtype=torch.int32, device="cuda")
+    r = api.FrameRenderer(device, frames, primitive_id_memory=[prim[i].data_ptr() for i in range(n)])
+    r.render_batched()
+    device.immediate.finish()
+    placed = prim.cpu().numpy().view(np.uint32)
+    for k in range(n):
+        assert np.array_equal(placed[k], r.read(k)["vis_prim"])
+        assert np.array_equal(placed[k], pyoracle.render_oracle(frames[k])["vis_prim"])
+    r.destroy()
+    # the library does not own placed memory: the tensor stays valid after destroy
+    assert int(prim[0, 0, 0].item()) in (-1, int(placed[0, 0, 0].view(np.int32)))
+
+
+def test_placed_texture_rejects_unaligned_memory(device):
+    import ctypes
+    import torch
+    buf = torch.zeros(64 * 64 + 4, dtype=torch.int32, device="cuda")
+    with pytest.raises(api.MalevichError):
+        api.Texture2D(device, 64, 64, api.FORMAT_R32_UINT, bind=api.BIND_UNORDERED_ACCESS,
+                      device_memory=buf.data_ptr() + 4)
+    lib = api.load_library()
+    h = ctypes.c_void_p()
+    assert lib.mlv_create_texture2d_on_memory(device.handle, None, ctypes.c_void_p(buf.data_ptr()),
+                                              ctypes.byref(h)) != 0
