@@ -182,6 +182,63 @@ def algorithmic_bytes(frame, dev_stats, written_pixels):
     return {"k_geometry": geometry, "k_tile": tile}
 
 
+def run_multiview_section(dev, args):
+    """Batched multi-view: 64 views at seeded resolutions in {256..1024}^2, 16 icosphere/heightfield
+    meshes of 2k-200k triangles, 4-16 draws per view, basic_vs + basic_ps. Launch shapes come from
+    the autotuner; the batched command list (one CUDA graph) is timed against per-draw launches
+    and compared with them view by view (colour and depth bit for bit)."""
+    import torch
+    from malevich_gb300 import api, autotune, scenes
+    frames = scenes.config3_batched(seed=3)
+    ctx = dev.immediate
+    base = ctx.tuning()
+    r = api.FrameRenderer(dev, frames)
+    r.render_batched()
+    tuned = autotune.autotune(dev, r, repeats=3, warmup=1)
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.int32, device="cuda")
+
+    def timed(fn, n):
+        for _ in range(3):
+            fn()
+        ctx.finish()
+        evs = []
+        for i in range(n):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                flush.fill_(i)
+                a.record(stream)
+            fn()
+            with torch.cuda.stream(stream):
+                b.record(stream)
+            evs.append((a, b))
+        ctx.finish()
+        return float(np.mean([a.elapsed_time(b) for a, b in evs]))
+
+    ctx.reset_stats()
+    batched_ms = timed(r.render_batched, args.steps)
+    st = ctx.stats()
+    batched = [r.read(i) for i in range(len(frames))]
+    per_draw_ms = timed(r.render_per_draw, max(3, args.steps // 2))
+    same = 0
+    for i in range(len(frames)):
+        o = r.read(i)
+        same += all(np.array_equal(o[k].view(np.uint32), batched[i][k].view(np.uint32)) for k in ("color", "depth"))
+    tris = sum(d.index_count // 3 for f in frames for d in f.draws)
+    pixels = sum(f.width * f.height for f in frames)
+    runs = st["batch_count"] or 1
+    r.destroy()
+    ctx.set_tuning(**base)
+    return {"views": len(frames), "draws": sum(len(f.draws) for f in frames), "input_triangles": tris,
+            "pixels": pixels, "batched_ms": round(batched_ms, 4), "per_draw_ms": round(per_draw_ms, 4),
+            "batched_speedup": round(per_draw_ms / batched_ms, 3),
+            "batched_mtri_per_s": round(tris / (batched_ms / 1e3) / 1e6, 1),
+            "assembled_per_run": st["assembled_triangle_count"] // runs,
+            "views_identical_to_per_draw": "%d/%d" % (same, len(frames)),
+            "autotuned": tuned["best"], "autotune_points": len(tuned["results"]),
+            "l2": "flushed between steps (256 MB write outside the timed events)"}
+
+
 def run_diff_sections(dev, args):
     """The differentiable configurations through the C ABI (no autograd): (4) forward + backward
     time per view for 16 views at 512x512 of a 50k-triangle sphere; (5) an Adam loop over 256 views
@@ -550,10 +607,11 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
 
-    diff = None
+    diff = multiview = None
     if not args.no_diff:
         r.destroy()
         r = None
+        multiview = run_multiview_section(dev, args)
         diff = run_diff_sections(dev, args)
 
     result = None
@@ -593,6 +651,7 @@ def main():
             "frame_stats": {k: int(v) for k, v in frame_stats.items()},
             "cpu_baseline": cpu,
             "clocks": clk,
+            "multiview": multiview,
             "differentiable": diff,
             "gpu_launches": launches,
             "wall_s_timed": round(wall, 4),

@@ -351,7 +351,8 @@ MLV_API mlv_status mlv_get_tile_infos(mlv_context context, uint32_t *tile_index,
  * mlv_diff_backward reads the checkpoint and grad_image = dL/dimage, recomputes the interpolation
  * and ADDS dL/dcolors, dL/dtexture (scattered through the bilinear weights) and dL/dpositions (the
  * barycentric terms, visibility fixed) into the gradient arrays it is given (any may be NULL).
- * All pointers are device memory (positions, uvs, barycentrics 8-byte aligned, texture 16-byte);
+ * All pointers are device memory (positions, uvs, barycentrics, grad_positions 8-byte aligned,
+ * texture and grad_texture 16-byte);
  * both calls are asynchronous on `cuda_stream`; the backward needs the checkpoint of a forward
  * with the same positions. */
 typedef struct mlv_diff_desc {

@@ -1,0 +1,88 @@
+"""Launch-shape autotuner for a batched workload.
+
+The reference has no counterpart: its tile and bin sizes are compile-time constants of a CPU
+binner (source/main.c:24-30) and its work per thread is one 8-wide SIMD triangle. On the GPU
+the same pipeline has free launch shapes that change the speed but never the output: the tile
+kernel's warps per CTA (how many 8x8 tiles a CTA carries), the geometry kernel's CTA size (how
+many input triangles one CTA sets up and bins), and the threshold above which a triangle's bins
+are counted and scattered cooperatively by a whole warp instead of by its own thread
+(triangles-per-warp against warps-per-triangle). The hierarchical-Z tile and the bins stay 8x8
+pixels: the tile grid is observable through the reference's per-tile depth bounds
+(main.c:1005-1010), so it is not tuned.
+
+`autotune` times a renderer's batched execution (its command list, replayed as a CUDA graph)
+for every point of a search space with CUDA events on the context's stream, flushing L2 between
+timed runs, and leaves the fastest point set on the context.
+"""
+import itertools
+
+SPACE = {
+    "tile_warps_per_block": (2, 4, 8),
+    "geometry_block": (128, 256, 512),
+    "big_triangle_tiles": (4, 8, 16, 32),
+}
+
+
+def candidates(space=None):
+    """Every point of the search space as a dict, in a fixed order."""
+    space = SPACE if space is None else space
+    keys = sorted(space)
+    return [dict(zip(keys, vals)) for vals in itertools.product(*(space[k] for k in keys))]
+
+
+def pick(results):
+    """The fastest point of [(point, ms)]; ties keep the earlier point."""
+    best = None
+    for point, ms in results:
+        if best is None or ms < best[1]:
+            best = (point, ms)
+    return best
+
+
+def event_timer(context, repeats=5, warmup=2, flush_bytes=256 << 20):
+    """A timer for `autotune`: runs fn warmup + repeats times on the context's stream and returns
+    the median device time of the timed runs in ms (L2 flushed before each)."""
+    import torch
+    stream = torch.cuda.ExternalStream(context.stream())
+    flush = torch.empty(flush_bytes // 4, dtype=torch.int32, device="cuda") if flush_bytes else None
+
+    def time_fn(fn):
+        for _ in range(warmup):
+            fn()
+        times = []
+        for i in range(repeats):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                if flush is not None:
+                    flush.fill_(i)
+                a.record(stream)
+            fn()
+            with torch.cuda.stream(stream):
+                b.record(stream)
+            b.synchronize()
+            times.append(a.elapsed_time(b))
+        times.sort()
+        return times[len(times) // 2]
+
+    return time_fn
+
+
+def autotune(device, renderer, space=None, time_fn=None, repeats=5, warmup=2):
+    """Sweeps the search space for `renderer.render_batched()` on the device's immediate
+    context, sets the fastest point and returns {"best": point, "ms": ms, "results": [...]}.
+    The outputs do not depend on the point (launch shapes only); `time_fn(fn) -> ms` may be
+    given (the default times with CUDA events)."""
+    ctx = device.immediate
+    time_fn = time_fn or event_timer(ctx, repeats=repeats, warmup=warmup)
+    base = ctx.tuning()
+    results = []
+    try:
+        for point in candidates(space):
+            ctx.set_tuning(**point)
+            results.append((point, float(time_fn(renderer.render_batched))))
+    except Exception:
+        ctx.set_tuning(**base)
+        raise
+    best, ms = pick(results)
+    ctx.set_tuning(**best)
+    return {"best": best, "ms": ms, "results": results}

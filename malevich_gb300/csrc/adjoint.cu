@@ -180,90 +180,135 @@ __global__ void __launch_bounds__(kDiffBlock) k_diff_forward(mlv_diff_desc d) {
     reinterpret_cast<float2 *>(d.barycentrics)[i] = bary;
 }
 
+// Sums v over the lanes of the caller's run (lane .. end, end the run's last lane) into its first
+// lane: a segmented suffix sum by shuffles; every lane of the warp calls it.
+template <int N>
+__device__ __forceinline__ void run_sum(float (&v)[N], uint32_t lane, int end) {
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            const float o = __shfl_down_sync(0xFFFFFFFFu, v[k], off);
+            if ((int)lane + off <= end) v[k] += o;
+        }
+    }
+}
+
+// One thread per pixel. Texel gradients go out as float4 atomics; the vertex-colour and position
+// gradients of a run of neighbouring pixels on the same triangle (the common case along a row)
+// are summed in registers first and leave as one set of atomics per run.
 __global__ void __launch_bounds__(kDiffBlock) k_diff_backward(mlv_diff_desc d) {
     const size_t npix = (size_t)d.width * d.height;
     const size_t i = (size_t)blockIdx.x * kDiffBlock + threadIdx.x;
-    if (i >= npix * d.num_views) return;
-    const uint32_t tri = d.primitive_ids[i];
-    if (tri == 0xFFFFFFFFu || tri >= d.n_tris) return;
-    const uint32_t view = (uint32_t)(i / npix);
-    const uint32_t p = (uint32_t)(i - (size_t)view * npix);
-    const float2 bary = reinterpret_cast<const float2 *>(d.barycentrics)[i];
-    if (bary.x < kMinBarycentric) return;  // dropped by the differentiable coverage
-    uint32_t vi[3];
-    load_triangle(d, tri, vi);
+    const uint32_t lane = threadIdx.x & 31;
+    uint32_t tri = 0xFFFFFFFFu, view = 0, p = 0;
+    float2 bary = make_float2(kDropped, kDropped);
+    if (i < npix * d.num_views) {
+        view = (uint32_t)(i / npix);
+        p = (uint32_t)(i - (size_t)view * npix);
+        tri = d.primitive_ids[i];
+        if (tri < d.n_tris) bary = reinterpret_cast<const float2 *>(d.barycentrics)[i];
+        if (tri >= d.n_tris || bary.x < kMinBarycentric) tri = 0xFFFFFFFFu;   // background or dropped
+    }
+    const bool live = tri != 0xFFFFFFFFu;
+    float gc[9], gp[6];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) gc[k] = 0.f;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) gp[k] = 0.f;
     PixelEval e;
-    shade(d, bary.x, bary.y, vi, e);
-    const float3 dout = make_float3(d.grad_image[3 * i], d.grad_image[3 * i + 1], d.grad_image[3 * i + 2]);
-    const float3 dcol = make_float3(dout.x * e.tex.x, dout.y * e.tex.y, dout.z * e.tex.z);
-    const float3 dtex = make_float3(dout.x * e.col.x, dout.y * e.col.y, dout.z * e.col.z);
-    const float l[3] = {e.l0, e.l1, e.l2};
+    if (live) {
+        uint32_t vi[3];
+        load_triangle(d, tri, vi);
+        shade(d, bary.x, bary.y, vi, e);
+        const float3 dout = make_float3(d.grad_image[3 * i], d.grad_image[3 * i + 1], d.grad_image[3 * i + 2]);
+        const float3 dcol = make_float3(dout.x * e.tex.x, dout.y * e.tex.y, dout.z * e.tex.z);
+        const float3 dtex = make_float3(dout.x * e.col.x, dout.y * e.col.y, dout.z * e.col.z);
+        const float l[3] = {e.l0, e.l1, e.l2};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            gc[3 * k] = l[k] * dcol.x;
+            gc[3 * k + 1] = l[k] * dcol.y;
+            gc[3 * k + 2] = l[k] * dcol.z;
+        }
+        if (d.grad_texture) {
+            // scatter through the bilinear weights (common_shader_core.h:143-161)
+            const int32_t tw1 = (int32_t)d.tex_width - 1, th1 = (int32_t)d.tex_height - 1;
+            const float a = 1.f - e.fs, b = 1.f - e.ft;
+            const float w[4] = {a * b, e.fs * b, a * e.ft, e.fs * e.ft};
+            const int32_t si[4] = {e.s0, e.s0 + 1, e.s0, e.s0 + 1}, ti[4] = {e.t0, e.t0, e.t0 + 1, e.t0 + 1};
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                float4 *g = reinterpret_cast<float4 *>(d.grad_texture) + (size_t)clampi(ti[q], th1) * d.tex_width +
+                            clampi(si[q], tw1);
+                atomicAdd(g, make_float4(w[q] * dtex.x, w[q] * dtex.y, w[q] * dtex.z, 0.f));
+            }
+        }
+        if (d.grad_positions) {
+            const float3 t00 = texel(d.texture, d.tex_width, d.tex_height, e.s0, e.t0);
+            const float3 t10 = texel(d.texture, d.tex_width, d.tex_height, e.s0 + 1, e.t0);
+            const float3 t01 = texel(d.texture, d.tex_width, d.tex_height, e.s0, e.t0 + 1);
+            const float3 t11 = texel(d.texture, d.tex_width, d.tex_height, e.s0 + 1, e.t0 + 1);
+            const float dfs = dtex.x * ((1.f - e.ft) * (t10.x - t00.x) + e.ft * (t11.x - t01.x)) +
+                              dtex.y * ((1.f - e.ft) * (t10.y - t00.y) + e.ft * (t11.y - t01.y)) +
+                              dtex.z * ((1.f - e.ft) * (t10.z - t00.z) + e.ft * (t11.z - t01.z));
+            const float dft =
+                dtex.x * (((1.f - e.fs) * t01.x + e.fs * t11.x) - ((1.f - e.fs) * t00.x + e.fs * t10.x)) +
+                dtex.y * (((1.f - e.fs) * t01.y + e.fs * t11.y) - ((1.f - e.fs) * t00.y + e.fs * t10.y)) +
+                dtex.z * (((1.f - e.fs) * t01.z + e.fs * t11.z) - ((1.f - e.fs) * t00.z + e.fs * t10.z));
+            const float du = dfs * (float)d.tex_width, dv = -dft * (float)d.tex_height;
+            // G_k = dL/dlambda_k, taken relative to G_0 (the barycentric derivatives sum to zero)
+            const float2 uv0 = __ldg(reinterpret_cast<const float2 *>(d.uvs) + e.vi[0]);
+            const float *c0 = d.colors + 3 * (size_t)e.vi[0];
+            float G[3];
+            G[0] = 0.f;
+#pragma unroll
+            for (int k = 1; k < 3; ++k) {
+                const float2 uvk = __ldg(reinterpret_cast<const float2 *>(d.uvs) + e.vi[k]);
+                const float *ck = d.colors + 3 * (size_t)e.vi[k];
+                G[k] = du * (uvk.x - uv0.x) + dv * (uvk.y - uv0.y) + dcol.x * (__ldg(ck) - __ldg(c0)) +
+                       dcol.y * (__ldg(ck + 1) - __ldg(c0 + 1)) + dcol.z * (__ldg(ck + 2) - __ldg(c0 + 2));
+            }
+            const float W = (float)d.width, H = (float)d.height;
+            CornerGeom g;
+            corner_geometry(d.positions + (size_t)view * d.n_verts * 2, e.vi, W, H, (float)(p % d.width),
+                            (float)(p / d.width), g);
+            const float rA = 1.0f / g.A;
+            const float S = G[1] * e.l1 + G[2] * e.l2;
+            // sum_k G_k d lambda_k / d v_j = (sum_k G_k d n_k / d v_j - S dA / d v_j) / A, n_k the numerators
+            const float gX0 = (G[2] * g.by - G[1] * g.cy - S * (g.e1y - g.e2y)) * rA;
+            const float gY0 = (G[1] * g.cx - G[2] * g.bx - S * (g.e2x - g.e1x)) * rA;
+            const float gX1 = (-G[2] * g.ay - S * g.e2y) * rA;
+            const float gY1 = (G[2] * g.ax + S * g.e2x) * rA;
+            const float gX2 = (G[1] * g.ay + S * g.e1y) * rA;
+            const float gY2 = (-G[1] * g.ax - S * g.e1x) * rA;
+            gp[0] = W * gX0; gp[1] = -H * gY0;
+            gp[2] = W * gX1; gp[3] = -H * gY1;
+            gp[4] = W * gX2; gp[5] = -H * gY2;
+        }
+    }
+    // runs of neighbouring pixels with the same (view, triangle)
+    const uint32_t ptri = __shfl_up_sync(0xFFFFFFFFu, tri, 1), pview = __shfl_up_sync(0xFFFFFFFFu, view, 1);
+    const bool head = lane == 0 || ptri != tri || pview != view;
+    const uint32_t heads = __ballot_sync(0xFFFFFFFFu, head);
+    const uint32_t later = heads & ~((2u << lane) - 1u);
+    const int end = later ? __ffs(later) - 2 : 31;
+    if (d.grad_colors) run_sum(gc, lane, end);
+    if (d.grad_positions) run_sum(gp, lane, end);
+    if (!(head && live)) return;
     if (d.grad_colors) {
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             float *g = d.grad_colors + 3 * (size_t)e.vi[k];
-            atomicAdd(g, l[k] * dcol.x);
-            atomicAdd(g + 1, l[k] * dcol.y);
-            atomicAdd(g + 2, l[k] * dcol.z);
-        }
-    }
-    const int32_t tw1 = (int32_t)d.tex_width - 1, th1 = (int32_t)d.tex_height - 1;
-    if (d.grad_texture) {
-        // scatter through the bilinear weights (common_shader_core.h:143-161)
-        const float a = 1.f - e.fs, b = 1.f - e.ft;
-        const float w[4] = {a * b, e.fs * b, a * e.ft, e.fs * e.ft};
-        const int32_t si[4] = {e.s0, e.s0 + 1, e.s0, e.s0 + 1}, ti[4] = {e.t0, e.t0, e.t0 + 1, e.t0 + 1};
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            float *g = d.grad_texture + ((size_t)clampi(ti[q], th1) * d.tex_width + clampi(si[q], tw1)) * 4;
-            atomicAdd(g, w[q] * dtex.x);
-            atomicAdd(g + 1, w[q] * dtex.y);
-            atomicAdd(g + 2, w[q] * dtex.z);
+            atomicAdd(g, gc[3 * k]);
+            atomicAdd(g + 1, gc[3 * k + 1]);
+            atomicAdd(g + 2, gc[3 * k + 2]);
         }
     }
     if (d.grad_positions) {
-        const float3 t00 = texel(d.texture, d.tex_width, d.tex_height, e.s0, e.t0);
-        const float3 t10 = texel(d.texture, d.tex_width, d.tex_height, e.s0 + 1, e.t0);
-        const float3 t01 = texel(d.texture, d.tex_width, d.tex_height, e.s0, e.t0 + 1);
-        const float3 t11 = texel(d.texture, d.tex_width, d.tex_height, e.s0 + 1, e.t0 + 1);
-        const float dfs = dtex.x * ((1.f - e.ft) * (t10.x - t00.x) + e.ft * (t11.x - t01.x)) +
-                          dtex.y * ((1.f - e.ft) * (t10.y - t00.y) + e.ft * (t11.y - t01.y)) +
-                          dtex.z * ((1.f - e.ft) * (t10.z - t00.z) + e.ft * (t11.z - t01.z));
-        const float dft = dtex.x * (((1.f - e.fs) * t01.x + e.fs * t11.x) - ((1.f - e.fs) * t00.x + e.fs * t10.x)) +
-                          dtex.y * (((1.f - e.fs) * t01.y + e.fs * t11.y) - ((1.f - e.fs) * t00.y + e.fs * t10.y)) +
-                          dtex.z * (((1.f - e.fs) * t01.z + e.fs * t11.z) - ((1.f - e.fs) * t00.z + e.fs * t10.z));
-        const float du = dfs * (float)d.tex_width, dv = -dft * (float)d.tex_height;
-        // G_k = dL/dlambda_k, taken relative to G_0 (the barycentric derivatives sum to zero)
-        const float2 uv0 = __ldg(reinterpret_cast<const float2 *>(d.uvs) + e.vi[0]);
-        const float *c0 = d.colors + 3 * (size_t)e.vi[0];
-        float G[3];
+        float2 *gpos = reinterpret_cast<float2 *>(d.grad_positions + (size_t)view * d.n_verts * 2);
 #pragma unroll
-        for (int k = 1; k < 3; ++k) {
-            const float2 uvk = __ldg(reinterpret_cast<const float2 *>(d.uvs) + e.vi[k]);
-            const float *ck = d.colors + 3 * (size_t)e.vi[k];
-            G[k] = du * (uvk.x - uv0.x) + dv * (uvk.y - uv0.y) + dcol.x * (__ldg(ck) - __ldg(c0)) +
-                   dcol.y * (__ldg(ck + 1) - __ldg(c0 + 1)) + dcol.z * (__ldg(ck + 2) - __ldg(c0 + 2));
-        }
-        const float W = (float)d.width, H = (float)d.height;
-        CornerGeom g;
-        corner_geometry(d.positions + (size_t)view * d.n_verts * 2, e.vi, W, H, (float)(p % d.width),
-                        (float)(p / d.width), g);
-        const float rA = 1.0f / g.A;
-        const float S = G[1] * e.l1 + G[2] * e.l2;
-        // sum_k G_k d lambda_k / d v_j = (sum_k G_k d n_k / d v_j - S dA / d v_j) / A, n_k the numerators
-        float gX[3], gY[3];
-        gX[0] = (G[2] * g.by - G[1] * g.cy - S * (g.e1y - g.e2y)) * rA;
-        gY[0] = (G[1] * g.cx - G[2] * g.bx - S * (g.e2x - g.e1x)) * rA;
-        gX[1] = (-G[2] * g.ay - S * g.e2y) * rA;
-        gY[1] = (G[2] * g.ax + S * g.e2x) * rA;
-        gX[2] = (G[1] * g.ay + S * g.e1y) * rA;
-        gY[2] = (-G[1] * g.ax - S * g.e1x) * rA;
-        float *gp = d.grad_positions + (size_t)view * d.n_verts * 2;
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            atomicAdd(gp + 2 * (size_t)e.vi[k], W * gX[k]);
-            atomicAdd(gp + 2 * (size_t)e.vi[k] + 1, -H * gY[k]);
-        }
+        for (int k = 0; k < 3; ++k) atomicAdd(gpos + e.vi[k], make_float2(gp[2 * k], gp[2 * k + 1]));
     }
 }
 
@@ -285,9 +330,9 @@ mlv_status check_desc(const mlv_diff_desc *d, bool backward) {
         set_last_error("the backward needs grad_image");
         return MLV_ERROR_INVALID_ARG;
     }
-    if (((uintptr_t)d->positions | (uintptr_t)d->uvs | (uintptr_t)d->barycentrics) & 7u ||
-        (uintptr_t)d->texture & 15u) {
-        set_last_error("positions, uvs and barycentrics need 8-byte alignment, texture 16-byte");
+    if (((uintptr_t)d->positions | (uintptr_t)d->uvs | (uintptr_t)d->barycentrics | (uintptr_t)d->grad_positions) & 7u ||
+        ((uintptr_t)d->texture | (uintptr_t)d->grad_texture) & 15u) {
+        set_last_error("positions, uvs, barycentrics, grad_positions need 8-byte alignment, texture, grad_texture 16-byte");
         return MLV_ERROR_INVALID_ARG;
     }
     if ((uint64_t)d->width * d->height * d->num_views > 0xFFFFFFFFull * kDiffBlock) {

@@ -185,7 +185,7 @@ struct mlv_command_list_t {
     std::vector<Segment> segments;
     // graph replay state
     cudaGraphExec_t exec = nullptr;
-    uint64_t exec_generation = ~0ull;
+    uint64_t exec_generation = ~0ull, exec_tuning = ~0ull;
     mlv_context_t *exec_context = nullptr;
     int executions = 0;
     DrawDesc *d_draws = nullptr;   // per-segment descriptor copies owned by the list
@@ -211,6 +211,7 @@ struct mlv_context_t {
     std::vector<Segment> recorded;     // deferred contexts
     Workspace ws;
     mlv_tuning tuning = {4, 1, 16, 256, 0, 0};
+    uint64_t tuning_generation = 0;    // bumped by mlv_set_tuning: captured graphs re-capture
     uint64_t host_stats[8] = {};       // vertex_count, input triangles, draws, batches, launches
     bool profiling = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pool;
@@ -1465,7 +1466,8 @@ MLV_API mlv_status mlv_execute_command_list(mlv_context c, mlv_command_list l) {
         if (l->executions == 1) MLV_TRY(sync_context(c));
         return MLV_OK;
     }
-    if (!l->exec || l->exec_generation != c->ws.generation || l->exec_context != c) {
+    if (!l->exec || l->exec_generation != c->ws.generation || l->exec_context != c ||
+        l->exec_tuning != c->tuning_generation) {
         if (l->exec) cudaGraphExecDestroy(l->exec);
         l->exec = nullptr;
         cudaGraph_t g = nullptr;
@@ -1487,6 +1489,7 @@ MLV_API mlv_status mlv_execute_command_list(mlv_context c, mlv_command_list l) {
         cudaGraphDestroy(g);
         if (e != cudaSuccess) return fail(MLV_ERROR_DEVICE, std::string("graph instantiate: ") + cudaGetErrorString(e));
         l->exec_generation = c->ws.generation;
+        l->exec_tuning = c->tuning_generation;
         l->exec_context = c;
     }
     CUDA_TRY(cudaGraphLaunch(l->exec, c->stream));
@@ -1548,6 +1551,7 @@ MLV_API mlv_status mlv_set_tuning(mlv_context c, const mlv_tuning *t) {
     if (t->geometry_block != 128 && t->geometry_block != 256 && t->geometry_block != 512)
         return fail(MLV_ERROR_INVALID_ARG, "geometry_block must be 128, 256 or 512");
     if (t->big_triangle_tiles < 1) return fail(MLV_ERROR_INVALID_ARG, "big_triangle_tiles must be >= 1");
+    if (memcmp(&c->tuning, t, sizeof(*t)) != 0) ++c->tuning_generation;
     c->tuning = *t;
     return MLV_OK;
 }

@@ -363,10 +363,17 @@ __device__ __forceinline__ void count_tiles(const BatchParams &bp, const DrawDes
 // A warp's triangles that span more than big_tiles tiles: at most 32 lanes x 7 clip fans.
 constexpr int kWarpQueue = 32 * 7;
 
+// Resident threads per SM the geometry kernel's register budget is sized for (1024: 64 registers).
+#ifndef MLV_GEOMETRY_THREADS_PER_SM
+#define MLV_GEOMETRY_THREADS_PER_SM 1024
+#endif
+
 template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK, 2048 / BLOCK / 2) k_geometry(BatchParams bp) {
+__global__ void __launch_bounds__(BLOCK, MLV_GEOMETRY_THREADS_PER_SM / BLOCK) k_geometry(BatchParams bp) {
     __shared__ uint32_t s_q[BLOCK / 32][kWarpQueue];   // job slots
     __shared__ uint32_t s_qn[BLOCK / 32];
+    __shared__ uint32_t s_warp[BLOCK / 32];
+    __shared__ uint32_t s_slot0;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (lane == 0) s_qn[warp] = 0;
     __syncwarp();
@@ -463,14 +470,20 @@ __global__ void __launch_bounds__(BLOCK, 2048 / BLOCK / 2) k_geometry(BatchParam
         }
         bp.tri_info[g] = (uint16_t)(mask | (clipped ? 0x100u : 0u));
     }
-    // job slots of the unclipped triangles: one counter update per warp
-    const uint32_t want = __ballot_sync(0xFFFFFFFFu, have_own);
-    uint32_t slot0 = 0;
-    if (lane == 0 && want) slot0 = atomicAdd(bp.counters + kCtrEmitted, (uint32_t)__popc(want));
-    slot0 = __shfl_sync(0xFFFFFFFFu, slot0, 0);
+    // job slots of the unclipped triangles: one counter update per block (the assembled-triangle
+    // statistic, main.c:1238, rides in the upper half of the scanned value)
+    uint32_t own_total;
+    const uint32_t own_rank =
+        block_exclusive_scan<BLOCK>((have_own ? 1u : 0u) | ((uint32_t)__popc(mask) << 16), s_warp, own_total);
+    if (threadIdx.x == 0) {
+        const uint32_t jobs = own_total & 0xFFFFu, assembled = own_total >> 16;
+        s_slot0 = jobs ? atomicAdd(bp.counters + kCtrEmitted, jobs) : 0u;
+        if (assembled) atomicAdd(bp.stats + kStatAssembled, (unsigned long long)assembled);
+    }
+    __syncthreads();
     uint32_t single_bin = 0xFFFFFFFFu;   // the bin of a one-tile triangle, counted per warp below
     if (have_own) {
-        const uint32_t slot = slot0 + (uint32_t)__popc(want & ((1u << lane) - 1u));
+        const uint32_t slot = s_slot0 + (own_rank & 0xFFFFu);
         bp.jobs[slot] = own;
         const uint32_t nt = own.nx * own.ny;
         if (nt == 1) {
@@ -487,11 +500,6 @@ __global__ void __launch_bounds__(BLOCK, 2048 / BLOCK / 2) k_geometry(BatchParam
     const uint32_t peers = __match_any_sync(0xFFFFFFFFu, single_bin);
     if (single_bin != 0xFFFFFFFFu && lane == __ffs(peers) - 1)
         atomicAdd(bp.bin_count + single_bin, (uint32_t)__popc(peers));
-    // assembled-triangle statistic (main.c:1238)
-    uint32_t n = __popc(mask);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xFFFFFFFFu, n, o);
-    if (lane == 0 && n) atomicAdd(bp.stats + kStatAssembled, (unsigned long long)n);
     // triangles spanning many tiles: the warp counts their tiles together
     __syncwarp();
     const uint32_t nq = s_qn[warp];
@@ -659,10 +667,23 @@ __global__ void __launch_bounds__(kScatterBlock) k_scatter(BatchParams bp) {
         if (lane == 0) s_qn[warp] = 0;
         __syncwarp();
         const uint32_t i = base + threadIdx.x;
+        BinJob job = {};
         if (i < njobs) {
             const uint4 *jp = reinterpret_cast<const uint4 *>(bp.jobs + i);
             const uint4 j0 = jp[0], j1 = jp[1];
-            BinJob job = {j0.x, j0.y, j0.z, j0.w, j1.x, j1.y, 0u, 0u};
+            job = {j0.x, j0.y, j0.z, j0.w, j1.x, j1.y, 0u, 0u};
+        }
+        // one-tile jobs of the warp that share a bin take their list positions with one atomic
+        const uint32_t single = (i < njobs && job.nx * job.ny == 1) ? job.first_bin : 0xFFFFFFFFu;
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, single);
+        if (single != 0xFFFFFFFFu) {
+            const int leader = __ffs(peers) - 1;
+            uint32_t top = 0;
+            if (lane == leader) top = atomicSub(bp.bin_count + single, (uint32_t)__popc(peers));
+            top = __shfl_sync(peers, top, leader);
+            const uint32_t r = (uint32_t)__popc(peers & ((1u << lane) - 1u));
+            bp.list[__ldg(bp.bin_start + single) + top - 1u - r] = job.key;
+        } else if (i < njobs) {
             if (job.nx * job.ny > bp.big_tiles) {
                 s_q[warp][atomicAdd(&s_qn[warp], 1u)] = job;
             } else {

@@ -518,17 +518,29 @@ def diff_scene(seed=4, n_views=16, size=512, freq=50, tex_size=1024, heightfield
     tex = rng.random((tex_size, tex_size, 4)).astype(np.float32)
     pos = np.zeros((n_views, n, 2), np.float32)
     z = np.zeros((n_views, n), np.float32)
+    f = 1.0 / np.tan(np.radians(50.0) / 2)
     for k in range(n_views):
-        q = rng.standard_normal(4)
-        q /= np.linalg.norm(q)
-        a, b, c, d = q
-        R = np.array([[a * a + b * b - c * c - d * d, 2 * (b * c - a * d), 2 * (b * d + a * c)],
-                      [2 * (b * c + a * d), a * a - b * b + c * c - d * d, 2 * (c * d - a * b)],
-                      [2 * (b * d - a * c), 2 * (c * d + a * b), a * a - b * b - c * c + d * d]])
-        Q = P @ R.T
-        dist = 3.0 if not heightfield_cells else 3.2
-        depth = Q[:, 2] + dist
-        f = 1.0 / np.tan(np.radians(50.0) / 2)
+        if heightfield_cells:
+            # a camera over the heightfield at a seeded azimuth and an elevation of 45-90 degrees,
+            # 2.4 from its centre, looking at it (the grid spans most of the view)
+            az, el = rng.uniform(0, 2 * np.pi), np.radians(rng.uniform(45.0, 90.0))
+            cam = 2.4 * np.array([np.cos(el) * np.cos(az), np.cos(el) * np.sin(az), np.sin(el)])
+            fwd = -cam / np.linalg.norm(cam)
+            right = np.array([-np.sin(az), np.cos(az), 0.0])
+            up = np.cross(right, fwd)
+            D = P - cam
+            Q = np.stack([D @ right, D @ up, D @ fwd], axis=1)
+            depth, dist = Q[:, 2], 2.4
+        else:
+            q = rng.standard_normal(4)
+            q /= np.linalg.norm(q)
+            a, b, c, d = q
+            R = np.array([[a * a + b * b - c * c - d * d, 2 * (b * c - a * d), 2 * (b * d + a * c)],
+                          [2 * (b * c + a * d), a * a - b * b + c * c - d * d, 2 * (c * d - a * b)],
+                          [2 * (b * d - a * c), 2 * (c * d + a * b), a * a - b * b - c * c + d * d]])
+            Q = P @ R.T
+            dist = 3.0
+            depth = Q[:, 2] + dist
         pos[k, :, 0] = 0.5 + 0.5 * f * Q[:, 0] / depth
         pos[k, :, 1] = 0.5 + 0.5 * f * Q[:, 1] / depth
         z[k] = (depth / (dist + 2.0)).astype(np.float32)

@@ -1,0 +1,89 @@
+"""The autotuner's search (CPU, with a fake timer) and, on the GPU, that tuning changes only the
+speed: the batched outputs after autotuning equal the default launch shapes' bit for bit."""
+import numpy as np
+import pytest
+
+from malevich_gb300 import autotune, scenes
+
+
+def test_candidates_cover_the_space_in_order():
+    space = {"b": (1, 2), "a": (3, 4, 5)}
+    pts = autotune.candidates(space)
+    assert len(pts) == 6
+    assert pts[0] == {"a": 3, "b": 1} and pts[-1] == {"a": 5, "b": 2}
+    assert len(autotune.candidates()) == 3 * 3 * 4
+
+
+def test_pick_takes_the_fastest_and_keeps_the_first_tie():
+    res = [({"x": 1}, 3.0), ({"x": 2}, 1.5), ({"x": 3}, 1.5), ({"x": 4}, 2.0)]
+    assert autotune.pick(res) == ({"x": 2}, 1.5)
+
+
+class _FakeCtx:
+    def __init__(self):
+        self.t = {"tile_warps_per_block": 4, "geometry_block": 256, "big_triangle_tiles": 16}
+        self.history = []
+
+    def tuning(self):
+        return dict(self.t)
+
+    def set_tuning(self, **kw):
+        self.t.update(kw)
+        self.history.append(dict(self.t))
+
+
+class _FakeDevice:
+    def __init__(self):
+        self.immediate = _FakeCtx()
+
+
+class _FakeRenderer:
+    def render_batched(self):
+        pass
+
+
+def test_autotune_sets_the_fastest_point():
+    dev = _FakeDevice()
+    cost = lambda: dev.immediate.t["tile_warps_per_block"] * 10 + abs(dev.immediate.t["geometry_block"] - 128) + \
+        dev.immediate.t["big_triangle_tiles"] * 0.1
+    out = autotune.autotune(dev, _FakeRenderer(), time_fn=lambda fn: (fn(), cost())[1])
+    assert out["best"] == {"big_triangle_tiles": 4, "geometry_block": 128, "tile_warps_per_block": 2}
+    assert dev.immediate.t == out["best"]
+    assert len(out["results"]) == 36
+
+
+def test_autotune_restores_the_tuning_on_error():
+    dev = _FakeDevice()
+    calls = []
+
+    def bad_timer(fn):
+        calls.append(1)
+        if len(calls) == 3:
+            raise RuntimeError("timer failed")
+        return 1.0
+
+    with pytest.raises(RuntimeError):
+        autotune.autotune(dev, _FakeRenderer(), time_fn=bad_timer)
+    assert dev.immediate.t == {"tile_warps_per_block": 4, "geometry_block": 256, "big_triangle_tiles": 16}
+
+
+@pytest.mark.gpu
+def test_autotuned_batched_output_equals_default(device):
+    from malevich_gb300 import api
+    frames = scenes.config3_batched(seed=11, n_views=6, n_meshes=5, resolutions=(128, 192), tri_range=(500, 8000),
+                                    draws_per_view=(2, 4), tex_size=64, n_textures=2)
+    ctx = device.immediate
+    base = ctx.tuning()
+    r = api.FrameRenderer(device, frames, visibility=True)
+    r.render_batched()
+    want = [r.read(i) for i in range(len(frames))]
+    out = autotune.autotune(device, r, space={"tile_warps_per_block": (2, 8), "geometry_block": (128, 512),
+                                              "big_triangle_tiles": (1, 32)}, repeats=2, warmup=1)
+    assert out["best"] == {k: ctx.tuning()[k] for k in out["best"]}
+    r.render_batched()
+    for i in range(len(frames)):
+        got = r.read(i)
+        for key in ("color", "depth", "vis_tri", "vis_draw", "vis_bary"):
+            assert np.array_equal(got[key].view(np.uint32), want[i][key].view(np.uint32)), (i, key)
+    r.destroy()
+    ctx.set_tuning(**base)
