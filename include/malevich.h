@@ -27,7 +27,7 @@ extern "C" {
 #define MLV_API
 #endif
 
-#define MLV_ABI_VERSION 1
+#define MLV_ABI_VERSION 2
 
 /* ------------------------------------------------------------------ status */
 
@@ -106,8 +106,20 @@ typedef enum mlv_primitive_topology {
  * fixed point) is positive (main.c:851-856): that is MLV_CULL_BACK, the default. */
 typedef enum mlv_cull_mode { MLV_CULL_NONE = 1, MLV_CULL_FRONT = 2, MLV_CULL_BACK = 3 } mlv_cull_mode;
 
+/* Coverage rule. The reference covers a pixel when (E0|E1|E2) > 0 at its sample point
+ * (main.c:1028): every edge inclusive; its top-left rule is a TODO (main.c:1014,1027). TOP_LEFT
+ * (new) covers a sample on an edge only for a left edge (interior to its right) or a top edge
+ * (horizontal, interior below it), so a pixel on an edge shared by two triangles is covered once. */
+typedef enum mlv_fill_rule { MLV_FILL_INCLUSIVE = 0, MLV_FILL_TOP_LEFT = 1 } mlv_fill_rule;
+
+/* Sample point. The reference samples coverage and attributes at the pixel corner (x, y)
+ * (main.c:1014-1025); PIXEL_CENTER (new) samples at (x + 1/2, y + 1/2). */
+typedef enum mlv_sample_position { MLV_SAMPLE_PIXEL_CORNER = 0, MLV_SAMPLE_PIXEL_CENTER = 1 } mlv_sample_position;
+
 typedef struct mlv_rasterizer_desc {
     mlv_cull_mode cull_mode;
+    mlv_fill_rule fill_rule;              /* 0: the reference's rule */
+    mlv_sample_position sample_position;  /* 0: the reference's sample point */
 } mlv_rasterizer_desc;
 
 /* Depth test. The reference tests GREATER_EQUAL (reversed Z, main.c:1166) against a tile
@@ -240,7 +252,7 @@ MLV_API mlv_status mlv_ps_set_shader_resources(mlv_context context, uint32_t sta
                                                const mlv_texture2d *textures);
 /* RS::viewport (main.c:94-96, 1277-1278); one viewport */
 MLV_API mlv_status mlv_rs_set_viewports(mlv_context context, uint32_t num_viewports, const mlv_viewport *viewports);
-/* cull mode (the reference hard-codes back-face culling, main.c:856) */
+/* cull mode (the reference hard-codes back-face culling, main.c:856), fill rule and sample point */
 MLV_API mlv_status mlv_rs_set_state(mlv_context context, const mlv_rasterizer_desc *desc);
 /* depth function (the reference hard-codes GREATER_EQUAL, main.c:1166) */
 MLV_API mlv_status mlv_om_set_depth_stencil_state(mlv_context context, const mlv_depth_stencil_desc *desc);

@@ -69,7 +69,7 @@ class Viewport(ctypes.Structure):
 
 
 class RasterizerDesc(ctypes.Structure):
-    _fields_ = [("cull_mode", ctypes.c_int)]
+    _fields_ = [("cull_mode", ctypes.c_int), ("fill_rule", ctypes.c_int), ("sample_position", ctypes.c_int)]
 
 
 class DepthStencilDesc(ctypes.Structure):
@@ -257,9 +257,9 @@ class Context:
     def rs_set_viewport(self, vp):
         _check(self.lib.mlv_rs_set_viewports(self.handle, 1, ctypes.byref(Viewport(*vp))))
 
-    def rs_set_cull(self, cull_internal):
+    def rs_set_cull(self, cull_internal, fill_rule=0, sample_center=0):
         mode = {scenes.CULL_NONE: CULL_NONE, scenes.CULL_BACK: CULL_BACK, scenes.CULL_FRONT: CULL_FRONT}[cull_internal]
-        _check(self.lib.mlv_rs_set_state(self.handle, ctypes.byref(RasterizerDesc(mode))))
+        _check(self.lib.mlv_rs_set_state(self.handle, ctypes.byref(RasterizerDesc(mode, fill_rule, sample_center))))
 
     def om_set_depth_func(self, depth_func_internal):
         f = COMPARISON_LESS if depth_func_internal == scenes.DEPTH_LESS else COMPARISON_GREATER_EQUAL
@@ -474,7 +474,7 @@ class FrameRenderer:
             ctx.vs_set_shader_resource(0, self._texture(d.vs_tex) if d.vs_tex is not None else None)
             ctx.ps_set_shader_resource(0, self._texture(d.ps_tex) if d.ps_tex is not None else None)
             ctx.rs_set_viewport(d.viewport)
-            ctx.rs_set_cull(d.cull)
+            ctx.rs_set_cull(d.cull, d.fill_rule, d.sample_center)
             ctx.om_set_depth_func(d.depth_func)
             if d.ib is not None:
                 ctx.draw_indexed(d.index_count, d.start_index, d.base_vertex)

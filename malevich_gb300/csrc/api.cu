@@ -123,6 +123,7 @@ struct PipelineState {
     mlv_viewport viewport = {0, 0, 0, 0, 0, 1};
     bool viewport_set = false;
     int cull = 1;          // internal: 0 none, 1 back, 2 front
+    int raster_flags = 0;  // kRasterTopLeft | kRasterCenter
     int depth_less = 0;
     mlv_texture2d rtv = nullptr, dsv = nullptr;
     mlv_texture2d vis_tri = nullptr, vis_draw = nullptr, vis_bary = nullptr, vis_prim = nullptr;
@@ -1106,13 +1107,21 @@ MLV_API mlv_status mlv_rs_set_viewports(mlv_context c, uint32_t n, const mlv_vie
 
 MLV_API mlv_status mlv_rs_set_state(mlv_context c, const mlv_rasterizer_desc *d) {
     if (!c) return fail(MLV_ERROR_INVALID_ARG, "context is NULL");
-    if (!d) { c->st.cull = 1; return MLV_OK; }
+    if (!d) { c->st.cull = 1; c->st.raster_flags = 0; return MLV_OK; }
+    int cull;
     switch (d->cull_mode) {
-        case MLV_CULL_NONE: c->st.cull = 0; break;
-        case MLV_CULL_BACK: c->st.cull = 1; break;
-        case MLV_CULL_FRONT: c->st.cull = 2; break;
+        case MLV_CULL_NONE: cull = 0; break;
+        case MLV_CULL_BACK: cull = 1; break;
+        case MLV_CULL_FRONT: cull = 2; break;
         default: return fail(MLV_ERROR_INVALID_ARG, "unknown cull mode");
     }
+    if (d->fill_rule != MLV_FILL_INCLUSIVE && d->fill_rule != MLV_FILL_TOP_LEFT)
+        return fail(MLV_ERROR_INVALID_ARG, "unknown fill rule");
+    if (d->sample_position != MLV_SAMPLE_PIXEL_CORNER && d->sample_position != MLV_SAMPLE_PIXEL_CENTER)
+        return fail(MLV_ERROR_INVALID_ARG, "unknown sample position");
+    c->st.cull = cull;
+    c->st.raster_flags = (d->fill_rule == MLV_FILL_TOP_LEFT ? kRasterTopLeft : 0) |
+                         (d->sample_position == MLV_SAMPLE_PIXEL_CENTER ? kRasterCenter : 0);
     return MLV_OK;
 }
 
@@ -1249,6 +1258,7 @@ static mlv_status build_draw(mlv_context c, uint32_t count, uint32_t start, int3
     d.vs = s.vs;
     d.ps = s.ps;
     d.cull = s.cull;
+    d.raster_flags = s.raster_flags;
     d.depth_less = s.depth_less;
     mlv_buffer cb = s.vs_cb[0];
     if (s.vs == MLV_VS_BASIC || s.vs == MLV_VS_VERTEX_LIGHTING || s.vs == MLV_VS_FULLSCREEN) {

@@ -8,6 +8,8 @@ namespace mlv {
 constexpr int kTile = 8;                 // 8x8 pixel tiles: the reference's bins (main.c:24-25)
 constexpr int kSubpix = 4;               // 28.4 fixed point (main.c:39)
 constexpr int kPsNone = 5;               // MLV_PS_NONE: depth and visibility only
+constexpr int kRasterTopLeft = 1;        // MLV_FILL_TOP_LEFT
+constexpr int kRasterCenter = 2;         // MLV_SAMPLE_PIXEL_CENTER
 constexpr int kMaxClipVertices = 16;     // main.c:38
 constexpr int kMaxViewsPerBatch = 4096;
 
@@ -37,6 +39,7 @@ struct DrawDesc {
     uint32_t tri_begin;                  // first input triangle of this draw in the batch
     uint32_t tri_count;
     int32_t vs, ps, cull, depth_less;    // cull: 0 none, 1 back (reference), 2 front
+    int32_t raster_flags;                // kRasterTopLeft | kRasterCenter (0: the reference)
     uint32_t view;                       // view (render target + depth) index in the batch
     uint32_t draw_in_view;               // position among the view's draws in this batch
     uint32_t draw_seq;                   // draw number since the render target's last clear

@@ -177,6 +177,11 @@ __device__ __forceinline__ bool setup_triangle(const DrawDesc &d, const Vtx &v0,
     set_edge(s.e + 6, area, x[0], y[0], x[1], y[1]);
     set_edge(s.e + 0, area, x[1], y[1], x[2], y[2]);
     set_edge(s.e + 3, area, x[2], y[2], x[0], y[0]);
+    if (d.raster_flags & kRasterCenter) {
+        // E at (x + 1/2, y + 1/2): ((a x) << 4) + 8 a + ((b y) << 4) + 8 b + c
+#pragma unroll
+        for (int k = 0; k < 9; k += 3) s.e[k + 2] = (int32_t)((uint32_t)s.e[k + 2] + (((uint32_t)s.e[k] + (uint32_t)s.e[k + 1]) << 3));
+    }
     float af = (float)(area >> (kSubpix * 2));
     if (af == 0.0f) af = 1.0f;
     s.inv_area = fabsf(1.f / af);
@@ -834,6 +839,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
         if (s == e) continue;
         const DrawDesc &D = bp.draws[V.draw_begin + dd];
         const bool less = D.depth_less != 0;
+        const bool top_left = (D.raster_flags & kRasterTopLeft) != 0;
         const unsigned long long sentinel = less ? ~0ull : 0ull;
         s_best[warp][lane] = sentinel;
         s_best[warp][lane + 32] = sentinel;
@@ -873,6 +879,11 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
                     st[kSOrigin] = (uint32_t)(bx0 - x0) | ((uint32_t)(by0 - y0) << 8);
                     st[kSWidth] = w | (((65536u + w - 1) / w) << 8);
                     st[kSKey] = key;
+                    // top-left rule: an edge value of 0 covers only on a left edge (a > 0) or a top
+                    // edge (a == 0, b > 0); the others need E >= 1 (bit k set: edge k needs it)
+                    st[kSPad] = ((int32_t)a0 > 0 || (a0 == 0 && (int32_t)b0 > 0) ? 0u : 1u) |
+                                ((int32_t)a1 > 0 || (a1 == 0 && (int32_t)b1 > 0) ? 0u : 2u) |
+                                ((int32_t)a2 > 0 || (a2 == 0 && (int32_t)b2 > 0) ? 0u : 4u);
                 }
             }
             if (capture) s_mask[warp][lane] = 0;
@@ -899,7 +910,10 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
                 const uint32_t E0 = st[kSE0] + col * st[kSA0] + row * st[kSB0];
                 const uint32_t E1 = st[kSE1] + col * st[kSA1] + row * st[kSB1];
                 const uint32_t E2 = st[kSE2] + col * st[kSA2] + row * st[kSB2];
-                if ((int32_t)(E0 | E1 | E2) > 0) {   // main.c:1028
+                const uint32_t nb = st[kSPad];
+                const bool covered = top_left ? (int32_t)((E0 - (nb & 1u)) | (E1 - ((nb >> 1) & 1u)) | (E2 - (nb >> 2))) >= 0
+                                              : (int32_t)(E0 | E1 | E2) > 0;   // main.c:1028
+                if (covered) {
                     const uint32_t org = st[kSOrigin];
                     const int p = (int)(((org >> 8) + row) * 8 + (org & 0xFFu) + col);
                     if (capture) atomicOr(&s_mask[warp][j], 1ull << p);

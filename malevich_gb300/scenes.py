@@ -57,6 +57,8 @@ class Draw:
     depth_func: int = DEPTH_GREATER_EQUAL
     start_index: int = 0
     base_vertex: int = 0
+    fill_rule: int = 0        # 0: the reference's inclusive rule; 1: top-left
+    sample_center: int = 0    # 0: sample at the pixel corner (the reference); 1: at its centre
 
     @property
     def vb_stride(self):

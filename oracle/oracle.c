@@ -440,6 +440,9 @@ static int assemble(const orc_draw *d, const float vout[3][12], uint32_t input, 
         set_edge(r.e[2], area, x[0], y[0], x[1], y[1]);
         set_edge(r.e[0], area, x[1], y[1], x[2], y[2]);
         set_edge(r.e[1], area, x[2], y[2], x[0], y[0]);
+        if (d->sample_center) /* E at (x + 1/2, y + 1/2): ((a x) << 4) + 8 a + ((b y) << 4) + 8 b + c */
+            for (int e = 0; e < 3; ++e)
+                r.e[e][2] = (int32_t)((uint32_t)r.e[e][2] + (((uint32_t)r.e[e][0] + (uint32_t)r.e[e][1]) << 3));
         float af = (float)(area >> (SUBPIX * 2));
         if (af == 0.0f) af = 1.0f;
         r.inv_area = fabsf(1.f / af);
@@ -620,8 +623,18 @@ int orc_draw_indexed(orc_target *t, const orc_draw *d, uint32_t draw_seq, orc_st
                         for (int e = 0; e < 3; ++e)
                             ev[e] = (((uint32_t)r->e[e][0] * x) << SUBPIX) + (((uint32_t)r->e[e][1] * y) << SUBPIX) +
                                     (uint32_t)r->e[e][2];
-                        if ((int32_t)(ev[0] | ev[1] | ev[2]) > 0 && valid[j * 8 + i])
-                            mask |= (uint64_t)1 << (j * 8 + i);
+                        int cov;
+                        if (d->fill_rule) {
+                            /* top-left: E > 0, or E == 0 on a left edge (interior to its right, a > 0)
+                             * or a top edge (horizontal, interior below it, a == 0 and b > 0) */
+                            uint32_t bias[3];
+                            for (int e = 0; e < 3; ++e)
+                                bias[e] = (r->e[e][0] > 0 || (r->e[e][0] == 0 && r->e[e][1] > 0)) ? 0u : 1u;
+                            cov = (int32_t)((ev[0] - bias[0]) | (ev[1] - bias[1]) | (ev[2] - bias[2])) >= 0;
+                        } else {
+                            cov = (int32_t)(ev[0] | ev[1] | ev[2]) > 0;
+                        }
+                        if (cov && valid[j * 8 + i]) mask |= (uint64_t)1 << (j * 8 + i);
                     }
             }
             if (masks) masks[q] = mask;

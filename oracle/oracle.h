@@ -55,6 +55,10 @@ typedef struct orc_draw {
     orc_texture vs_tex, ps_tex;
     float viewport[6];           /* top_left_x, top_left_y, width, height, min_depth, max_depth */
     int32_t cull, depth_func;
+    /* Modes the reference lacks (0 = the reference): fill_rule 1 = top-left (an edge value of 0
+     * covers only on a top or left edge, instead of the inclusive (E0|E1|E2) > 0 of main.c:1028);
+     * sample_center 1 = test and interpolate at the pixel centre instead of its corner (main.c:1014). */
+    int32_t fill_rule, sample_center;
 } orc_draw;
 
 typedef struct orc_target {

@@ -34,7 +34,7 @@ class OrcDraw(ctypes.Structure):
                 ("ib", ctypes.c_void_p), ("index_count", ctypes.c_uint32), ("start_index", ctypes.c_uint32),
                 ("base_vertex", ctypes.c_int32), ("cb", ctypes.c_void_p), ("vs_tex", OrcTexture),
                 ("ps_tex", OrcTexture), ("viewport", ctypes.c_float * 6), ("cull", ctypes.c_int32),
-                ("depth_func", ctypes.c_int32)]
+                ("depth_func", ctypes.c_int32), ("fill_rule", ctypes.c_int32), ("sample_center", ctypes.c_int32)]
 
 
 class OrcTarget(ctypes.Structure):
@@ -117,6 +117,8 @@ def _draw_struct(d, keep):
     s.index_count = d.index_count
     s.start_index = d.start_index
     s.base_vertex = d.base_vertex
+    s.fill_rule = getattr(d, "fill_rule", 0)
+    s.sample_center = getattr(d, "sample_center", 0)
     s.cb = _ptr(cb)
     s.vs_tex = _tex(d.vs_tex, keep)
     s.ps_tex = _tex(d.ps_tex, keep)
