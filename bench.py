@@ -185,9 +185,9 @@ def algorithmic_bytes(frame, dev_stats, written_pixels):
 def run_single_draw_section(dev, args):
     """The plain single draw: a level-5 icosphere (20,480 triangles) with basic_vs + basic_ps over a
     1024x1024 RGBA8 noise texture into 1280x720 RGBA8 + D32 (depth LESS, cleared to 1.0). The frame
-    (both clears and the draw) replays as a one-frame command list (a CUDA graph); timed as 200
-    back-to-back frames (its 8 MB working set stays in L2, which is stated) and as single frames
-    with L2 flushed before each. Algorithmic bytes per frame: indices + unique vertices (32 B) + the
+    (both clears and the draw) is timed as 100 back-to-back frames recorded in one command list
+    (one CUDA graph launch; its 8 MB working set stays in L2, which is stated) and as single-frame
+    graph launches with L2 flushed before each (these include the launch latency). Algorithmic bytes per frame: indices + unique vertices (32 B) + the
     texture footprint (min(size, 4 taps x 4 B x fragments)) + colour and depth written once."""
     import torch
     from malevich_gb300 import api, scenes
@@ -201,16 +201,24 @@ def run_single_draw_section(dev, args):
     for _ in range(5):
         r.render_batched()
     ctx.finish()
-    n = 200
-    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with torch.cuda.stream(stream):
-        a.record(stream)
-    for _ in range(n):
-        r.render_batched()
-    with torch.cuda.stream(stream):
-        b.record(stream)
+    # 100 frames back to back in one command list (one graph launch): the device time per frame
+    n = 100
+    rep = r.record_repeated(n)
+    for _ in range(3):
+        ctx.execute_command_list(rep)
     ctx.finish()
-    warm_ms = a.elapsed_time(b) / n
+    reps = []
+    for _ in range(5):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            a.record(stream)
+        ctx.execute_command_list(rep)
+        with torch.cuda.stream(stream):
+            b.record(stream)
+        reps.append((a, b))
+    ctx.finish()
+    warm_ms = float(np.median([x.elapsed_time(y) for x, y in reps])) / n
+    rep.destroy()
     cold = []
     for i in range(20):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -223,6 +231,12 @@ def run_single_draw_section(dev, args):
         cold.append((e0, e1))
     ctx.finish()
     cold_ms = float(np.median([x.elapsed_time(y) for x, y in cold]))
+    ctx.set_profiling(True)
+    ctx.reset_stats()
+    for _ in range(10):
+        r.render_batched()
+    stages = {k: round(v[0] / max(v[1], 1), 4) for k, v in ctx.stage_times().items()}
+    ctx.set_profiling(False)
     got = r.read(0)
     r.destroy()
     ost = pyoracle.render_oracle(frame)
@@ -236,7 +250,7 @@ def run_single_draw_section(dev, args):
     return {"workload": "icosphere L5, 20,480 triangles, 1280x720 RGBA8 + D32, basic_vs + basic_ps, LESS",
             "ms_per_frame_back_to_back": round(warm_ms, 5), "ms_per_frame_l2_flushed": round(cold_ms, 5),
             "mtri_per_s": round(tris / (warm_ms / 1e3) / 1e6, 1), "gpix_per_s": round(frags / (warm_ms / 1e3) / 1e9, 3),
-            "fragments_written": frags, "depth_bit_exact_vs_oracle": same_depth,
+            "fragments_written": frags, "depth_bit_exact_vs_oracle": same_depth, "stage_ms_eager": stages,
             "algorithmic_bytes_per_frame": int(nbytes),
             "roofline": {"bound": "hbm", "achieved_gbs_l2_flushed": round(nbytes / (cold_ms / 1e3) / 1e9, 1),
                          "peak": peak, "peak_kind": peak_kind,
@@ -532,7 +546,7 @@ def main():
         return rc
 
     import torch
-    from malevich_gb300 import api, build, scenes
+    from malevich_gb300 import api, build, replicas, scenes
     build.build()
     torch.cuda.set_device(local)
     dev = api.Device(local)
@@ -584,15 +598,11 @@ def main():
     clk = clocks.stop()
     st1 = ctx.stats()
     step_ms = [a.elapsed_time(b) for a, b in evs]
-    ms = float(np.mean(step_ms))
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = replicas.job_time(float(np.mean(step_ms)), dist, "cuda")    # the slowest rank's step
     launches = int(st1["kernel_launches"] - st0["kernel_launches"])
     frame_stats = {k: (st1[k] - st0[k]) // args.steps for k in st1}
     tris = frame.input_triangles
-    value = tris * world / (ms / 1e3) / 1e6
+    value = replicas.total_units(tris, dist, "cuda") / (ms / 1e3) / 1e6   # every rank's frame
 
     img = r.read(0)["depth"]
     r_img_written = int(np.count_nonzero(img != np.float32(frame.clear_depth)))
@@ -662,11 +672,7 @@ def main():
     for _ in range(args.steps):
         e2e_step()
     torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = replicas.job_time((time.perf_counter() - t0) / args.steps, dist, "cuda")
 
     diff = multiview = single = None
     if not args.no_diff:

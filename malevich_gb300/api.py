@@ -497,6 +497,17 @@ class FrameRenderer:
             dctx.destroy()
         return self.command_list
 
+    def record_repeated(self, times):
+        """A command list that plays the frames `times` times in a row on the same targets (each
+        repetition clears and draws again): back-to-back frames in one graph launch."""
+        dctx = self.device.create_deferred_context()
+        for _ in range(times):
+            for fr, tg, pr in zip(self.frames, self.targets, self.prim_targets):
+                self._issue(dctx, fr, tg, pr)
+        lst = dctx.finish_command_list()
+        dctx.destroy()
+        return lst
+
     def render_batched(self):
         """All draws of all frames as one batched launch sequence (a CUDA graph after the first run)."""
         self.device.immediate.execute_command_list(self.record())
