@@ -154,11 +154,11 @@ struct Workspace {
     TriRaster *raster = nullptr;
     TriShade *shade = nullptr;
     TriGeom *geom = nullptr;
-    BinJob *jobs = nullptr;
     uint32_t record_cap = 0;          // slots: input triangles + clip-fan overflow
     uint32_t overflow_cap = 0;        // overflow slots the last sizing reserved
     bool keep_geom = false;
     uint16_t *tri_info = nullptr;
+    uint2 *bins_of = nullptr;
     uint32_t *rank = nullptr;
     uint32_t tri_cap = 0;
     uint32_t *bin_count = nullptr, *bin_start = nullptr;
@@ -329,11 +329,10 @@ static mlv_status ensure_workspace(mlv_context_t *c, const BatchSizes &s, bool k
         uint64_t n = std::max<uint64_t>(slots, (uint64_t)w.record_cap + w.record_cap / 2);
         n = std::max<uint64_t>(n, 4096);
         if (n > 0x7FFFFFFFull) return fail(MLV_ERROR_CAPACITY_EXCEEDED, "more than 2^31 triangle slots");
-        cudaFree(w.raster); cudaFree(w.shade); cudaFree(w.geom); cudaFree(w.jobs);
-        w.raster = nullptr; w.shade = nullptr; w.geom = nullptr; w.jobs = nullptr;
+        cudaFree(w.raster); cudaFree(w.shade); cudaFree(w.geom);
+        w.raster = nullptr; w.shade = nullptr; w.geom = nullptr;
         MLV_TRY(dev_alloc((void **)&w.raster, n * sizeof(TriRaster)));
         MLV_TRY(dev_alloc((void **)&w.shade, n * sizeof(TriShade)));
-        MLV_TRY(dev_alloc((void **)&w.jobs, n * sizeof(BinJob)));
         w.keep_geom = keep_geom || w.keep_geom;
         if (w.keep_geom) MLV_TRY(dev_alloc((void **)&w.geom, n * sizeof(TriGeom)));
         w.record_cap = (uint32_t)n;
@@ -347,8 +346,11 @@ static mlv_status ensure_workspace(mlv_context_t *c, const BatchSizes &s, bool k
         if (before != w.tri_info) {
             cudaFree(w.rank);
             w.rank = nullptr;
-            uint32_t cap2 = 0;
+            cudaFree(w.bins_of);
+            w.bins_of = nullptr;
+            uint32_t cap2 = 0, cap3 = 0;
             MLV_TRY(grow(&w.rank, cap2, cap, sizeof(uint32_t)));
+            MLV_TRY(grow(&w.bins_of, cap3, cap, sizeof(uint2)));
             changed = true;
         }
         w.tri_cap = cap;
@@ -599,7 +601,7 @@ static mlv_status launch_draws(mlv_context_t *c, const Plan &p, DrawDesc *d_draw
     bp.shade = w.shade;
     bp.geom = w.keep_geom ? w.geom : nullptr;
     bp.tri_info = w.tri_info;
-    bp.jobs = w.jobs;
+    bp.bins_of = w.bins_of;
     bool want_rank = c->capture_infos;
     for (const ViewDesc &v : p.views) want_rank = want_rank || v.vis_tri != nullptr;
     bp.want_rank = want_rank ? 1u : 0u;
@@ -809,7 +811,7 @@ MLV_API mlv_status mlv_create_device(int ordinal, mlv_device *out) {
 }
 
 static void free_workspace(Workspace &w) {
-    cudaFree(w.raster); cudaFree(w.shade); cudaFree(w.geom); cudaFree(w.jobs); cudaFree(w.tri_info); cudaFree(w.rank);
+    cudaFree(w.raster); cudaFree(w.shade); cudaFree(w.geom); cudaFree(w.tri_info); cudaFree(w.bins_of); cudaFree(w.rank);
     cudaFree(w.bin_count); cudaFree(w.bin_start); cudaFree(w.list); cudaFree(w.info_mask);
     cudaFree(w.scan_status); cudaFree(w.scan_status2); cudaFree(w.counters); cudaFree(w.stats);
     cudaFree(w.error); cudaFree(w.d_draws); cudaFree(w.d_views); cudaFree(w.d_fills); cudaFree(w.vs_out);

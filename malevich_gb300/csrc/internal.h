@@ -8,6 +8,7 @@ namespace mlv {
 constexpr int kTile = 8;                 // 8x8 pixel tiles: the reference's bins (main.c:24-25)
 constexpr int kSubpix = 4;               // 28.4 fixed point (main.c:39)
 constexpr int kPsNone = 5;               // MLV_PS_NONE: depth and visibility only
+constexpr uint32_t kBinsClipped = 0xFFFFFFFFu;
 constexpr int kRasterTopLeft = 1;        // MLV_FILL_TOP_LEFT
 constexpr int kRasterCenter = 2;         // MLV_SAMPLE_PIXEL_CENTER
 constexpr int kMaxClipVertices = 16;     // main.c:38
@@ -94,8 +95,9 @@ struct FillJob {
 };
 constexpr uint32_t kFillChunk = 8192;
 
-// One assembled triangle's share of the binner's scatter (main.c:950-962): its key and the bins of
-// its tile rectangle, bin(x, y) = first_bin + y * row_stride + x * col_stride.
+// One emitted triangle's share of the binner (main.c:924-962), rebuilt from its record's bounds
+// where needed (never stored): its key and the bins of its tile rectangle,
+// bin(x, y) = first_bin + y * row_stride + x * col_stride.
 struct BinJob {
     uint32_t key, first_bin, nx, ny;
     uint32_t col_stride, row_stride, pad0, pad1;
@@ -125,7 +127,8 @@ struct BatchParams {
     TriShade *shade;
     TriGeom *geom;                       // nullptr unless the geometry is kept
     uint16_t *tri_info;                  // [total_tris]: emitted-fan mask | clipped << 8
-    BinJob *jobs;                        // [total_tris + overflow_capacity], kCtrEmitted of them written
+    uint2 *bins_of;                      // [total_tris]: an unclipped triangle's (first bin, nx | ny << 16);
+                                         // (0, 0) no bins, (0, kBinsClipped) clipped: see its fans
     uint32_t *rank;                      // [total_tris]: assembled triangles before g (exclusive)
     uint32_t *bin_count;                 // [total_bins], zero between batches
     uint32_t *bin_start;                 // [total_bins + 1]
@@ -141,7 +144,7 @@ struct BatchParams {
 
 enum Counter : int {
     kCtrRankTicket = 0, kCtrRankDone, kCtrRankEpoch,
-    kCtrOverflow, kCtrEmitted,           // per-batch: clip-fan slots used, bin jobs written
+    kCtrOverflow, kCtrReserved,          // per-batch: clip-fan slots used; unused
     kCtrScanTicket, kCtrScanDone, kCtrScanEpoch,
     kCtrCount = 16
 };

@@ -356,17 +356,32 @@ __device__ __forceinline__ uint32_t record_of(const BatchParams &bp, uint32_t ke
     return bp.total_tris + (uint32_t)__ldg(&bp.raster[g].w[0].x) + (c - 1);
 }
 
-__device__ __forceinline__ void count_tiles(const BatchParams &bp, const DrawDesc &d, const ViewDesc &vw,
-                                            int32_t tx0, int32_t ty0, int32_t tx1, int32_t ty1) {
-    for (int32_t ty = ty0; ty <= ty1; ++ty)
-        for (int32_t tx = tx0; tx <= tx1; ++tx) {
-            uint32_t bin = vw.bin_base + ((uint32_t)ty * vw.tiles_x + (uint32_t)tx) * vw.draw_count + d.draw_in_view;
-            atomicAdd(bp.bin_count + bin, 1u);
-        }
+// The tiles (bins) of one emitted triangle from its clamped pixel bounds: the binner's tile range
+// (main.c:924-936). k_geometry counts them and k_scatter fills them; both call this on the same
+// bounds (k_scatter re-reads them from the raster record), so they agree on every bin.
+__device__ __forceinline__ bool bin_job(const ViewDesc &vw, uint32_t draw_in_view, int32_t minx, int32_t miny,
+                                        int32_t maxx, int32_t maxy, uint32_t key, BinJob &job) {
+    int32_t tx0, ty0, tx1, ty1;
+    tile_range(vw, minx, miny, maxx, maxy, tx0, ty0, tx1, ty1);
+    job.key = key;
+    job.nx = tx1 >= tx0 ? (uint32_t)(tx1 - tx0 + 1) : 0u;
+    job.ny = ty1 >= ty0 ? (uint32_t)(ty1 - ty0 + 1) : 0u;
+    job.col_stride = vw.draw_count;
+    job.row_stride = vw.tiles_x * vw.draw_count;
+    job.first_bin = vw.bin_base + ((uint32_t)max(ty0, 0) * vw.tiles_x + (uint32_t)max(tx0, 0)) * vw.draw_count +
+                    draw_in_view;
+    job.pad0 = job.pad1 = 0;
+    return job.nx != 0 && job.ny != 0;
 }
 
-// A warp's triangles that span more than big_tiles tiles: at most 32 lanes x 7 clip fans.
-constexpr int kWarpQueue = 32 * 7;
+__device__ __forceinline__ uint32_t job_bin(const BinJob &j, uint32_t t) {
+    const uint32_t y = t / j.nx, x = t - y * j.nx;
+    return j.first_bin + y * j.row_stride + x * j.col_stride;
+}
+
+// Clip-fan triangles of a warp spanning more than big_tiles tiles, handled by the whole warp; when
+// the queue is full the lane handles its fan alone.
+constexpr int kFanQueue = 16;
 
 // Resident threads per SM the geometry kernel's register budget is sized for (1024: 64 registers).
 #ifndef MLV_GEOMETRY_THREADS_PER_SM
@@ -375,16 +390,14 @@ constexpr int kWarpQueue = 32 * 7;
 
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK, MLV_GEOMETRY_THREADS_PER_SM / BLOCK) k_geometry(BatchParams bp) {
-    __shared__ uint32_t s_q[BLOCK / 32][kWarpQueue];   // job slots
+    __shared__ BinJob s_q[BLOCK / 32][kFanQueue];
     __shared__ uint32_t s_qn[BLOCK / 32];
-    __shared__ uint32_t s_warp[BLOCK / 32];
-    __shared__ uint32_t s_slot0;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (lane == 0) s_qn[warp] = 0;
     __syncwarp();
     const uint32_t g = blockIdx.x * BLOCK + threadIdx.x;
     uint32_t mask = 0;
-    BinJob own;                 // the job of an unclipped triangle, given its slot warp-wide below
+    BinJob own;                 // the bins of an unclipped triangle, counted warp-wide below
     bool have_own = false;
     if (g < bp.total_tris) {
         const uint32_t draw = find_draw(bp, g);
@@ -404,34 +417,6 @@ __global__ void __launch_bounds__(BLOCK, MLV_GEOMETRY_THREADS_PER_SM / BLOCK) k_
                  (p0[2] < 0.f && p1[2] < 0.f && p2[2] < 0.f) ||
                  (p0[2] > +p0[3] && p1[2] > +p1[3] && p2[2] > +p2[3]);
         bool clipped = false;
-        // the bin job of one emitted triangle; false when it touches no tile
-        auto make_job = [&](uint32_t key, const Setup &su, BinJob &job) {
-            int32_t tx0, ty0, tx1, ty1;
-            tile_range(vw, su.minx, su.miny, su.maxx, su.maxy, tx0, ty0, tx1, ty1);
-            job.key = key;
-            job.nx = tx1 >= tx0 ? (uint32_t)(tx1 - tx0 + 1) : 0u;
-            job.ny = ty1 >= ty0 ? (uint32_t)(ty1 - ty0 + 1) : 0u;
-            job.col_stride = vw.draw_count;
-            job.row_stride = vw.tiles_x * vw.draw_count;
-            job.first_bin = vw.bin_base + ((uint32_t)max(ty0, 0) * vw.tiles_x + (uint32_t)max(tx0, 0)) * vw.draw_count +
-                            d.draw_in_view;
-            job.pad0 = job.pad1 = 0;
-            return job.nx != 0 && job.ny != 0;
-        };
-        // clip-fan triangles: counts the bins and records the job for k_scatter one by one
-        auto bin_record = [&](uint32_t key, const Setup &su) {
-            BinJob job;
-            if (!make_job(key, su, job)) return;
-            const uint32_t slot = atomicAdd(bp.counters + kCtrEmitted, 1u);
-            bp.jobs[slot] = job;
-            if (job.nx * job.ny > bp.big_tiles) {
-                s_q[warp][atomicAdd(&s_qn[warp], 1u)] = slot;   // counted by the whole warp below
-                return;
-            }
-            for (uint32_t y = 0; y < job.ny; ++y)
-                for (uint32_t x = 0; x < job.nx; ++x)
-                    atomicAdd(bp.bin_count + job.first_bin + y * job.row_stride + x * job.col_stride, 1u);
-        };
         if (!reject) {
             clipped = !((p0[0] >= -p0[3] && p1[0] >= -p1[3] && p2[0] >= -p2[3]) &&
                         (p0[0] <= +p0[3] && p1[0] <= +p1[3] && p2[0] <= +p2[3]) &&
@@ -444,7 +429,7 @@ __global__ void __launch_bounds__(BLOCK, MLV_GEOMETRY_THREADS_PER_SM / BLOCK) k_
                 if (setup_triangle(d, v[0], v[1], v[2], su)) {
                     write_record(bp, g, draw, d.ps, su, v[0], v[1], v[2]);
                     mask = 1;
-                    have_own = make_job(g << 3, su, own);
+                    have_own = bin_job(vw, d.draw_in_view, su.minx, su.miny, su.maxx, su.maxy, g << 3, own);
                 }
             } else {
                 Vtx poly[kMaxClipVertices], tmp[kMaxClipVertices];
@@ -466,7 +451,14 @@ __global__ void __launch_bounds__(BLOCK, MLV_GEOMETRY_THREADS_PER_SM / BLOCK) k_
                                 const uint32_t slot = bp.total_tris + base + (uint32_t)f;
                                 write_record(bp, slot, draw, d.ps, su, poly[0], poly[f + 1], poly[f + 2]);
                                 mask |= 1u << f;
-                                bin_record((g << 3) | (uint32_t)(f + 1), su);
+                                BinJob job;
+                                if (!bin_job(vw, d.draw_in_view, su.minx, su.miny, su.maxx, su.maxy, 0u, job)) continue;
+                                const uint32_t nt = job.nx * job.ny;
+                                if (nt > bp.big_tiles) {
+                                    const uint32_t q = atomicAdd(&s_qn[warp], 1u);
+                                    if (q < kFanQueue) { s_q[warp][q] = job; continue; }
+                                }
+                                for (uint32_t t = 0; t < nt; ++t) atomicAdd(bp.bin_count + job_bin(job, t), 1u);
                             }
                         }
                     }
@@ -474,47 +466,40 @@ __global__ void __launch_bounds__(BLOCK, MLV_GEOMETRY_THREADS_PER_SM / BLOCK) k_
             }
         }
         bp.tri_info[g] = (uint16_t)(mask | (clipped ? 0x100u : 0u));
+        bp.bins_of[g] = have_own ? make_uint2(own.first_bin, own.nx | (own.ny << 16))
+                                 : make_uint2(0u, clipped && mask ? kBinsClipped : 0u);
     }
-    // job slots of the unclipped triangles: one counter update per block (the assembled-triangle
-    // statistic, main.c:1238, rides in the upper half of the scanned value)
-    uint32_t own_total;
-    const uint32_t own_rank =
-        block_exclusive_scan<BLOCK>((have_own ? 1u : 0u) | ((uint32_t)__popc(mask) << 16), s_warp, own_total);
-    if (threadIdx.x == 0) {
-        const uint32_t jobs = own_total & 0xFFFFu, assembled = own_total >> 16;
-        s_slot0 = jobs ? atomicAdd(bp.counters + kCtrEmitted, jobs) : 0u;
-        if (assembled) atomicAdd(bp.stats + kStatAssembled, (unsigned long long)assembled);
-    }
-    __syncthreads();
-    uint32_t single_bin = 0xFFFFFFFFu;   // the bin of a one-tile triangle, counted per warp below
-    if (have_own) {
-        const uint32_t slot = s_slot0 + (own_rank & 0xFFFFu);
-        bp.jobs[slot] = own;
-        const uint32_t nt = own.nx * own.ny;
-        if (nt == 1) {
-            single_bin = own.first_bin;
-        } else if (nt > bp.big_tiles) {
-            s_q[warp][atomicAdd(&s_qn[warp], 1u)] = slot;   // counted by the whole warp below
-        } else {
-            for (uint32_t y = 0; y < own.ny; ++y)
-                for (uint32_t x = 0; x < own.nx; ++x)
-                    atomicAdd(bp.bin_count + own.first_bin + y * own.row_stride + x * own.col_stride, 1u);
-        }
-    }
+    // assembled-triangle statistic (main.c:1238)
+    uint32_t n = __popc(mask);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xFFFFFFFFu, n, o);
+    if (lane == 0 && n) atomicAdd(bp.stats + kStatAssembled, (unsigned long long)n);
     // neighbouring triangles of a mesh mostly share their tile: one update per distinct bin
+    const uint32_t nt_own = have_own ? own.nx * own.ny : 0u;
+    const uint32_t single_bin = nt_own == 1 ? own.first_bin : 0xFFFFFFFFu;
     const uint32_t peers = __match_any_sync(0xFFFFFFFFu, single_bin);
     if (single_bin != 0xFFFFFFFFu && lane == __ffs(peers) - 1)
         atomicAdd(bp.bin_count + single_bin, (uint32_t)__popc(peers));
+    if (nt_own > 1 && nt_own <= bp.big_tiles)
+        for (uint32_t t = 0; t < nt_own; ++t) atomicAdd(bp.bin_count + job_bin(own, t), 1u);
     // triangles spanning many tiles: the warp counts their tiles together
+    uint32_t big = __ballot_sync(0xFFFFFFFFu, nt_own > bp.big_tiles);
+    while (big) {
+        const int src = __ffs(big) - 1;
+        big &= big - 1;
+        BinJob j;
+        j.first_bin = __shfl_sync(0xFFFFFFFFu, own.first_bin, src);
+        j.nx = __shfl_sync(0xFFFFFFFFu, own.nx, src);
+        j.ny = __shfl_sync(0xFFFFFFFFu, own.ny, src);
+        j.col_stride = __shfl_sync(0xFFFFFFFFu, own.col_stride, src);
+        j.row_stride = __shfl_sync(0xFFFFFFFFu, own.row_stride, src);
+        for (uint32_t t = lane; t < j.nx * j.ny; t += 32) atomicAdd(bp.bin_count + job_bin(j, t), 1u);
+    }
     __syncwarp();
-    const uint32_t nq = s_qn[warp];
+    const uint32_t nq = min(s_qn[warp], (uint32_t)kFanQueue);
     for (uint32_t b = 0; b < nq; ++b) {
-        const BinJob job = bp.jobs[s_q[warp][b]];
-        const uint32_t nt = job.nx * job.ny;
-        for (uint32_t i = lane; i < nt; i += 32) {
-            const uint32_t y = i / job.nx, x = i - y * job.nx;
-            atomicAdd(bp.bin_count + job.first_bin + y * job.row_stride + x * job.col_stride, 1u);
-        }
+        const BinJob j = s_q[warp][b];
+        for (uint32_t t = lane; t < j.nx * j.ny; t += 32) atomicAdd(bp.bin_count + job_bin(j, t), 1u);
     }
 }
 
@@ -651,10 +636,25 @@ __global__ void __launch_bounds__(kScanBlock) k_scan(BatchParams bp) {
 
 constexpr int kScatterBlock = 256;
 
-// One thread per bin job (an emitted triangle): its key goes to the list of every bin of its tile
-// rectangle (main.c:950-962). Jobs over more than big_tiles bins are spread over the warp.
+// Fills the bin lists (main.c:950-962): one thread per input triangle. An unclipped triangle's
+// tile range comes from the 8-byte descriptor k_geometry wrote for it (bins_of); a clipped one's
+// fans are rebuilt from the bounds in their records, as k_geometry built them. The key goes to the
+// list of every bin of the range (the order inside a bin does not matter, see k_tile). One-tile triangles of a warp that share a bin take their list
+// positions with one atomic; triangles over more than big_tiles bins are filled by the whole warp.
+__device__ __forceinline__ bool record_job(const BatchParams &bp, const ViewDesc &vw, uint32_t draw_in_view,
+                                           uint32_t rec, uint32_t key, BinJob &job) {
+    const int4 w3 = bp.raster[rec].w[3];
+    return bin_job(vw, draw_in_view, (int16_t)(w3.z & 0xFFFF), w3.z >> 16, (int16_t)(w3.w & 0xFFFF), w3.w >> 16, key,
+                   job);
+}
+
+__device__ __forceinline__ void put(const BatchParams &bp, uint32_t bin, uint32_t key) {
+    const uint32_t pos = atomicSub(bp.bin_count + bin, 1u) - 1u;
+    bp.list[__ldg(bp.bin_start + bin) + pos] = key;
+}
+
 __global__ void __launch_bounds__(kScatterBlock) k_scatter(BatchParams bp) {
-    __shared__ BinJob s_q[kScatterBlock / 32][32];
+    __shared__ BinJob s_q[kScatterBlock / 32][kFanQueue];
     __shared__ uint32_t s_qn[kScatterBlock / 32];
     if (ld_volatile_u32(bp.error)) return;
     const uint32_t total = bp.bin_start[bp.total_bins];
@@ -667,19 +667,42 @@ __global__ void __launch_bounds__(kScatterBlock) k_scatter(BatchParams bp) {
         return;
     }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t njobs = ld_volatile_u32(bp.counters + kCtrEmitted);
-    for (uint32_t base = blockIdx.x * kScatterBlock; base < njobs; base += gridDim.x * kScatterBlock) {
+    for (uint32_t base = blockIdx.x * kScatterBlock; base < bp.total_tris; base += gridDim.x * kScatterBlock) {
         if (lane == 0) s_qn[warp] = 0;
         __syncwarp();
-        const uint32_t i = base + threadIdx.x;
-        BinJob job = {};
-        if (i < njobs) {
-            const uint4 *jp = reinterpret_cast<const uint4 *>(bp.jobs + i);
-            const uint4 j0 = jp[0], j1 = jp[1];
-            job = {j0.x, j0.y, j0.z, j0.w, j1.x, j1.y, 0u, 0u};
+        const uint32_t g = base + threadIdx.x;
+        const uint2 bd = g < bp.total_tris ? bp.bins_of[g] : make_uint2(0u, 0u);
+        BinJob own;
+        uint32_t nt_own = 0;
+        if (bd.y != 0u && bd.y != kBinsClipped) {
+            own.key = g << 3;
+            own.first_bin = bd.x;
+            own.nx = bd.y & 0xFFFFu;
+            own.ny = bd.y >> 16;
+            nt_own = own.nx * own.ny;
+            if (nt_own > 1) {   // the bin strides of its view (a one-tile triangle needs none)
+                const ViewDesc &vw = bp.views[bp.draws[find_draw(bp, g)].view];
+                own.col_stride = vw.draw_count;
+                own.row_stride = vw.tiles_x * vw.draw_count;
+            }
+        } else if (bd.y == kBinsClipped) {
+            const uint32_t info = bp.tri_info[g];
+            const DrawDesc &d = bp.draws[find_draw(bp, g)];
+            const ViewDesc &vw = bp.views[d.view];
+            const uint32_t fbase = (uint32_t)__ldg(&bp.raster[g].w[0].x);
+            for (uint32_t f = 0; f < 7; ++f) {
+                if (!(info >> f & 1u)) continue;
+                BinJob job;
+                if (!record_job(bp, vw, d.draw_in_view, bp.total_tris + fbase + f, (g << 3) | (f + 1), job)) continue;
+                const uint32_t nt = job.nx * job.ny;
+                if (nt > bp.big_tiles) {
+                    const uint32_t q = atomicAdd(&s_qn[warp], 1u);
+                    if (q < kFanQueue) { s_q[warp][q] = job; continue; }
+                }
+                for (uint32_t t = 0; t < nt; ++t) put(bp, job_bin(job, t), job.key);
+            }
         }
-        // one-tile jobs of the warp that share a bin take their list positions with one atomic
-        const uint32_t single = (i < njobs && job.nx * job.ny == 1) ? job.first_bin : 0xFFFFFFFFu;
+        const uint32_t single = nt_own == 1 ? own.first_bin : 0xFFFFFFFFu;
         const uint32_t peers = __match_any_sync(0xFFFFFFFFu, single);
         if (single != 0xFFFFFFFFu) {
             const int leader = __ffs(peers) - 1;
@@ -687,45 +710,43 @@ __global__ void __launch_bounds__(kScatterBlock) k_scatter(BatchParams bp) {
             if (lane == leader) top = atomicSub(bp.bin_count + single, (uint32_t)__popc(peers));
             top = __shfl_sync(peers, top, leader);
             const uint32_t r = (uint32_t)__popc(peers & ((1u << lane) - 1u));
-            bp.list[__ldg(bp.bin_start + single) + top - 1u - r] = job.key;
-        } else if (i < njobs) {
-            if (job.nx * job.ny > bp.big_tiles) {
-                s_q[warp][atomicAdd(&s_qn[warp], 1u)] = job;
-            } else {
-                // up to 4 bins at a time: the atomics and bin_start loads are independent, so they
-                // are all in flight together instead of one round trip after another
-                const uint32_t nt = job.nx * job.ny;
-                for (uint32_t t0 = 0; t0 < nt; t0 += 4) {
-                    uint32_t bin[4], pos[4], st[4];
+            bp.list[__ldg(bp.bin_start + single) + top - 1u - r] = own.key;
+        } else if (nt_own > 1 && nt_own <= bp.big_tiles) {
+            // up to 4 bins at a time: the atomics and bin_start loads are independent, so they
+            // are all in flight together instead of one round trip after another
+            for (uint32_t t0 = 0; t0 < nt_own; t0 += 4) {
+                uint32_t bin[4], pos[4], st[4];
 #pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        const uint32_t t = t0 + k;
-                        const uint32_t y = t / job.nx, x = t - y * job.nx;
-                        bin[k] = job.first_bin + y * job.row_stride + x * job.col_stride;
+                for (int k = 0; k < 4; ++k) bin[k] = job_bin(own, min(t0 + k, nt_own - 1));
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    if (t0 + k < nt_own) {
+                        pos[k] = atomicSub(bp.bin_count + bin[k], 1u) - 1u;
+                        st[k] = __ldg(bp.bin_start + bin[k]);
                     }
 #pragma unroll
-                    for (int k = 0; k < 4; ++k)
-                        if (t0 + k < nt) {
-                            pos[k] = atomicSub(bp.bin_count + bin[k], 1u) - 1u;
-                            st[k] = __ldg(bp.bin_start + bin[k]);
-                        }
-#pragma unroll
-                    for (int k = 0; k < 4; ++k)
-                        if (t0 + k < nt) bp.list[st[k] + pos[k]] = job.key;
-                }
+                for (int k = 0; k < 4; ++k)
+                    if (t0 + k < nt_own) bp.list[st[k] + pos[k]] = own.key;
             }
         }
+        uint32_t big = __ballot_sync(0xFFFFFFFFu, nt_own > bp.big_tiles);
+        while (big) {
+            const int src = __ffs(big) - 1;
+            big &= big - 1;
+            BinJob j;
+            j.key = __shfl_sync(0xFFFFFFFFu, own.key, src);
+            j.first_bin = __shfl_sync(0xFFFFFFFFu, own.first_bin, src);
+            j.nx = __shfl_sync(0xFFFFFFFFu, own.nx, src);
+            j.ny = __shfl_sync(0xFFFFFFFFu, own.ny, src);
+            j.col_stride = __shfl_sync(0xFFFFFFFFu, own.col_stride, src);
+            j.row_stride = __shfl_sync(0xFFFFFFFFu, own.row_stride, src);
+            for (uint32_t t = lane; t < j.nx * j.ny; t += 32) put(bp, job_bin(j, t), j.key);
+        }
         __syncwarp();
-        const uint32_t nq = s_qn[warp];
+        const uint32_t nq = min(s_qn[warp], (uint32_t)kFanQueue);
         for (uint32_t b = 0; b < nq; ++b) {
-            const BinJob job = s_q[warp][b];
-            const uint32_t nt = job.nx * job.ny;
-            for (uint32_t t = lane; t < nt; t += 32) {
-                const uint32_t y = t / job.nx, x = t - y * job.nx;
-                const uint32_t bin = job.first_bin + y * job.row_stride + x * job.col_stride;
-                const uint32_t pos = atomicSub(bp.bin_count + bin, 1u) - 1u;
-                bp.list[bp.bin_start[bin] + pos] = job.key;
-            }
+            const BinJob j = s_q[warp][b];
+            for (uint32_t t = lane; t < j.nx * j.ny; t += 32) put(bp, job_bin(j, t), j.key);
         }
         __syncwarp();
     }
@@ -1121,7 +1142,8 @@ cudaError_t launch_scan(const BatchParams &bp, cudaStream_t stream) {
 }
 
 cudaError_t launch_scatter(const BatchParams &bp, int num_sms, cudaStream_t stream) {
-    // the job count is only known on the device: a grid of up to 8 blocks per SM strides over it
+    // a grid of up to 8 blocks per SM strides over the input triangles (a grid of one thread per
+    // triangle measured slower: more triangles in flight contend for the same bin counters)
     uint32_t blocks = (bp.total_tris + kScatterBlock - 1) / kScatterBlock;
     uint32_t cap = (uint32_t)num_sms * 8;
     if (blocks > cap) blocks = cap;

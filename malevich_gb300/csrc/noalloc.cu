@@ -52,10 +52,10 @@ constexpr size_t kStatusWords = kMaxTiles / 4096 + 2;
 constexpr size_t kOffBinCount = align256(kOffStatus + sizeof(unsigned long long) * kStatusWords);
 constexpr size_t kOffBinStart = align256(kOffBinCount + sizeof(uint32_t) * (kMaxTiles + 1));
 constexpr size_t kOffTriInfo = align256(kOffBinStart + sizeof(uint32_t) * (kMaxTiles + 1));
-constexpr size_t kOffRaster = align256(kOffTriInfo + sizeof(uint16_t) * (kMaxTriangles + 1));
+constexpr size_t kOffBinsOf = align256(kOffTriInfo + sizeof(uint16_t) * (kMaxTriangles + 1));
+constexpr size_t kOffRaster = align256(kOffBinsOf + sizeof(uint2) * kMaxTriangles);
 constexpr size_t kOffShade = align256(kOffRaster + sizeof(TriRaster) * (kMaxTriangles + kMaxFanSlots));
-constexpr size_t kOffJobs = align256(kOffShade + sizeof(TriShade) * (kMaxTriangles + kMaxFanSlots));
-constexpr size_t kOffVsOut = align256(kOffJobs + sizeof(BinJob) * (kMaxTriangles + kMaxFanSlots));
+constexpr size_t kOffVsOut = align256(kOffShade + sizeof(TriShade) * (kMaxTriangles + kMaxFanSlots));
 constexpr size_t kOffList = align256(kOffVsOut + sizeof(float4) * 3 * kMaxVertices);
 constexpr size_t kScratchBytes = align256(kOffList + sizeof(uint32_t) * kMaxBinEntries);
 static_assert(kScratchBytes == MLV_NOALLOC_SCRATCH_BYTES, "header and layout disagree on the scratch size");
@@ -278,7 +278,7 @@ extern "C" MLV_API mlv_status mlv_draw_indexed_noalloc(const mlv_noalloc_draw *a
     bp.raster = (TriRaster *)(base + kOffRaster);
     bp.shade = (TriShade *)(base + kOffShade);
     bp.tri_info = (uint16_t *)(base + kOffTriInfo);
-    bp.jobs = (BinJob *)(base + kOffJobs);
+    bp.bins_of = (uint2 *)(base + kOffBinsOf);
     bp.bin_count = (uint32_t *)(base + kOffBinCount);
     bp.bin_start = (uint32_t *)(base + kOffBinStart);
     bp.list = (uint32_t *)(base + kOffList);
