@@ -657,10 +657,11 @@ def main():
     import ctypes
 
     def e2e_step():
+        # queued uploads from pinned memory (unchanged until the readback below synchronises)
         for buf, a in host_bufs:
-            ctx.lib.mlv_update_buffer(ctx.handle, buf.handle, 0, a.ctypes.data_as(ctypes.c_void_p), a.nbytes)
+            ctx.lib.mlv_update_buffer_async(ctx.handle, buf.handle, 0, a.ctypes.data_as(ctypes.c_void_p), a.nbytes)
         for tex, a in host_tex:
-            ctx.lib.mlv_update_texture2d(ctx.handle, tex.handle, a.ctypes.data_as(ctypes.c_void_p), 0)
+            ctx.lib.mlv_update_texture2d_async(ctx.handle, tex.handle, a.ctypes.data_as(ctypes.c_void_p), 0)
         r.render_batched()
         ctx.lib.mlv_read_texture2d(ctx.handle, rt.handle, out_img.ctypes.data_as(ctypes.c_void_p), 0)
 

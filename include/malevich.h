@@ -222,6 +222,15 @@ MLV_API mlv_status mlv_update_buffer(mlv_context context, mlv_buffer buffer, uin
                                      uint64_t size);
 MLV_API mlv_status mlv_update_texture2d(mlv_context context, mlv_texture2d texture, const void *data,
                                         uint32_t row_pitch);
+/* New: the same copies queued on the context's stream without waiting (Direct3D 11 has no
+ * counterpart; compare a dynamic resource's Map with NO_OVERWRITE). `data` must stay valid and
+ * unchanged until the context next synchronises (mlv_finish, a readback, mlv_get_stats): with
+ * pinned host memory the copy runs in the background. Queued work that was issued earlier still
+ * reads the old contents. */
+MLV_API mlv_status mlv_update_buffer_async(mlv_context context, mlv_buffer buffer, uint64_t offset,
+                                           const void *data, uint64_t size);
+MLV_API mlv_status mlv_update_texture2d_async(mlv_context context, mlv_texture2d texture, const void *data,
+                                              uint32_t row_pitch);
 /* Waits for the context's queued work, then copies the texture to host memory. */
 MLV_API mlv_status mlv_read_texture2d(mlv_context context, mlv_texture2d texture, void *dst, uint32_t row_pitch);
 

@@ -36,6 +36,7 @@ EXPORTS = [
     "mlv_get_immediate_context", "mlv_create_deferred_context", "mlv_destroy_context", "mlv_create_buffer",
     "mlv_destroy_buffer", "mlv_create_texture2d", "mlv_create_texture2d_on_memory", "mlv_destroy_texture2d", "mlv_buffer_device_pointer",
     "mlv_texture2d_device_pointer", "mlv_update_buffer", "mlv_update_texture2d", "mlv_read_texture2d",
+    "mlv_update_buffer_async", "mlv_update_texture2d_async",
     "mlv_ia_set_primitive_topology", "mlv_ia_set_index_buffer", "mlv_ia_set_vertex_buffers",
     "mlv_vs_set_shader", "mlv_vs_set_constant_buffers", "mlv_vs_set_shader_resources", "mlv_ps_set_shader",
     "mlv_ps_set_shader_resources", "mlv_rs_set_viewports", "mlv_rs_set_state", "mlv_om_set_depth_stencil_state",
@@ -123,6 +124,8 @@ def load_library(path=LIB_PATH):
     lib.mlv_texture2d_device_pointer.argtypes = [vp, ctypes.POINTER(vp)]
     lib.mlv_update_buffer.argtypes = [vp, vp, ctypes.c_uint64, vp, ctypes.c_uint64]
     lib.mlv_update_texture2d.argtypes = [vp, vp, vp, ctypes.c_uint32]
+    lib.mlv_update_buffer_async.argtypes = [vp, vp, ctypes.c_uint64, vp, ctypes.c_uint64]
+    lib.mlv_update_texture2d_async.argtypes = [vp, vp, vp, ctypes.c_uint32]
     lib.mlv_read_texture2d.argtypes = [vp, vp, vp, ctypes.c_uint32]
     lib.mlv_ia_set_primitive_topology.argtypes = [vp, ctypes.c_int]
     lib.mlv_ia_set_index_buffer.argtypes = [vp, vp, ctypes.c_int, ctypes.c_uint32]
@@ -306,6 +309,17 @@ class Context:
     def update_texture(self, tex, data):
         arr = np.ascontiguousarray(data)
         _check(self.lib.mlv_update_texture2d(self.handle, tex.handle, _ptr(arr), 0))
+
+    def update_buffer_async(self, buf, arr, offset=0):
+        """Queued upload: `arr` (C-contiguous) must stay unchanged until the next synchronisation."""
+        if not arr.flags["C_CONTIGUOUS"]:
+            raise ValueError("update_buffer_async needs a C-contiguous array it can keep")
+        _check(self.lib.mlv_update_buffer_async(self.handle, buf.handle, offset, _ptr(arr), arr.nbytes))
+
+    def update_texture_async(self, tex, arr):
+        if not arr.flags["C_CONTIGUOUS"]:
+            raise ValueError("update_texture_async needs a C-contiguous array it can keep")
+        _check(self.lib.mlv_update_texture2d_async(self.handle, tex.handle, _ptr(arr), 0))
 
     def finish_command_list(self):
         h = ctypes.c_void_p()

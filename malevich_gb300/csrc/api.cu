@@ -1023,6 +1023,32 @@ MLV_API mlv_status mlv_update_texture2d(mlv_context c, mlv_texture2d t, const vo
     return MLV_OK;
 }
 
+// Queued uploads. A batch still unchecked may be re-run at the next synchronisation (when it
+// overflowed its workspace), and a re-run must read the contents it was issued with, so the
+// context first synchronises if anything is pending; otherwise the copy is only queued.
+MLV_API mlv_status mlv_update_buffer_async(mlv_context c, mlv_buffer b, uint64_t offset, const void *data,
+                                           uint64_t size) {
+    MLV_TRY(need_immediate(c));
+    if (!b || !data) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
+    if (offset + size > b->size) return fail(MLV_ERROR_INVALID_ARG, "update outside the buffer");
+    MLV_TRY(set_device(c->device));
+    if (!c->pending.empty()) MLV_TRY(sync_context(c));
+    CUDA_TRY(cudaMemcpyAsync(b->ptr + offset, data, size, cudaMemcpyHostToDevice, c->stream));
+    if (!b->shadow.empty()) memcpy(b->shadow.data() + offset, data, size);
+    return MLV_OK;
+}
+
+MLV_API mlv_status mlv_update_texture2d_async(mlv_context c, mlv_texture2d t, const void *data, uint32_t row_pitch) {
+    MLV_TRY(need_immediate(c));
+    if (!t || !data) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
+    MLV_TRY(set_device(c->device));
+    if (!c->pending.empty()) MLV_TRY(sync_context(c));
+    size_t row = (size_t)t->width * t->texel_bytes;
+    CUDA_TRY(cudaMemcpy2DAsync(t->ptr, row, data, row_pitch ? row_pitch : row, row, t->height, cudaMemcpyHostToDevice,
+                               c->stream));
+    return MLV_OK;
+}
+
 MLV_API mlv_status mlv_read_texture2d(mlv_context c, mlv_texture2d t, void *dst, uint32_t row_pitch) {
     MLV_TRY(need_immediate(c));
     if (!t || !dst) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");

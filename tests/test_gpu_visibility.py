@@ -68,3 +68,31 @@ def test_placed_texture_rejects_unaligned_memory(device):
     h = ctypes.c_void_p()
     assert lib.mlv_create_texture2d_on_memory(device.handle, None, ctypes.c_void_p(buf.data_ptr()),
                                               ctypes.byref(h)) != 0
+
+
+def test_queued_uploads_keep_queued_work_on_the_old_contents(device):
+    """A queued upload after a queued draw does not change what that draw reads (the context
+    synchronises first), and the next draw reads the new contents."""
+    fr = scenes.small_scene(31, 64, 48, n_objects=2, level=2)
+    r = api.FrameRenderer(device, fr)
+    ctx = device.immediate
+    r.render_per_draw()
+    want_old = r.read(0)
+    vb_buf, vb_arr = next(v for k, v in r._buffers.items() if k[1] == api.BIND_VERTEX_BUFFER)
+    moved = np.ascontiguousarray(vb_arr.copy())
+    moved[:, 0] += 0.25                       # shift the first mesh's object-space x
+    r.render_per_draw()                       # queued
+    ctx.update_buffer_async(vb_buf, moved)    # queued behind it
+    ctx.finish()
+    assert np.array_equal(r.read(0)["depth"].view(np.uint32), want_old["depth"].view(np.uint32))
+    r.render_per_draw()
+    new = r.read(0)
+    for d in fr.draws:
+        if d.vb is vb_arr:
+            d.vb = moved
+    want_new = pyoracle.render_oracle(fr)
+    assert np.array_equal(new["depth"].view(np.uint32), want_new["depth"].view(np.uint32))
+    assert not np.array_equal(new["depth"], want_old["depth"])
+    ctx.update_buffer_async(vb_buf, np.ascontiguousarray(vb_arr))
+    ctx.finish()
+    r.destroy()
