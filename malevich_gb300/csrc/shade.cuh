@@ -142,14 +142,18 @@ __device__ __forceinline__ float4 sample_latlon(const TexDesc &t, float dx, floa
     return bilinear(t, uv_x, uv_y);
 }
 
+// The colour-only transcendentals below use CUDA's fast intrinsics (__expf, __powf: a few ulp,
+// i.e. about 1e-3 of an 8-bit step after packing), as the reference uses SVML's approximations
+// (math.h:21-23); they feed nothing but UNORM8 colour, which is compared within +-1 LSB.
+
 // vertex_lighting_vs.c:34-35 and env_lighting_ps.c:20-21: (1 - e^(-c))^(1/2.2)
 __device__ __forceinline__ float tonemap(float c) {
-    return powf(1.0f - expf(c * -1.0f), (float)(1.0 / 2.2));
+    return __powf(1.0f - __expf(c * -1.0f), (float)(1.0 / 2.2));
 }
 
 // f256_srgb_from_linear_approx (math.h:419-422)
 __device__ __forceinline__ float srgb_approx(float c) {
-    float v = (float)1.055 * powf(c, (float)0.416666667) + (float)-0.055;
+    float v = (float)1.055 * __powf(c, (float)0.416666667) + (float)-0.055;
     return (v > 0.0f) ? v : 0.0f;
 }
 
