@@ -618,14 +618,15 @@ static mlv_status launch_draws(mlv_context_t *c, const Plan &p, DrawDesc *d_draw
     c->host_stats[3] += 1;
     if (bp.total_tris == 0) return MLV_OK;   // nothing to assemble: no kernel has work
     cudaEvent_t e;
+    // the clip-fan slot counter starts at zero for every batch (reset before the first kernel, so
+    // that the batch's kernels follow one another directly)
+    CUDA_TRY(cudaMemsetAsync(w.counters + kCtrOverflow, 0, 2 * sizeof(uint32_t), c->stream));
     if (bp.total_vertices) {
         ev_begin(c, 5, &e);
         CUDA_TRY(launch_vertex(bp, c->stream));
         ev_end(c, e);
         c->host_stats[4] += 1;
     }
-    // the clip-fan slot and bin-job counters start at zero for every batch
-    CUDA_TRY(cudaMemsetAsync(w.counters + kCtrOverflow, 0, 2 * sizeof(uint32_t), c->stream));
     ev_begin(c, 1, &e);
     CUDA_TRY(launch_geometry(bp, c->tuning.geometry_block, c->stream));
     ev_end(c, e);

@@ -25,6 +25,7 @@
 // the tile kernel computes with shared-memory atomics, then shades only the winner.
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <utility>
 
 #include "internal.h"
 #include "shade.cuh"
@@ -48,6 +49,13 @@ __device__ __forceinline__ void st_release_u64(unsigned long long *p, unsigned l
 __device__ __forceinline__ uint32_t ld_volatile_u32(const uint32_t *p) {
     return *(const volatile uint32_t *)p;
 }
+
+// Programmatic dependent launch: the pipeline's kernels are launched so that the next one may be
+// scheduled while the previous one finishes. Each waits for its predecessor's completion (and the
+// visibility of its writes) before touching any of its outputs, and lets its dependents launch
+// once its own work is done.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
 constexpr uint32_t kFlagAggregate = 1, kFlagInclusive = 2;
 constexpr uint32_t kSpinLimit = 1u << 22;   // bounded wait: about half a second with the backoff
@@ -309,6 +317,7 @@ __device__ __forceinline__ uint32_t find_vertex_draw(const BatchParams &bp, uint
 }
 
 __global__ void __launch_bounds__(kVertexBlock) k_vertex(BatchParams bp) {
+    pdl_wait();
     const uint32_t v = blockIdx.x * kVertexBlock + threadIdx.x;
     if (v >= bp.total_vertices) return;
     const DrawDesc &d = bp.draws[find_vertex_draw(bp, v)];
@@ -328,6 +337,7 @@ __global__ void __launch_bounds__(kVertexBlock) k_vertex(BatchParams bp) {
     out[0] = make_float4(o[0], o[1], o[2], o[3]);
     out[1] = make_float4(o[4], o[5], o[6], o[7]);
     out[2] = make_float4(o[8], 0.0f, 0.0f, 0.0f);
+    pdl_trigger();
 }
 
 // Vertex k of a triangle: from the shaded-vertex buffer, or shaded here (per-index path, and for
@@ -392,6 +402,7 @@ template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK, MLV_GEOMETRY_THREADS_PER_SM / BLOCK) k_geometry(BatchParams bp) {
     __shared__ BinJob s_q[BLOCK / 32][kFanQueue];
     __shared__ uint32_t s_qn[BLOCK / 32];
+    pdl_wait();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (lane == 0) s_qn[warp] = 0;
     __syncwarp();
@@ -501,6 +512,7 @@ __global__ void __launch_bounds__(BLOCK, MLV_GEOMETRY_THREADS_PER_SM / BLOCK) k_
         const BinJob j = s_q[warp][b];
         for (uint32_t t = lane; t < j.nx * j.ny; t += 32) atomicAdd(bp.bin_count + job_bin(j, t), 1u);
     }
+    pdl_trigger();
 }
 
 // ------------------------------------------------------------------ assembled-triangle ranks
@@ -512,6 +524,7 @@ constexpr int kRankBlock = 256, kRankItems = 8;
 __global__ void __launch_bounds__(kRankBlock) k_rank(BatchParams bp) {
     __shared__ uint32_t s_bid, s_epoch, s_prefix;
     __shared__ uint32_t s_warp[kRankBlock / 32];
+    pdl_wait();
     if (threadIdx.x == 0) {
         s_bid = atomicAdd(bp.counters + kCtrRankTicket, 1u);
         s_epoch = ld_volatile_u32(bp.counters + kCtrRankEpoch);
@@ -552,6 +565,7 @@ __global__ void __launch_bounds__(kRankBlock) k_rank(BatchParams bp) {
             __threadfence();
         }
     }
+    pdl_trigger();
 }
 
 // ------------------------------------------------------------------ bin scan
@@ -561,6 +575,7 @@ constexpr int kScanBlock = 256, kScanItems = 16;   // 4096 bins per block, read 
 __global__ void __launch_bounds__(kScanBlock) k_scan(BatchParams bp) {
     __shared__ uint32_t s_bid, s_epoch, s_prefix;
     __shared__ uint32_t s_warp[kScanBlock / 32];
+    pdl_wait();
     if (ld_volatile_u32(bp.error)) return;   // uniform: set only by earlier kernels
     if (threadIdx.x == 0) {
         s_bid = atomicAdd(bp.counters + kCtrScanTicket, 1u);
@@ -630,6 +645,7 @@ __global__ void __launch_bounds__(kScanBlock) k_scan(BatchParams bp) {
             __threadfence();
         }
     }
+    pdl_trigger();
 }
 
 // ------------------------------------------------------------------ bin scatter
@@ -656,6 +672,7 @@ __device__ __forceinline__ void put(const BatchParams &bp, uint32_t bin, uint32_
 __global__ void __launch_bounds__(kScatterBlock) k_scatter(BatchParams bp) {
     __shared__ BinJob s_q[kScatterBlock / 32][kFanQueue];
     __shared__ uint32_t s_qn[kScatterBlock / 32];
+    pdl_wait();
     if (ld_volatile_u32(bp.error)) return;
     const uint32_t total = bp.bin_start[bp.total_bins];
     if (total > bp.list_capacity) {
@@ -750,6 +767,7 @@ __global__ void __launch_bounds__(kScatterBlock) k_scatter(BatchParams bp) {
         }
         __syncwarp();
     }
+    pdl_trigger();
 }
 
 // ------------------------------------------------------------------ tile kernel
@@ -810,6 +828,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
     __shared__ uint32_t s_stage[WARPS][32 * kStage];
     __shared__ uint32_t s_pref[WARPS][32];
     __shared__ unsigned long long s_mask[WARPS][32];
+    pdl_wait();
     if (ld_volatile_u32(bp.error)) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         // commit the batch's staged statistics (k_geometry and k_scan finished before this kernel)
@@ -1041,11 +1060,13 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
         V.tile_min[t] = hiz_min;
         V.tile_max[t] = hiz_max;
     }
+    pdl_trigger();
 }
 
 // ------------------------------------------------------------------ clears
 
 __global__ void k_fill_u32(uint32_t *p, size_t n, uint32_t value, const uint32_t *error) {
+    pdl_wait();
     if (error && ld_volatile_u32(error)) return;
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const size_t n4 = n / 4;
@@ -1065,6 +1086,7 @@ constexpr int kFillBlock = 256;
 
 __global__ void __launch_bounds__(kFillBlock) k_fill_many(const FillJob *jobs, uint32_t njobs, uint32_t nchunks,
                                                           const uint32_t *error) {
+    pdl_wait();
     if (error && ld_volatile_u32(error)) return;
     for (uint32_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
         uint32_t lo = 0, hi = njobs;   // last job with chunk_begin <= c
@@ -1085,16 +1107,34 @@ __global__ void __launch_bounds__(kFillBlock) k_fill_many(const FillJob *jobs, u
             for (uint32_t k = threadIdx.x; k < cnt; k += kFillBlock) p[k] = j.value;
         }
     }
+    pdl_trigger();
 }
 
 // ------------------------------------------------------------------ host-side launchers
+
+// Launches a pipeline kernel with programmatic stream serialisation: it may be scheduled while
+// the previous kernel on the stream finishes (it waits for that kernel in pdl_wait()).
+template <typename... Params, typename... Args>
+static cudaError_t launch_chained(void (*kernel)(Params...), uint32_t grid, uint32_t block, cudaStream_t stream,
+                                  Args &&...args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 cudaError_t launch_fill_many(const FillJob *d_jobs, uint32_t njobs, uint32_t nchunks, const uint32_t *error,
                              cudaStream_t stream) {
     if (njobs == 0 || nchunks == 0) return cudaSuccess;
     const uint32_t blocks = nchunks < 152u * 8u ? nchunks : 152u * 8u;
-    k_fill_many<<<blocks, kFillBlock, 0, stream>>>(d_jobs, njobs, nchunks, error);
-    return cudaGetLastError();
+    return launch_chained(k_fill_many, blocks, kFillBlock, stream, d_jobs, njobs, nchunks, error);
 }
 
 void set_clip_planes(const float planes[6][4], cudaStream_t stream) {
@@ -1107,38 +1147,33 @@ cudaError_t launch_fill_u32(uint32_t *p, size_t n, uint32_t value, const uint32_
     size_t blocks = (n / 4 + threads - 1) / threads;
     if (blocks < 1) blocks = 1;
     if (blocks > 152 * 16) blocks = 152 * 16;
-    k_fill_u32<<<(unsigned)blocks, threads, 0, stream>>>(p, n, value, error);
-    return cudaGetLastError();
+    return launch_chained(k_fill_u32, (uint32_t)blocks, (uint32_t)threads, stream, p, n, value, error);
 }
 
 cudaError_t launch_vertex(const BatchParams &bp, cudaStream_t stream) {
     if (bp.total_vertices == 0) return cudaSuccess;
-    k_vertex<<<(bp.total_vertices + kVertexBlock - 1) / kVertexBlock, kVertexBlock, 0, stream>>>(bp);
-    return cudaGetLastError();
+    return launch_chained(k_vertex, (bp.total_vertices + kVertexBlock - 1) / kVertexBlock, kVertexBlock, stream, bp);
 }
 
 cudaError_t launch_geometry(const BatchParams &bp, uint32_t block, cudaStream_t stream) {
     if (bp.total_tris == 0) return cudaSuccess;
     switch (block) {
-        case 128: k_geometry<128><<<(bp.total_tris + 127) / 128, 128, 0, stream>>>(bp); break;
-        case 512: k_geometry<512><<<(bp.total_tris + 511) / 512, 512, 0, stream>>>(bp); break;
-        default: k_geometry<256><<<(bp.total_tris + 255) / 256, 256, 0, stream>>>(bp); break;
+        case 128: return launch_chained(k_geometry<128>, (bp.total_tris + 127) / 128, 128, stream, bp);
+        case 512: return launch_chained(k_geometry<512>, (bp.total_tris + 511) / 512, 512, stream, bp);
+        default: return launch_chained(k_geometry<256>, (bp.total_tris + 255) / 256, 256, stream, bp);
     }
-    return cudaGetLastError();
 }
 
 cudaError_t launch_rank(const BatchParams &bp, cudaStream_t stream) {
     const uint32_t per = kRankBlock * kRankItems;
     const uint32_t blocks = (bp.total_tris + per - 1) / per;
-    k_rank<<<blocks ? blocks : 1, kRankBlock, 0, stream>>>(bp);
-    return cudaGetLastError();
+    return launch_chained(k_rank, blocks ? blocks : 1, kRankBlock, stream, bp);
 }
 
 cudaError_t launch_scan(const BatchParams &bp, cudaStream_t stream) {
     const uint32_t per = kScanBlock * kScanItems;
     const uint32_t blocks = (bp.total_bins + per - 1) / per;
-    k_scan<<<blocks ? blocks : 1, kScanBlock, 0, stream>>>(bp);
-    return cudaGetLastError();
+    return launch_chained(k_scan, blocks ? blocks : 1, kScanBlock, stream, bp);
 }
 
 cudaError_t launch_scatter(const BatchParams &bp, int num_sms, cudaStream_t stream) {
@@ -1148,17 +1183,15 @@ cudaError_t launch_scatter(const BatchParams &bp, int num_sms, cudaStream_t stre
     uint32_t cap = (uint32_t)num_sms * 8;
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
-    k_scatter<<<blocks, kScatterBlock, 0, stream>>>(bp);
-    return cudaGetLastError();
+    return launch_chained(k_scatter, blocks, kScatterBlock, stream, bp);
 }
 
 cudaError_t launch_tile(const BatchParams &bp, uint32_t warps, cudaStream_t stream) {
     switch (warps) {
-        case 2: k_tile<2><<<(bp.total_tiles + 1) / 2, 64, 0, stream>>>(bp); break;
-        case 8: k_tile<8><<<(bp.total_tiles + 7) / 8, 256, 0, stream>>>(bp); break;
-        default: k_tile<4><<<(bp.total_tiles + 3) / 4, 128, 0, stream>>>(bp); break;
+        case 2: return launch_chained(k_tile<2>, (bp.total_tiles + 1) / 2, 64, stream, bp);
+        case 8: return launch_chained(k_tile<8>, (bp.total_tiles + 7) / 8, 256, stream, bp);
+        default: return launch_chained(k_tile<4>, (bp.total_tiles + 3) / 4, 128, stream, bp);
     }
-    return cudaGetLastError();
 }
 
 }  // namespace mlv
