@@ -18,6 +18,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <unordered_map>
 #include <unordered_set>
 #include <vector>
 
@@ -415,11 +416,51 @@ struct Plan {
     std::vector<DrawDesc> draws;
     std::vector<ViewDesc> views;
     BatchSizes sizes;
+    std::unordered_set<mlv_texture2d> folded;   // cleared targets the tile kernel clears itself
 };
+
+// Folds the segment's clears of targets that one view of the plan binds (and that the clear's kind
+// fits: colour, depth, u32 fill of a visibility target) into that view. Clears precede every draw
+// of a segment and each view covers its whole target, so the tile kernel, starting every tile
+// from the clear value and writing all of its pixels, leaves what clear-then-draw leaves.
+template <typename Groups>
+static void fold_clears(const Segment &seg, const Groups &groups, Plan &p) {
+    if (seg.clears.empty()) return;
+    std::unordered_map<mlv_texture2d, int> uses;
+    for (size_t g = 0; g < groups.size(); ++g) {
+        const DrawCmd &first = seg.draws[groups[g].second[0]];
+        for (mlv_texture2d t : {first.rtv, first.dsv, first.vis_tri, first.vis_draw, first.vis_bary, first.vis_prim})
+            if (t) ++uses[t];
+    }
+    // the last clear of each target wins
+    std::unordered_map<mlv_texture2d, const ClearCmd *> last;
+    for (const ClearCmd &cl : seg.clears) last[cl.target] = &cl;
+    for (size_t g = 0; g < groups.size(); ++g) {
+        const DrawCmd &first = seg.draws[groups[g].second[0]];
+        ViewDesc &v = p.views[g];
+        auto fold = [&](mlv_texture2d t, int kind, uint32_t flag, uint32_t &value) {
+            if (!t || uses[t] != 1) return;
+            auto it = last.find(t);
+            if (it == last.end() || it->second->kind != kind) return;
+            v.clear_flags |= flag;
+            value = it->second->value;
+            p.folded.insert(t);
+        };
+        fold(first.rtv, 0, kClearColor, v.clear_color);
+        uint32_t depth_bits = 0;
+        fold(first.dsv, 1, kClearDepth, depth_bits);
+        if (v.clear_flags & kClearDepth) v.clear_depth = last[first.dsv]->depth;
+        fold(first.vis_tri, 2, kClearTri, v.clear_tri);
+        fold(first.vis_draw, 2, kClearDraw, v.clear_draw);
+        fold(first.vis_prim, 2, kClearPrim, v.clear_prim);
+        fold(first.vis_bary, 2, kClearBary, v.clear_bary);
+    }
+}
 
 static mlv_status plan_segment(const Segment &seg, Plan &p, uint32_t fan_slots_hint = 0) {
     p.draws.clear();
     p.views.clear();
+    p.folded.clear();
     p.sizes = BatchSizes();
     // group draws by (render target, depth) keeping their order inside a view
     std::vector<std::pair<std::pair<mlv_texture2d, mlv_texture2d>, std::vector<size_t>>> groups;
@@ -473,6 +514,7 @@ static mlv_status plan_segment(const Segment &seg, Plan &p, uint32_t fan_slots_h
         bins += (uint64_t)v.tiles_x * v.tiles_y * v.draw_count;
         p.views.push_back(v);
     }
+    if (tri > 0) fold_clears(seg, groups, p);   // no triangles: no tile kernel runs
     if (bins > 0x7FFFFFFFull || tiles > 0x7FFFFFFFu || verts > 0x7FFFFFFFull / 3)
         return fail(MLV_ERROR_CAPACITY_EXCEEDED, "batch has too many bins or vertices");
     p.sizes.vertices = verts;
@@ -525,13 +567,15 @@ static void collect_events(mlv_context_t *c) {
 // The fills of a segment's clears, one job per written array (a depth clear also resets the
 // target's tile minima to 0, main.c:1212-1214, and the tile maxima that depth LESS uses to 1).
 // A target cleared twice keeps its last clear, so the jobs write disjoint memory.
-static uint32_t build_fills(const Segment &seg, std::vector<FillJob> &jobs) {
+static uint32_t build_fills(const Segment &seg, std::vector<FillJob> &jobs,
+                            const std::unordered_set<mlv_texture2d> *folded = nullptr) {
     jobs.clear();
     std::unordered_set<mlv_texture2d> seen;
     for (auto it = seg.clears.rbegin(); it != seg.clears.rend(); ++it) {
         const ClearCmd &cl = *it;
         mlv_texture2d t = cl.target;
         if (!seen.insert(t).second) continue;
+        if (folded && folded->count(t)) continue;   // the tile kernel clears it
         uint32_t value = cl.value;
         if (cl.kind == 1) memcpy(&value, &cl.depth, 4);
         jobs.push_back({(uint32_t *)t->ptr, (uint64_t)t->width * t->height * (t->texel_bytes / 4), value, 0});
@@ -648,10 +692,14 @@ static mlv_status launch_draws(mlv_context_t *c, const Plan &p, DrawDesc *d_draw
 }
 
 static mlv_status execute_segment_eager(mlv_context_t *c, const Segment &seg, uint32_t seq, bool rerun = false) {
-    MLV_TRY(run_clears(c, seg));
-    if (seg.draws.empty()) return MLV_OK;
+    if (seg.draws.empty()) return run_clears(c, seg);
     Plan p;
     MLV_TRY(plan_segment(seg, p, c->tuning.initial_clip_fan_slots));
+    {
+        std::vector<FillJob> jobs;
+        const uint32_t chunks = build_fills(seg, jobs, &p.folded);
+        MLV_TRY(run_fills(c, jobs, chunks, nullptr));
+    }
     MLV_TRY(ensure_workspace(c, p.sizes, false));
     CUDA_TRY(cudaMemcpyAsync(c->ws.d_draws, p.draws.data(), sizeof(DrawDesc) * p.draws.size(),
                              cudaMemcpyHostToDevice, c->stream));
@@ -1431,7 +1479,7 @@ static mlv_status run_list(mlv_context_t *c, mlv_command_list l, uint32_t seq, b
     std::vector<uint32_t> fill_chunks(l->segments.size());
     size_t nf = 0;
     for (size_t i = 0; i < l->segments.size(); ++i) {
-        fill_chunks[i] = build_fills(l->segments[i], fills[i]);
+        fill_chunks[i] = build_fills(l->segments[i], fills[i], &plans[i].folded);
         nf += fills[i].size();
     }
     if (upload || !l->d_fills) {

@@ -64,8 +64,17 @@ struct ViewDesc {
     uint32_t tile_base;                  // first tile of this view in the batch's tile space
     uint32_t draw_begin, draw_count;     // the view's draws are contiguous in the draw array
     uint32_t bin_base;                   // bin of (tile t, draw d) = bin_base + t * draw_count + d
-    uint32_t pad[4];
+    // Clears folded into the tile kernel: a target the batch's segment cleared (and bound in this
+    // view only) starts at its clear value in every tile, and every one of its pixels is written
+    // once, instead of a separate fill (kClear* bits; the depth clear also resets hierarchical Z).
+    uint32_t clear_flags;
+    uint32_t clear_color, clear_tri, clear_draw, clear_prim, clear_bary;
+    float clear_depth;
+    uint32_t pad[1];
 };
+
+constexpr uint32_t kClearColor = 1, kClearDepth = 2, kClearTri = 4, kClearDraw = 8, kClearPrim = 16,
+                   kClearBary = 32;
 
 // Per assembled triangle, read by the tile kernel for every (tile, triangle) pair: 64 bytes.
 //   w0 = e0.a, e0.b, e0.c, e1.a      w1 = e1.b, e1.c, e2.a, e2.b

@@ -821,6 +821,19 @@ enum : int {
     kSPad
 };
 
+// Writes the folded clears (ViewDesc::clear_flags) of a pixel that no draw of the batch wrote;
+// depth is the running value, which for such a pixel is the clear value.
+__device__ __forceinline__ void write_cleared(const ViewDesc &V, size_t o, float depth) {
+    const uint32_t f = V.clear_flags;
+    if (f & kClearColor) V.color[o] = V.clear_color;
+    if (f & kClearDepth) V.depth[o] = depth;
+    if (f & kClearTri) V.vis_tri[o] = V.clear_tri;
+    if (f & kClearDraw) V.vis_draw[o] = V.clear_draw;
+    if (f & kClearPrim) V.vis_prim[o] = V.clear_prim;
+    if (f & kClearBary)
+        reinterpret_cast<uint2 *>(V.vis_bary)[o] = make_uint2(V.clear_bary, V.clear_bary);
+}
+
 template <int WARPS>
 __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
     __shared__ unsigned long long s_best[WARPS][64];
@@ -849,7 +862,6 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
     // the bin boundaries of this tile's draws, one per lane (lane d holds bin_start[bin0 + d])
     const uint32_t my_start = lane <= dc ? __ldg(bp.bin_start + bin0 + lane) : 0u;
     const uint32_t last = dc < 32 ? __shfl_sync(0xFFFFFFFFu, my_start, dc) : __ldg(bp.bin_start + bin0 + dc);
-    if (__shfl_sync(0xFFFFFFFFu, my_start, 0) == last) return;   // no draw binned a triangle here
 
     const int32_t x0 = (int32_t)tx * kTile, y0 = (int32_t)ty * kTile;
     // lane owns pixels p0 = lane (rows 0-3) and p1 = lane + 32 (rows 4-7)
@@ -857,12 +869,24 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
     const bool valid0 = px < (int32_t)V.width && py0 < (int32_t)V.height;
     const bool valid1 = px < (int32_t)V.width && py1 < (int32_t)V.height;
     const size_t o0 = (size_t)py0 * V.width + px, o1 = (size_t)py1 * V.width + px;
-    float dcur0 = valid0 ? V.depth[o0] : 0.0f;
-    float dcur1 = valid1 ? V.depth[o1] : 0.0f;
+    const bool depth_cleared = (V.clear_flags & kClearDepth) != 0;
+    if (__shfl_sync(0xFFFFFFFFu, my_start, 0) == last) {   // no draw binned a triangle here
+        if (V.clear_flags) {
+            if (valid0) write_cleared(V, o0, V.clear_depth);
+            if (valid1) write_cleared(V, o1, V.clear_depth);
+            if (lane == 0 && depth_cleared) {   // clear_depth_stencil_view's tile bounds (main.c:1212-1214)
+                V.tile_min[t] = 0.0f;
+                V.tile_max[t] = 1.0f;
+            }
+        }
+        return;
+    }
+    float dcur0 = valid0 ? (depth_cleared ? V.clear_depth : V.depth[o0]) : 0.0f;
+    float dcur1 = valid1 ? (depth_cleared ? V.clear_depth : V.depth[o1]) : 0.0f;
     uint32_t win0 = 0xFFFFFFFFu, win1 = 0xFFFFFFFFu;
     s_depth[warp][lane] = dcur0;
     s_depth[warp][lane + 32] = dcur1;
-    float hiz_min = V.tile_min[t], hiz_max = V.tile_max[t];
+    float hiz_min = depth_cleared ? 0.0f : V.tile_min[t], hiz_max = depth_cleared ? 1.0f : V.tile_max[t];
     uint32_t *stage = s_stage[warp];
     uint32_t *pref = s_pref[warp];
     const bool capture = bp.info_mask != nullptr;
@@ -1043,6 +1067,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
             const float u = interp(r0.w, r1.w, r2.w), v = interp(uv2.x, uv2.y, uv2.z);
             const float3 c = run_ps(D.ps, a0, a1, a2, u, v, D.ps_tex);
             V.color[o] = pack_color(c.x, c.y, c.z);
+        } else if (V.clear_flags & kClearColor) {
+            V.color[o] = V.clear_color;   // a null pixel shader leaves the (folded) clear colour
         }
         V.depth[o] = z;
         if (V.vis_tri && bp.rank) {
@@ -1055,6 +1081,11 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
         if (V.vis_draw) V.vis_draw[o] = D.draw_seq;
         if (V.vis_prim) V.vis_prim[o] = (key >> 3) - D.tri_begin;
         if (V.vis_bary) reinterpret_cast<float2 *>(V.vis_bary)[o] = make_float2(b1, b2);
+    }
+    // pixels no draw wrote still owe their folded clears
+    if (V.clear_flags) {
+        if (valid0 && win0 == 0xFFFFFFFFu) write_cleared(V, o0, dcur0);
+        if (valid1 && win1 == 0xFFFFFFFFu) write_cleared(V, o1, dcur1);
     }
     if (lane == 0) {
         V.tile_min[t] = hiz_min;
