@@ -174,11 +174,14 @@ def algorithmic_bytes(frame, dev_stats, written_pixels):
         if t is not None and id(t.data) not in seen:
             seen.add(id(t.data))
             tex += t.data.nbytes
-    # k_tile: bin bounds, list entries, each assembled triangle's records once, the depth buffer
-    # read once, colour + depth written for every written pixel, the sampled texture once (capped
-    # at the footprint of 4 taps per written pixel)
+    # k_tile: bin bounds, list entries, each assembled triangle's records once, the sampled texture
+    # once (capped at the footprint of 4 taps per written pixel), and the targets: when the frame
+    # clears both, the clears are folded into the kernel, which writes colour + depth of every
+    # pixel and reads none; otherwise it reads the depth buffer and writes the written pixels
     tex = min(tex, written_pixels * 4 * 8)
-    tile = bins * 4 + entries * 4 + assembled * (64 + 80) + w * h * 4 + written_pixels * 8 + tex
+    folded = frame.clear_color is not None and frame.clear_depth is not None
+    targets = w * h * 8 if folded else w * h * 4 + written_pixels * 8
+    tile = bins * 4 + entries * 4 + assembled * (64 + 80) + targets + tex
     return {"k_geometry": geometry, "k_tile": tile}
 
 
