@@ -497,37 +497,49 @@ def profile_diff(dev, views):
 
 
 def run_reference_arm(args, rank, world):
+    """The reference's CPU implementation of the path on this host's cores, on the same frame: its
+    own core (compiled from its sources into oracle/_ref, AVX2, x86-64 only) where it was built,
+    else the oracle port of it (oracle/oracle.c, OpenMP). Rank 0 alone runs it."""
     if rank != 0:
         return 0
+    import platform
     from malevich_gb300 import scenes
     frame = scenes.config2_scene(seed=args.seed)
     from oracle import pyoracle
-    lib = pyoracle.oracle_lib()
     cores = os.cpu_count() or 1
-    lib.orc_set_threads(cores)
-    for _ in range(max(1, min(args.warmup, 1))):
-        pyoracle.render_oracle(frame)
+    use_ref = platform.machine() in ("x86_64", "AMD64") and pyoracle.reference_available(frame.width, frame.height)
+    if use_ref:
+        render = lambda: pyoracle.render_reference(frame, threads=cores)["stats"]
+        kind, note = "reference", "the reference's own core (AVX2 + OpenMP), compiled from its sources"
+    else:
+        pyoracle.oracle_lib().orc_set_threads(cores)
+        render = lambda: pyoracle.render_oracle(frame)["stats"]
+        kind, note = "port", ("the reference's own core is AVX2 C and does not build on this host (%s); the "
+                              "oracle port of it (oracle/oracle.c, OpenMP) runs instead" % platform.machine())
+    warmup = max(3, min(args.warmup, 5))
+    for _ in range(warmup):
+        render()
     times, stats = [], None
-    for _ in range(max(1, min(args.steps, 3))):
+    for _ in range(max(1, min(args.steps, 5))):
         t0 = time.perf_counter()
-        stats = pyoracle.render_oracle(frame)["stats"]
+        stats = render()
         times.append(time.perf_counter() - t0)
     dt = statistics.median(times)
     tris = frame.input_triangles
     value = tris / dt / 1e6
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Mtri/s", "n_gpus": world,
-        "steps": len(times), "warmup": 1, "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True,
+        "steps": len(times), "warmup": warmup, "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "input_triangles": tris, "resolution": [frame.width, frame.height],
                    "draws": len(frame.draws)},
-        "gpix_per_s": round(stats["fragments_written"] / dt / 1e9, 6),
-        "cpu_baseline": {"value": round(value, 4), "unit": "Mtri/s", "cores": cores, "kind": "port",
+        "cpu_baseline": {"value": round(value, 4), "unit": "Mtri/s", "cores": cores, "kind": kind,
                          "sample": "%d full frames of the workload (median)" % len(times)},
         "e2e": {"value": round(value, 4), "unit": "Mtri/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": ("the reference's own core is AVX2 C and does not build on this aarch64 host; the oracle "
-                 "port of it (oracle/oracle.c, OpenMP) runs instead"),
+        "note": note,
     }
+    if "fragments_written" in stats:
+        line["gpix_per_s"] = round(stats["fragments_written"] / dt / 1e9, 6)
     print(json.dumps(line))
     return 0
 
