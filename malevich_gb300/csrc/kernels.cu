@@ -15,7 +15,9 @@
 //   k_tile      one warp per 8x8 tile: hierarchical Z, coverage, depth, pixel shader, output
 //               merger, write-back (main.c:983-1189, 577-603), for every draw of the batch that
 //               touches the tile, in draw order, with colour and depth held on-chip until one
-//               write-back.
+//               write-back; the segment's clears of the batch's targets are folded in.
+//   k_fill_many the clears that are not folded (one launch per segment).
+// The kernels are launched with programmatic stream serialisation (see pdl_wait).
 //
 // Why the order inside a bin does not matter: there is no blending (main.c:1180-1181) and pixel
 // shaders have no side effects, so after a draw a pixel holds the output of the *last* fragment
@@ -1123,7 +1125,7 @@ __global__ void __launch_bounds__(kFillBlock) k_fill_many(const FillJob *jobs, u
         uint32_t lo = 0, hi = njobs;   // last job with chunk_begin <= c
         while (hi - lo > 1) {
             const uint32_t mid = (lo + hi) >> 1;
-            if (__ldg(&jobs[mid].chunk_begin) <= c) lo = mid; else hi = mid;
+            if (__ldg(&jobs[mid].chunk_begin) <= c) lo = mid; else hi = mid;   // fill jobs
         }
         const FillJob j = jobs[lo];
         const uint64_t begin = (uint64_t)(c - j.chunk_begin) * kFillChunk;
