@@ -212,7 +212,7 @@ struct mlv_context_t {
     PipelineState st;
     std::vector<Segment> recorded;     // deferred contexts
     Workspace ws;
-    mlv_tuning tuning = {4, 1, 16, 256, 0, 0};
+    mlv_tuning tuning = {4, 1, 16, 128, 0, 0};   // measured defaults; the autotuner refines them
     uint64_t tuning_generation = 0;    // bumped by mlv_set_tuning: captured graphs re-capture
     uint64_t host_stats[8] = {};       // vertex_count, input triangles, draws, batches, launches
     bool profiling = false;

@@ -297,7 +297,7 @@ extern "C" MLV_API mlv_status mlv_draw_indexed_noalloc(const mlv_noalloc_draw *a
     }
     if (tris) {
         NA_CUDA(launch_vertex(bp, stream));
-        NA_CUDA(launch_geometry(bp, 256, stream));
+        NA_CUDA(launch_geometry(bp, 128, stream));
         NA_CUDA(launch_scan(bp, stream));
         NA_CUDA(launch_scatter(bp, g_num_sms[dev] ? g_num_sms[dev] : 152, stream));
         NA_CUDA(launch_tile(bp, 4, stream));
