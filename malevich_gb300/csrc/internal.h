@@ -78,7 +78,10 @@ constexpr uint32_t kClearColor = 1, kClearDepth = 2, kClearTri = 4, kClearDraw =
 
 // Per assembled triangle, read by the tile kernel for every (tile, triangle) pair: 64 bytes.
 //   w0 = e0.a, e0.b, e0.c, e1.a      w1 = e1.b, e1.c, e2.a, e2.b
-//   w2 = e2.c, inv_area, zbound, z0  w3 = z1, z2, bbox min (x | y << 16), bbox max (x | y << 16)
+//   w2 = e2.c, inv_area, zbound, z0  w3 = z1, z2, box min (x | y << 16), box max (x | y << 16)
+// The box is the reference's pixel box shrunk to the samples the triangle can cover. The slot of a
+// clipped input triangle holds no record: its w0.x is the base of its fans' slots and w0.y, w0.z
+// the fans' box shrinks (6 bits a fan), from which the reference's boxes are rebuilt for binning.
 struct TriRaster {
     int4 w[4];
 };

@@ -151,7 +151,9 @@ struct Setup {
     float inv_area, zbound;
     float ss[3][4];         // screen-space reg0 of the three vertices
     float rw[3];
-    int32_t minx, miny, maxx, maxy;
+    int32_t minx, miny, maxx, maxy;      // the reference's pixel box: binning
+    int32_t tminx, tminy, tmaxx, tmaxy;  // the same box shrunk to the samples it can cover: tile kernel
+    uint32_t box_delta;                  // the shrink: x min | y min << 1 (0-1), x max << 2 | y max << 4 (0-3)
 };
 
 // set_edge_function, main.c:563-575 (wrapping int32)
@@ -211,6 +213,24 @@ __device__ __forceinline__ bool setup_triangle(const DrawDesc &d, const Vtx &v0,
     mxx = max(mxx, -8);
     mxy = max(mxy, -8);
     s.minx = mnx; s.miny = mny; s.maxx = mxx; s.maxy = mxy;
+    // A covered sample lies in the closed triangle, so inside its snapped vertex bounds: x * 16 (+ 8
+    // at pixel centres) in [xmin, xmax]. (A degenerate triangle covers none: its edge values are of
+    // mixed sign off its line and all 0 on it.) That holds while the edge values are exact, which
+    // they are for vertex extents up to 1024 pixels: |E| stays below 2^31 over the box, so the
+    // wrapping sums equal the true values. The box shrinks by at most 1 at the minimum and 3 at the
+    // maximum, so the deltas fit 6 bits and give the reference box back (k_scatter, clip fans).
+    const int32_t xlo = min(x[0], min(x[1], x[2])), xhi = max(x[0], max(x[1], x[2]));
+    const int32_t ylo = min(y[0], min(y[1], y[2])), yhi = max(y[0], max(y[1], y[2]));
+    int32_t dlx = 0, dly = 0, dhx = 0, dhy = 0;
+    if ((uint32_t)xhi - (uint32_t)xlo <= 16384u && (uint32_t)yhi - (uint32_t)ylo <= 16384u) {
+        const int32_t off = (d.raster_flags & kRasterCenter) ? 8 : 0;
+        dlx = min(max(((xlo - off + 15) >> kSubpix) - mnx, 0), 1);
+        dly = min(max(((ylo - off + 15) >> kSubpix) - mny, 0), 1);
+        dhx = min(max(mxx - ((xhi - off) >> kSubpix), 0), 3);
+        dhy = min(max(mxy - ((yhi - off) >> kSubpix), 0), 3);
+    }
+    s.tminx = mnx + dlx; s.tminy = mny + dly; s.tmaxx = mxx - dhx; s.tmaxy = mxy - dhy;
+    s.box_delta = (uint32_t)(dlx | dly << 1 | dhx << 2 | dhy << 4);
     return true;
 }
 
@@ -222,7 +242,7 @@ __device__ __forceinline__ void write_record(const BatchParams &bp, uint32_t rec
     r[1] = make_int4(s.e[4], s.e[5], s.e[6], s.e[7]);
     r[2] = make_int4(s.e[8], __float_as_int(s.inv_area), __float_as_int(s.zbound), __float_as_int(s.ss[0][2]));
     r[3] = make_int4(__float_as_int(s.ss[1][2]), __float_as_int(s.ss[2][2]),
-                     (s.minx & 0xFFFF) | (s.miny << 16), (s.maxx & 0xFFFF) | (s.maxy << 16));
+                     (s.tminx & 0xFFFF) | (s.tminy << 16), (s.tmaxx & 0xFFFF) | (s.tmaxy << 16));
     if (bp.geom) {
         TriGeom &g = bp.geom[rec];
 #pragma unroll
@@ -469,13 +489,14 @@ __global__ void __launch_bounds__(BLOCK, MLV_GEOMETRY_THREADS_PER_SM / BLOCK) k_
                         atomicMin(bp.error + 1, bp.batch_seq);
                         atomicMax(bp.error + 4, base + (uint32_t)nf);
                     } else {
-                        bp.raster[g].w[0].x = (int)base;   // slot g holds the fans' base
+                        uint32_t deltas[2] = {0u, 0u};   // 6 bits a fan: fans 0-4, then 5-6
                         for (int f = 0; f < nf && f < 7; ++f) {
                             Setup su;
                             if (setup_triangle(d, poly[0], poly[f + 1], poly[f + 2], su)) {
                                 const uint32_t slot = bp.total_tris + base + (uint32_t)f;
                                 write_record(bp, slot, draw, d.ps, su, poly[0], poly[f + 1], poly[f + 2]);
                                 mask |= 1u << f;
+                                deltas[f < 5 ? 0 : 1] |= su.box_delta << (6 * (f < 5 ? f : f - 5));
                                 BinJob job;
                                 if (!bin_job(vw, d.draw_in_view, su.minx, su.miny, su.maxx, su.maxy, 0u, job)) continue;
                                 const uint32_t nt = job.nx * job.ny;
@@ -486,6 +507,8 @@ __global__ void __launch_bounds__(BLOCK, MLV_GEOMETRY_THREADS_PER_SM / BLOCK) k_
                                 for (uint32_t t = 0; t < nt; ++t) atomicAdd(bp.bin_count + job_bin(job, t), 1u);
                             }
                         }
+                        // slot g (no record of its own) holds the fans' base and box deltas
+                        bp.raster[g].w[0] = make_int4((int)base, (int)deltas[0], (int)deltas[1], 0);
                     }
                 }
             }
@@ -668,14 +691,18 @@ constexpr int kScatterBlock = 256;
 
 // Fills the bin lists (main.c:950-962): one thread per input triangle. An unclipped triangle's
 // tile range comes from the 8-byte descriptor k_geometry wrote for it (bins_of); a clipped one's
-// fans are rebuilt from the bounds in their records, as k_geometry built them. The key goes to the
-// list of every bin of the range (the order inside a bin does not matter, see k_tile). One-tile triangles of a warp that share a bin take their list
-// positions with one atomic; triangles over more than big_tiles bins are filled by the whole warp.
+// fans' ranges are rebuilt from the boxes in their records widened by the shrinks k_geometry kept,
+// which gives back the boxes k_geometry binned. The key goes to the list of every bin of the range
+// (the order inside a bin does not matter, see k_tile). One-tile triangles of a warp that share a
+// bin take their list positions with one atomic; triangles over more than big_tiles bins are
+// filled by the whole warp.
 __device__ __forceinline__ bool record_job(const BatchParams &bp, const ViewDesc &vw, uint32_t draw_in_view,
-                                           uint32_t rec, uint32_t key, BinJob &job) {
+                                           uint32_t rec, uint32_t key, uint32_t delta, BinJob &job) {
+    // the record holds the shrunk box (Setup::box_delta): widen it back to the reference's
     const int4 w3 = bp.raster[rec].w[3];
-    return bin_job(vw, draw_in_view, (int16_t)(w3.z & 0xFFFF), w3.z >> 16, (int16_t)(w3.w & 0xFFFF), w3.w >> 16, key,
-                   job);
+    return bin_job(vw, draw_in_view, (int16_t)(w3.z & 0xFFFF) - (int32_t)(delta & 1u), (w3.z >> 16) - (int32_t)(delta >> 1 & 1u),
+                   (int16_t)(w3.w & 0xFFFF) + (int32_t)(delta >> 2 & 3u), (w3.w >> 16) + (int32_t)(delta >> 4 & 3u),
+                   key, job);
 }
 
 __device__ __forceinline__ void put(const BatchParams &bp, uint32_t bin, uint32_t key) {
@@ -724,7 +751,11 @@ __global__ void __launch_bounds__(kScatterBlock) k_scatter(BatchParams bp) {
             for (uint32_t f = 0; f < 7; ++f) {
                 if (!(info >> f & 1u)) continue;
                 BinJob job;
-                if (!record_job(bp, vw, d.draw_in_view, bp.total_tris + fbase + f, (g << 3) | (f + 1), job)) continue;
+                // the fan's box deltas: slot g's words y (fans 0-4) and z (fans 5-6), 6 bits each
+                const uint32_t dw = (uint32_t)__ldg(f < 5 ? &bp.raster[g].w[0].y : &bp.raster[g].w[0].z);
+                if (!record_job(bp, vw, d.draw_in_view, bp.total_tris + fbase + f, (g << 3) | (f + 1),
+                                (dw >> (6 * (f < 5 ? f : f - 5))) & 63u, job))
+                    continue;
                 const uint32_t nt = job.nx * job.ny;
                 if (nt > bp.big_tiles) {
                     const uint32_t q = atomicAdd(&s_qn[warp], 1u);
