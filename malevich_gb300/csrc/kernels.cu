@@ -393,6 +393,35 @@ __device__ __forceinline__ void triangle_vertex(const BatchParams &bp, const Dra
     run_vs(d.vs, in, d.cb, d.vs_tex, o);
 }
 
+// The position of vertex k of a triangle, for the clip tests and setup; its attributes are read
+// only once the triangle survives them (triangle_attributes), as most triangles of a large scene
+// do not. Returns the vertex's slot in the shaded-vertex buffer, or kNoSlot when o already holds
+// the whole vertex (shaded here, or a null pixel shader, which reads no attributes).
+constexpr uint32_t kNoSlot = 0xFFFFFFFFu;
+
+__device__ __forceinline__ uint32_t triangle_position(const BatchParams &bp, const DrawDesc &d, uint32_t idx_pos,
+                                                      float *o) {
+    if (d.vs_cached && d.ps != kPsNone) {
+        int64_t idx = d.ib ? (int64_t)__ldg(d.ib + idx_pos) : (int64_t)idx_pos;
+        idx += d.base_vertex;
+        if (idx >= 0 && idx < (int64_t)d.vertex_count) {
+            const uint32_t slot = d.vs_base + (uint32_t)idx;
+            const float4 a = __ldg(bp.vs_out + 3 * (size_t)slot);
+            o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+            return slot;
+        }
+    }
+    triangle_vertex(bp, d, idx_pos, o);
+    return kNoSlot;
+}
+
+__device__ __forceinline__ void triangle_attributes(const BatchParams &bp, uint32_t slot, float *o) {
+    if (slot == kNoSlot) return;
+    const float4 *src = bp.vs_out + 3 * (size_t)slot;
+    const float4 b = __ldg(src + 1), c = __ldg(src + 2);
+    o[4] = b.x; o[5] = b.y; o[6] = b.z; o[7] = b.w; o[8] = c.x;
+}
+
 // Slot of the record a triangle key names (see BatchParams).
 __device__ __forceinline__ uint32_t record_of(const BatchParams &bp, uint32_t key) {
     const uint32_t g = key >> 3, c = key & 7u;
@@ -450,8 +479,9 @@ __global__ void __launch_bounds__(BLOCK, MLV_GEOMETRY_THREADS_PER_SM / BLOCK) k_
         const ViewDesc &vw = bp.views[d.view];
         const uint32_t local = g - d.tri_begin;
         Vtx v[3];
+        uint32_t slot[3];
 #pragma unroll
-        for (int k = 0; k < 3; ++k) triangle_vertex(bp, d, d.start_index + 3 * local + k, v[k].v);
+        for (int k = 0; k < 3; ++k) slot[k] = triangle_position(bp, d, d.start_index + 3 * local + k, v[k].v);
         const float *p0 = v[0].v, *p1 = v[1].v, *p2 = v[2].v;
         // main.c:759-781
         bool reject = p0[3] == 0 || p1[3] == 0 || p2[3] == 0;
@@ -472,11 +502,15 @@ __global__ void __launch_bounds__(BLOCK, MLV_GEOMETRY_THREADS_PER_SM / BLOCK) k_
             if (!clipped) {
                 Setup su;
                 if (setup_triangle(d, v[0], v[1], v[2], su)) {
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) triangle_attributes(bp, slot[k], v[k].v);
                     write_record(bp, g, draw, d.ps, su, v[0], v[1], v[2]);
                     mask = 1;
                     have_own = bin_job(vw, d.draw_in_view, su.minx, su.miny, su.maxx, su.maxy, g << 3, own);
                 }
             } else {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) triangle_attributes(bp, slot[k], v[k].v);
                 Vtx poly[kMaxClipVertices], tmp[kMaxClipVertices];
                 poly[0] = v[0]; poly[1] = v[1]; poly[2] = v[2];
                 int count = 3;
