@@ -55,6 +55,10 @@ def parse():
     ap.add_argument("--diff-steps", type=int, default=100)
     ap.add_argument("--profile-once", action="store_true",
                     help="render the frame once (batched, eager) and exit: a short launch sequence for ncu")
+    ap.add_argument("--profile-workload", default="scene", choices=["scene", "single"],
+                    help="--profile-once: the scene frame or the single draw (icosphere L5 at 1280x720)")
+    ap.add_argument("--warps-per-tile", type=int, default=0,
+                    help="--profile-once: this tile-kernel shape (1, 2, 4 or 8) instead of the default")
     ap.add_argument("--profile-diff-views", type=int, default=0,
                     help="run the differentiable loop's visibility pass, forward and adjoint once over this "
                          "many views of its 256x256 heightfield workload and exit (a short sequence for ncu)")
@@ -194,12 +198,15 @@ def run_single_draw_section(dev, args):
     graph launches with L2 flushed before each (these include the launch latency). Algorithmic bytes per frame: indices + unique vertices (32 B) + the
     texture footprint (min(size, 4 taps x 4 B x fragments)) + colour and depth written once."""
     import torch
-    from malevich_gb300 import api, scenes
+    from malevich_gb300 import api, autotune, scenes
     from oracle import pyoracle
     frame = scenes.config1_plain()
     ctx = dev.immediate
+    base_tuning = ctx.tuning()
     r = api.FrameRenderer(dev, frame)
     r.render_batched()
+    # its own launch shapes: one mesh crowds its triangles into few tiles
+    tuned = autotune.autotune(dev, r, repeats=5, warmup=2) if not args.no_autotune else None
     stream = torch.cuda.ExternalStream(ctx.stream())
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.int32, device="cuda")
     for _ in range(5):
@@ -243,6 +250,7 @@ def run_single_draw_section(dev, args):
     ctx.set_profiling(False)
     got = r.read(0)
     r.destroy()
+    ctx.set_tuning(**base_tuning)
     ost = pyoracle.render_oracle(frame)
     same_depth = bool(np.array_equal(got["depth"].view(np.uint32), ost["depth"].view(np.uint32)))
     frags = int(ost["stats"]["fragments_written"])
@@ -254,6 +262,7 @@ def run_single_draw_section(dev, args):
     return {"workload": "icosphere L5, 20,480 triangles, 1280x720 RGBA8 + D32, basic_vs + basic_ps, LESS",
             "ms_per_frame_back_to_back": round(warm_ms, 5), "ms_per_frame_l2_flushed": round(cold_ms, 5),
             "mtri_per_s": round(tris / (warm_ms / 1e3) / 1e6, 1), "gpix_per_s": round(frags / (warm_ms / 1e3) / 1e9, 3),
+            "launch_shapes": tuned["best"] if tuned else "defaults",
             "fragments_written": frags, "depth_bit_exact_vs_oracle": same_depth, "stage_ms_eager": stages,
             "algorithmic_bytes_per_frame": int(nbytes),
             "roofline": {"bound": "hbm", "achieved_gbs_l2_flushed": round(nbytes / (cold_ms / 1e3) / 1e9, 1),
@@ -571,9 +580,12 @@ def main():
         print(json.dumps({"profile_diff": profile_diff(dev, args.profile_diff_views)}))
         dev.destroy()
         return 0
-    frame = scenes.config2_scene(seed=args.seed)
+    frame = scenes.config1_plain() if args.profile_once and args.profile_workload == "single" \
+        else scenes.config2_scene(seed=args.seed)
     r = api.FrameRenderer(dev, frame)
     if args.profile_once:
+        if args.warps_per_tile:
+            ctx.set_tuning(warps_per_tile=args.warps_per_tile)
         r.render_batched()
         ctx.finish()
         print(json.dumps({"profile_once": True, "stats": ctx.stats()}))

@@ -327,8 +327,10 @@ MLV_API mlv_status mlv_reset_stats(mlv_context context);
 /* Launch-shape knobs of the tile kernel, picked by the autotuner (malevich_gb300/autotune.py).
  * The hierarchical-Z tile stays 8x8 pixels: it is observable (main.c:1005-1010). */
 typedef struct mlv_tuning {
-    uint32_t tile_warps_per_block;    /* warps per CTA of the tile kernel: 2, 4 or 8 */
-    uint32_t lanes_per_triangle;      /* reserved, must be 1 (the tile kernel balances pixels itself) */
+    uint32_t tile_warps_per_block;    /* warps per CTA of the tile kernel (one tile each): 2, 4 or 8 */
+    uint32_t warps_per_tile;          /* 1, or 2, 4 or 8 warps sharing each tile's triangles (one tile per
+                                         CTA; tile_warps_per_block is then not used): for frames whose
+                                         triangles crowd into few tiles */
     uint32_t big_triangle_tiles;      /* triangles spanning more tiles are binned cooperatively */
     uint32_t geometry_block;          /* threads per CTA of the geometry kernel: 128, 256 or 512 */
     /* First sizes of the two buffers only the device can size (0 = automatic). When a batch needs

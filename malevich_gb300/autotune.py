@@ -3,7 +3,9 @@
 The reference has no counterpart: its tile and bin sizes are compile-time constants of a CPU
 binner (source/main.c:24-30) and its work per thread is one 8-wide SIMD triangle. On the GPU
 the same pipeline has free launch shapes that change the speed but never the output: the tile
-kernel's warps per CTA (how many 8x8 tiles a CTA carries), the geometry kernel's CTA size (how
+kernel's warps per CTA (how many 8x8 tiles a CTA carries, one warp each) or, instead, how many
+warps share one tile's triangles (for frames whose triangles crowd into few tiles), the geometry
+kernel's CTA size (how
 many input triangles one CTA sets up and bins), and the threshold above which a triangle's bins
 are counted and scattered cooperatively by a whole warp instead of by its own thread
 (triangles-per-warp against warps-per-triangle). The hierarchical-Z tile and the bins stay 8x8
@@ -18,16 +20,24 @@ import itertools
 
 SPACE = {
     "tile_warps_per_block": (2, 4, 8),
+    "warps_per_tile": (1, 2, 4, 8),
     "geometry_block": (128, 256, 512),
     "big_triangle_tiles": (4, 8, 16, 32),
 }
 
 
 def candidates(space=None):
-    """Every point of the search space as a dict, in a fixed order."""
+    """Every point of the search space as a dict, in a fixed order. With several warps per tile
+    the tile kernel runs one tile per CTA and tile_warps_per_block has no effect, so those points
+    are kept for one value of it only (4 when the space has it, else its first)."""
     space = SPACE if space is None else space
     keys = sorted(space)
-    return [dict(zip(keys, vals)) for vals in itertools.product(*(space[k] for k in keys))]
+    points = [dict(zip(keys, vals)) for vals in itertools.product(*(space[k] for k in keys))]
+    if "warps_per_tile" in space and "tile_warps_per_block" in space:
+        tw = space["tile_warps_per_block"]
+        keep = 4 if 4 in tw else tw[0]
+        points = [p for p in points if p["warps_per_tile"] == 1 or p["tile_warps_per_block"] == keep]
+    return points
 
 
 def pick(results):

@@ -35,7 +35,7 @@ cudaError_t launch_geometry(const BatchParams &bp, uint32_t block, cudaStream_t 
 cudaError_t launch_scan(const BatchParams &bp, cudaStream_t stream);
 cudaError_t launch_rank(const BatchParams &bp, cudaStream_t stream);
 cudaError_t launch_scatter(const BatchParams &bp, int num_sms, cudaStream_t stream);
-cudaError_t launch_tile(const BatchParams &bp, uint32_t warps, cudaStream_t stream);
+cudaError_t launch_tile(const BatchParams &bp, uint32_t warps, uint32_t warps_per_tile, cudaStream_t stream);
 }  // namespace mlv
 
 using namespace mlv;
@@ -685,7 +685,7 @@ static mlv_status launch_draws(mlv_context_t *c, const Plan &p, DrawDesc *d_draw
     CUDA_TRY(launch_scatter(bp, c->device->num_sms, c->stream));
     ev_end(c, e);
     ev_begin(c, 4, &e);
-    CUDA_TRY(launch_tile(bp, c->tuning.tile_warps_per_block, c->stream));
+    CUDA_TRY(launch_tile(bp, c->tuning.tile_warps_per_block, c->tuning.warps_per_tile, c->stream));
     ev_end(c, e);
     c->host_stats[4] += 4;
     return MLV_OK;
@@ -1634,7 +1634,8 @@ MLV_API mlv_status mlv_set_tuning(mlv_context c, const mlv_tuning *t) {
     if (!c || !t) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
     if (t->tile_warps_per_block != 2 && t->tile_warps_per_block != 4 && t->tile_warps_per_block != 8)
         return fail(MLV_ERROR_INVALID_ARG, "tile_warps_per_block must be 2, 4 or 8");
-    if (t->lanes_per_triangle != 1) return fail(MLV_ERROR_UNSUPPORTED, "lanes_per_triangle must be 1");
+    if (t->warps_per_tile != 1 && t->warps_per_tile != 2 && t->warps_per_tile != 4 && t->warps_per_tile != 8)
+        return fail(MLV_ERROR_INVALID_ARG, "warps_per_tile must be 1, 2, 4 or 8");
     if (t->geometry_block != 128 && t->geometry_block != 256 && t->geometry_block != 512)
         return fail(MLV_ERROR_INVALID_ARG, "geometry_block must be 128, 256 or 512");
     if (t->big_triangle_tiles < 1) return fail(MLV_ERROR_INVALID_ARG, "big_triangle_tiles must be >= 1");

@@ -913,6 +913,175 @@ __device__ __forceinline__ void write_cleared(const ViewDesc &V, size_t o, float
         reinterpret_cast<uint2 *>(V.vis_bary)[o] = make_uint2(V.clear_bary, V.clear_bary);
 }
 
+// One chunk of up to 32 entries [chunk, min(chunk + 32, e)) of a tile's bin for one draw. Each lane
+// stages one triangle (hierarchical-Z test, main.c:1005-1010; its box clipped to the tile), then
+// the warp walks the (triangle, pixel) work items of all of them, 32 at a time, and folds every
+// covered fragment (main.c:1015-1028) whose depth (main.c:1092-1102, 1131-1132) passes the test
+// against the depth at draw start (main.c:1164-1168) into best[pixel]: an atomic max (min for
+// LESS) of the 64-bit (depth, key). best and depth are the tile's 64 pixels, row-major; stage,
+// pref and mask are the warp's own.
+__device__ __forceinline__ void tile_chunk(const BatchParams &bp, uint32_t chunk, uint32_t e, int32_t x0, int32_t y0,
+                                           bool less, bool top_left, float hiz, uint32_t *stage, uint32_t *pref,
+                                           unsigned long long *mask, unsigned long long *best, const float *depth,
+                                           bool capture, int lane) {
+    const uint32_t i = chunk + lane;
+    uint32_t cnt = 0;
+    if (i < e) {
+        const uint32_t key = bp.list[i];
+        const uint32_t rec = record_of(bp, key);
+        const int4 *R = bp.raster[rec].w;
+        const int4 w2 = R[2], w3 = R[3];
+        const float zb = __int_as_float(w2.z);
+        const bool rejected = less ? (zb > hiz) : (zb < hiz);   // main.c:1005-1010 (mirrored for LESS)
+        int32_t bx0 = (int16_t)(w3.z & 0xFFFF), by0 = w3.z >> 16;
+        int32_t bx1 = (int16_t)(w3.w & 0xFFFF), by1 = w3.w >> 16;
+        bx0 = max(bx0, x0); by0 = max(by0, y0);
+        bx1 = min(bx1, x0 + kTile - 1); by1 = min(by1, y0 + kTile - 1);
+        if (!rejected && bx1 >= bx0 && by1 >= by0) {
+            const int4 w0 = R[0], w1 = R[1];
+            const uint32_t a0 = w0.x, b0 = w0.y, c0 = w0.z, a1 = w0.w, b1 = w1.x, c1 = w1.y, a2 = w1.z, b2 = w1.w,
+                           c2 = w2.x;
+            const uint32_t w = (uint32_t)(bx1 - bx0 + 1), h = (uint32_t)(by1 - by0 + 1);
+            cnt = w * h;
+            uint32_t *st = stage + lane * kStage;
+            // main.c:1015-1025: ((a*x)<<4) + ((b*y)<<4) + c, wrapping int32
+            st[kSE0] = ((a0 * (uint32_t)bx0) << kSubpix) + ((b0 * (uint32_t)by0) << kSubpix) + c0;
+            st[kSE1] = ((a1 * (uint32_t)bx0) << kSubpix) + ((b1 * (uint32_t)by0) << kSubpix) + c1;
+            st[kSE2] = ((a2 * (uint32_t)bx0) << kSubpix) + ((b2 * (uint32_t)by0) << kSubpix) + c2;
+            st[kSA0] = a0 << kSubpix; st[kSA1] = a1 << kSubpix; st[kSA2] = a2 << kSubpix;
+            st[kSB0] = b0 << kSubpix; st[kSB1] = b1 << kSubpix; st[kSB2] = b2 << kSubpix;
+            const float z0 = __int_as_float(w2.w);
+            st[kSInvArea] = (uint32_t)w2.y;
+            st[kSZ0] = (uint32_t)w2.w;
+            st[kSDz1] = __float_as_uint(__int_as_float(w3.x) - z0);
+            st[kSDz2] = __float_as_uint(__int_as_float(w3.y) - z0);
+            st[kSOrigin] = (uint32_t)(bx0 - x0) | ((uint32_t)(by0 - y0) << 8);
+            st[kSWidth] = w | (((65536u + w - 1) / w) << 8);
+            st[kSKey] = key;
+            // top-left rule: an edge value of 0 covers only on a left edge (a > 0) or a top edge
+            // (a == 0, b > 0); the others need E >= 1 (bit k set: edge k needs it)
+            st[kSPad] = ((int32_t)a0 > 0 || (a0 == 0 && (int32_t)b0 > 0) ? 0u : 1u) |
+                        ((int32_t)a1 > 0 || (a1 == 0 && (int32_t)b1 > 0) ? 0u : 2u) |
+                        ((int32_t)a2 > 0 || (a2 == 0 && (int32_t)b2 > 0) ? 0u : 4u);
+        }
+    }
+    if (capture) mask[lane] = 0;
+    // exclusive offsets of the (triangle, pixel) work items
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    pref[lane] = incl;
+    const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    __syncwarp();
+    for (uint32_t item = lane; item < total; item += 32) {
+        uint32_t j = 0;   // triangle of this item: number of prefixes <= item
+#pragma unroll
+        for (uint32_t step = 16; step; step >>= 1)
+            if (pref[j + step - 1] <= item) j += step;
+        const uint32_t *st = stage + j * kStage;
+        const uint32_t local = item - (j ? pref[j - 1] : 0u);
+        const uint32_t wr = st[kSWidth];
+        const uint32_t row = (local * (wr >> 8)) >> 16;
+        const uint32_t col = local - row * (wr & 0xFFu);
+        const uint32_t E0 = st[kSE0] + col * st[kSA0] + row * st[kSB0];
+        const uint32_t E1 = st[kSE1] + col * st[kSA1] + row * st[kSB1];
+        const uint32_t E2 = st[kSE2] + col * st[kSA2] + row * st[kSB2];
+        const uint32_t nb = st[kSPad];
+        const bool covered = top_left ? (int32_t)((E0 - (nb & 1u)) | (E1 - ((nb >> 1) & 1u)) | (E2 - (nb >> 2))) >= 0
+                                      : (int32_t)(E0 | E1 | E2) > 0;   // main.c:1028
+        if (covered) {
+            const uint32_t org = st[kSOrigin];
+            const int p = (int)(((org >> 8) + row) * 8 + (org & 0xFFu) + col);
+            if (capture) atomicOr(&mask[j], 1ull << p);
+            // main.c:1092-1102 and 1131-1132 for reg0.z
+            const float inv_area = __uint_as_float(st[kSInvArea]);
+            const float bb1 = (float)((int32_t)E1 >> (kSubpix * 2)) * inv_area;
+            const float bb2 = (float)((int32_t)E2 >> (kSubpix * 2)) * inv_area;
+            float z = __uint_as_float(st[kSZ0]) + __uint_as_float(st[kSDz1]) * bb1;
+            z = z + __uint_as_float(st[kSDz2]) * bb2;
+            const float dstart = depth[p];
+            const bool cand = less ? (z < dstart) : (z >= dstart);   // main.c:1164-1168
+            if (cand) {
+                const unsigned long long k = ((unsigned long long)depth_key(z) << 32) | st[kSKey];
+                if (less) atomicMin(&best[p], k);
+                else atomicMax(&best[p], k);
+            }
+        }
+    }
+    __syncwarp();
+    if (capture && i < e) bp.info_mask[i] = cnt ? mask[lane] : 0ull;
+    __syncwarp();
+}
+
+// The pixel shader and output merger for the fragment that won pixel (x, y): interpolation with
+// the reference's quantised barycentrics and perspective correction (main.c:1089-1160), the
+// shader (main.c:1172), packing (main.c:1176-1178), the colour and depth write (main.c:1180-1181)
+// and the visibility outputs.
+__device__ __forceinline__ void shade_pixel(const BatchParams &bp, const ViewDesc &V, uint32_t key, int32_t x,
+                                            int32_t y) {
+    const size_t o = (size_t)y * V.width + x;
+    const uint32_t rec = record_of(bp, key);
+    const int4 *R = bp.raster[rec].w;
+    const int4 w0 = R[0], w1 = R[1], w2 = R[2], w3 = R[3];
+    const float4 *S = bp.shade[rec].s;
+    const float4 s0 = S[0];
+    const uint32_t dr = __float_as_uint(s0.w);
+    const DrawDesc &D = bp.draws[dr];
+    const uint32_t E1 = (((uint32_t)w0.w * (uint32_t)x) << kSubpix) + (((uint32_t)w1.x * (uint32_t)y) << kSubpix) + (uint32_t)w1.y;
+    const uint32_t E2 = (((uint32_t)w1.z * (uint32_t)x) << kSubpix) + (((uint32_t)w1.w * (uint32_t)y) << kSubpix) + (uint32_t)w2.x;
+    const float inv_area = __int_as_float(w2.y);
+    const float b1 = (float)((int32_t)E1 >> (kSubpix * 2)) * inv_area;
+    const float b2 = (float)((int32_t)E2 >> (kSubpix * 2)) * inv_area;
+    const float z0 = __int_as_float(w2.w), z1 = __int_as_float(w3.x), z2 = __int_as_float(w3.y);
+    float z = z0 + (z1 - z0) * b1;
+    z = z + (z2 - z0) * b2;
+    if (D.ps != kPsNone) {
+        // perspective correction, main.c:1106-1115
+        float den = (1.0f - (b1 + b2)) * s0.x;
+        den = den + b1 * s0.y;
+        den = den + b2 * s0.z;
+        den = 1.0f / den;
+        const float pb1 = (b1 * s0.y) * den;
+        const float pb2 = (b2 * s0.z) * den;
+        const float4 r0 = S[1], r1 = S[2], r2 = S[3], uv2 = S[4];
+        auto interp = [&](float v0, float v1, float v2) {
+            float tmp = v0 + (v1 - v0) * pb1;
+            return tmp + (v2 - v0) * pb2;
+        };
+        const float a0 = interp(r0.x, r1.x, r2.x), a1 = interp(r0.y, r1.y, r2.y), a2 = interp(r0.z, r1.z, r2.z);
+        const float u = interp(r0.w, r1.w, r2.w), v = interp(uv2.x, uv2.y, uv2.z);
+        const float3 c = run_ps(D.ps, a0, a1, a2, u, v, D.ps_tex);
+        V.color[o] = pack_color(c.x, c.y, c.z);
+    } else if (V.clear_flags & kClearColor) {
+        V.color[o] = V.clear_color;   // a null pixel shader leaves the (folded) clear colour
+    }
+    V.depth[o] = z;
+    if (V.vis_tri && bp.rank) {
+        // the reference's triangle id: its index among the draw's assembled triangles
+        const uint32_t g = key >> 3, cf = key & 7u;
+        const uint32_t fmask = bp.tri_info[g] & 0xFFu;
+        const uint32_t below = cf ? (uint32_t)__popc(fmask & ((1u << (cf - 1)) - 1u)) : 0u;
+        V.vis_tri[o] = bp.rank[g] - bp.rank[D.tri_begin] + below;
+    }
+    if (V.vis_draw) V.vis_draw[o] = D.draw_seq;
+    if (V.vis_prim) V.vis_prim[o] = (key >> 3) - D.tri_begin;
+    if (V.vis_bary) reinterpret_cast<float2 *>(V.vis_bary)[o] = make_float2(b1, b2);
+}
+
+// Commits the batch's staged statistics (k_geometry and k_scan finished before the tile kernel).
+__device__ __forceinline__ void commit_stats(const BatchParams &bp) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        for (int k = 0; k < 3; ++k) {
+            bp.stats[kStatTotal + k] += bp.stats[k];
+            bp.stats[k] = 0;
+        }
+    }
+}
+
+// One warp per tile, WARPS tiles per CTA.
 template <int WARPS>
 __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
     __shared__ unsigned long long s_best[WARPS][64];
@@ -922,13 +1091,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
     __shared__ unsigned long long s_mask[WARPS][32];
     pdl_wait();
     if (ld_volatile_u32(bp.error)) return;
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        // commit the batch's staged statistics (k_geometry and k_scan finished before this kernel)
-        for (int k = 0; k < 3; ++k) {
-            bp.stats[kStatTotal + k] += bp.stats[k];
-            bp.stats[k] = 0;
-        }
-    }
+    commit_stats(bp);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t gtile = blockIdx.x * WARPS + warp;
     if (gtile >= bp.total_tiles) return;
@@ -966,8 +1129,6 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
     s_depth[warp][lane] = dcur0;
     s_depth[warp][lane + 32] = dcur1;
     float hiz_min = depth_cleared ? 0.0f : V.tile_min[t], hiz_max = depth_cleared ? 1.0f : V.tile_max[t];
-    uint32_t *stage = s_stage[warp];
-    uint32_t *pref = s_pref[warp];
     const bool capture = bp.info_mask != nullptr;
 
     for (uint32_t dd = 0; dd < dc; ++dd) {
@@ -987,98 +1148,9 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
         s_best[warp][lane] = sentinel;
         s_best[warp][lane + 32] = sentinel;
         const float hiz = less ? hiz_max : hiz_min;
-        for (uint32_t chunk = s; chunk < e; chunk += 32) {
-            const uint32_t i = chunk + lane;
-            uint32_t cnt = 0;
-            if (i < e) {
-                const uint32_t key = bp.list[i];
-                const uint32_t rec = record_of(bp, key);
-                const int4 *R = bp.raster[rec].w;
-                const int4 w2 = R[2], w3 = R[3];
-                const float zb = __int_as_float(w2.z);
-                const bool rejected = less ? (zb > hiz) : (zb < hiz);   // main.c:1005-1010 (mirrored for LESS)
-                int32_t bx0 = (int16_t)(w3.z & 0xFFFF), by0 = w3.z >> 16;
-                int32_t bx1 = (int16_t)(w3.w & 0xFFFF), by1 = w3.w >> 16;
-                bx0 = max(bx0, x0); by0 = max(by0, y0);
-                bx1 = min(bx1, x0 + kTile - 1); by1 = min(by1, y0 + kTile - 1);
-                if (!rejected && bx1 >= bx0 && by1 >= by0) {
-                    const int4 w0 = R[0], w1 = R[1];
-                    const uint32_t a0 = w0.x, b0 = w0.y, c0 = w0.z, a1 = w0.w, b1 = w1.x, c1 = w1.y, a2 = w1.z,
-                                   b2 = w1.w, c2 = w2.x;
-                    const uint32_t w = (uint32_t)(bx1 - bx0 + 1), h = (uint32_t)(by1 - by0 + 1);
-                    cnt = w * h;
-                    uint32_t *st = stage + lane * kStage;
-                    // main.c:1015-1025: ((a*x)<<4) + ((b*y)<<4) + c, wrapping int32
-                    st[kSE0] = ((a0 * (uint32_t)bx0) << kSubpix) + ((b0 * (uint32_t)by0) << kSubpix) + c0;
-                    st[kSE1] = ((a1 * (uint32_t)bx0) << kSubpix) + ((b1 * (uint32_t)by0) << kSubpix) + c1;
-                    st[kSE2] = ((a2 * (uint32_t)bx0) << kSubpix) + ((b2 * (uint32_t)by0) << kSubpix) + c2;
-                    st[kSA0] = a0 << kSubpix; st[kSA1] = a1 << kSubpix; st[kSA2] = a2 << kSubpix;
-                    st[kSB0] = b0 << kSubpix; st[kSB1] = b1 << kSubpix; st[kSB2] = b2 << kSubpix;
-                    const float z0 = __int_as_float(w2.w);
-                    st[kSInvArea] = (uint32_t)w2.y;
-                    st[kSZ0] = (uint32_t)w2.w;
-                    st[kSDz1] = __float_as_uint(__int_as_float(w3.x) - z0);
-                    st[kSDz2] = __float_as_uint(__int_as_float(w3.y) - z0);
-                    st[kSOrigin] = (uint32_t)(bx0 - x0) | ((uint32_t)(by0 - y0) << 8);
-                    st[kSWidth] = w | (((65536u + w - 1) / w) << 8);
-                    st[kSKey] = key;
-                    // top-left rule: an edge value of 0 covers only on a left edge (a > 0) or a top
-                    // edge (a == 0, b > 0); the others need E >= 1 (bit k set: edge k needs it)
-                    st[kSPad] = ((int32_t)a0 > 0 || (a0 == 0 && (int32_t)b0 > 0) ? 0u : 1u) |
-                                ((int32_t)a1 > 0 || (a1 == 0 && (int32_t)b1 > 0) ? 0u : 2u) |
-                                ((int32_t)a2 > 0 || (a2 == 0 && (int32_t)b2 > 0) ? 0u : 4u);
-                }
-            }
-            if (capture) s_mask[warp][lane] = 0;
-            // exclusive offsets of the (triangle, pixel) work items
-            uint32_t incl = cnt;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-                if (lane >= o) incl += y;
-            }
-            pref[lane] = incl;
-            const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-            __syncwarp();
-            for (uint32_t item = lane; item < total; item += 32) {
-                uint32_t j = 0;   // triangle of this item: number of prefixes <= item
-#pragma unroll
-                for (uint32_t step = 16; step; step >>= 1)
-                    if (pref[j + step - 1] <= item) j += step;
-                const uint32_t *st = stage + j * kStage;
-                const uint32_t local = item - (j ? pref[j - 1] : 0u);
-                const uint32_t wr = st[kSWidth];
-                const uint32_t row = (local * (wr >> 8)) >> 16;
-                const uint32_t col = local - row * (wr & 0xFFu);
-                const uint32_t E0 = st[kSE0] + col * st[kSA0] + row * st[kSB0];
-                const uint32_t E1 = st[kSE1] + col * st[kSA1] + row * st[kSB1];
-                const uint32_t E2 = st[kSE2] + col * st[kSA2] + row * st[kSB2];
-                const uint32_t nb = st[kSPad];
-                const bool covered = top_left ? (int32_t)((E0 - (nb & 1u)) | (E1 - ((nb >> 1) & 1u)) | (E2 - (nb >> 2))) >= 0
-                                              : (int32_t)(E0 | E1 | E2) > 0;   // main.c:1028
-                if (covered) {
-                    const uint32_t org = st[kSOrigin];
-                    const int p = (int)(((org >> 8) + row) * 8 + (org & 0xFFu) + col);
-                    if (capture) atomicOr(&s_mask[warp][j], 1ull << p);
-                    // main.c:1092-1102 and 1131-1132 for reg0.z
-                    const float inv_area = __uint_as_float(st[kSInvArea]);
-                    const float bb1 = (float)((int32_t)E1 >> (kSubpix * 2)) * inv_area;
-                    const float bb2 = (float)((int32_t)E2 >> (kSubpix * 2)) * inv_area;
-                    float z = __uint_as_float(st[kSZ0]) + __uint_as_float(st[kSDz1]) * bb1;
-                    z = z + __uint_as_float(st[kSDz2]) * bb2;
-                    const float dstart = s_depth[warp][p];
-                    const bool cand = less ? (z < dstart) : (z >= dstart);   // main.c:1164-1168
-                    if (cand) {
-                        const unsigned long long k = ((unsigned long long)depth_key(z) << 32) | st[kSKey];
-                        if (less) atomicMin(&s_best[warp][p], k);
-                        else atomicMax(&s_best[warp][p], k);
-                    }
-                }
-            }
-            __syncwarp();
-            if (capture && i < e) bp.info_mask[i] = cnt ? s_mask[warp][lane] : 0ull;
-            __syncwarp();
-        }
+        for (uint32_t chunk = s; chunk < e; chunk += 32)
+            tile_chunk(bp, chunk, e, x0, y0, less, top_left, hiz, s_stage[warp], s_pref[warp], s_mask[warp],
+                       s_best[warp], s_depth[warp], capture, lane);
         // fold this draw's winners into the running state; hierarchical Z update (write_tile, main.c:589-603)
         const unsigned long long k0 = s_best[warp][lane], k1 = s_best[warp][lane + 32];
         if (k0 != sentinel) { dcur0 = depth_from_key((uint32_t)(k0 >> 32)); win0 = (uint32_t)k0; }
@@ -1111,55 +1183,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
         if (q < n) src = nth_set_bit(half ? m1 : m0, half ? q - n0 : q);
         const uint32_t wa = __shfl_sync(0xFFFFFFFFu, win0, src), wb = __shfl_sync(0xFFFFFFFFu, win1, src);
         if (q >= n) continue;
-        const uint32_t key = half ? wb : wa;
-        const int32_t x = x0 + (int32_t)(src & 7), y = y0 + (int32_t)(src >> 3) + (half ? 4 : 0);
-        const size_t o = (size_t)y * V.width + x;
-        const uint32_t rec = record_of(bp, key);
-        const int4 *R = bp.raster[rec].w;
-        const int4 w0 = R[0], w1 = R[1], w2 = R[2], w3 = R[3];
-        const float4 *S = bp.shade[rec].s;
-        const float4 s0 = S[0];
-        const uint32_t dr = __float_as_uint(s0.w);
-        const DrawDesc &D = bp.draws[dr];
-        const uint32_t E1 = (((uint32_t)w0.w * (uint32_t)x) << kSubpix) + (((uint32_t)w1.x * (uint32_t)y) << kSubpix) + (uint32_t)w1.y;
-        const uint32_t E2 = (((uint32_t)w1.z * (uint32_t)x) << kSubpix) + (((uint32_t)w1.w * (uint32_t)y) << kSubpix) + (uint32_t)w2.x;
-        const float inv_area = __int_as_float(w2.y);
-        const float b1 = (float)((int32_t)E1 >> (kSubpix * 2)) * inv_area;
-        const float b2 = (float)((int32_t)E2 >> (kSubpix * 2)) * inv_area;
-        const float z0 = __int_as_float(w2.w), z1 = __int_as_float(w3.x), z2 = __int_as_float(w3.y);
-        float z = z0 + (z1 - z0) * b1;
-        z = z + (z2 - z0) * b2;
-        if (D.ps != kPsNone) {
-            // perspective correction, main.c:1106-1115
-            float den = (1.0f - (b1 + b2)) * s0.x;
-            den = den + b1 * s0.y;
-            den = den + b2 * s0.z;
-            den = 1.0f / den;
-            const float pb1 = (b1 * s0.y) * den;
-            const float pb2 = (b2 * s0.z) * den;
-            const float4 r0 = S[1], r1 = S[2], r2 = S[3], uv2 = S[4];
-            auto interp = [&](float v0, float v1, float v2) {
-                float tmp = v0 + (v1 - v0) * pb1;
-                return tmp + (v2 - v0) * pb2;
-            };
-            const float a0 = interp(r0.x, r1.x, r2.x), a1 = interp(r0.y, r1.y, r2.y), a2 = interp(r0.z, r1.z, r2.z);
-            const float u = interp(r0.w, r1.w, r2.w), v = interp(uv2.x, uv2.y, uv2.z);
-            const float3 c = run_ps(D.ps, a0, a1, a2, u, v, D.ps_tex);
-            V.color[o] = pack_color(c.x, c.y, c.z);
-        } else if (V.clear_flags & kClearColor) {
-            V.color[o] = V.clear_color;   // a null pixel shader leaves the (folded) clear colour
-        }
-        V.depth[o] = z;
-        if (V.vis_tri && bp.rank) {
-            // the reference's triangle id: its index among the draw's assembled triangles
-            const uint32_t g = key >> 3, cf = key & 7u;
-            const uint32_t fmask = bp.tri_info[g] & 0xFFu;
-            const uint32_t below = cf ? (uint32_t)__popc(fmask & ((1u << (cf - 1)) - 1u)) : 0u;
-            V.vis_tri[o] = bp.rank[g] - bp.rank[D.tri_begin] + below;
-        }
-        if (V.vis_draw) V.vis_draw[o] = D.draw_seq;
-        if (V.vis_prim) V.vis_prim[o] = (key >> 3) - D.tri_begin;
-        if (V.vis_bary) reinterpret_cast<float2 *>(V.vis_bary)[o] = make_float2(b1, b2);
+        shade_pixel(bp, V, half ? wb : wa, x0 + (int32_t)(src & 7), y0 + (int32_t)(src >> 3) + (half ? 4 : 0));
     }
     // pixels no draw wrote still owe their folded clears
     if (V.clear_flags) {
@@ -1167,6 +1191,119 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
         if (valid1 && win1 == 0xFFFFFFFFu) write_cleared(V, o1, dcur1);
     }
     if (lane == 0) {
+        V.tile_min[t] = hiz_min;
+        V.tile_max[t] = hiz_max;
+    }
+    pdl_trigger();
+}
+
+// One tile per CTA, its triangles shared by WARPS warps: each warp takes an equal share of a bin's
+// entries (most bins hold fewer than 32, so chunk-wise sharing would leave the other warps idle),
+// all fold into the CTA's best keys. For frames whose triangles crowd into few tiles (a single
+// large mesh): k_tile leaves most of the GPU idle behind those tiles' warps. Same results
+// as k_tile: the per-pixel max (min) of (depth, key) does not depend on which warp finds it, and
+// thread t < 64 owns pixel t for the fold, the hierarchical-Z bounds and the pixel shader.
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_tile_coop(BatchParams bp) {
+    static_assert(WARPS >= 2, "threads 0-63 own the tile's pixels");
+    __shared__ unsigned long long s_best[64];
+    __shared__ float s_depth[64];
+    __shared__ float s_hiz[2];
+    __shared__ uint32_t s_stage[WARPS][32 * kStage];
+    __shared__ uint32_t s_pref[WARPS][32];
+    __shared__ unsigned long long s_mask[WARPS][32];
+    pdl_wait();
+    if (ld_volatile_u32(bp.error)) return;   // uniform: set only by earlier kernels
+    commit_stats(bp);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t gtile = blockIdx.x;
+    if (gtile >= bp.total_tiles) return;
+    const uint32_t vi = find_view(bp, gtile);
+    const ViewDesc &V = bp.views[vi];
+    const uint32_t t = gtile - V.tile_base;
+    const uint32_t tx = t % V.tiles_x, ty = t / V.tiles_x;
+    const uint32_t bin0 = V.bin_base + t * V.draw_count;
+    const uint32_t dc = V.draw_count;
+    const uint32_t my_start = lane <= dc ? __ldg(bp.bin_start + bin0 + lane) : 0u;
+    const uint32_t last = dc < 32 ? __shfl_sync(0xFFFFFFFFu, my_start, dc) : __ldg(bp.bin_start + bin0 + dc);
+
+    const int32_t x0 = (int32_t)tx * kTile, y0 = (int32_t)ty * kTile;
+    const int pix = (int)threadIdx.x;           // pixel of threads 0-63: row-major in the tile
+    const bool owner = pix < 64;
+    const int32_t px = x0 + (pix & 7), py = y0 + (pix >> 3);
+    const bool valid = owner && px < (int32_t)V.width && py < (int32_t)V.height;
+    const size_t o = (size_t)py * V.width + px;
+    const bool depth_cleared = (V.clear_flags & kClearDepth) != 0;
+    if (__shfl_sync(0xFFFFFFFFu, my_start, 0) == last) {   // uniform: no draw binned a triangle here
+        if (V.clear_flags) {
+            if (valid) write_cleared(V, o, V.clear_depth);
+            if (threadIdx.x == 0 && depth_cleared) {   // main.c:1212-1214
+                V.tile_min[t] = 0.0f;
+                V.tile_max[t] = 1.0f;
+            }
+        }
+        return;
+    }
+    float dcur = valid ? (depth_cleared ? V.clear_depth : V.depth[o]) : 0.0f;
+    uint32_t win = 0xFFFFFFFFu;
+    if (owner) s_depth[pix] = dcur;
+    float hiz_min = depth_cleared ? 0.0f : V.tile_min[t], hiz_max = depth_cleared ? 1.0f : V.tile_max[t];
+    const bool capture = bp.info_mask != nullptr;
+
+    for (uint32_t dd = 0; dd < dc; ++dd) {
+        uint32_t s, e;
+        if (dd + 1 < 32) {
+            s = __shfl_sync(0xFFFFFFFFu, my_start, dd);
+            e = __shfl_sync(0xFFFFFFFFu, my_start, dd + 1);
+        } else {
+            s = __ldg(bp.bin_start + bin0 + dd);
+            e = __ldg(bp.bin_start + bin0 + dd + 1);
+        }
+        if (s == e) continue;   // uniform over the CTA
+        const DrawDesc &D = bp.draws[V.draw_begin + dd];
+        const bool less = D.depth_less != 0;
+        const bool top_left = (D.raster_flags & kRasterTopLeft) != 0;
+        const unsigned long long sentinel = less ? ~0ull : 0ull;
+        if (owner) s_best[pix] = sentinel;
+        __syncthreads();   // the keys are reset and the depths at draw start are in place
+        const float hiz = less ? hiz_max : hiz_min;
+        const uint32_t n = e - s, per = (n + WARPS - 1) / WARPS;
+        const uint32_t ws = s + min(n, per * (uint32_t)warp), we = s + min(n, per * (uint32_t)(warp + 1));
+        for (uint32_t chunk = ws; chunk < we; chunk += 32)
+            tile_chunk(bp, chunk, we, x0, y0, less, top_left, hiz, s_stage[warp], s_pref[warp], s_mask[warp],
+                       s_best, s_depth, capture, lane);
+        __syncthreads();   // every warp's fragments are in
+        if (owner) {
+            const unsigned long long k = s_best[pix];
+            if (k != sentinel) { dcur = depth_from_key((uint32_t)(k >> 32)); win = (uint32_t)k; }
+            s_depth[pix] = dcur;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            // write_tile's bounds (main.c:589-603), combined in the same order as k_tile: pixel
+            // lane, then lane + 32, then across lanes
+            const bool v0 = x0 + (lane & 7) < (int32_t)V.width && y0 + (lane >> 3) < (int32_t)V.height;
+            const bool v1 = x0 + (lane & 7) < (int32_t)V.width && y0 + (lane >> 3) + 4 < (int32_t)V.height;
+            const float d0 = s_depth[lane], d1 = s_depth[lane + 32];
+            float mn = 1.0f, mx = 0.0f;
+            if (v0) { mn = fmin_ref(mn, d0); mx = fmax_ref(mx, d0); }
+            if (v1) { mn = fmin_ref(mn, d1); mx = fmax_ref(mx, d1); }
+#pragma unroll
+            for (int sh = 16; sh > 0; sh >>= 1) {
+                float a = __shfl_xor_sync(0xFFFFFFFFu, mn, sh), b = __shfl_xor_sync(0xFFFFFFFFu, mx, sh);
+                mn = fmin_ref(mn, a);
+                mx = fmax_ref(mx, b);
+            }
+            if (lane == 0) { s_hiz[0] = mn; s_hiz[1] = mx; }
+        }
+        __syncthreads();
+        hiz_min = s_hiz[0];
+        hiz_max = s_hiz[1];
+    }
+
+    if (valid && win != 0xFFFFFFFFu) shade_pixel(bp, V, win, px, py);
+    if (valid && win == 0xFFFFFFFFu && V.clear_flags) write_cleared(V, o, dcur);
+    if (threadIdx.x == 0) {
         V.tile_min[t] = hiz_min;
         V.tile_max[t] = hiz_max;
     }
@@ -1296,7 +1433,10 @@ cudaError_t launch_scatter(const BatchParams &bp, int num_sms, cudaStream_t stre
     return launch_chained(k_scatter, blocks, kScatterBlock, stream, bp);
 }
 
-cudaError_t launch_tile(const BatchParams &bp, uint32_t warps, cudaStream_t stream) {
+cudaError_t launch_tile(const BatchParams &bp, uint32_t warps, uint32_t warps_per_tile, cudaStream_t stream) {
+    if (warps_per_tile == 2) return launch_chained(k_tile_coop<2>, bp.total_tiles, 64, stream, bp);
+    if (warps_per_tile == 4) return launch_chained(k_tile_coop<4>, bp.total_tiles, 128, stream, bp);
+    if (warps_per_tile == 8) return launch_chained(k_tile_coop<8>, bp.total_tiles, 256, stream, bp);
     switch (warps) {
         case 2: return launch_chained(k_tile<2>, (bp.total_tiles + 1) / 2, 64, stream, bp);
         case 8: return launch_chained(k_tile<8>, (bp.total_tiles + 7) / 8, 256, stream, bp);

@@ -24,7 +24,7 @@ cudaError_t launch_vertex(const BatchParams &bp, cudaStream_t stream);
 cudaError_t launch_geometry(const BatchParams &bp, uint32_t block, cudaStream_t stream);
 cudaError_t launch_scan(const BatchParams &bp, cudaStream_t stream);
 cudaError_t launch_scatter(const BatchParams &bp, int num_sms, cudaStream_t stream);
-cudaError_t launch_tile(const BatchParams &bp, uint32_t warps, cudaStream_t stream);
+cudaError_t launch_tile(const BatchParams &bp, uint32_t warps, uint32_t warps_per_tile, cudaStream_t stream);
 void set_last_error(const std::string &msg);
 }  // namespace mlv
 
@@ -300,7 +300,7 @@ extern "C" MLV_API mlv_status mlv_draw_indexed_noalloc(const mlv_noalloc_draw *a
         NA_CUDA(launch_geometry(bp, 128, stream));
         NA_CUDA(launch_scan(bp, stream));
         NA_CUDA(launch_scatter(bp, g_num_sms[dev] ? g_num_sms[dev] : 152, stream));
-        NA_CUDA(launch_tile(bp, 4, stream));
+        NA_CUDA(launch_tile(bp, 4, 1, stream));
     }
     // ---- wait, then report what only the device knows
     uint32_t err[8] = {0};

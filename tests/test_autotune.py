@@ -11,7 +11,11 @@ def test_candidates_cover_the_space_in_order():
     pts = autotune.candidates(space)
     assert len(pts) == 6
     assert pts[0] == {"a": 3, "b": 1} and pts[-1] == {"a": 5, "b": 2}
-    assert len(autotune.candidates()) == 3 * 3 * 4
+    # several warps per tile make the warps-per-CTA knob moot: (3 + 3) tile shapes
+    assert len(autotune.candidates()) == (3 + 3) * 3 * 4
+    pts = autotune.candidates({"tile_warps_per_block": (2, 8), "warps_per_tile": (1, 4)})
+    assert pts == [{"tile_warps_per_block": 2, "warps_per_tile": 1}, {"tile_warps_per_block": 2, "warps_per_tile": 4},
+                   {"tile_warps_per_block": 8, "warps_per_tile": 1}]
 
 
 def test_pick_takes_the_fastest_and_keeps_the_first_tie():
@@ -21,7 +25,7 @@ def test_pick_takes_the_fastest_and_keeps_the_first_tie():
 
 class _FakeCtx:
     def __init__(self):
-        self.t = {"tile_warps_per_block": 4, "geometry_block": 256, "big_triangle_tiles": 16}
+        self.t = {"tile_warps_per_block": 4, "warps_per_tile": 1, "geometry_block": 256, "big_triangle_tiles": 16}
         self.history = []
 
     def tuning(self):
@@ -47,9 +51,10 @@ def test_autotune_sets_the_fastest_point():
     cost = lambda: dev.immediate.t["tile_warps_per_block"] * 10 + abs(dev.immediate.t["geometry_block"] - 128) + \
         dev.immediate.t["big_triangle_tiles"] * 0.1
     out = autotune.autotune(dev, _FakeRenderer(), time_fn=lambda fn: (fn(), cost())[1])
-    assert out["best"] == {"big_triangle_tiles": 4, "geometry_block": 128, "tile_warps_per_block": 2}
+    assert out["best"] == {"big_triangle_tiles": 4, "geometry_block": 128, "tile_warps_per_block": 2,
+                           "warps_per_tile": 1}
     assert dev.immediate.t == out["best"]
-    assert len(out["results"]) == 36
+    assert len(out["results"]) == 72
 
 
 def test_autotune_restores_the_tuning_on_error():
@@ -64,7 +69,8 @@ def test_autotune_restores_the_tuning_on_error():
 
     with pytest.raises(RuntimeError):
         autotune.autotune(dev, _FakeRenderer(), time_fn=bad_timer)
-    assert dev.immediate.t == {"tile_warps_per_block": 4, "geometry_block": 256, "big_triangle_tiles": 16}
+    assert dev.immediate.t == {"tile_warps_per_block": 4, "warps_per_tile": 1, "geometry_block": 256,
+                               "big_triangle_tiles": 16}
 
 
 @pytest.mark.gpu
