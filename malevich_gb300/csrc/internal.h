@@ -46,7 +46,8 @@ struct DrawDesc {
     uint32_t draw_seq;                   // draw number since the render target's last clear
     uint32_t vs_cached;                  // 1: vertices were shaded once by k_vertex into vs_out
     float cb[48];                        // PerFrameCB snapshot
-    float screen_from_ndc[16];           // main.c:825-830, computed on the host as the reference does
+    float screen_from_ndc[16];           // main.c:825-830, computed on the host as the reference does;
+                                         // entries 1, 2, 4, 6, 8, 9, 12-14 are 0 and 15 is 1 (relied on)
     int32_t vp_w, vp_h;                  // (i32)viewport.width/height
     uint32_t vs_base, vs_count;          // this draw's range in vs_out (count 0 when not cached)
     TexDesc vs_tex, ps_tex;

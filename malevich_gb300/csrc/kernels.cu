@@ -165,6 +165,25 @@ __device__ __forceinline__ void set_edge(int32_t *e, int32_t area, int32_t x0, i
     e[0] = (int32_t)a; e[1] = (int32_t)b; e[2] = (int32_t)c;
 }
 
+// The viewport transform of main.c:823-839, out[r] = ((m[4r]p0 + m[4r+1]p1) + m[4r+2]p2) + m[4r+3]p3,
+// for the matrix the host builds (main.c:825-830): its entries 1, 2, 4, 6, 8, 9, 12, 13, 14 are 0
+// and entry 15 is 1. With finite inputs, the products by those zeros are signed zeros, which can
+// change a row's sum only when the sum is itself zero; so a row is its two other products unless
+// that gives zero (or an input is not finite), when the whole product is taken as written.
+__device__ __forceinline__ void viewport_transform(const float *m, float p0, float p1, float p2, float p3,
+                                                   float *out) {
+    const float x = m[0] * p0 + m[3] * p3;
+    const float y = m[5] * p1 + m[7] * p3;
+    const float z = m[10] * p2 + m[11] * p3;
+    const bool finite = fabsf(p0) < INFINITY && fabsf(p1) < INFINITY && fabsf(p2) < INFINITY && fabsf(p3) < INFINITY;
+    if (finite && x != 0.0f && y != 0.0f && z != 0.0f && p3 != 0.0f) {
+        out[0] = x; out[1] = y; out[2] = z; out[3] = p3;
+        return;
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r) out[r] = dot4_lr(m + 4 * r, p0, p1, p2, p3);
+}
+
 // Projection, viewport, 28.4 snap, signed area, cull, edge functions, 1/w, depth bound and pixel
 // bounds for one (possibly clip-generated) triangle: main.c:798-904. Returns false when culled.
 __device__ __forceinline__ bool setup_triangle(const DrawDesc &d, const Vtx &v0, const Vtx &v1, const Vtx &v2,
@@ -177,8 +196,7 @@ __device__ __forceinline__ bool setup_triangle(const DrawDesc &d, const Vtx &v0,
         float rw = 1.0f / tv[k]->v[3];
         float p0 = tv[k]->v[0] * rw, p1 = tv[k]->v[1] * rw, p2 = tv[k]->v[2] * rw, p3 = tv[k]->v[3] * rw;
         s.rw[k] = rw;
-#pragma unroll
-        for (int r = 0; r < 4; ++r) s.ss[k][r] = dot4_lr(m + 4 * r, p0, p1, p2, p3);
+        viewport_transform(m, p0, p1, p2, p3, s.ss[k]);
         x[k] = snap28_4(s.ss[k][0]);
         y[k] = snap28_4(s.ss[k][1]);
     }
@@ -913,19 +931,32 @@ __device__ __forceinline__ void write_cleared(const ViewDesc &V, size_t o, float
         reinterpret_cast<uint2 *>(V.vis_bary)[o] = make_uint2(V.clear_bary, V.clear_bary);
 }
 
+// Triangles with more (triangle, pixel) work items in the tile than this are tested at every pixel
+// of the tile by the whole warp, two pixels a lane, instead of through the work-item list: the
+// list costs a few instructions per item per lane (finding the item's triangle and decoding it),
+// the whole-tile test a fixed amount per triangle.
+constexpr uint32_t kWholeTileItems = 24;
+
+// Keeps the better of two (depth, key) pairs: the larger for GREATER_EQUAL, the smaller for LESS.
+__device__ __forceinline__ unsigned long long better_key(bool less, unsigned long long a, unsigned long long b) {
+    return less ? (a < b ? a : b) : (a > b ? a : b);
+}
+
 // One chunk of up to 32 entries [chunk, min(chunk + 32, e)) of a tile's bin for one draw. Each lane
 // stages one triangle (hierarchical-Z test, main.c:1005-1010; its box clipped to the tile), then
-// the warp walks the (triangle, pixel) work items of all of them, 32 at a time, and folds every
-// covered fragment (main.c:1015-1028) whose depth (main.c:1092-1102, 1131-1132) passes the test
-// against the depth at draw start (main.c:1164-1168) into best[pixel]: an atomic max (min for
-// LESS) of the 64-bit (depth, key). best and depth are the tile's 64 pixels, row-major; stage,
-// pref and mask are the warp's own.
+// the warp walks the (triangle, pixel) work items of the small ones, 32 at a time, and tests the
+// large ones at every pixel of the tile, and folds every covered fragment (main.c:1015-1028) whose
+// depth (main.c:1092-1102, 1131-1132) passes the test against the depth at draw start
+// (main.c:1164-1168) into the pixel's best (depth, key): for work items an atomic max (min for
+// LESS) on best[pixel], for whole-tile tests the lane's own fa (pixel lane) and fb (pixel lane + 32),
+// which the caller folds into best after the draw. best and depth are the tile's 64 pixels,
+// row-major; stage, pref and mask are the warp's own.
 __device__ __forceinline__ void tile_chunk(const BatchParams &bp, uint32_t chunk, uint32_t e, int32_t x0, int32_t y0,
                                            bool less, bool top_left, float hiz, uint32_t *stage, uint32_t *pref,
                                            unsigned long long *mask, unsigned long long *best, const float *depth,
-                                           bool capture, int lane) {
+                                           bool capture, int lane, unsigned long long &fa, unsigned long long &fb) {
     const uint32_t i = chunk + lane;
-    uint32_t cnt = 0;
+    uint32_t cnt = 0;   // work items of this lane's triangle in the tile
     if (i < e) {
         const uint32_t key = bp.list[i];
         const uint32_t rec = record_of(bp, key);
@@ -959,15 +990,16 @@ __device__ __forceinline__ void tile_chunk(const BatchParams &bp, uint32_t chunk
             st[kSWidth] = w | (((65536u + w - 1) / w) << 8);
             st[kSKey] = key;
             // top-left rule: an edge value of 0 covers only on a left edge (a > 0) or a top edge
-            // (a == 0, b > 0); the others need E >= 1 (bit k set: edge k needs it)
+            // (a == 0, b > 0); the others need E >= 1 (bit k set: edge k needs it); box height above
             st[kSPad] = ((int32_t)a0 > 0 || (a0 == 0 && (int32_t)b0 > 0) ? 0u : 1u) |
                         ((int32_t)a1 > 0 || (a1 == 0 && (int32_t)b1 > 0) ? 0u : 2u) |
-                        ((int32_t)a2 > 0 || (a2 == 0 && (int32_t)b2 > 0) ? 0u : 4u);
+                        ((int32_t)a2 > 0 || (a2 == 0 && (int32_t)b2 > 0) ? 0u : 4u) | (h << 8);
         }
     }
     if (capture) mask[lane] = 0;
-    // exclusive offsets of the (triangle, pixel) work items
-    uint32_t incl = cnt;
+    const bool whole = cnt > kWholeTileItems;
+    // exclusive offsets of the (triangle, pixel) work items of the small triangles
+    uint32_t incl = whole ? 0u : cnt;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
         uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
@@ -990,7 +1022,7 @@ __device__ __forceinline__ void tile_chunk(const BatchParams &bp, uint32_t chunk
         const uint32_t E1 = st[kSE1] + col * st[kSA1] + row * st[kSB1];
         const uint32_t E2 = st[kSE2] + col * st[kSA2] + row * st[kSB2];
         const uint32_t nb = st[kSPad];
-        const bool covered = top_left ? (int32_t)((E0 - (nb & 1u)) | (E1 - ((nb >> 1) & 1u)) | (E2 - (nb >> 2))) >= 0
+        const bool covered = top_left ? (int32_t)((E0 - (nb & 1u)) | (E1 - ((nb >> 1) & 1u)) | (E2 - ((nb >> 2) & 1u))) >= 0
                                       : (int32_t)(E0 | E1 | E2) > 0;   // main.c:1028
         if (covered) {
             const uint32_t org = st[kSOrigin];
@@ -1010,6 +1042,58 @@ __device__ __forceinline__ void tile_chunk(const BatchParams &bp, uint32_t chunk
                 else atomicMax(&best[p], k);
             }
         }
+    }
+    // the large triangles: every lane tests its two pixels, (lane & 7, lane >> 3) and 4 rows below
+    uint32_t big = __ballot_sync(0xFFFFFFFFu, whole);
+    if (big) {
+        const float da = depth[lane], db = depth[lane + 32];
+        const int32_t cx = lane & 7, cy = lane >> 3;
+        do {
+            const int j = __ffs(big) - 1;
+            big &= big - 1;
+            const uint32_t *st = stage + j * kStage;
+            const uint32_t org = st[kSOrigin], nb = st[kSPad];
+            // offsets from the box origin; outside the box nothing is tested (main.c:1015-1025)
+            const uint32_t dx = (uint32_t)(cx - (int32_t)(org & 0xFFu)), dy = (uint32_t)(cy - (int32_t)(org >> 8));
+            const uint32_t w = st[kSWidth] & 0xFFu, h = nb >> 8;
+            const bool in_x = dx < w;
+            const bool in_a = in_x && dy < h, in_b = in_x && dy + 4u < h;
+            const uint32_t sb0 = st[kSB0], sb1 = st[kSB1], sb2 = st[kSB2];
+            const uint32_t E0a = st[kSE0] + dx * st[kSA0] + dy * sb0, E0b = E0a + (sb0 << 2);
+            const uint32_t E1a = st[kSE1] + dx * st[kSA1] + dy * sb1, E1b = E1a + (sb1 << 2);
+            const uint32_t E2a = st[kSE2] + dx * st[kSA2] + dy * sb2, E2b = E2a + (sb2 << 2);
+            bool ca, cb;
+            if (top_left) {
+                ca = (int32_t)((E0a - (nb & 1u)) | (E1a - ((nb >> 1) & 1u)) | (E2a - ((nb >> 2) & 1u))) >= 0;
+                cb = (int32_t)((E0b - (nb & 1u)) | (E1b - ((nb >> 1) & 1u)) | (E2b - ((nb >> 2) & 1u))) >= 0;
+            } else {
+                ca = (int32_t)(E0a | E1a | E2a) > 0;   // main.c:1028
+                cb = (int32_t)(E0b | E1b | E2b) > 0;
+            }
+            ca = ca && in_a;
+            cb = cb && in_b;
+            if (capture) {
+                const uint32_t ma = __ballot_sync(0xFFFFFFFFu, ca), mb = __ballot_sync(0xFFFFFFFFu, cb);
+                if (lane == 0) mask[j] = (unsigned long long)ma | ((unsigned long long)mb << 32);
+            }
+            const float inv_area = __uint_as_float(st[kSInvArea]);
+            const float z0 = __uint_as_float(st[kSZ0]), dz1 = __uint_as_float(st[kSDz1]), dz2 = __uint_as_float(st[kSDz2]);
+            const unsigned long long key = st[kSKey];
+            if (ca) {
+                const float bb1 = (float)((int32_t)E1a >> (kSubpix * 2)) * inv_area;
+                const float bb2 = (float)((int32_t)E2a >> (kSubpix * 2)) * inv_area;
+                float z = z0 + dz1 * bb1;
+                z = z + dz2 * bb2;
+                if (less ? (z < da) : (z >= da)) fa = better_key(less, fa, ((unsigned long long)depth_key(z) << 32) | key);
+            }
+            if (cb) {
+                const float bb1 = (float)((int32_t)E1b >> (kSubpix * 2)) * inv_area;
+                const float bb2 = (float)((int32_t)E2b >> (kSubpix * 2)) * inv_area;
+                float z = z0 + dz1 * bb1;
+                z = z + dz2 * bb2;
+                if (less ? (z < db) : (z >= db)) fb = better_key(less, fb, ((unsigned long long)depth_key(z) << 32) | key);
+            }
+        } while (big);
     }
     __syncwarp();
     if (capture && i < e) bp.info_mask[i] = cnt ? mask[lane] : 0ull;
@@ -1148,11 +1232,13 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
         s_best[warp][lane] = sentinel;
         s_best[warp][lane + 32] = sentinel;
         const float hiz = less ? hiz_max : hiz_min;
+        unsigned long long fa = sentinel, fb = sentinel;
         for (uint32_t chunk = s; chunk < e; chunk += 32)
             tile_chunk(bp, chunk, e, x0, y0, less, top_left, hiz, s_stage[warp], s_pref[warp], s_mask[warp],
-                       s_best[warp], s_depth[warp], capture, lane);
+                       s_best[warp], s_depth[warp], capture, lane, fa, fb);
         // fold this draw's winners into the running state; hierarchical Z update (write_tile, main.c:589-603)
-        const unsigned long long k0 = s_best[warp][lane], k1 = s_best[warp][lane + 32];
+        const unsigned long long k0 = better_key(less, s_best[warp][lane], fa);
+        const unsigned long long k1 = better_key(less, s_best[warp][lane + 32], fb);
         if (k0 != sentinel) { dcur0 = depth_from_key((uint32_t)(k0 >> 32)); win0 = (uint32_t)k0; }
         if (k1 != sentinel) { dcur1 = depth_from_key((uint32_t)(k1 >> 32)); win1 = (uint32_t)k1; }
         s_depth[warp][lane] = dcur0;
@@ -1269,9 +1355,13 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_tile_coop(BatchParam
         const float hiz = less ? hiz_max : hiz_min;
         const uint32_t n = e - s, per = (n + WARPS - 1) / WARPS;
         const uint32_t ws = s + min(n, per * (uint32_t)warp), we = s + min(n, per * (uint32_t)(warp + 1));
+        unsigned long long fa = sentinel, fb = sentinel;
         for (uint32_t chunk = ws; chunk < we; chunk += 32)
             tile_chunk(bp, chunk, we, x0, y0, less, top_left, hiz, s_stage[warp], s_pref[warp], s_mask[warp],
-                       s_best, s_depth, capture, lane);
+                       s_best, s_depth, capture, lane, fa, fb);
+        // the warp's whole-tile results: lane holds pixels lane and lane + 32
+        if (fa != sentinel) { if (less) atomicMin(&s_best[lane], fa); else atomicMax(&s_best[lane], fa); }
+        if (fb != sentinel) { if (less) atomicMin(&s_best[lane + 32], fb); else atomicMax(&s_best[lane + 32], fb); }
         __syncthreads();   // every warp's fragments are in
         if (owner) {
             const unsigned long long k = s_best[pix];

@@ -46,17 +46,15 @@ __device__ __forceinline__ int32_t cvt_rn(float x) {
     return __float2int_rn(x);
 }
 
-// main.c:843-848: floor(x_ss * 16 + 0.5) with the add in double. For |v| < 2^23 the float
-// floor(v) and the comparison against floor(v) + 0.5 are exact, so no double arithmetic is needed.
+// main.c:843-848: floor(x_ss * 16 + 0.5) with the add in double. For |v| < 2^23 the float sum
+// v + 0.5 is exact (the unit in the last place of v is at most 0.5), so it is floored in float.
 __device__ __forceinline__ int32_t snap28_4(float x_ss) {
     float v = x_ss * 16.0f;
     if (!(fabsf(v) < 8388608.0f)) {
         if (!(v >= -2147483648.0f && v < 2147483648.0f)) return (int32_t)0x80000000u;
         return (int32_t)v;
     }
-    float f = floorf(v);
-    int32_t i = (int32_t)f;
-    return (v >= f + 0.5f) ? i + 1 : i;
+    return __float2int_rd(v + 0.5f);
 }
 
 // encode_color_as_u32 (math.h:322-324): R in the low byte, truncating conversions
