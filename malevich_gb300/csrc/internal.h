@@ -11,6 +11,7 @@ constexpr int kPsNone = 5;               // MLV_PS_NONE: depth and visibility on
 constexpr uint32_t kBinsClipped = 0xFFFFFFFFu;
 constexpr int kRasterTopLeft = 1;        // MLV_FILL_TOP_LEFT
 constexpr int kRasterCenter = 2;         // MLV_SAMPLE_PIXEL_CENTER
+constexpr uint32_t kBinGhost = 0x80000000u;  // bin count bit: binned triangles without samples only
 constexpr int kMaxClipVertices = 16;     // main.c:38
 constexpr int kMaxViewsPerBatch = 4096;
 

@@ -491,6 +491,8 @@ __global__ void __launch_bounds__(BLOCK, MLV_GEOMETRY_THREADS_PER_SM / BLOCK) k_
     uint32_t mask = 0;
     BinJob own;                 // the bins of an unclipped triangle, counted warp-wide below
     bool have_own = false;
+    uint32_t ghost_entries = 0; // bins of a triangle that covers no sample (statistics only)
+    uint32_t ghost_bin = 0xFFFFFFFFu;   // its bin when it has one, marked warp-wide below
     if (g < bp.total_tris) {
         const uint32_t draw = find_draw(bp, g);
         const DrawDesc &d = bp.draws[draw];
@@ -520,11 +522,29 @@ __global__ void __launch_bounds__(BLOCK, MLV_GEOMETRY_THREADS_PER_SM / BLOCK) k_
             if (!clipped) {
                 Setup su;
                 if (setup_triangle(d, v[0], v[1], v[2], su)) {
-#pragma unroll
-                    for (int k = 0; k < 3; ++k) triangle_attributes(bp, slot[k], v[k].v);
-                    write_record(bp, g, draw, d.ps, su, v[0], v[1], v[2]);
+                    // A triangle whose sample box is empty covers no sample: the reference bins it
+                    // (its statistics count it) but it can write nothing, so it gets no record and
+                    // no list entries, only its bins' activity (see the counting below). Kept
+                    // whole when TileInfo masks are captured (the reference's list them, empty).
+                    const bool ghost = bp.info_mask == nullptr && (su.tminx > su.tmaxx || su.tminy > su.tmaxy);
                     mask = 1;
-                    have_own = bin_job(vw, d.draw_in_view, su.minx, su.miny, su.maxx, su.maxy, g << 3, own);
+                    if (!ghost) {
+#pragma unroll
+                        for (int k = 0; k < 3; ++k) triangle_attributes(bp, slot[k], v[k].v);
+                        write_record(bp, g, draw, d.ps, su, v[0], v[1], v[2]);
+                        have_own = bin_job(vw, d.draw_in_view, su.minx, su.miny, su.maxx, su.maxy, g << 3, own);
+                    } else {
+                        // its bins are only marked active (bit 31 of the count, which k_scan counts
+                        // as activity and clears); the entry statistic is added below
+                        BinJob job;
+                        if (bin_job(vw, d.draw_in_view, su.minx, su.miny, su.maxx, su.maxy, 0u, job)) {
+                            ghost_entries = job.nx * job.ny;
+                            if (ghost_entries == 1) ghost_bin = job.first_bin;
+                            else
+                                for (uint32_t t = 0; t < ghost_entries; ++t)
+                                    atomicOr(bp.bin_count + job_bin(job, t), kBinGhost);
+                        }
+                    }
                 }
             } else {
 #pragma unroll
@@ -574,6 +594,16 @@ __global__ void __launch_bounds__(BLOCK, MLV_GEOMETRY_THREADS_PER_SM / BLOCK) k_
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xFFFFFFFFu, n, o);
     if (lane == 0 && n) atomicAdd(bp.stats + kStatAssembled, (unsigned long long)n);
+    // triangles without samples: their bins for the entry statistic (main.c:937-944), and the
+    // one-tile ones' activity marks, one per distinct bin per warp
+    if (__any_sync(0xFFFFFFFFu, ghost_entries != 0)) {
+        uint32_t ge = ghost_entries;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) ge += __shfl_xor_sync(0xFFFFFFFFu, ge, o);
+        if (lane == 0) atomicAdd(bp.stats + kStatBinEntries, (unsigned long long)ge);
+        const uint32_t gpeers = __match_any_sync(0xFFFFFFFFu, ghost_bin);
+        if (ghost_bin != 0xFFFFFFFFu && lane == __ffs(gpeers) - 1) atomicOr(bp.bin_count + ghost_bin, kBinGhost);
+    }
     // neighbouring triangles of a mesh mostly share their tile: one update per distinct bin
     const uint32_t nt_own = have_own ? own.nx * own.ny : 0u;
     const uint32_t single_bin = nt_own == 1 ? own.first_bin : 0xFFFFFFFFu;
@@ -687,10 +717,14 @@ __global__ void __launch_bounds__(kScanBlock) k_scan(BatchParams bp) {
 #pragma unroll
         for (int i = 0; i < kScanItems; ++i) vals[i] = base + i < n ? bp.bin_count[base + i] : 0u;
     }
+    // bit 31: only triangles without samples (k_geometry) were binned here; active, no entries
+    uint32_t ghosts = 0;
 #pragma unroll
     for (int i = 0; i < kScanItems; ++i) {
-        sum += vals[i];
         active += vals[i] ? 1u : 0u;
+        ghosts |= (vals[i] >> 31) << i;
+        vals[i] &= ~kBinGhost;
+        sum += vals[i];
     }
     uint32_t total;
     uint32_t excl = block_exclusive_scan<kScanBlock>(sum, s_warp, total);
@@ -705,6 +739,11 @@ __global__ void __launch_bounds__(kScanBlock) k_scan(BatchParams bp) {
     for (int i = 0; i < kScanItems; ++i) {
         outv[i] = run;
         run += vals[i];
+    }
+    if (ghosts) {   // the count is k_scatter's cursor and must end at 0: clear the mark
+#pragma unroll
+        for (int i = 0; i < kScanItems; ++i)
+            if (ghosts >> i & 1u) bp.bin_count[base + i] = vals[i];
     }
     if (base + kScanItems <= n) {
 #pragma unroll
