@@ -677,10 +677,18 @@ def main():
         pinned.append(t)
         return t.numpy()
 
-    for key, (buf, arr) in r._buffers.items():
-        if key[1] in (api.BIND_VERTEX_BUFFER, api.BIND_INDEX_BUFFER):
-            host_bufs.append((buf, pin(arr)))
+    # in the order the frame consumes them: the vertex stage reads vertex buffers and its texture,
+    # geometry the index buffers, the tile kernel the pixel shader's texture; each stage waits only
+    # for its own inputs' copies, so the later copies overlap the earlier stages
+    vs_tex_ids = {id(d.vs_tex.data) for d in frame.draws if d.vs_tex is not None}
+    for want in (api.BIND_VERTEX_BUFFER, api.BIND_INDEX_BUFFER):
+        for key, (buf, arr) in r._buffers.items():
+            if key[1] == want:
+                host_bufs.append((buf, pin(arr)))
     host_tex = [(tex, pin(t.data)) for tex, t in r._textures.values()]
+    host_vs_tex = [x for x, (_, t) in zip(host_tex, r._textures.values()) if id(t.data) in vs_tex_ids]
+    host_ps_tex = [x for x, (_, t) in zip(host_tex, r._textures.values()) if id(t.data) not in vs_tex_ids]
+    n_vb = sum(1 for key in r._buffers if key[1] == api.BIND_VERTEX_BUFFER)
     h2d = sum(a.nbytes for _, a in host_bufs) + sum(a.nbytes for _, a in host_tex)
     rt = r.targets[0][0]
     out_img = torch.empty((frame.height, frame.width), dtype=torch.int32).pin_memory().numpy().view(np.uint32)
@@ -688,12 +696,22 @@ def main():
     lib = api.load_library()
     import ctypes
 
+    def upload_buf(buf, a):
+        ctx.lib.mlv_update_buffer_async(ctx.handle, buf.handle, 0, a.ctypes.data_as(ctypes.c_void_p), a.nbytes)
+
+    def upload_tex(tex, a):
+        ctx.lib.mlv_update_texture2d_async(ctx.handle, tex.handle, a.ctypes.data_as(ctypes.c_void_p), 0)
+
     def e2e_step():
         # queued uploads from pinned memory (unchanged until the readback below synchronises)
-        for buf, a in host_bufs:
-            ctx.lib.mlv_update_buffer_async(ctx.handle, buf.handle, 0, a.ctypes.data_as(ctypes.c_void_p), a.nbytes)
-        for tex, a in host_tex:
-            ctx.lib.mlv_update_texture2d_async(ctx.handle, tex.handle, a.ctypes.data_as(ctypes.c_void_p), 0)
+        for buf, a in host_bufs[:n_vb]:
+            upload_buf(buf, a)
+        for tex, a in host_vs_tex:
+            upload_tex(tex, a)
+        for buf, a in host_bufs[n_vb:]:
+            upload_buf(buf, a)
+        for tex, a in host_ps_tex:
+            upload_tex(tex, a)
         r.render_batched()
         ctx.lib.mlv_read_texture2d(ctx.handle, rt.handle, out_img.ctypes.data_as(ctypes.c_void_p), 0)
 

@@ -222,11 +222,14 @@ MLV_API mlv_status mlv_update_buffer(mlv_context context, mlv_buffer buffer, uin
                                      uint64_t size);
 MLV_API mlv_status mlv_update_texture2d(mlv_context context, mlv_texture2d texture, const void *data,
                                         uint32_t row_pitch);
-/* New: the same copies queued on the context's stream without waiting (Direct3D 11 has no
- * counterpart; compare a dynamic resource's Map with NO_OVERWRITE). `data` must stay valid and
- * unchanged until the context next synchronises (mlv_finish, a readback, mlv_get_stats): with
- * pinned host memory the copy runs in the background. Queued work that was issued earlier still
- * reads the old contents. */
+/* New: the same copies queued without waiting (Direct3D 11 has no counterpart; compare a dynamic
+ * resource's Map with NO_OVERWRITE). `data` must stay valid and unchanged until the context next
+ * synchronises (mlv_finish, a readback, mlv_get_stats): with pinned host memory the copy runs in
+ * the background. Queued work that was issued earlier (on the context's stream, by the library
+ * or by the caller) still reads the old contents. The copy runs on the context's copy stream, and
+ * later batches wait for it only at the stage that first reads the resource (vertex buffers and
+ * VS textures at the vertex stage, index buffers at geometry, PS textures at the tile kernel), so
+ * the later copies of a frame overlap its earlier stages. */
 MLV_API mlv_status mlv_update_buffer_async(mlv_context context, mlv_buffer buffer, uint64_t offset,
                                            const void *data, uint64_t size);
 MLV_API mlv_status mlv_update_texture2d_async(mlv_context context, mlv_texture2d texture, const void *data,

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -77,6 +78,9 @@ struct mlv_device_t {
     float clip_planes[6][4];
     mlv_context_t *immediate = nullptr;
     std::mutex mu;
+    // bumped when a resource gets its upload event (first queued upload): captured command lists
+    // re-capture, so that their graphs wait for it
+    std::atomic<uint64_t> upload_generation{0};
 };
 
 struct mlv_buffer_t {
@@ -85,6 +89,7 @@ struct mlv_buffer_t {
     uint64_t size = 0;
     uint32_t bind = 0;
     std::vector<uint8_t> shadow;   // host copy of constant buffers (snapshotted at draw time)
+    cudaEvent_t ready = nullptr;   // recorded after its last queued upload (copy stream)
 };
 
 struct mlv_texture2d_t {
@@ -98,6 +103,7 @@ struct mlv_texture2d_t {
     uint32_t tiles_x = 0, tiles_y = 0;
     uint32_t draws_since_clear = 0;                    // render targets: numbers draws for visibility
     bool owns_memory = true;                           // false: placed on caller memory
+    cudaEvent_t ready = nullptr;                       // recorded after its last queued upload
 };
 
 static uint32_t texel_bytes(mlv_format f) {
@@ -135,6 +141,9 @@ struct DrawCmd {
     DrawDesc desc;                 // view / draw_in_view / tri_begin filled by the planner
     mlv_texture2d rtv, dsv, vis_tri, vis_draw, vis_bary, vis_prim;
     uint32_t index_count;
+    // the inputs, for the waits on their queued uploads (see Plan)
+    mlv_buffer vb_res = nullptr, ib_res = nullptr;
+    mlv_texture2d vs_res = nullptr, ps_res = nullptr;
 };
 
 struct ClearCmd {
@@ -187,7 +196,7 @@ struct mlv_command_list_t {
     std::vector<Segment> segments;
     // graph replay state
     cudaGraphExec_t exec = nullptr;
-    uint64_t exec_generation = ~0ull, exec_tuning = ~0ull;
+    uint64_t exec_generation = ~0ull, exec_tuning = ~0ull, exec_uploads = ~0ull;
     mlv_context_t *exec_context = nullptr;
     int executions = 0;
     DrawDesc *d_draws = nullptr;   // per-segment descriptor copies owned by the list
@@ -226,6 +235,11 @@ struct mlv_context_t {
     uint32_t batch_seq = 0;
     std::vector<PendingJob> pending;
     uint32_t *h_error = nullptr;       // pinned mirror of the device error words + counters
+    // queued uploads run on their own stream, so that a batch's kernels wait only for the inputs
+    // they read, when they read them (vertex buffers and VS textures before the vertex stage,
+    // index buffers before geometry, PS textures before the tile kernel)
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t work_mark = nullptr;   // the context stream's work so far, which uploads follow
     // last single-draw segment, for mlv_get_tile_infos
     bool last_single = false;
     uint32_t last_total_bins = 0, last_tiles_x = 0, last_draw_count = 0;
@@ -417,7 +431,13 @@ struct Plan {
     std::vector<ViewDesc> views;
     BatchSizes sizes;
     std::unordered_set<mlv_texture2d> folded;   // cleared targets the tile kernel clears itself
+    // upload events of the batch's inputs, waited for before the stage that first reads them
+    std::vector<cudaEvent_t> wait_vertex, wait_index, wait_pixel;
 };
+
+static void add_wait(std::vector<cudaEvent_t> &v, cudaEvent_t e) {
+    if (e && std::find(v.begin(), v.end(), e) == v.end()) v.push_back(e);
+}
 
 // Folds the segment's clears of targets that one view of the plan binds (and that the clear's kind
 // fits: colour, depth, u32 fill of a visibility target) into that view. Clears precede every draw
@@ -461,7 +481,16 @@ static mlv_status plan_segment(const Segment &seg, Plan &p, uint32_t fan_slots_h
     p.draws.clear();
     p.views.clear();
     p.folded.clear();
+    p.wait_vertex.clear();
+    p.wait_index.clear();
+    p.wait_pixel.clear();
     p.sizes = BatchSizes();
+    for (const DrawCmd &dc : seg.draws) {
+        if (dc.vb_res) add_wait(p.wait_vertex, dc.vb_res->ready);
+        if (dc.vs_res) add_wait(p.wait_vertex, dc.vs_res->ready);
+        if (dc.ib_res) add_wait(p.wait_index, dc.ib_res->ready);
+        if (dc.ps_res) add_wait(p.wait_pixel, dc.ps_res->ready);
+    }
     // group draws by (render target, depth) keeping their order inside a view
     std::vector<std::pair<std::pair<mlv_texture2d, mlv_texture2d>, std::vector<size_t>>> groups;
     for (size_t i = 0; i < seg.draws.size(); ++i) {
@@ -661,16 +690,26 @@ static mlv_status launch_draws(mlv_context_t *c, const Plan &p, DrawDesc *d_draw
     bp.error = w.error;
     c->host_stats[3] += 1;
     if (bp.total_tris == 0) return MLV_OK;   // nothing to assemble: no kernel has work
+    // waits on queued uploads (inside a graph capture: external event waits, evaluated at launch)
+    auto wait_for = [&](const std::vector<cudaEvent_t> &evs) -> cudaError_t {
+        for (cudaEvent_t ev : evs) {
+            cudaError_t r = cudaStreamWaitEvent(c->stream, ev, c->capturing_graph ? cudaEventWaitExternal : 0);
+            if (r != cudaSuccess) return r;
+        }
+        return cudaSuccess;
+    };
     cudaEvent_t e;
     // the clip-fan slot counter starts at zero for every batch (reset before the first kernel, so
     // that the batch's kernels follow one another directly)
     CUDA_TRY(cudaMemsetAsync(w.counters + kCtrOverflow, 0, 2 * sizeof(uint32_t), c->stream));
+    CUDA_TRY(wait_for(p.wait_vertex));
     if (bp.total_vertices) {
         ev_begin(c, 5, &e);
         CUDA_TRY(launch_vertex(bp, c->stream));
         ev_end(c, e);
         c->host_stats[4] += 1;
     }
+    CUDA_TRY(wait_for(p.wait_index));
     ev_begin(c, 1, &e);
     CUDA_TRY(launch_geometry(bp, c->tuning.geometry_block, c->stream));
     ev_end(c, e);
@@ -684,6 +723,7 @@ static mlv_status launch_draws(mlv_context_t *c, const Plan &p, DrawDesc *d_draw
     ev_begin(c, 3, &e);
     CUDA_TRY(launch_scatter(bp, c->device->num_sms, c->stream));
     ev_end(c, e);
+    CUDA_TRY(wait_for(p.wait_pixel));
     ev_begin(c, 4, &e);
     CUDA_TRY(launch_tile(bp, c->tuning.tile_warps_per_block, c->tuning.warps_per_tile, c->stream));
     ev_end(c, e);
@@ -795,6 +835,7 @@ static mlv_status check_and_recover(mlv_context_t *c) {
 }
 
 static mlv_status sync_context(mlv_context_t *c) {
+    if (c->copy_stream) CUDA_TRY(cudaStreamSynchronize(c->copy_stream));
     CUDA_TRY(cudaStreamSynchronize(c->stream));
     collect_events(c);
     return check_and_recover(c);
@@ -877,6 +918,11 @@ static void destroy_context_internal(mlv_context_t *c) {
         cudaEventDestroy(pr.second);
     }
     if (c->h_error) cudaFreeHost(c->h_error);
+    if (c->copy_stream) {
+        cudaStreamSynchronize(c->copy_stream);
+        cudaStreamDestroy(c->copy_stream);
+    }
+    if (c->work_mark) cudaEventDestroy(c->work_mark);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -940,8 +986,12 @@ MLV_API mlv_status mlv_create_buffer(mlv_device d, const mlv_buffer_desc *desc, 
 MLV_API mlv_status mlv_destroy_buffer(mlv_buffer b) {
     if (!b) return fail(MLV_ERROR_INVALID_ARG, "buffer is NULL");
     cudaSetDevice(b->device->ordinal);
-    if (b->device->immediate) cudaStreamSynchronize(b->device->immediate->stream);
+    if (b->device->immediate) {
+        if (b->device->immediate->copy_stream) cudaStreamSynchronize(b->device->immediate->copy_stream);
+        cudaStreamSynchronize(b->device->immediate->stream);
+    }
     cudaFree(b->ptr);
+    if (b->ready) cudaEventDestroy(b->ready);
     delete b;
     return MLV_OK;
 }
@@ -1025,10 +1075,14 @@ MLV_API mlv_status mlv_create_texture2d_on_memory(mlv_device d, const mlv_textur
 MLV_API mlv_status mlv_destroy_texture2d(mlv_texture2d t) {
     if (!t) return fail(MLV_ERROR_INVALID_ARG, "texture is NULL");
     cudaSetDevice(t->device->ordinal);
-    if (t->device->immediate) cudaStreamSynchronize(t->device->immediate->stream);
+    if (t->device->immediate) {
+        if (t->device->immediate->copy_stream) cudaStreamSynchronize(t->device->immediate->copy_stream);
+        cudaStreamSynchronize(t->device->immediate->stream);
+    }
     if (t->owns_memory) cudaFree(t->ptr);
     cudaFree(t->tile_min);
     cudaFree(t->tile_max);
+    if (t->ready) cudaEventDestroy(t->ready);
     delete t;
     return MLV_OK;
 }
@@ -1074,7 +1128,22 @@ MLV_API mlv_status mlv_update_texture2d(mlv_context c, mlv_texture2d t, const vo
 
 // Queued uploads. A batch still unchecked may be re-run at the next synchronisation (when it
 // overflowed its workspace), and a re-run must read the contents it was issued with, so the
-// context first synchronises if anything is pending; otherwise the copy is only queued.
+// context first synchronises if anything is pending; otherwise the copy is only queued, on the
+// context's copy stream behind everything already issued on its stream, and the resource's event
+// marks its completion for the batches that read it (Plan::wait_*).
+static mlv_status begin_upload(mlv_context_t *c, cudaEvent_t *ready) {
+    if (!c->copy_stream) {
+        CUDA_TRY(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+        CUDA_TRY(cudaEventCreateWithFlags(&c->work_mark, cudaEventDisableTiming));
+    }
+    if (!*ready) {
+        CUDA_TRY(cudaEventCreateWithFlags(ready, cudaEventDisableTiming));
+        c->device->upload_generation.fetch_add(1);
+    }
+    CUDA_TRY(cudaEventRecord(c->work_mark, c->stream));
+    CUDA_TRY(cudaStreamWaitEvent(c->copy_stream, c->work_mark, 0));
+    return MLV_OK;
+}
 MLV_API mlv_status mlv_update_buffer_async(mlv_context c, mlv_buffer b, uint64_t offset, const void *data,
                                            uint64_t size) {
     MLV_TRY(need_immediate(c));
@@ -1082,7 +1151,9 @@ MLV_API mlv_status mlv_update_buffer_async(mlv_context c, mlv_buffer b, uint64_t
     if (offset + size > b->size) return fail(MLV_ERROR_INVALID_ARG, "update outside the buffer");
     MLV_TRY(set_device(c->device));
     if (!c->pending.empty()) MLV_TRY(sync_context(c));
-    CUDA_TRY(cudaMemcpyAsync(b->ptr + offset, data, size, cudaMemcpyHostToDevice, c->stream));
+    MLV_TRY(begin_upload(c, &b->ready));
+    CUDA_TRY(cudaMemcpyAsync(b->ptr + offset, data, size, cudaMemcpyHostToDevice, c->copy_stream));
+    CUDA_TRY(cudaEventRecord(b->ready, c->copy_stream));
     if (!b->shadow.empty()) memcpy(b->shadow.data() + offset, data, size);
     return MLV_OK;
 }
@@ -1092,9 +1163,11 @@ MLV_API mlv_status mlv_update_texture2d_async(mlv_context c, mlv_texture2d t, co
     if (!t || !data) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
     MLV_TRY(set_device(c->device));
     if (!c->pending.empty()) MLV_TRY(sync_context(c));
+    MLV_TRY(begin_upload(c, &t->ready));
     size_t row = (size_t)t->width * t->texel_bytes;
     CUDA_TRY(cudaMemcpy2DAsync(t->ptr, row, data, row_pitch ? row_pitch : row, row, t->height, cudaMemcpyHostToDevice,
-                               c->stream));
+                               c->copy_stream));
+    CUDA_TRY(cudaEventRecord(t->ready, c->copy_stream));
     return MLV_OK;
 }
 
@@ -1371,6 +1444,10 @@ static mlv_status build_draw(mlv_context c, uint32_t count, uint32_t start, int3
     out.vis_bary = s.vis_bary;
     out.vis_prim = s.vis_prim;
     out.index_count = count;
+    out.vb_res = s.vb;
+    out.ib_res = indexed ? s.ib : nullptr;
+    out.vs_res = vt;
+    out.ps_res = pt;
     return MLV_OK;
 }
 
@@ -1553,8 +1630,9 @@ MLV_API mlv_status mlv_execute_command_list(mlv_context c, mlv_command_list l) {
         if (l->executions == 1) MLV_TRY(sync_context(c));
         return MLV_OK;
     }
+    const uint64_t uploads = c->device->upload_generation.load();
     if (!l->exec || l->exec_generation != c->ws.generation || l->exec_context != c ||
-        l->exec_tuning != c->tuning_generation) {
+        l->exec_tuning != c->tuning_generation || l->exec_uploads != uploads) {
         if (l->exec) cudaGraphExecDestroy(l->exec);
         l->exec = nullptr;
         cudaGraph_t g = nullptr;
@@ -1577,6 +1655,7 @@ MLV_API mlv_status mlv_execute_command_list(mlv_context c, mlv_command_list l) {
         if (e != cudaSuccess) return fail(MLV_ERROR_DEVICE, std::string("graph instantiate: ") + cudaGetErrorString(e));
         l->exec_generation = c->ws.generation;
         l->exec_tuning = c->tuning_generation;
+        l->exec_uploads = uploads;
         l->exec_context = c;
     }
     CUDA_TRY(cudaGraphLaunch(l->exec, c->stream));
