@@ -377,12 +377,14 @@ def run_diff_sections(dev, args):
     # --- configuration 5: batched + differentiable optimisation loop. Everything runs on the
     # immediate context's stream: the visibility command list (one graph launch for all views,
     # null pixel shader, primitive ids written straight into one [views][H][W] array), the
-    # forward, the loss gradient, the adjoint and Adam.
+    # forward, the loss gradient, the adjoint and Adam. A device object of its own, so that its
+    # workspace (and the HBM footprint reported) is the loop's alone.
     torch.cuda.synchronize()
     free0, total = torch.cuda.mem_get_info()
+    dev5 = api.Device(dev.ordinal)
     sc = scenes.diff_scene(seed=5, n_views=256, size=256, tex_size=2048, heightfield_cells=316)
     rng = np.random.default_rng(55)
-    ctx = dev.immediate
+    ctx = dev5.immediate
     cstream = torch.cuda.ExternalStream(ctx.stream())
     csp = ctypes.c_void_p(ctx.stream())
     with torch.cuda.stream(cstream):
@@ -391,7 +393,7 @@ def run_diff_sections(dev, args):
         V, S = sc["pos"].shape[0], sc["width"]
         prim = torch.empty((V, S, S), dtype=torch.int32, device="cuda")
         frames = scenes.diff_frames(sc, shade=False)
-        vr = api.FrameRenderer(dev, frames, primitive_id_memory=[prim[i].data_ptr() for i in range(V)])
+        vr = api.FrameRenderer(dev5, frames, primitive_id_memory=[prim[i].data_ptr() for i in range(V)])
         vr.render_batched()                  # sizes the workspace, captures the graph
         ds = DiffScene(sc, prim)
         pos = torch.from_numpy(sc["pos"]).cuda()
@@ -471,6 +473,7 @@ def run_diff_sections(dev, args):
                       "step": "visibility (batched command list, one CUDA graph launch, null pixel shader) + "
                               "mlv_diff_forward + loss gradient + mlv_diff_backward + torch Adam"}
     vr.destroy()
+    dev5.destroy()
     return out
 
 

@@ -396,6 +396,7 @@ class Device:
         h = ctypes.c_void_p()
         _check(lib.mlv_create_device(ordinal, ctypes.byref(h)))
         self.handle = h
+        self.ordinal = ordinal
         c = ctypes.c_void_p()
         _check(lib.mlv_get_immediate_context(h, ctypes.byref(c)))
         self.immediate = Context(c, self)

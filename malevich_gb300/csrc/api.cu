@@ -325,6 +325,7 @@ static mlv_status ensure_fixed(mlv_context_t *c) {
 
 struct BatchSizes {
     uint64_t tris = 0, overflow = 0, bins = 0, tiles = 0, draws = 0, views = 0, vertices = 0;
+    bool shade = false;   // some draw has a pixel shader: the 80-byte shading records are needed
 };
 
 static mlv_status reset_scan_state(Workspace &w) {
@@ -340,14 +341,18 @@ static mlv_status ensure_workspace(mlv_context_t *c, const BatchSizes &s, bool k
     MLV_TRY(ensure_fixed(c));
     bool changed = false;
     const uint64_t slots = s.tris + std::max<uint64_t>(s.overflow, w.overflow_cap);
-    if (slots > w.record_cap || !w.raster || (keep_geom && !w.geom)) {
+    // shading records only once a batch has a pixel shader (a depth or visibility pass with the
+    // null pixel shader needs none: 80 of its 144 bytes per triangle slot)
+    const bool shade = s.shade || w.shade != nullptr;
+    if (slots > w.record_cap || !w.raster || (keep_geom && !w.geom) || (shade && !w.shade)) {
         uint64_t n = std::max<uint64_t>(slots, (uint64_t)w.record_cap + w.record_cap / 2);
+        if (slots <= w.record_cap && w.raster) n = w.record_cap;   // only the shading records are new
         n = std::max<uint64_t>(n, 4096);
         if (n > 0x7FFFFFFFull) return fail(MLV_ERROR_CAPACITY_EXCEEDED, "more than 2^31 triangle slots");
         cudaFree(w.raster); cudaFree(w.shade); cudaFree(w.geom);
         w.raster = nullptr; w.shade = nullptr; w.geom = nullptr;
         MLV_TRY(dev_alloc((void **)&w.raster, n * sizeof(TriRaster)));
-        MLV_TRY(dev_alloc((void **)&w.shade, n * sizeof(TriShade)));
+        if (shade) MLV_TRY(dev_alloc((void **)&w.shade, n * sizeof(TriShade)));
         w.keep_geom = keep_geom || w.keep_geom;
         if (w.keep_geom) MLV_TRY(dev_alloc((void **)&w.geom, n * sizeof(TriGeom)));
         w.record_cap = (uint32_t)n;
@@ -528,6 +533,7 @@ static mlv_status plan_segment(const Segment &seg, Plan &p, uint32_t fan_slots_h
             DrawDesc d = dc.desc;
             d.view = (uint32_t)g;
             d.draw_in_view = (uint32_t)k;
+            if (groups[g].second.size() > 1) d.raster_flags |= kDrawSharesView;
             d.tri_begin = tri;
             tri += d.tri_count;
             // shade each vertex once when the draw references most of its buffer; a draw that
@@ -556,6 +562,9 @@ static mlv_status plan_segment(const Segment &seg, Plan &p, uint32_t fan_slots_h
     p.sizes.tiles = tiles;
     p.sizes.draws = p.draws.size();
     p.sizes.views = p.views.size();
+    // shading records: for pixel shaders, and for the draw index of a view with several draws
+    for (const DrawDesc &d : p.draws)
+        p.sizes.shade = p.sizes.shade || d.ps != kPsNone || (d.raster_flags & kDrawSharesView);
     return MLV_OK;
 }
 
@@ -1548,6 +1557,7 @@ static mlv_status run_list(mlv_context_t *c, mlv_command_list l, uint32_t seq, b
         maxs.draws = std::max(maxs.draws, s.draws);
         maxs.views = std::max(maxs.views, s.views);
         maxs.vertices = std::max(maxs.vertices, s.vertices);
+        maxs.shade = maxs.shade || s.shade;
         nd += plans[i].draws.size();
         nv += plans[i].views.size();
     }

@@ -11,6 +11,7 @@ constexpr int kPsNone = 5;               // MLV_PS_NONE: depth and visibility on
 constexpr uint32_t kBinsClipped = 0xFFFFFFFFu;
 constexpr int kRasterTopLeft = 1;        // MLV_FILL_TOP_LEFT
 constexpr int kRasterCenter = 2;         // MLV_SAMPLE_PIXEL_CENTER
+constexpr int kDrawSharesView = 4;       // (DrawDesc::raster_flags) the view has other draws too
 constexpr uint32_t kBinGhost = 0x80000000u;  // bin count bit: binned triangles without samples only
 constexpr int kMaxClipVertices = 16;     // main.c:38
 constexpr int kMaxViewsPerBatch = 4096;
@@ -41,7 +42,7 @@ struct DrawDesc {
     uint32_t tri_begin;                  // first input triangle of this draw in the batch
     uint32_t tri_count;
     int32_t vs, ps, cull, depth_less;    // cull: 0 none, 1 back (reference), 2 front
-    int32_t raster_flags;                // kRasterTopLeft | kRasterCenter (0: the reference)
+    int32_t raster_flags;                // kRasterTopLeft | kRasterCenter (0: the reference) | kDrawSharesView
     uint32_t view;                       // view (render target + depth) index in the batch
     uint32_t draw_in_view;               // position among the view's draws in this batch
     uint32_t draw_seq;                   // draw number since the render target's last clear

@@ -253,8 +253,8 @@ __device__ __forceinline__ bool setup_triangle(const DrawDesc &d, const Vtx &v0,
 }
 
 __device__ __forceinline__ void write_record(const BatchParams &bp, uint32_t rec, uint32_t draw, int ps,
-                                             const Setup &s, const Vtx &v0, const Vtx &v1, const Vtx &v2,
-                                             uint32_t extra = 0) {
+                                             bool sole_draw, const Setup &s, const Vtx &v0, const Vtx &v1,
+                                             const Vtx &v2, uint32_t extra = 0) {
     int4 *r = bp.raster[rec].w;
     r[0] = make_int4(s.e[0], s.e[1], s.e[2], s.e[3]);
     r[1] = make_int4(s.e[4], s.e[5], s.e[6], s.e[7]);
@@ -268,9 +268,11 @@ __device__ __forceinline__ void write_record(const BatchParams &bp, uint32_t rec
             g.x[k] = s.ss[k][0]; g.y[k] = s.ss[k][1]; g.z[k] = s.ss[k][2]; g.w[k] = s.ss[k][3];
         }
     }
+    // A null pixel shader reads no 1/w and no attributes; the tile kernel still takes the draw
+    // index from the record when the view has several draws (sole_draw: it has one)
+    if (ps == kPsNone && sole_draw) return;
     float4 *h = bp.shade[rec].s;
     h[0] = make_float4(s.rw[0], s.rw[1], s.rw[2], __uint_as_float(draw));
-    if (ps == kPsNone) return;   // a null pixel shader reads no attributes
     h[1] = make_float4(v0.v[4], v0.v[5], v0.v[6], v0.v[7]);
     h[2] = make_float4(v1.v[4], v1.v[5], v1.v[6], v1.v[7]);
     h[3] = make_float4(v2.v[4], v2.v[5], v2.v[6], v2.v[7]);
@@ -531,7 +533,7 @@ __global__ void __launch_bounds__(BLOCK, MLV_GEOMETRY_THREADS_PER_SM / BLOCK) k_
                     if (!ghost) {
 #pragma unroll
                         for (int k = 0; k < 3; ++k) triangle_attributes(bp, slot[k], v[k].v);
-                        write_record(bp, g, draw, d.ps, su, v[0], v[1], v[2]);
+                        write_record(bp, g, draw, d.ps, !(d.raster_flags & kDrawSharesView), su, v[0], v[1], v[2]);
                         have_own = bin_job(vw, d.draw_in_view, su.minx, su.miny, su.maxx, su.maxy, g << 3, own);
                     } else {
                         // its bins are only marked active (bit 31 of the count, which k_scan counts
@@ -566,7 +568,8 @@ __global__ void __launch_bounds__(BLOCK, MLV_GEOMETRY_THREADS_PER_SM / BLOCK) k_
                             Setup su;
                             if (setup_triangle(d, poly[0], poly[f + 1], poly[f + 2], su)) {
                                 const uint32_t slot = bp.total_tris + base + (uint32_t)f;
-                                write_record(bp, slot, draw, d.ps, su, poly[0], poly[f + 1], poly[f + 2]);
+                                write_record(bp, slot, draw, d.ps, !(d.raster_flags & kDrawSharesView), su, poly[0],
+                                             poly[f + 1], poly[f + 2]);
                                 mask |= 1u << f;
                                 deltas[f < 5 ? 0 : 1] |= su.box_delta << (6 * (f < 5 ? f : f - 5));
                                 BinJob job;
@@ -1149,10 +1152,11 @@ __device__ __forceinline__ void shade_pixel(const BatchParams &bp, const ViewDes
     const uint32_t rec = record_of(bp, key);
     const int4 *R = bp.raster[rec].w;
     const int4 w0 = R[0], w1 = R[1], w2 = R[2], w3 = R[3];
-    const float4 *S = bp.shade[rec].s;
-    const float4 s0 = S[0];
-    const uint32_t dr = __float_as_uint(s0.w);
-    const DrawDesc &D = bp.draws[dr];
+    // the winner's draw: the view's only one, or the index its shading record keeps
+    const bool sole = V.draw_count == 1;
+    float4 s0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (!sole) s0 = bp.shade[rec].s[0];
+    const DrawDesc &D = bp.draws[sole ? V.draw_begin : __float_as_uint(s0.w)];
     const uint32_t E1 = (((uint32_t)w0.w * (uint32_t)x) << kSubpix) + (((uint32_t)w1.x * (uint32_t)y) << kSubpix) + (uint32_t)w1.y;
     const uint32_t E2 = (((uint32_t)w1.z * (uint32_t)x) << kSubpix) + (((uint32_t)w1.w * (uint32_t)y) << kSubpix) + (uint32_t)w2.x;
     const float inv_area = __int_as_float(w2.y);
@@ -1162,6 +1166,8 @@ __device__ __forceinline__ void shade_pixel(const BatchParams &bp, const ViewDes
     float z = z0 + (z1 - z0) * b1;
     z = z + (z2 - z0) * b2;
     if (D.ps != kPsNone) {
+        const float4 *S = bp.shade[rec].s;
+        if (sole) s0 = S[0];
         // perspective correction, main.c:1106-1115
         float den = (1.0f - (b1 + b2)) * s0.x;
         den = den + b1 * s0.y;

@@ -96,3 +96,24 @@ def test_queued_uploads_keep_queued_work_on_the_old_contents(device):
     ctx.update_buffer_async(vb_buf, np.ascontiguousarray(vb_arr))
     ctx.finish()
     r.destroy()
+
+
+@pytest.mark.parametrize("batched", [True, False])
+def test_null_pixel_shader_among_shaded_draws_of_one_view(device, batched):
+    """A view whose draws mix the null pixel shader with shaded ones: depth, ids and barycentrics
+    of every draw, the colour of the shaded draws' pixels (the null shader's pixels keep the
+    colour below them)."""
+    fr = scenes.small_scene(61, 80, 56, n_objects=4, level=3)
+    for k, d in enumerate(fr.draws):
+        if k % 2 == 1:
+            d.ps = scenes.PS_NONE
+    want = pyoracle.render_oracle(fr)
+    r = api.FrameRenderer(device, fr, visibility=True)
+    for _ in range(2 if batched else 1):
+        r.render_batched() if batched else r.render_per_draw()
+    got = r.read(0)
+    r.destroy()
+    for key in ("depth", "vis_tri", "vis_draw", "vis_bary"):
+        assert np.array_equal(got[key].view(np.uint32), want[key].view(np.uint32)), key
+    from helpers import assert_color_close
+    assert_color_close(got["color"], want["color"])
