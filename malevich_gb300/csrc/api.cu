@@ -772,14 +772,26 @@ static mlv_status execute_segment_eager(mlv_context_t *c, const Segment &seg, ui
 
 // Reads the device error words; on an overflow regrows the workspace and re-runs the pending
 // work from the failed batch on. Called with the stream idle.
-static mlv_status check_and_recover(mlv_context_t *c) {
+// The error words and counters into the pinned host mirror, queued on the context's stream.
+static mlv_status queue_error_fetch(mlv_context_t *c) {
+    CUDA_TRY(cudaMemcpyAsync(c->h_error, c->ws.error, sizeof(uint32_t) * 8, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaMemcpyAsync(c->h_error + 8, c->ws.counters, sizeof(uint32_t) * kCtrCount, cudaMemcpyDeviceToHost,
+                             c->stream));
+    return MLV_OK;
+}
+
+// fetched: the mirror already holds the words as of the stream's end (queue_error_fetch, then a
+// synchronisation). *reran: set when batches were re-run.
+static mlv_status check_and_recover(mlv_context_t *c, bool fetched = false, bool *reran = nullptr) {
     if (!c->ws.error) {
         c->pending.clear();
         return MLV_OK;
     }
     for (int attempt = 0; attempt < 4; ++attempt) {
-        CUDA_TRY(cudaMemcpy(c->h_error, c->ws.error, sizeof(uint32_t) * 8, cudaMemcpyDeviceToHost));
-        CUDA_TRY(cudaMemcpy(c->h_error + 8, c->ws.counters, sizeof(uint32_t) * kCtrCount, cudaMemcpyDeviceToHost));
+        if (!(fetched && attempt == 0)) {
+            CUDA_TRY(cudaMemcpy(c->h_error, c->ws.error, sizeof(uint32_t) * 8, cudaMemcpyDeviceToHost));
+            CUDA_TRY(cudaMemcpy(c->h_error + 8, c->ws.counters, sizeof(uint32_t) * kCtrCount, cudaMemcpyDeviceToHost));
+        }
         const uint32_t err = c->h_error[0];
         if (c->h_error[2]) {
             // out-of-range indices read zeros, as Direct3D 11 does; report once
@@ -829,6 +841,7 @@ static mlv_status check_and_recover(mlv_context_t *c) {
         std::vector<PendingJob> jobs;
         jobs.swap(c->pending);
         const uint32_t failed = c->h_error[1];
+        if (reran) *reran = true;
         for (const PendingJob &j : jobs) {
             if (j.seq < failed) continue;
             if (j.segment) {
@@ -1180,13 +1193,22 @@ MLV_API mlv_status mlv_update_texture2d_async(mlv_context c, mlv_texture2d t, co
     return MLV_OK;
 }
 
+// The copy is queued behind the context's work together with the error words, so one
+// synchronisation covers both; when that shows a batch must be re-run, the copy is made again.
 MLV_API mlv_status mlv_read_texture2d(mlv_context c, mlv_texture2d t, void *dst, uint32_t row_pitch) {
     MLV_TRY(need_immediate(c));
     if (!t || !dst) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
     MLV_TRY(set_device(c->device));
-    MLV_TRY(sync_context(c));
-    size_t row = (size_t)t->width * t->texel_bytes;
-    CUDA_TRY(cudaMemcpy2D(dst, row_pitch ? row_pitch : row, t->ptr, row, row, t->height, cudaMemcpyDeviceToHost));
+    if (c->copy_stream) CUDA_TRY(cudaStreamSynchronize(c->copy_stream));   // queued uploads land first
+    const size_t row = (size_t)t->width * t->texel_bytes, pitch = row_pitch ? row_pitch : row;
+    CUDA_TRY(cudaMemcpy2DAsync(dst, pitch, t->ptr, row, row, t->height, cudaMemcpyDeviceToHost, c->stream));
+    const bool fetched = c->ws.error != nullptr;
+    if (fetched) MLV_TRY(queue_error_fetch(c));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    collect_events(c);
+    bool reran = false;
+    MLV_TRY(check_and_recover(c, fetched, &reran));
+    if (reran) CUDA_TRY(cudaMemcpy2D(dst, pitch, t->ptr, row, row, t->height, cudaMemcpyDeviceToHost));
     return MLV_OK;
 }
 

@@ -1261,6 +1261,13 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
     const bool capture = bp.info_mask != nullptr;
 
     for (uint32_t dd = 0; dd < dc; ++dd) {
+        if (dc < 32) {   // skip to the next draw with entries here (lane d: draw d has some)
+            const uint32_t next = __shfl_down_sync(0xFFFFFFFFu, my_start, 1);   // every lane takes part
+            const uint32_t rest = __ballot_sync(0xFFFFFFFFu, (uint32_t)lane >= dd && (uint32_t)lane < dc &&
+                                                                 my_start != next);
+            if (!rest) break;
+            dd = (uint32_t)__ffs(rest) - 1u;
+        }
         uint32_t s, e;
         if (dd + 1 < 32) {
             s = __shfl_sync(0xFFFFFFFFu, my_start, dd);
@@ -1382,6 +1389,13 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_tile_coop(BatchParam
     const bool capture = bp.info_mask != nullptr;
 
     for (uint32_t dd = 0; dd < dc; ++dd) {
+        if (dc < 32) {   // skip to the next draw with entries here (lane d: draw d has some)
+            const uint32_t next = __shfl_down_sync(0xFFFFFFFFu, my_start, 1);   // every lane takes part
+            const uint32_t rest = __ballot_sync(0xFFFFFFFFu, (uint32_t)lane >= dd && (uint32_t)lane < dc &&
+                                                                 my_start != next);
+            if (!rest) break;
+            dd = (uint32_t)__ffs(rest) - 1u;
+        }
         uint32_t s, e;
         if (dd + 1 < 32) {
             s = __shfl_sync(0xFFFFFFFFu, my_start, dd);
