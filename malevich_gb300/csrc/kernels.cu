@@ -592,6 +592,10 @@ __global__ void __launch_bounds__(BLOCK, MLV_GEOMETRY_THREADS_PER_SM / BLOCK) k_
         bp.bins_of[g] = have_own ? make_uint2(own.first_bin, own.nx | (own.ny << 16))
                                  : make_uint2(0u, clipped && mask ? kBinsClipped : 0u);
     }
+    if (!__any_sync(0xFFFFFFFFu, mask != 0u)) {   // the warp assembled nothing: nothing to count
+        pdl_trigger();
+        return;
+    }
     // assembled-triangle statistic (main.c:1238)
     uint32_t n = __popc(mask);
 #pragma unroll
@@ -824,6 +828,7 @@ __global__ void __launch_bounds__(kScatterBlock) k_scatter(BatchParams bp) {
         __syncwarp();
         const uint32_t g = base + threadIdx.x;
         const uint2 bd = g < bp.total_tris ? bp.bins_of[g] : make_uint2(0u, 0u);
+        if (!__any_sync(0xFFFFFFFFu, bd.y != 0u)) continue;   // none of the warp's triangles has bins
         BinJob own;
         uint32_t nt_own = 0;
         if (bd.y != 0u && bd.y != kBinsClipped) {
