@@ -199,7 +199,9 @@ MLV_API mlv_status mlv_destroy_context(mlv_context context);
 
 /* ------------------------------------------------------------------ resources
  * The reference borrows caller pointers (IA::p_index_buffer, IA::p_vertex_buffer, Texture2D::p_data,
- * OM::p_colors/p_depth, main.c:71-107). Here resources own device memory; init data is copied. */
+ * OM::p_colors/p_depth, main.c:71-107). Here resources own device memory; init data is copied.
+ * Destroying a resource waits for the immediate context's queued work; a command list recorded
+ * with it must not be executed afterwards (as in Direct3D 11). */
 MLV_API mlv_status mlv_create_buffer(mlv_device device, const mlv_buffer_desc *desc, const void *init_data,
                                      mlv_buffer *out_buffer);
 MLV_API mlv_status mlv_destroy_buffer(mlv_buffer buffer);
