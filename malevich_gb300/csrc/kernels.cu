@@ -823,11 +823,16 @@ __global__ void __launch_bounds__(kScatterBlock) k_scatter(BatchParams bp) {
         return;
     }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (uint32_t base = blockIdx.x * kScatterBlock; base < bp.total_tris; base += gridDim.x * kScatterBlock) {
+    const uint32_t stride = gridDim.x * kScatterBlock;
+    uint32_t g_first = blockIdx.x * kScatterBlock + threadIdx.x;
+    uint2 bd_next = g_first < bp.total_tris ? bp.bins_of[g_first] : make_uint2(0u, 0u);
+    for (uint32_t base = blockIdx.x * kScatterBlock; base < bp.total_tris; base += stride) {
         if (lane == 0) s_qn[warp] = 0;
         __syncwarp();
         const uint32_t g = base + threadIdx.x;
-        const uint2 bd = g < bp.total_tris ? bp.bins_of[g] : make_uint2(0u, 0u);
+        const uint2 bd = bd_next;
+        // the next iteration's descriptor is in flight while this one's bins are filled
+        bd_next = g + stride < bp.total_tris ? bp.bins_of[g + stride] : make_uint2(0u, 0u);
         if (!__any_sync(0xFFFFFFFFu, bd.y != 0u)) continue;   // none of the warp's triangles has bins
         BinJob own;
         uint32_t nt_own = 0;
@@ -1323,7 +1328,10 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
         const uint32_t q = q0 + lane;
         const uint32_t half = q < n0 ? 0u : 1u;
         uint32_t src = 0;
-        if (q < n) src = nth_set_bit(half ? m1 : m0, half ? q - n0 : q);
+        if (q < n) {
+            const uint32_t m = half ? m1 : m0, k = half ? q - n0 : q;
+            src = m == 0xFFFFFFFFu ? k : nth_set_bit(m, k);   // a full half needs no search
+        }
         const uint32_t wa = __shfl_sync(0xFFFFFFFFu, win0, src), wb = __shfl_sync(0xFFFFFFFFu, win1, src);
         if (q >= n) continue;
         shade_pixel(bp, V, half ? wb : wa, x0 + (int32_t)(src & 7), y0 + (int32_t)(src >> 3) + (half ? 4 : 0));
