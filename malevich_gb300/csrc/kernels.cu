@@ -783,6 +783,70 @@ __global__ void __launch_bounds__(kScanBlock) k_scan(BatchParams bp) {
     pdl_trigger();
 }
 
+// The same scan for batches of up to kSmallScanBins bins, in one CTA: no look-back, no tickets,
+// so a small frame (one draw at 1280x720: 14,400 bins) does not wait on a chain of CTAs.
+constexpr int kSmallScanBlock = 1024;
+constexpr uint32_t kSmallScanBins = kSmallScanBlock * kScanItems;
+
+__global__ void __launch_bounds__(kSmallScanBlock) k_scan_small(BatchParams bp) {
+    __shared__ uint32_t s_warp[kSmallScanBlock / 32];
+    pdl_wait();
+    if (ld_volatile_u32(bp.error)) return;   // uniform: set only by earlier kernels
+    const uint32_t n = bp.total_bins;
+    const uint32_t base = threadIdx.x * kScanItems;
+    uint32_t vals[kScanItems];
+    if (base + kScanItems <= n) {
+#pragma unroll
+        for (int q = 0; q < kScanItems / 4; ++q) {
+            const uint4 v4 = reinterpret_cast<const uint4 *>(bp.bin_count + base)[q];
+            vals[4 * q] = v4.x; vals[4 * q + 1] = v4.y; vals[4 * q + 2] = v4.z; vals[4 * q + 3] = v4.w;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < kScanItems; ++i) vals[i] = base + i < n ? bp.bin_count[base + i] : 0u;
+    }
+    uint32_t sum = 0, active = 0, ghosts = 0;
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) {   // bit 31: a bin of triangles without samples only
+        active += vals[i] ? 1u : 0u;
+        ghosts |= (vals[i] >> 31) << i;
+        vals[i] &= ~kBinGhost;
+        sum += vals[i];
+    }
+    uint32_t total;
+    uint32_t run = block_exclusive_scan<kSmallScanBlock>(sum, s_warp, total);
+    if (ghosts) {
+#pragma unroll
+        for (int i = 0; i < kScanItems; ++i)
+            if (ghosts >> i & 1u) bp.bin_count[base + i] = vals[i];
+    }
+    uint32_t outv[kScanItems];
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) {
+        outv[i] = run;
+        run += vals[i];
+    }
+    if (base + kScanItems <= n) {
+#pragma unroll
+        for (int q = 0; q < kScanItems / 4; ++q)
+            reinterpret_cast<uint4 *>(bp.bin_start + base)[q] =
+                make_uint4(outv[4 * q], outv[4 * q + 1], outv[4 * q + 2], outv[4 * q + 3]);
+    } else {
+#pragma unroll
+        for (int i = 0; i < kScanItems; ++i)
+            if (base + i < n) bp.bin_start[base + i] = outv[i];
+    }
+    // active-bin statistic (main.c:937-944)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) active += __shfl_xor_sync(0xFFFFFFFFu, active, o);
+    if ((threadIdx.x & 31) == 0 && active) atomicAdd(bp.stats + kStatActiveBins, (unsigned long long)active);
+    if (threadIdx.x == 0) {
+        bp.bin_start[n] = total;
+        atomicAdd(bp.stats + kStatBinEntries, (unsigned long long)total);
+    }
+    pdl_trigger();
+}
+
 // ------------------------------------------------------------------ bin scatter
 
 constexpr int kScatterBlock = 256;
@@ -1580,6 +1644,7 @@ cudaError_t launch_rank(const BatchParams &bp, cudaStream_t stream) {
 }
 
 cudaError_t launch_scan(const BatchParams &bp, cudaStream_t stream) {
+    if (bp.total_bins <= kSmallScanBins) return launch_chained(k_scan_small, 1u, (uint32_t)kSmallScanBlock, stream, bp);
     const uint32_t per = kScanBlock * kScanItems;
     const uint32_t blocks = (bp.total_bins + per - 1) / per;
     return launch_chained(k_scan, blocks ? blocks : 1, kScanBlock, stream, bp);
