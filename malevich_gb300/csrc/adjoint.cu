@@ -197,7 +197,7 @@ __device__ __forceinline__ void run_sum(float (&v)[N], uint32_t lane, int end) {
 // One thread per pixel. Texel gradients go out as float4 atomics; the vertex-colour and position
 // gradients of a run of neighbouring pixels on the same triangle (the common case along a row)
 // are summed in registers first and leave as one set of atomics per run.
-__global__ void __launch_bounds__(kDiffBlock) k_diff_backward(mlv_diff_desc d) {
+__global__ void __launch_bounds__(kDiffBlock, 4) k_diff_backward(mlv_diff_desc d) {
     const size_t npix = (size_t)d.width * d.height;
     const size_t i = (size_t)blockIdx.x * kDiffBlock + threadIdx.x;
     const uint32_t lane = threadIdx.x & 31;
