@@ -770,8 +770,6 @@ static mlv_status execute_segment_eager(mlv_context_t *c, const Segment &seg, ui
     return MLV_OK;
 }
 
-// Reads the device error words; on an overflow regrows the workspace and re-runs the pending
-// work from the failed batch on. Called with the stream idle.
 // The error words and counters into the pinned host mirror, queued on the context's stream.
 static mlv_status queue_error_fetch(mlv_context_t *c) {
     CUDA_TRY(cudaMemcpyAsync(c->h_error, c->ws.error, sizeof(uint32_t) * 8, cudaMemcpyDeviceToHost, c->stream));
@@ -780,8 +778,10 @@ static mlv_status queue_error_fetch(mlv_context_t *c) {
     return MLV_OK;
 }
 
-// fetched: the mirror already holds the words as of the stream's end (queue_error_fetch, then a
-// synchronisation). *reran: set when batches were re-run.
+// Reads the device error words; on an overflow regrows the workspace and re-runs the pending
+// work from the failed batch on. Called with the stream idle. fetched: the mirror already holds
+// the words as of the stream's end (queue_error_fetch, then a synchronisation). *reran: set when
+// batches were re-run.
 static mlv_status check_and_recover(mlv_context_t *c, bool fetched = false, bool *reran = nullptr) {
     if (!c->ws.error) {
         c->pending.clear();
