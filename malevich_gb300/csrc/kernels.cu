@@ -10,12 +10,14 @@
 //   k_rank      only when visibility or TileInfo outputs are requested: the reference's compact
 //               triangle index (its `out_triangle_index`, main.c:873-875), by an exclusive scan of
 //               the per-input-triangle output counts.
-//   k_scan      exclusive scan of the bin counts (main.c:937-946).
+//   k_scan      exclusive scan of the bin counts (main.c:937-946); k_scan_small for batches of
+//               up to 16,384 bins (one CTA).
 //   k_scatter   bin lists (main.c:950-962); the order inside a bin does not matter (see k_tile).
 //   k_tile      one warp per 8x8 tile: hierarchical Z, coverage, depth, pixel shader, output
 //               merger, write-back (main.c:983-1189, 577-603), for every draw of the batch that
 //               touches the tile, in draw order, with colour and depth held on-chip until one
 //               write-back; the segment's clears of the batch's targets are folded in.
+//               k_tile_coop: the same with 2, 4 or 8 warps sharing each tile's triangles.
 //   k_fill_many the clears that are not folded (one launch per segment).
 // The kernels are launched with programmatic stream serialisation (see pdl_wait).
 //
