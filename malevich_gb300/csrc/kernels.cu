@@ -1024,17 +1024,17 @@ __device__ __forceinline__ uint32_t nth_set_bit(uint32_t m, uint32_t k) {
 
 // Per-triangle parameters staged in shared memory for the work-expansion loop (17 words per
 // triangle, an odd stride, so lanes reading different triangles hit different banks).
-constexpr int kStage = 17;
-enum : int {
-    kSE0 = 0, kSE1, kSE2,          // edge values at the clipped bounding box's first pixel
-    kSA0, kSA1, kSA2,              // x steps (a << 4)
-    kSB0, kSB1, kSB2,              // y steps (b << 4)
-    kSInvArea, kSZ0, kSDz1, kSDz2, // barycentric scale and depth plane
-    kSOrigin,                      // box origin in the tile: x | y << 8
-    kSWidth,                       // box width | reciprocal << 8 (row = local * recip >> 16)
-    kSKey,                         // triangle key
-    kSPad
-};
+// Per-triangle parameters staged in shared memory for the work-expansion loop: 20 words (five
+// 16-byte groups, read with vector loads) per triangle:
+//   q0 = E0, A0, B0, E1     edge values at the box's first pixel (E), x steps A = a << 4,
+//   q1 = A1, B1, E2, A2     y steps B = b << 4
+//   q2 = B2, width, pad, origin
+//   q3 = 1/area, z0, z1 - z0, z2 - z0
+//   q4 = key, -, -, -
+// width: box width | reciprocal << 8 (row = local * recip >> 16); pad: the top-left rule's bias
+// bits (edge k needs E >= 1) | box height << 8; origin: box origin in the tile, x | y << 8.
+// Eight lanes storing their triangles (80-byte stride) hit distinct banks.
+constexpr int kStage = 20;
 
 // Writes the folded clears (ViewDesc::clear_flags) of a pixel that no draw of the batch wrote;
 // depth is the running value, which for such a pixel is the clear value.
@@ -1092,26 +1092,24 @@ __device__ __forceinline__ void tile_chunk(const BatchParams &bp, uint32_t chunk
                            c2 = w2.x;
             const uint32_t w = (uint32_t)(bx1 - bx0 + 1), h = (uint32_t)(by1 - by0 + 1);
             cnt = w * h;
-            uint32_t *st = stage + lane * kStage;
+            uint4 *sq = reinterpret_cast<uint4 *>(stage + lane * kStage);
             // main.c:1015-1025: ((a*x)<<4) + ((b*y)<<4) + c, wrapping int32
-            st[kSE0] = ((a0 * (uint32_t)bx0) << kSubpix) + ((b0 * (uint32_t)by0) << kSubpix) + c0;
-            st[kSE1] = ((a1 * (uint32_t)bx0) << kSubpix) + ((b1 * (uint32_t)by0) << kSubpix) + c1;
-            st[kSE2] = ((a2 * (uint32_t)bx0) << kSubpix) + ((b2 * (uint32_t)by0) << kSubpix) + c2;
-            st[kSA0] = a0 << kSubpix; st[kSA1] = a1 << kSubpix; st[kSA2] = a2 << kSubpix;
-            st[kSB0] = b0 << kSubpix; st[kSB1] = b1 << kSubpix; st[kSB2] = b2 << kSubpix;
-            const float z0 = __int_as_float(w2.w);
-            st[kSInvArea] = (uint32_t)w2.y;
-            st[kSZ0] = (uint32_t)w2.w;
-            st[kSDz1] = __float_as_uint(__int_as_float(w3.x) - z0);
-            st[kSDz2] = __float_as_uint(__int_as_float(w3.y) - z0);
-            st[kSOrigin] = (uint32_t)(bx0 - x0) | ((uint32_t)(by0 - y0) << 8);
-            st[kSWidth] = w | (((65536u + w - 1) / w) << 8);
-            st[kSKey] = key;
+            const uint32_t e0 = ((a0 * (uint32_t)bx0) << kSubpix) + ((b0 * (uint32_t)by0) << kSubpix) + c0;
+            const uint32_t e1 = ((a1 * (uint32_t)bx0) << kSubpix) + ((b1 * (uint32_t)by0) << kSubpix) + c1;
+            const uint32_t e2 = ((a2 * (uint32_t)bx0) << kSubpix) + ((b2 * (uint32_t)by0) << kSubpix) + c2;
             // top-left rule: an edge value of 0 covers only on a left edge (a > 0) or a top edge
-            // (a == 0, b > 0); the others need E >= 1 (bit k set: edge k needs it); box height above
-            st[kSPad] = ((int32_t)a0 > 0 || (a0 == 0 && (int32_t)b0 > 0) ? 0u : 1u) |
-                        ((int32_t)a1 > 0 || (a1 == 0 && (int32_t)b1 > 0) ? 0u : 2u) |
-                        ((int32_t)a2 > 0 || (a2 == 0 && (int32_t)b2 > 0) ? 0u : 4u) | (h << 8);
+            // (a == 0, b > 0); the others need E >= 1 (bit k set: edge k needs it)
+            const uint32_t pad = ((int32_t)a0 > 0 || (a0 == 0 && (int32_t)b0 > 0) ? 0u : 1u) |
+                                 ((int32_t)a1 > 0 || (a1 == 0 && (int32_t)b1 > 0) ? 0u : 2u) |
+                                 ((int32_t)a2 > 0 || (a2 == 0 && (int32_t)b2 > 0) ? 0u : 4u) | (h << 8);
+            const float z0 = __int_as_float(w2.w);
+            sq[0] = make_uint4(e0, a0 << kSubpix, b0 << kSubpix, e1);
+            sq[1] = make_uint4(a1 << kSubpix, b1 << kSubpix, e2, a2 << kSubpix);
+            sq[2] = make_uint4(b2 << kSubpix, w | (((65536u + w - 1) / w) << 8), pad,
+                               (uint32_t)(bx0 - x0) | ((uint32_t)(by0 - y0) << 8));
+            sq[3] = make_uint4((uint32_t)w2.y, (uint32_t)w2.w, __float_as_uint(__int_as_float(w3.x) - z0),
+                               __float_as_uint(__int_as_float(w3.y) - z0));
+            sq[4] = make_uint4(key, 0u, 0u, 0u);
         }
     }
     if (capture) mask[lane] = 0;
@@ -1131,31 +1129,33 @@ __device__ __forceinline__ void tile_chunk(const BatchParams &bp, uint32_t chunk
 #pragma unroll
         for (uint32_t step = 16; step; step >>= 1)
             if (pref[j + step - 1] <= item) j += step;
-        const uint32_t *st = stage + j * kStage;
+        const uint4 *sq = reinterpret_cast<const uint4 *>(stage + j * kStage);
         const uint32_t local = item - (j ? pref[j - 1] : 0u);
-        const uint32_t wr = st[kSWidth];
+        const uint4 q0 = sq[0], q1 = sq[1], q2 = sq[2];
+        const uint32_t wr = q2.y;
         const uint32_t row = (local * (wr >> 8)) >> 16;
         const uint32_t col = local - row * (wr & 0xFFu);
-        const uint32_t E0 = st[kSE0] + col * st[kSA0] + row * st[kSB0];
-        const uint32_t E1 = st[kSE1] + col * st[kSA1] + row * st[kSB1];
-        const uint32_t E2 = st[kSE2] + col * st[kSA2] + row * st[kSB2];
-        const uint32_t nb = st[kSPad];
+        const uint32_t E0 = q0.x + col * q0.y + row * q0.z;
+        const uint32_t E1 = q0.w + col * q1.x + row * q1.y;
+        const uint32_t E2 = q1.z + col * q1.w + row * q2.x;
+        const uint32_t nb = q2.z;
         const bool covered = top_left ? (int32_t)((E0 - (nb & 1u)) | (E1 - ((nb >> 1) & 1u)) | (E2 - ((nb >> 2) & 1u))) >= 0
                                       : (int32_t)(E0 | E1 | E2) > 0;   // main.c:1028
         if (covered) {
-            const uint32_t org = st[kSOrigin];
+            const uint32_t org = q2.w;
             const int p = (int)(((org >> 8) + row) * 8 + (org & 0xFFu) + col);
             if (capture) atomicOr(&mask[j], 1ull << p);
             // main.c:1092-1102 and 1131-1132 for reg0.z
-            const float inv_area = __uint_as_float(st[kSInvArea]);
+            const uint4 q3 = sq[3];
+            const float inv_area = __uint_as_float(q3.x);
             const float bb1 = (float)((int32_t)E1 >> (kSubpix * 2)) * inv_area;
             const float bb2 = (float)((int32_t)E2 >> (kSubpix * 2)) * inv_area;
-            float z = __uint_as_float(st[kSZ0]) + __uint_as_float(st[kSDz1]) * bb1;
-            z = z + __uint_as_float(st[kSDz2]) * bb2;
+            float z = __uint_as_float(q3.y) + __uint_as_float(q3.z) * bb1;
+            z = z + __uint_as_float(q3.w) * bb2;
             const float dstart = depth[p];
             const bool cand = less ? (z < dstart) : (z >= dstart);   // main.c:1164-1168
             if (cand) {
-                const unsigned long long k = ((unsigned long long)depth_key(z) << 32) | st[kSKey];
+                const unsigned long long k = ((unsigned long long)depth_key(z) << 32) | sq[4].x;
                 if (less) atomicMin(&best[p], k);
                 else atomicMax(&best[p], k);
             }
@@ -1169,17 +1169,18 @@ __device__ __forceinline__ void tile_chunk(const BatchParams &bp, uint32_t chunk
         do {
             const int j = __ffs(big) - 1;
             big &= big - 1;
-            const uint32_t *st = stage + j * kStage;
-            const uint32_t org = st[kSOrigin], nb = st[kSPad];
+            const uint4 *sq = reinterpret_cast<const uint4 *>(stage + j * kStage);
+            const uint4 q0 = sq[0], q1 = sq[1], q2 = sq[2];
+            const uint32_t org = q2.w, nb = q2.z;
             // offsets from the box origin; outside the box nothing is tested (main.c:1015-1025)
             const uint32_t dx = (uint32_t)(cx - (int32_t)(org & 0xFFu)), dy = (uint32_t)(cy - (int32_t)(org >> 8));
-            const uint32_t w = st[kSWidth] & 0xFFu, h = nb >> 8;
+            const uint32_t w = q2.y & 0xFFu, h = nb >> 8;
             const bool in_x = dx < w;
             const bool in_a = in_x && dy < h, in_b = in_x && dy + 4u < h;
-            const uint32_t sb0 = st[kSB0], sb1 = st[kSB1], sb2 = st[kSB2];
-            const uint32_t E0a = st[kSE0] + dx * st[kSA0] + dy * sb0, E0b = E0a + (sb0 << 2);
-            const uint32_t E1a = st[kSE1] + dx * st[kSA1] + dy * sb1, E1b = E1a + (sb1 << 2);
-            const uint32_t E2a = st[kSE2] + dx * st[kSA2] + dy * sb2, E2b = E2a + (sb2 << 2);
+            const uint32_t sb0 = q0.z, sb1 = q1.y, sb2 = q2.x;
+            const uint32_t E0a = q0.x + dx * q0.y + dy * sb0, E0b = E0a + (sb0 << 2);
+            const uint32_t E1a = q0.w + dx * q1.x + dy * sb1, E1b = E1a + (sb1 << 2);
+            const uint32_t E2a = q1.z + dx * q1.w + dy * sb2, E2b = E2a + (sb2 << 2);
             bool ca, cb;
             if (top_left) {
                 ca = (int32_t)((E0a - (nb & 1u)) | (E1a - ((nb >> 1) & 1u)) | (E2a - ((nb >> 2) & 1u))) >= 0;
@@ -1194,9 +1195,10 @@ __device__ __forceinline__ void tile_chunk(const BatchParams &bp, uint32_t chunk
                 const uint32_t ma = __ballot_sync(0xFFFFFFFFu, ca), mb = __ballot_sync(0xFFFFFFFFu, cb);
                 if (lane == 0) mask[j] = (unsigned long long)ma | ((unsigned long long)mb << 32);
             }
-            const float inv_area = __uint_as_float(st[kSInvArea]);
-            const float z0 = __uint_as_float(st[kSZ0]), dz1 = __uint_as_float(st[kSDz1]), dz2 = __uint_as_float(st[kSDz2]);
-            const unsigned long long key = st[kSKey];
+            const uint4 q3 = sq[3];
+            const float inv_area = __uint_as_float(q3.x);
+            const float z0 = __uint_as_float(q3.y), dz1 = __uint_as_float(q3.z), dz2 = __uint_as_float(q3.w);
+            const unsigned long long key = sq[4].x;
             if (ca) {
                 const float bb1 = (float)((int32_t)E1a >> (kSubpix * 2)) * inv_area;
                 const float bb2 = (float)((int32_t)E2a >> (kSubpix * 2)) * inv_area;
@@ -1291,7 +1293,7 @@ template <int WARPS>
 __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
     __shared__ unsigned long long s_best[WARPS][64];
     __shared__ float s_depth[WARPS][64];
-    __shared__ uint32_t s_stage[WARPS][32 * kStage];
+    __shared__ __align__(16) uint32_t s_stage[WARPS][32 * kStage];
     __shared__ uint32_t s_pref[WARPS][32];
     __shared__ unsigned long long s_mask[WARPS][32];
     pdl_wait();
@@ -1426,7 +1428,7 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_tile_coop(BatchParam
     __shared__ unsigned long long s_best[64];
     __shared__ float s_depth[64];
     __shared__ float s_hiz[2];
-    __shared__ uint32_t s_stage[WARPS][32 * kStage];
+    __shared__ __align__(16) uint32_t s_stage[WARPS][32 * kStage];
     __shared__ uint32_t s_pref[WARPS][32];
     __shared__ unsigned long long s_mask[WARPS][32];
     pdl_wait();
