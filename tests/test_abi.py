@@ -51,3 +51,25 @@ def test_no_device_reports_device_error(lib):
         pytest.skip("a GPU is present")
     h = ctypes.c_void_p()
     assert lib.mlv_create_device(0, ctypes.byref(h)) == 4
+
+
+def _struct_fields(name):
+    """Field names of a `typedef struct name {...} name;` in the header, in order."""
+    src = open(os.path.join(ROOT, "include", "malevich.h")).read()
+    body = re.search(r"typedef struct %s \{(.*?)\} %s;" % (name, name), src, re.S).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    names = []
+    for decl in body.split(";"):
+        decl = decl.strip()
+        if decl:
+            names += [n.strip().split("[")[0] for n in decl.split(None, 1)[1].split(",")]
+    return names
+
+
+@pytest.mark.parametrize("cname,pytype", [("mlv_tuning", "Tuning"), ("mlv_stats", "Stats"),
+                                          ("mlv_rasterizer_desc", "RasterizerDesc")])
+def test_python_structs_mirror_the_header(cname, pytype):
+    cls = getattr(api, pytype, None)
+    if cls is None:
+        pytest.skip("%s has no ctypes mirror" % cname)
+    assert [n for n, _ in cls._fields_] == _struct_fields(cname)
