@@ -877,6 +877,8 @@ __device__ __forceinline__ void put(const BatchParams &bp, uint32_t bin, uint32_
 __global__ void __launch_bounds__(kScatterBlock) k_scatter(BatchParams bp) {
     __shared__ BinJob s_q[kScatterBlock / 32][kFanQueue];
     __shared__ uint32_t s_qn[kScatterBlock / 32];
+    __shared__ BinJob s_big[kScatterBlock / 32][32];      // the warp's triangles over many bins
+    __shared__ uint32_t s_bigpref[kScatterBlock / 32][32]; // inclusive prefix of their bin counts
     pdl_wait();
     if (ld_volatile_u32(bp.error)) return;
     const uint32_t total = bp.bin_start[bp.total_bins];
@@ -961,18 +963,43 @@ __global__ void __launch_bounds__(kScatterBlock) k_scatter(BatchParams bp) {
                     if (t0 + k < nt_own) bp.list[st[k] + pos[k]] = own.key;
             }
         }
-        uint32_t big = __ballot_sync(0xFFFFFFFFu, nt_own > bp.big_tiles);
-        while (big) {
-            const int src = __ffs(big) - 1;
-            big &= big - 1;
-            BinJob j;
-            j.key = __shfl_sync(0xFFFFFFFFu, own.key, src);
-            j.first_bin = __shfl_sync(0xFFFFFFFFu, own.first_bin, src);
-            j.nx = __shfl_sync(0xFFFFFFFFu, own.nx, src);
-            j.ny = __shfl_sync(0xFFFFFFFFu, own.ny, src);
-            j.col_stride = __shfl_sync(0xFFFFFFFFu, own.col_stride, src);
-            j.row_stride = __shfl_sync(0xFFFFFFFFu, own.row_stride, src);
-            for (uint32_t t = lane; t < j.nx * j.ny; t += 32) put(bp, job_bin(j, t), j.key);
+        // triangles over more than big_tiles bins are filled by the whole warp, 32 (triangle, bin)
+        // pairs per round. Each big triangle normally starts a new round; when that leaves many
+        // rounds part-empty (triangles of a few dozen bins), the pairs of all of them are packed
+        // into as few rounds as they need instead.
+        const uint32_t nbig = nt_own > bp.big_tiles ? nt_own : 0u;
+        const uint32_t bigmask = __ballot_sync(0xFFFFFFFFu, nbig != 0u);
+        if (bigmask) {
+            const uint32_t rounds_each = __reduce_add_sync(0xFFFFFFFFu, (nbig + 31u) >> 5);
+            const uint32_t rounds_packed = (__reduce_add_sync(0xFFFFFFFFu, nbig) + 31u) >> 5;
+            uint32_t incl = rounds_packed < rounds_each ? nbig : (nbig + 31u) & ~31u;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            const uint32_t total_big = __shfl_sync(0xFFFFFFFFu, incl, 31);
+            if (nbig) {   // compacted: the k-th big triangle and the end of its pairs
+                const uint32_t k = __popc(bigmask & ((1u << lane) - 1u));
+                s_big[warp][k] = own;
+                s_bigpref[warp][k] = incl;
+            }
+            __syncwarp();
+            // each lane's pairs are item = lane, lane + 32, ...: its triangle only moves forward,
+            // so the job stays in registers until the lane crosses the end of a triangle
+            uint32_t jb = 0, base = 0, end = s_bigpref[warp][0];
+            BinJob job = s_big[warp][0];
+            for (uint32_t item = lane; item < total_big; item += 32) {
+                if (item >= end) {
+                    do {
+                        ++jb;
+                        base = end;
+                        end = s_bigpref[warp][jb];
+                    } while (item >= end);
+                    job = s_big[warp][jb];
+                }
+                if (item - base < job.nx * job.ny) put(bp, job_bin(job, item - base), job.key);
+            }
         }
         __syncwarp();
         const uint32_t nq = min(s_qn[warp], (uint32_t)kFanQueue);
