@@ -205,7 +205,8 @@ MLV_API mlv_status mlv_destroy_context(mlv_context context);
 MLV_API mlv_status mlv_create_buffer(mlv_device device, const mlv_buffer_desc *desc, const void *init_data,
                                      mlv_buffer *out_buffer);
 MLV_API mlv_status mlv_destroy_buffer(mlv_buffer buffer);
-/* row_pitch: bytes between rows of init_data (0 = tightly packed). Depth textures carry the
+/* row_pitch: bytes between rows of init_data (0 = tightly packed; a pitch shorter than a row is
+ * MLV_ERROR_INVALID_ARG, here and in the texture updates and readback). Depth textures carry the
  * per-8x8-tile hierarchical-Z state (main.c:230). */
 MLV_API mlv_status mlv_create_texture2d(mlv_device device, const mlv_texture2d_desc *desc, const void *init_data,
                                         uint32_t row_pitch, mlv_texture2d *out_texture);

@@ -1018,6 +1018,12 @@ MLV_API mlv_status mlv_destroy_buffer(mlv_buffer b) {
     return MLV_OK;
 }
 
+// A host image's rows are row_pitch bytes apart (0: tightly packed); shorter than a row is an error.
+static mlv_status check_pitch(uint64_t row, uint32_t row_pitch) {
+    if (row_pitch != 0 && row_pitch < row) return fail(MLV_ERROR_INVALID_ARG, "row_pitch is shorter than a row");
+    return MLV_OK;
+}
+
 static mlv_status create_texture2d(mlv_device d, const mlv_texture2d_desc *desc, const void *init,
                                    uint32_t row_pitch, void *placed, mlv_texture2d *out) {
     if (!d || !desc || !out) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
@@ -1025,6 +1031,7 @@ static mlv_status create_texture2d(mlv_device d, const mlv_texture2d_desc *desc,
     if (!tb) return fail(MLV_ERROR_INVALID_ARG, "unknown texture format");
     if (desc->width == 0 || desc->height == 0 || desc->width > 16384 || desc->height > 16384)
         return fail(MLV_ERROR_INVALID_ARG, "texture size must be 1..16384");
+    if (init) MLV_TRY(check_pitch((uint64_t)desc->width * tb, row_pitch));
     MLV_TRY(set_device(d));
     auto *t = new mlv_texture2d_t();
     t->device = d;
@@ -1130,7 +1137,7 @@ static mlv_status need_immediate(mlv_context c) {
 MLV_API mlv_status mlv_update_buffer(mlv_context c, mlv_buffer b, uint64_t offset, const void *data, uint64_t size) {
     MLV_TRY(need_immediate(c));
     if (!b || !data) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
-    if (offset + size > b->size) return fail(MLV_ERROR_INVALID_ARG, "update outside the buffer");
+    if (offset > b->size || size > b->size - offset) return fail(MLV_ERROR_INVALID_ARG, "update outside the buffer");
     MLV_TRY(set_device(c->device));
     MLV_TRY(sync_context(c));   // queued draws may still read the old contents
     CUDA_TRY(cudaMemcpy(b->ptr + offset, data, size, cudaMemcpyHostToDevice));
@@ -1141,9 +1148,10 @@ MLV_API mlv_status mlv_update_buffer(mlv_context c, mlv_buffer b, uint64_t offse
 MLV_API mlv_status mlv_update_texture2d(mlv_context c, mlv_texture2d t, const void *data, uint32_t row_pitch) {
     MLV_TRY(need_immediate(c));
     if (!t || !data) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
+    size_t row = (size_t)t->width * t->texel_bytes;
+    MLV_TRY(check_pitch(row, row_pitch));
     MLV_TRY(set_device(c->device));
     MLV_TRY(sync_context(c));
-    size_t row = (size_t)t->width * t->texel_bytes;
     CUDA_TRY(cudaMemcpy2D(t->ptr, row, data, row_pitch ? row_pitch : row, row, t->height, cudaMemcpyHostToDevice));
     return MLV_OK;
 }
@@ -1170,7 +1178,7 @@ MLV_API mlv_status mlv_update_buffer_async(mlv_context c, mlv_buffer b, uint64_t
                                            uint64_t size) {
     MLV_TRY(need_immediate(c));
     if (!b || !data) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
-    if (offset + size > b->size) return fail(MLV_ERROR_INVALID_ARG, "update outside the buffer");
+    if (offset > b->size || size > b->size - offset) return fail(MLV_ERROR_INVALID_ARG, "update outside the buffer");
     MLV_TRY(set_device(c->device));
     if (!c->pending.empty()) MLV_TRY(sync_context(c));
     MLV_TRY(begin_upload(c, &b->ready));
@@ -1183,10 +1191,11 @@ MLV_API mlv_status mlv_update_buffer_async(mlv_context c, mlv_buffer b, uint64_t
 MLV_API mlv_status mlv_update_texture2d_async(mlv_context c, mlv_texture2d t, const void *data, uint32_t row_pitch) {
     MLV_TRY(need_immediate(c));
     if (!t || !data) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
+    size_t row = (size_t)t->width * t->texel_bytes;
+    MLV_TRY(check_pitch(row, row_pitch));
     MLV_TRY(set_device(c->device));
     if (!c->pending.empty()) MLV_TRY(sync_context(c));
     MLV_TRY(begin_upload(c, &t->ready));
-    size_t row = (size_t)t->width * t->texel_bytes;
     CUDA_TRY(cudaMemcpy2DAsync(t->ptr, row, data, row_pitch ? row_pitch : row, row, t->height, cudaMemcpyHostToDevice,
                                c->copy_stream));
     CUDA_TRY(cudaEventRecord(t->ready, c->copy_stream));
@@ -1198,9 +1207,10 @@ MLV_API mlv_status mlv_update_texture2d_async(mlv_context c, mlv_texture2d t, co
 MLV_API mlv_status mlv_read_texture2d(mlv_context c, mlv_texture2d t, void *dst, uint32_t row_pitch) {
     MLV_TRY(need_immediate(c));
     if (!t || !dst) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
+    const size_t row = (size_t)t->width * t->texel_bytes, pitch = row_pitch ? row_pitch : row;
+    MLV_TRY(check_pitch(row, row_pitch));
     MLV_TRY(set_device(c->device));
     if (c->copy_stream) CUDA_TRY(cudaStreamSynchronize(c->copy_stream));   // queued uploads land first
-    const size_t row = (size_t)t->width * t->texel_bytes, pitch = row_pitch ? row_pitch : row;
     CUDA_TRY(cudaMemcpy2DAsync(dst, pitch, t->ptr, row, row, t->height, cudaMemcpyDeviceToHost, c->stream));
     const bool fetched = c->ws.error != nullptr;
     if (fetched) MLV_TRY(queue_error_fetch(c));

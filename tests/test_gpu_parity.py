@@ -1,6 +1,7 @@
 """GPU draw path (through the C ABI) against the checkers: the reference's golden outputs and
 the oracle restatement. Coverage, triangle ids, draw ids, barycentrics and depth are compared
 bit for bit; UNORM8 colour within +-1 LSB (see helpers.COLOR_TOL)."""
+import ctypes
 import os
 
 import numpy as np
@@ -200,6 +201,35 @@ def test_gpu_status_codes(device):
     finally:
         rt.destroy()
         ds.destroy()
+
+
+def test_gpu_copy_arguments_are_checked(device):
+    """Copies outside a buffer (also where offset + size wraps around 64 bits) and row pitches
+    shorter than a row are INVALID_ARG, refused before any copy is issued."""
+    ctx, lib = device.immediate, api.load_library()
+    buf = api.Buffer(device, byte_width=64)
+    tex = api.Texture2D(device, 8, 4, api.FORMAT_R8G8B8A8_UNORM)
+    src = np.zeros(64, np.uint8)
+    img = np.zeros((4, 8), np.uint32)
+    p = src.ctypes.data_as(ctypes.c_void_p)
+    q = img.ctypes.data_as(ctypes.c_void_p)
+    try:
+        for offset, size in ((60, 8), (65, 0), (2 ** 64 - 4, 8)):
+            assert lib.mlv_update_buffer(ctx.handle, buf.handle, offset, p, size) == 1, (offset, size)
+            assert lib.mlv_update_buffer_async(ctx.handle, buf.handle, offset, p, size) == 1, (offset, size)
+        assert lib.mlv_update_buffer(ctx.handle, buf.handle, 56, p, 8) == 0
+        assert lib.mlv_update_texture2d(ctx.handle, tex.handle, q, 28) == 1
+        assert lib.mlv_update_texture2d_async(ctx.handle, tex.handle, q, 16) == 1
+        assert lib.mlv_read_texture2d(ctx.handle, tex.handle, q, 31) == 1
+        desc = api.Texture2DDesc(8, 4, api.FORMAT_R8G8B8A8_UNORM, api.BIND_SHADER_RESOURCE)
+        h = ctypes.c_void_p()
+        assert lib.mlv_create_texture2d(device.handle, ctypes.byref(desc), q, 4, ctypes.byref(h)) == 1
+        img[:] = np.arange(32, dtype=np.uint32).reshape(4, 8)
+        assert lib.mlv_update_texture2d(ctx.handle, tex.handle, q, 32) == 0
+        assert np.array_equal(ctx.read_texture(tex), img)
+    finally:
+        buf.destroy()
+        tex.destroy()
 
 
 def test_gpu_workspace_overflow_is_regrown_and_rerun():
