@@ -1246,10 +1246,11 @@ MLV_API mlv_status mlv_ia_set_vertex_buffers(mlv_context c, uint32_t start, uint
     if (!bufs || !strides) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
     if (bufs[0] && (strides[0] < 32 || (strides[0] & 3)))
         return fail(MLV_ERROR_INVALID_ARG, "vertex stride must be >= 32 and a multiple of 4");
-    c->st.vb = bufs[0];
+    const uint32_t offset = offsets ? offsets[0] : 0;
+    if (offset & 3) return fail(MLV_ERROR_INVALID_ARG, "vertex buffer offset must be a multiple of 4");
+    c->st.vb = bufs[0];   // a refused call leaves the bound state as it was
     c->st.vb_stride = strides[0];
-    c->st.vb_offset = offsets ? offsets[0] : 0;
-    if (c->st.vb_offset & 3) return fail(MLV_ERROR_INVALID_ARG, "vertex buffer offset must be a multiple of 4");
+    c->st.vb_offset = offset;
     return MLV_OK;
 }
 
@@ -1436,7 +1437,7 @@ static mlv_status build_draw(mlv_context c, uint32_t count, uint32_t start, int3
     uint64_t avail = s.vb->size > s.vb_offset ? s.vb->size - s.vb_offset : 0;
     d.vertex_count = avail >= 32 ? (uint32_t)std::min<uint64_t>((avail - 32) / s.vb_stride + 1, 0xFFFFFFFFu) : 0;
     if (indexed) {
-        uint64_t nidx = (s.ib->size - s.ib_offset) / 4;
+        const uint64_t nidx = s.ib->size > s.ib_offset ? (s.ib->size - s.ib_offset) / 4 : 0;
         if ((uint64_t)start + count > nidx) return fail(MLV_ERROR_INVALID_ARG, "draw reads past the index buffer");
         d.ib = (const uint32_t *)(s.ib->ptr + s.ib_offset);
     } else {
