@@ -1270,21 +1270,24 @@ MLV_API mlv_status mlv_ps_set_shader(mlv_context c, mlv_pixel_shader_id s) {
 
 MLV_API mlv_status mlv_vs_set_constant_buffers(mlv_context c, uint32_t start, uint32_t n, const mlv_buffer *bufs) {
     if (!c || (n && !bufs)) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
-    if (start + n > MLV_CONSTANT_BUFFER_SLOT_COUNT) return fail(MLV_ERROR_INVALID_ARG, "slot out of range");
+    if (start > MLV_CONSTANT_BUFFER_SLOT_COUNT || n > MLV_CONSTANT_BUFFER_SLOT_COUNT - start)
+        return fail(MLV_ERROR_INVALID_ARG, "slot out of range");
     for (uint32_t i = 0; i < n; ++i) c->st.vs_cb[start + i] = bufs[i];
     return MLV_OK;
 }
 
 MLV_API mlv_status mlv_vs_set_shader_resources(mlv_context c, uint32_t start, uint32_t n, const mlv_texture2d *t) {
     if (!c || (n && !t)) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
-    if (start + n > MLV_SHADER_RESOURCE_SLOT_COUNT) return fail(MLV_ERROR_INVALID_ARG, "slot out of range");
+    if (start > MLV_SHADER_RESOURCE_SLOT_COUNT || n > MLV_SHADER_RESOURCE_SLOT_COUNT - start)
+        return fail(MLV_ERROR_INVALID_ARG, "slot out of range");
     for (uint32_t i = 0; i < n; ++i) c->st.vs_srv[start + i] = t[i];
     return MLV_OK;
 }
 
 MLV_API mlv_status mlv_ps_set_shader_resources(mlv_context c, uint32_t start, uint32_t n, const mlv_texture2d *t) {
     if (!c || (n && !t)) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
-    if (start + n > MLV_SHADER_RESOURCE_SLOT_COUNT) return fail(MLV_ERROR_INVALID_ARG, "slot out of range");
+    if (start > MLV_SHADER_RESOURCE_SLOT_COUNT || n > MLV_SHADER_RESOURCE_SLOT_COUNT - start)
+        return fail(MLV_ERROR_INVALID_ARG, "slot out of range");
     for (uint32_t i = 0; i < n; ++i) c->st.ps_srv[start + i] = t[i];
     return MLV_OK;
 }
@@ -1661,6 +1664,7 @@ static mlv_status run_list(mlv_context_t *c, mlv_command_list l, uint32_t seq, b
 MLV_API mlv_status mlv_execute_command_list(mlv_context c, mlv_command_list l) {
     MLV_TRY(need_immediate(c));
     if (!l) return fail(MLV_ERROR_INVALID_ARG, "list is NULL");
+    if (l->device != c->device) return fail(MLV_ERROR_INVALID_ARG, "the list was recorded for another device");
     MLV_TRY(set_device(c->device));
     const uint32_t seq = ++c->batch_seq;
     c->last_single = false;
