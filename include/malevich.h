@@ -386,7 +386,7 @@ MLV_API mlv_status mlv_get_tile_infos(mlv_context context, uint32_t *tile_index,
  * with the same positions. */
 typedef struct mlv_diff_desc {
     uint32_t n_verts, n_tris;
-    const uint32_t *index_buffer;     /* 3 * n_tris */
+    const uint32_t *index_buffer;     /* 3 * n_tris, each < n_verts (the kernels do not check) */
     const float *colors;              /* 3 * n_verts */
     const float *uvs;                 /* 2 * n_verts */
     const float *texture;             /* tex_height * tex_width * 4 */
