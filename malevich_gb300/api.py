@@ -232,6 +232,10 @@ class Context:
     def __init__(self, handle, device, deferred=False):
         self.handle, self.device, self.deferred = handle, device, deferred
         self.lib = load_library()
+        self._queued = []   # sources of queued uploads: alive until the context next synchronises
+
+    def _synchronised(self):
+        self._queued.clear()
 
     # state (Pipeline fields, source/main.c:109-115)
     def ia_set_index_buffer(self, buf, offset=0):
@@ -295,31 +299,38 @@ class Context:
 
     def finish(self):
         _check(self.lib.mlv_finish(self.handle))
+        self._synchronised()
 
     def read_texture(self, tex):
         dt, extra = _DTYPES[tex.format]
         out = np.empty((tex.height, tex.width) + extra, dt)
         _check(self.lib.mlv_read_texture2d(self.handle, tex.handle, _ptr(out), 0))
+        self._synchronised()
         return out
 
     def update_buffer(self, buf, data, offset=0):
         arr = np.ascontiguousarray(data)
         _check(self.lib.mlv_update_buffer(self.handle, buf.handle, offset, _ptr(arr), arr.nbytes))
+        self._synchronised()
 
     def update_texture(self, tex, data):
         arr = np.ascontiguousarray(data)
         _check(self.lib.mlv_update_texture2d(self.handle, tex.handle, _ptr(arr), 0))
+        self._synchronised()
 
     def update_buffer_async(self, buf, arr, offset=0):
-        """Queued upload: `arr` (C-contiguous) must stay unchanged until the next synchronisation."""
+        """Queued upload: `arr` (C-contiguous) must stay unchanged until the next synchronisation;
+        the context keeps a reference to it until then."""
         if not arr.flags["C_CONTIGUOUS"]:
             raise ValueError("update_buffer_async needs a C-contiguous array it can keep")
         _check(self.lib.mlv_update_buffer_async(self.handle, buf.handle, offset, _ptr(arr), arr.nbytes))
+        self._queued.append(arr)
 
     def update_texture_async(self, tex, arr):
         if not arr.flags["C_CONTIGUOUS"]:
             raise ValueError("update_texture_async needs a C-contiguous array it can keep")
         _check(self.lib.mlv_update_texture2d_async(self.handle, tex.handle, _ptr(arr), 0))
+        self._queued.append(arr)
 
     def finish_command_list(self):
         h = ctypes.c_void_p()
@@ -337,10 +348,12 @@ class Context:
     def stats(self):
         s = Stats()
         _check(self.lib.mlv_get_stats(self.handle, ctypes.byref(s)))
+        self._synchronised()
         return s.as_dict()
 
     def reset_stats(self):
         _check(self.lib.mlv_reset_stats(self.handle))
+        self._synchronised()
 
     def tuning(self):
         t = Tuning()
