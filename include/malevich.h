@@ -187,6 +187,8 @@ typedef struct mlv_per_frame_cb {
 
 /* Creates a device on CUDA device `cuda_ordinal` (the reference has one implicit global). */
 MLV_API mlv_status mlv_create_device(int cuda_ordinal, mlv_device *out_device);
+/* Waits for the immediate context's work and frees it. The device's buffers, textures, deferred
+ * contexts and command lists must be destroyed first (they refer to the device). */
 MLV_API mlv_status mlv_destroy_device(mlv_device device);
 /* The immediate context: draws execute as they are issued (main.c:1284-1296 calls
  * draw_indexed once per object). */
