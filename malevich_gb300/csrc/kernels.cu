@@ -964,9 +964,10 @@ __global__ void __launch_bounds__(kScatterBlock) k_scatter(BatchParams bp) {
             }
         }
         // triangles over more than big_tiles bins are filled by the whole warp, 32 (triangle, bin)
-        // pairs per round. Each big triangle normally starts a new round; when that leaves many
-        // rounds part-empty (triangles of a few dozen bins), the pairs of all of them are packed
-        // into as few rounds as they need instead.
+        // pairs per round. Each big triangle normally starts a new round (its pair count is padded
+        // to a multiple of 32 and the padding skipped); when that leaves many rounds part-empty
+        // (triangles of a few dozen bins), the pairs of all of them are packed into as few rounds
+        // as they need instead.
         const uint32_t nbig = nt_own > bp.big_tiles ? nt_own : 0u;
         const uint32_t bigmask = __ballot_sync(0xFFFFFFFFu, nbig != 0u);
         if (bigmask) {
