@@ -59,6 +59,9 @@ def parse():
                     help="--profile-once: the scene frame or the single draw (icosphere L5 at 1280x720)")
     ap.add_argument("--warps-per-tile", type=int, default=0,
                     help="--profile-once: this tile-kernel shape (1, 2, 4 or 8) instead of the default")
+    ap.add_argument("--port-vs-reference", action="store_true",
+                    help="with --impl reference: time the reference's own core and the oracle port on the same "
+                         "frame and threads (x86-64 only) and exit")
     ap.add_argument("--profile-diff-views", type=int, default=0,
                     help="run the differentiable loop's visibility pass, forward and adjoint once over this "
                          "many views of its 256x256 heightfield workload and exit (a short sequence for ncu)")
@@ -143,7 +146,8 @@ def ncu_traffic(kernel):
 
 
 def cpu_baseline(frame, frames):
-    """The oracle port of the reference's pipeline core, all host threads, on `frames` frames."""
+    """The oracle port of the reference's pipeline core, all host threads, on `frames` frames.
+    Returns the seconds per frame, the threads used and the last frame's output."""
     from oracle import pyoracle
     lib = pyoracle.oracle_lib()
     cores = os.cpu_count() or 1
@@ -154,14 +158,46 @@ def cpu_baseline(frame, frames):
     for _ in range(frames):
         out = pyoracle.render_oracle(frame)
     dt = (time.perf_counter() - t0) / frames
-    return dt, cores, out["stats"]
+    return dt, cores, out
+
+
+def unique_vertices(frame):
+    n = 0
+    for d in frame.draws:
+        n += len(np.unique(d.ib[d.start_index:d.start_index + d.index_count])) if d.ib is not None else d.index_count
+    return n
+
+
+def frame_bytes(frame, fragments):
+    """Algorithmic bytes of one frame, as the hot-path measurement plan defines them:
+    4 I (indices) + 32 V (each unique vertex's 32-byte input once) + per texture
+    min(its bytes, 4 taps x texel bytes x the fragments (pixel textures) or vertices (vertex
+    textures) that sample it) + 8 W H (colour and depth written once; the frame's clears are
+    folded into that write, so no target is read). Every datum the frame must touch, once."""
+    from malevich_gb300 import scenes
+    idx = sum(d.index_count for d in frame.draws)
+    verts = unique_vertices(frame)
+    texel = {scenes.FMT_RGBA8: 4, scenes.FMT_RGBA16F: 8, scenes.FMT_RGBA32F: 16}
+    tex, seen = 0, set()
+    for d in frame.draws:
+        # only the shaders that sample: vertex_lighting_vs; basic, env_lighting and colour x texel PS
+        vs_t = d.vs_tex if d.vs == scenes.VS_VERTEX_LIGHTING else None
+        ps_t = d.ps_tex if d.ps in (scenes.PS_BASIC, scenes.PS_ENV_LIGHTING, scenes.PS_COLOR_TIMES_TEXEL) else None
+        for t, users in ((ps_t, fragments), (vs_t, verts)):
+            if t is not None and id(t.data) not in seen:
+                seen.add(id(t.data))
+                tex += min(t.data.nbytes, 4 * texel[t.format] * users)
+    loaded = 0 if (frame.clear_color is not None and frame.clear_depth is not None) else 4 * frame.width * frame.height
+    return {"indices": 4 * idx, "vertices": 32 * verts, "textures": tex,
+            "targets": 8 * frame.width * frame.height + loaded}
 
 
 def algorithmic_bytes(frame, dev_stats, written_pixels):
-    """Algorithmic DRAM bytes of one launch of the two main kernels: every datum the kernel must
-    touch counted once (re-reads that caches serve are not algorithmic). Records are counted for
-    every assembled triangle, although those that cover no sample get none (3% of the scene
-    frame's): an overcount of about 1% of k_tile's bytes."""
+    """Bytes one launch of each of the two main kernels must move, counting the pipeline's own
+    intermediate records as well (unlike frame_bytes): every datum the kernel touches counted once
+    (re-reads that caches serve are not counted). Records are counted for every assembled
+    triangle, although those that cover no sample get none (3% of the scene frame's): an
+    overcount of about 1% of k_tile's bytes."""
     idx = sum(d.index_count for d in frame.draws) * 4
     uniq = 0
     for d in frame.draws:
@@ -336,8 +372,7 @@ def run_diff_sections(dev, args):
     fitting texture and vertex colours to a target rendered from a noise texture and colours."""
     import ctypes
     import torch
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    from diffrender import DiffScene, visibility
+    from malevich_gb300.diff import DiffScene, visibility
     from malevich_gb300 import api, scenes
     lib = api.load_library()
     stream = torch.cuda.current_stream()
@@ -484,8 +519,7 @@ def profile_diff(dev, views):
     loop's workload (256x256, 200k-triangle heightfield, 2048x2048 texture)."""
     import ctypes
     import torch
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    from diffrender import DiffScene
+    from malevich_gb300.diff import DiffScene
     from malevich_gb300 import api, scenes
     lib = api.load_library()
     sc = scenes.diff_scene(seed=5, n_views=views, size=256, tex_size=2048, heightfield_cells=316)
@@ -511,6 +545,50 @@ def profile_diff(dev, views):
     return {"views": views, "stats": st}
 
 
+# The oracle port against the reference's own core on one x86-64 host (the reference's core is AVX2
+# and builds only there), same frame, same threads: `python bench.py --impl reference
+# --port-vs-reference` on that host prints these figures again.
+PORT_VS_REFERENCE = {
+    "host": "Intel Xeon @ 2.70 GHz, 8 logical cores (x86-64 build host)",
+    "frame": "scene-scale frame, seed 2, 1,032,584 input triangles",
+    "threads_8": {"reference_s_per_frame": 0.4249, "port_s_per_frame": 0.1448, "reference_over_port": 2.93},
+    "threads_1": {"reference_s_per_frame": 0.9560, "port_s_per_frame": 0.8730, "reference_over_port": 1.10},
+    "reading": "the port is faster than the reference on the same host, so a GPU ratio against the port "
+               "understates the ratio against the reference",
+}
+
+
+def port_vs_reference(args):
+    """Times the reference's own core and the oracle port on the same frame and threads (x86-64 with
+    the reference built only), median of 7 frames after 2 warm-up frames each."""
+    import platform
+    from malevich_gb300 import scenes
+    from oracle import pyoracle
+    frame = scenes.config2_scene(seed=args.seed)
+    if platform.machine() not in ("x86_64", "AMD64") or not pyoracle.reference_available(frame.width, frame.height):
+        print(json.dumps({"port_vs_reference": "unavailable: the reference's core is built only on x86-64"}))
+        return 0
+    out = {"host_threads": os.cpu_count(), "frame_triangles": frame.input_triangles}
+    for th in (os.cpu_count() or 1, 1):
+        pyoracle.oracle_lib().orc_set_threads(th)
+
+        def timed(fn):
+            fn()
+            fn()
+            ts = []
+            for _ in range(7):
+                t0 = time.perf_counter()
+                fn()
+                ts.append(time.perf_counter() - t0)
+            return statistics.median(ts)
+        tr = timed(lambda: pyoracle.render_reference(frame, threads=th))
+        to = timed(lambda: pyoracle.render_oracle(frame))
+        out["threads_%d" % th] = {"reference_s_per_frame": round(tr, 4), "port_s_per_frame": round(to, 4),
+                                  "reference_over_port": round(tr / to, 3)}
+    print(json.dumps({"port_vs_reference": out}))
+    return 0
+
+
 def run_reference_arm(args, rank, world):
     """The reference's CPU implementation of the path on this host's cores, on the same frame: its
     own core (compiled from its sources into oracle/_ref, AVX2, x86-64 only) where it was built,
@@ -531,11 +609,11 @@ def run_reference_arm(args, rank, world):
         render = lambda: pyoracle.render_oracle(frame)["stats"]
         kind, note = "port", ("the reference's own core is AVX2 C and does not build on this host (%s); the "
                               "oracle port of it (oracle/oracle.c, OpenMP) runs instead" % platform.machine())
-    warmup = max(3, min(args.warmup, 5))
+    warmup = max(3, args.warmup)
     for _ in range(warmup):
         render()
     times, stats = [], None
-    for _ in range(max(1, min(args.steps, 5))):
+    for _ in range(max(1, args.steps)):
         t0 = time.perf_counter()
         stats = render()
         times.append(time.perf_counter() - t0)
@@ -552,6 +630,7 @@ def run_reference_arm(args, rank, world):
                          "sample": "%d full frames of the workload (median)" % len(times)},
         "e2e": {"value": round(value, 4), "unit": "Mtri/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": note,
+        "port_vs_reference": PORT_VS_REFERENCE,
     }
     if "fragments_written" in stats:
         line["gpix_per_s"] = round(stats["fragments_written"] / dt / 1e9, 6)
@@ -568,6 +647,8 @@ def main():
         import torch.distributed as dist
         torch.cuda.set_device(local)
         dist.init_process_group("nccl" if args.impl == "gb300" else "gloo")
+    if args.impl == "reference" and args.port_vs_reference:
+        return port_vs_reference(args) if rank == 0 else 0
     if args.impl == "reference":
         rc = run_reference_arm(args, rank, world)
         if dist:
@@ -641,7 +722,8 @@ def main():
     tris = frame.input_triangles
     value = replicas.total_units(tris, dist, "cuda") / (ms / 1e3) / 1e6   # every rank's frame
 
-    img = r.read(0)["depth"]
+    timed_out = r.read(0)
+    img, img_color = timed_out["depth"], timed_out["color"]
     r_img_written = int(np.count_nonzero(img != np.float32(frame.clear_depth)))
 
     # --- per-draw (immediate context, one launch sequence per draw), same flushing
@@ -743,13 +825,27 @@ def main():
         # fragments written (Gpix/s numerator) and the CPU baseline come from the oracle
         cpu = None
         fragments = None
+        outliers = None
         written_px = int((r_img_written) if r_img_written is not None else frame.width * frame.height)
         if not args.no_cpu_baseline:
-            dt, cores, ost = cpu_baseline(frame, args.cpu_sample_frames)
-            fragments = ost["fragments_written"]
+            dt, cores, oout = cpu_baseline(frame, args.cpu_sample_frames)
+            fragments = oout["stats"]["fragments_written"]
             cpu = {"value": round(tris / dt / 1e6, 4), "unit": "Mtri/s", "cores": cores, "kind": "port",
-                   "sample": "%d full frames of the workload" % args.cpu_sample_frames}
+                   "sample": "%d full frames of the workload" % args.cpu_sample_frames,
+                   "port_vs_reference": "on an x86-64 host with 8 threads the reference's own core took %.2fx "
+                                        "the port's time on this frame (see --port-vs-reference)"
+                                        % PORT_VS_REFERENCE["threads_8"]["reference_over_port"]}
+            # colour parity of the timed frame against the oracle: pixels beyond +-1 LSB
+            dc = np.abs(img_color.view(np.uint8).reshape(img_color.shape + (4,)).astype(np.int16) -
+                        oout["color"].view(np.uint8).reshape(oout["color"].shape + (4,)).astype(np.int16)).max(axis=-1)
+            nbad = int((dc > 1).sum())
+            outliers = {"against": "oracle", "pixels_beyond_1lsb": nbad, "pixels": int(dc.size),
+                        "fraction": round(nbad / dc.size, 7), "max_diff": int(dc.max()),
+                        "depth_bit_exact": bool(np.array_equal(img.view(np.uint32), oout["depth"].view(np.uint32)))}
         peak, peak_kind = measured_peaks()
+        fb = frame_bytes(frame, fragments if fragments is not None else written_px)
+        fbytes = sum(fb.values())
+        frame_achieved = fbytes / (ms / 1e3) / 1e9
         ab = algorithmic_bytes(frame, frame_stats, written_px)
         dominant = "k_tile" if stage_avg.get("tile", 0) >= stage_avg.get("geometry", 0) else "k_geometry"
         dur_ms = stage_avg["tile" if dominant == "k_tile" else "geometry"]
@@ -768,10 +864,18 @@ def main():
                          "batched_speedup": round(pd_ms / ms, 3)},
             "e2e": {"value": round(tris * world / e2e_s / 1e6, 3), "unit": "Mtri/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_s * 1e3, 3)},
-            "roofline": {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 1), "peak": peak,
-                         "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
-                         "algorithmic_bytes": int(ab[dominant]), "duration_ms": round(dur_ms, 4),
-                         "traffic": ncu_traffic(dominant)},
+            "roofline": {"bound": "hbm", "achieved": round(frame_achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(frame_achieved / peak, 4), "peak_kind": peak_kind,
+                         "counts": "the whole frame: 4 I + 32 V + sampled textures (capped at 4 taps per "
+                                   "fragment or vertex) + 8 W H, over ms_per_step",
+                         "algorithmic_bytes": int(fbytes), "bytes": {k: int(v) for k, v in fb.items()},
+                         "traffic": ncu_traffic("frame"),
+                         "kernel": {"name": dominant, "duration_ms": round(dur_ms, 4),
+                                    "counts": "the kernel's own inputs and outputs once, the pipeline's "
+                                              "intermediate records and bin lists included",
+                                    "bytes": int(ab[dominant]), "achieved": round(achieved, 1),
+                                    "frac": round(achieved / peak, 4), "traffic": ncu_traffic(dominant)}},
+            "colour_outliers": outliers,
             "stage_ms": {k: round(v, 4) for k, v in stage_avg.items()},
             "frame_stats": {k: int(v) for k, v in frame_stats.items()},
             "cpu_baseline": cpu,

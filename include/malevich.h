@@ -27,7 +27,7 @@ extern "C" {
 #define MLV_API
 #endif
 
-#define MLV_ABI_VERSION 2
+#define MLV_ABI_VERSION 3
 
 /* ------------------------------------------------------------------ status */
 
@@ -346,7 +346,18 @@ typedef struct mlv_tuning {
      * regrows the buffer and re-runs the batch, so these only trade memory for a re-run. */
     uint32_t initial_bin_entries;
     uint32_t initial_clip_fan_slots;
+    /* A batch of one draw with at most this many input triangles (and no triangle-id target and no
+     * TileInfo capture) takes the small-draw path: three kernels instead of five, no binning, the
+     * vertex shader run per index as the reference does. Same outputs; 0 disables it. */
+    uint32_t small_draw_triangles;
+    uint32_t debug_flags;             /* MLV_DEBUG_*: failure-detection tests only; 0 in normal use */
 } mlv_tuning;
+
+/* The bin scan's first block never publishes its prefix, so the bounded waits of the blocks after
+ * it run out: the batch writes nothing and the next synchronisation returns MLV_ERROR_TIMEOUT,
+ * after which the context works again. Takes effect on batches with more than 16,384 bins that
+ * use the binned path (a 1920x1080 target, for instance). */
+#define MLV_DEBUG_STALL_LOOKBACK 0x1u
 
 MLV_API mlv_status mlv_get_tuning(mlv_context context, mlv_tuning *out_tuning);
 MLV_API mlv_status mlv_set_tuning(mlv_context context, const mlv_tuning *tuning);
@@ -355,7 +366,9 @@ MLV_API mlv_status mlv_set_tuning(mlv_context context, const mlv_tuning *tuning)
  * When enabled, CUDA events bracket every stage on the context's stream; reading synchronises.
  * Stages: 0 clear, 1 geometry (IA + primitive assembly + bin count, and the vertex shader for
  * draws shaded per index), 2 bin scan, 3 bin scatter, 4 tile (raster+PS+OM), 5 vertex shading
- * (once per vertex). Times in milliseconds, summed since the last reset. */
+ * (once per vertex). On the small-draw path (mlv_tuning::small_draw_triangles) stage 1 is the
+ * raster kernel (vertex shader, setup and the small triangles' coverage and depth), 3 the queued
+ * large triangles and 4 the resolve (PS + OM). Times in milliseconds, summed since the last reset. */
 #define MLV_STAGE_COUNT 6
 MLV_API mlv_status mlv_set_profiling(mlv_context context, int enable);
 MLV_API mlv_status mlv_get_stage_times(mlv_context context, double *ms, uint64_t *launches);
@@ -415,7 +428,8 @@ MLV_API mlv_status mlv_om_set_primitive_id_target(mlv_context context, mlv_textu
  * rule is no allocation after start-up, or code issuing work while another component of the
  * process captures a CUDA graph, where an allocation would be captured or refused. The call draws
  * one indexed (or, with index_buffer NULL, non-indexed) draw into caller-owned device memory with
- * the same kernels and results as mlv_draw_indexed. Its scratch (triangle records, bins, lists,
+ * the same results as mlv_draw_indexed (any shader pairing, MLV_PS_NONE included; no visibility
+ * targets and the reference's fill rule and sample point). Its scratch (triangle records, bins, lists,
  * counters) is one static device array of MLV_NOALLOC_SCRATCH_BYTES that every GPU which loads
  * this library holds until the process exits; the call allocates nothing.
  *  - Limits: MLV_NOALLOC_MAX_TRIANGLES input triangles, MLV_NOALLOC_MAX_TILES 8x8 tiles in the
@@ -446,9 +460,14 @@ typedef struct mlv_noalloc_texture {
 } mlv_noalloc_texture;
 
 typedef struct mlv_noalloc_draw {
-    const void *vertex_buffer;   /* device pointer */
+    const void *vertex_buffer;   /* device pointer to vertex_count vertices: the first 32 bytes of
+                                    vertex vertex_count - 1, at (vertex_count - 1) * vertex_stride,
+                                    must lie inside the allocation */
     uint32_t vertex_stride, vertex_count;
     const uint32_t *index_buffer;/* device pointer, or NULL for implicit indices */
+    uint32_t index_buffer_count; /* 32-bit indices the index buffer holds; the call rejects
+                                    start_index + index_count > index_buffer_count with
+                                    MLV_ERROR_INVALID_ARG (ignored when index_buffer is NULL) */
     uint32_t index_count, start_index;
     int32_t base_vertex;
     mlv_vertex_shader_id vs;

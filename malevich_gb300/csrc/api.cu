@@ -37,6 +37,9 @@ cudaError_t launch_scan(const BatchParams &bp, cudaStream_t stream);
 cudaError_t launch_rank(const BatchParams &bp, cudaStream_t stream);
 cudaError_t launch_scatter(const BatchParams &bp, int num_sms, cudaStream_t stream);
 cudaError_t launch_tile(const BatchParams &bp, uint32_t warps, uint32_t warps_per_tile, cudaStream_t stream);
+cudaError_t launch_direct_raster(const BatchParams &bp, cudaStream_t stream);
+cudaError_t launch_direct_queue(const BatchParams &bp, int num_sms, cudaStream_t stream);
+cudaError_t launch_direct_resolve(const BatchParams &bp, cudaStream_t stream);
 }  // namespace mlv
 
 using namespace mlv;
@@ -77,6 +80,7 @@ struct mlv_device_t {
     int num_sms = 0;
     float clip_planes[6][4];
     mlv_context_t *immediate = nullptr;
+    std::vector<mlv_context_t *> deferred;   // live deferred contexts (guarded by mu)
     std::mutex mu;
     // bumped when a resource gets its upload event (first queued upload): captured command lists
     // re-capture, so that their graphs wait for it
@@ -188,6 +192,11 @@ struct Workspace {
     uint32_t fill_cap = 0;
     float4 *vs_out = nullptr;
     uint32_t vs_cap = 0;
+    // small-draw path: the view's per-pixel keys (zero between draws) and the large-triangle queue
+    unsigned long long *keys = nullptr;
+    uint32_t keys_cap = 0;
+    uint4 *queue = nullptr;
+    uint32_t queue_cap = 0;
     uint64_t generation = 0;
 };
 
@@ -214,6 +223,9 @@ struct PendingJob {
     uint32_t seq;
 };
 
+// Single draws of up to this many input triangles take the small-draw path by default.
+constexpr uint32_t kDefaultSmallDraw = 32768;
+
 struct mlv_context_t {
     mlv_device device = nullptr;
     bool deferred = false;
@@ -221,7 +233,7 @@ struct mlv_context_t {
     PipelineState st;
     std::vector<Segment> recorded;     // deferred contexts
     Workspace ws;
-    mlv_tuning tuning = {4, 1, 16, 128, 0, 0};   // measured defaults; the autotuner refines them
+    mlv_tuning tuning = {4, 1, 16, 128, 0, 0, kDefaultSmallDraw, 0};   // measured defaults; the autotuner refines them
     uint64_t tuning_generation = 0;    // bumped by mlv_set_tuning: captured graphs re-capture
     uint64_t host_stats[8] = {};       // vertex_count, input triangles, draws, batches, launches
     bool profiling = false;
@@ -279,15 +291,6 @@ static mlv_status set_device(mlv_device d) {
     return MLV_OK;
 }
 
-// screen_from_ndc, main.c:825-830, with the reference's mixed float/double arithmetic
-static void screen_from_ndc(const mlv_viewport &vp, float *m) {
-    float r[16] = {(float)(vp.width * 0.5), 0, 0, (float)(vp.width * 0.5 + vp.top_left_x),
-                   0, (float)(-vp.height * 0.5), 0, (float)(vp.height * 0.5 + vp.top_left_y),
-                   0, 0, vp.max_depth - vp.min_depth, vp.min_depth,
-                   0, 0, 0, 1};
-    memcpy(m, r, sizeof(r));
-}
-
 static TexDesc tex_desc(mlv_texture2d t) {
     TexDesc d = {};
     if (!t) return d;
@@ -325,6 +328,7 @@ static mlv_status ensure_fixed(mlv_context_t *c) {
 
 struct BatchSizes {
     uint64_t tris = 0, overflow = 0, bins = 0, tiles = 0, draws = 0, views = 0, vertices = 0;
+    uint64_t direct_pixels = 0;   // small-draw path: the view's pixels (one key each)
     bool shade = false;   // some draw has a pixel shader: the 80-byte shading records are needed
 };
 
@@ -418,6 +422,13 @@ static mlv_status ensure_workspace(mlv_context_t *c, const BatchSizes &s, bool k
         MLV_TRY(grow(&w.vs_out, w.vs_cap, s.vertices * 3, sizeof(float4)));
         if (before != w.vs_out) changed = true;
     }
+    if (s.direct_pixels) {
+        unsigned long long *before = w.keys;
+        MLV_TRY(grow(&w.keys, w.keys_cap, s.direct_pixels, sizeof(unsigned long long), true));
+        uint4 *qb = w.queue;
+        MLV_TRY(grow(&w.queue, w.queue_cap, std::max<uint64_t>(s.tris, 16384), sizeof(uint4)));
+        if (before != w.keys || qb != w.queue) changed = true;
+    }
     {
         DrawDesc *b1 = w.d_draws;
         ViewDesc *b2 = w.d_views;
@@ -435,6 +446,7 @@ struct Plan {
     std::vector<DrawDesc> draws;
     std::vector<ViewDesc> views;
     BatchSizes sizes;
+    bool direct = false;   // the small-draw path (one draw, no binning)
     std::unordered_set<mlv_texture2d> folded;   // cleared targets the tile kernel clears itself
     // upload events of the batch's inputs, waited for before the stage that first reads them
     std::vector<cudaEvent_t> wait_vertex, wait_index, wait_pixel;
@@ -482,7 +494,16 @@ static void fold_clears(const Segment &seg, const Groups &groups, Plan &p) {
     }
 }
 
-static mlv_status plan_segment(const Segment &seg, Plan &p, uint32_t fan_slots_hint = 0) {
+// Whether a planned batch takes the small-draw path: one draw of at most `small_draw` input
+// triangles, with no triangle-id target and no TileInfo capture (both need the binned path's ranks
+// and lists). The outputs are the same either way.
+static bool plan_is_direct(const Plan &p, uint32_t small_draw, bool capture) {
+    return p.draws.size() == 1 && p.views.size() == 1 && p.draws[0].tri_count > 0 &&
+           p.draws[0].tri_count <= small_draw && !capture && p.views[0].vis_tri == nullptr;
+}
+
+static mlv_status plan_segment(const Segment &seg, Plan &p, uint32_t fan_slots_hint = 0, uint32_t small_draw = 0,
+                               bool capture = false) {
     p.draws.clear();
     p.views.clear();
     p.folded.clear();
@@ -538,8 +559,7 @@ static mlv_status plan_segment(const Segment &seg, Plan &p, uint32_t fan_slots_h
             tri += d.tri_count;
             // shade each vertex once when the draw references most of its buffer; a draw that
             // touches a small part of a large buffer keeps per-index shading
-            d.vs_cached = (d.ib != nullptr && d.vertex_count > 0 && d.tri_count > 0 &&
-                           (uint64_t)d.vertex_count <= 2ull * 3ull * d.tri_count) ? 1u : 0u;
+            d.vs_cached = host_shade_once(d.ib, d.vertex_count, d.tri_count) ? 1u : 0u;
             d.vs_base = (uint32_t)verts;
             d.vs_count = d.vs_cached ? d.vertex_count : 0u;
             verts += d.vs_count;
@@ -565,6 +585,15 @@ static mlv_status plan_segment(const Segment &seg, Plan &p, uint32_t fan_slots_h
     // shading records: for pixel shaders, and for the draw index of a view with several draws
     for (const DrawDesc &d : p.draws)
         p.sizes.shade = p.sizes.shade || d.ps != kPsNone || (d.raster_flags & kDrawSharesView);
+    p.direct = plan_is_direct(p, small_draw, capture);
+    if (p.direct) {
+        // the vertex shader runs per index inside the raster kernel (main.c:698-734's way)
+        DrawDesc &d = p.draws[0];
+        d.vs_cached = 0;
+        d.vs_count = 0;
+        p.sizes.vertices = 0;
+        p.sizes.direct_pixels = (uint64_t)p.views[0].width * p.views[0].height;
+    }
     return MLV_OK;
 }
 
@@ -697,6 +726,10 @@ static mlv_status launch_draws(mlv_context_t *c, const Plan &p, DrawDesc *d_draw
     bp.counters = w.counters;
     bp.stats = w.stats;
     bp.error = w.error;
+    bp.debug_flags = c->tuning.debug_flags;
+    bp.keys = w.keys;
+    bp.queue = w.queue;
+    bp.queue_capacity = w.queue_cap;
     c->host_stats[3] += 1;
     if (bp.total_tris == 0) return MLV_OK;   // nothing to assemble: no kernel has work
     // waits on queued uploads (inside a graph capture: external event waits, evaluated at launch)
@@ -711,6 +744,24 @@ static mlv_status launch_draws(mlv_context_t *c, const Plan &p, DrawDesc *d_draw
     // the clip-fan slot counter starts at zero for every batch (reset before the first kernel, so
     // that the batch's kernels follow one another directly)
     CUDA_TRY(cudaMemsetAsync(w.counters + kCtrOverflow, 0, 2 * sizeof(uint32_t), c->stream));
+    if (p.direct) {
+        // the small-draw path: raster (vertex shader, setup, small triangles), queued large
+        // triangles, resolve; stages 1, 3 and 4 of the stage timers
+        CUDA_TRY(wait_for(p.wait_vertex));
+        CUDA_TRY(wait_for(p.wait_index));
+        ev_begin(c, 1, &e);
+        CUDA_TRY(launch_direct_raster(bp, c->stream));
+        ev_end(c, e);
+        ev_begin(c, 3, &e);
+        CUDA_TRY(launch_direct_queue(bp, c->device->num_sms, c->stream));
+        ev_end(c, e);
+        CUDA_TRY(wait_for(p.wait_pixel));
+        ev_begin(c, 4, &e);
+        CUDA_TRY(launch_direct_resolve(bp, c->stream));
+        ev_end(c, e);
+        c->host_stats[4] += 3;
+        return MLV_OK;
+    }
     CUDA_TRY(wait_for(p.wait_vertex));
     if (bp.total_vertices) {
         ev_begin(c, 5, &e);
@@ -743,7 +794,7 @@ static mlv_status launch_draws(mlv_context_t *c, const Plan &p, DrawDesc *d_draw
 static mlv_status execute_segment_eager(mlv_context_t *c, const Segment &seg, uint32_t seq, bool rerun = false) {
     if (seg.draws.empty()) return run_clears(c, seg);
     Plan p;
-    MLV_TRY(plan_segment(seg, p, c->tuning.initial_clip_fan_slots));
+    MLV_TRY(plan_segment(seg, p, c->tuning.initial_clip_fan_slots, c->tuning.small_draw_triangles, c->capture_infos));
     {
         std::vector<FillJob> jobs;
         const uint32_t chunks = build_fills(seg, jobs, &p.folded);
@@ -806,6 +857,7 @@ static mlv_status check_and_recover(mlv_context_t *c, bool fetched = false, bool
         if (err & kErrLookbackTimeout) {
             MLV_TRY(reset_error_words(c->ws));
             CUDA_TRY(cudaMemset(c->ws.bin_count, 0, sizeof(uint32_t) * c->ws.bin_cap));
+            if (c->ws.keys) CUDA_TRY(cudaMemset(c->ws.keys, 0, sizeof(unsigned long long) * c->ws.keys_cap));
             MLV_TRY(reset_scan_state(c->ws));
             c->pending.clear();
             return fail(MLV_ERROR_TIMEOUT, "a bounded device-side wait gave up (decoupled look-back)");
@@ -813,7 +865,14 @@ static mlv_status check_and_recover(mlv_context_t *c, bool fetched = false, bool
         // regrow: records from the device's assembled count, list from the reported entry count
         const uint32_t need_list = c->h_error[3];
         const uint32_t need_fans = c->h_error[4];
+        const uint32_t need_queue = c->h_error[5];
         Workspace &w = c->ws;
+        if ((err & kErrQueueOverflow) && need_queue > w.queue_cap) {
+            uint32_t cap = w.queue_cap;
+            MLV_TRY(grow(&w.queue, cap, (uint64_t)need_queue + need_queue / 4 + 1024, sizeof(uint4)));
+            w.queue_cap = cap;
+            ++w.generation;
+        }
         if (err & kErrRecordOverflow) {
             // the clip-fan region must hold `need_fans` slots beyond the input triangles
             BatchSizes s;
@@ -834,6 +893,7 @@ static mlv_status check_and_recover(mlv_context_t *c, bool fetched = false, bool
         // statistics, which the re-run stages again)
         CUDA_TRY(cudaMemset(w.stats, 0, sizeof(unsigned long long) * kStatTotal));
         CUDA_TRY(cudaMemset(w.bin_count, 0, sizeof(uint32_t) * w.bin_cap));
+        if (w.keys) CUDA_TRY(cudaMemset(w.keys, 0, sizeof(unsigned long long) * w.keys_cap));
         MLV_TRY(reset_scan_state(w));
         MLV_TRY(reset_error_words(w));
         // Jobs before the first failing batch completed; from it on every kernel that writes a
@@ -895,15 +955,7 @@ MLV_API mlv_status mlv_create_device(int ordinal, mlv_device *out) {
     auto *d = new mlv_device_t();
     d->ordinal = ordinal;
     cudaDeviceGetAttribute(&d->num_sms, cudaDevAttrMultiProcessorCount, ordinal);
-    // the clipper's plane normals: v4f32_normalize (math.h:267-270) of the six planes of
-    // main.c:652-657, evaluated with the reference's float/double mix
-    static const float raw[6][4] = {{1, 0, 0, 1}, {-1, 0, 0, 1}, {0, 1, 0, 1}, {0, -1, 0, 1}, {0, 0, 1, 1}, {0, 0, -1, 1}};
-    for (int p = 0; p < 6; ++p) {
-        float dot = raw[p][0] * raw[p][0] + raw[p][1] * raw[p][1] + raw[p][2] * raw[p][2] + raw[p][3] * raw[p][3];
-        float len = (float)sqrt((double)dot);
-        float inv = (float)(1.0 / (double)len);
-        for (int k = 0; k < 4; ++k) d->clip_planes[p][k] = raw[p][k] * inv;
-    }
+    host_clip_planes(d->clip_planes);
     set_clip_planes(d->clip_planes, 0);
     cudaError_t e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
@@ -927,6 +979,7 @@ static void free_workspace(Workspace &w) {
     cudaFree(w.bin_count); cudaFree(w.bin_start); cudaFree(w.list); cudaFree(w.info_mask);
     cudaFree(w.scan_status); cudaFree(w.scan_status2); cudaFree(w.counters); cudaFree(w.stats);
     cudaFree(w.error); cudaFree(w.d_draws); cudaFree(w.d_views); cudaFree(w.d_fills); cudaFree(w.vs_out);
+    cudaFree(w.keys); cudaFree(w.queue);
     w = Workspace();
 }
 
@@ -967,6 +1020,10 @@ MLV_API mlv_status mlv_create_deferred_context(mlv_device d, mlv_context *out) {
     auto *c = new mlv_context_t();
     c->device = d;
     c->deferred = true;
+    {
+        std::lock_guard<std::mutex> lock(d->mu);
+        d->deferred.push_back(c);
+    }
     *out = c;
     return MLV_OK;
 }
@@ -974,8 +1031,30 @@ MLV_API mlv_status mlv_create_deferred_context(mlv_device d, mlv_context *out) {
 MLV_API mlv_status mlv_destroy_context(mlv_context c) {
     if (!c) return fail(MLV_ERROR_INVALID_ARG, "context is NULL");
     if (!c->deferred) return fail(MLV_ERROR_INVALID_ARG, "the immediate context is owned by its device");
+    {
+        std::lock_guard<std::mutex> lock(c->device->mu);
+        auto &v = c->device->deferred;
+        v.erase(std::remove(v.begin(), v.end(), c), v.end());
+    }
     delete c;
     return MLV_OK;
+}
+
+// A destroyed resource is unbound from every context of its device (as Direct3D 11 keeps bound
+// views alive, a later state check or draw must not reach freed memory through the binding).
+static void unbind_everywhere(mlv_device d, const void *res) {
+    auto unbind = [res](PipelineState &st) {
+        if (st.ib == res) st.ib = nullptr;
+        if (st.vb == res) st.vb = nullptr;
+        for (auto &b : st.vs_cb) if (b == res) b = nullptr;
+        for (auto &t : st.vs_srv) if (t == res) t = nullptr;
+        for (auto &t : st.ps_srv) if (t == res) t = nullptr;
+        for (mlv_texture2d *t : {&st.rtv, &st.dsv, &st.vis_tri, &st.vis_draw, &st.vis_bary, &st.vis_prim})
+            if (*t == res) *t = nullptr;
+    };
+    std::lock_guard<std::mutex> lock(d->mu);
+    if (d->immediate) unbind(d->immediate->st);
+    for (mlv_context_t *c : d->deferred) unbind(c->st);
 }
 
 MLV_API mlv_status mlv_create_buffer(mlv_device d, const mlv_buffer_desc *desc, const void *init, mlv_buffer *out) {
@@ -1012,6 +1091,7 @@ MLV_API mlv_status mlv_destroy_buffer(mlv_buffer b) {
         if (b->device->immediate->copy_stream) cudaStreamSynchronize(b->device->immediate->copy_stream);
         cudaStreamSynchronize(b->device->immediate->stream);
     }
+    unbind_everywhere(b->device, b);
     cudaFree(b->ptr);
     if (b->ready) cudaEventDestroy(b->ready);
     delete b;
@@ -1108,6 +1188,7 @@ MLV_API mlv_status mlv_destroy_texture2d(mlv_texture2d t) {
         if (t->device->immediate->copy_stream) cudaStreamSynchronize(t->device->immediate->copy_stream);
         cudaStreamSynchronize(t->device->immediate->stream);
     }
+    unbind_everywhere(t->device, t);
     if (t->owns_memory) cudaFree(t->ptr);
     cudaFree(t->tile_min);
     cudaFree(t->tile_max);
@@ -1461,7 +1542,7 @@ static mlv_status build_draw(mlv_context c, uint32_t count, uint32_t start, int3
             return fail(MLV_ERROR_INVALID_STATE, "VS constant buffer 0 must hold a 192-byte PerFrameCB");
     }
     if (cb && !cb->shadow.empty()) memcpy(d.cb, cb->shadow.data(), std::min(sizeof(d.cb), cb->shadow.size()));
-    screen_from_ndc(vp, d.screen_from_ndc);
+    host_screen_from_ndc(vp, d.screen_from_ndc);
     d.vp_w = (int32_t)vp.width;
     d.vp_h = (int32_t)vp.height;
     mlv_texture2d vt = s.vs_srv[0], pt = s.ps_srv[0];
@@ -1584,8 +1665,10 @@ static mlv_status run_list(mlv_context_t *c, mlv_command_list l, uint32_t seq, b
     BatchSizes maxs;
     size_t nd = 0, nv = 0;
     for (size_t i = 0; i < l->segments.size(); ++i) {
-        MLV_TRY(plan_segment(l->segments[i], plans[i], c->tuning.initial_clip_fan_slots));
+        MLV_TRY(plan_segment(l->segments[i], plans[i], c->tuning.initial_clip_fan_slots,
+                             c->tuning.small_draw_triangles, c->capture_infos));
         const BatchSizes &s = plans[i].sizes;
+        maxs.direct_pixels = std::max(maxs.direct_pixels, s.direct_pixels);
         maxs.tris = std::max(maxs.tris, s.tris);
         maxs.overflow = std::max(maxs.overflow, s.overflow);
         maxs.bins = std::max(maxs.bins, s.bins);
@@ -1765,6 +1848,7 @@ MLV_API mlv_status mlv_set_tuning(mlv_context c, const mlv_tuning *t) {
     if (t->geometry_block != 128 && t->geometry_block != 256 && t->geometry_block != 512)
         return fail(MLV_ERROR_INVALID_ARG, "geometry_block must be 128, 256 or 512");
     if (t->big_triangle_tiles < 1) return fail(MLV_ERROR_INVALID_ARG, "big_triangle_tiles must be >= 1");
+    if (t->debug_flags & ~(uint32_t)MLV_DEBUG_STALL_LOOKBACK) return fail(MLV_ERROR_INVALID_ARG, "unknown debug flag");
     if (memcmp(&c->tuning, t, sizeof(*t)) != 0) ++c->tuning_generation;
     c->tuning = *t;
     return MLV_OK;

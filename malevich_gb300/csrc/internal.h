@@ -1,7 +1,11 @@
 // Internal data layout shared by the host runtime (api.cu) and the kernels (kernels.cu).
 #pragma once
+#include <cmath>
 #include <cstdint>
+#include <cstring>
 #include <vector_types.h>
+
+#include "malevich.h"
 
 namespace mlv {
 
@@ -23,7 +27,11 @@ enum : uint32_t {
     kErrListOverflow = 1u << 2,
     kErrBigOverflow = 1u << 3,
     kErrBadIndex = 1u << 4,
+    kErrQueueOverflow = 1u << 5,         // small-draw path: more large-triangle chunks than the queue holds
 };
+
+// Debug flags (mlv_tuning::debug_flags, MLV_DEBUG_*), for failure-detection tests only.
+constexpr uint32_t kDebugStallLookback = 1u;
 
 struct TexDesc {
     const void *data;
@@ -154,12 +162,19 @@ struct BatchParams {
     uint32_t *counters;                  // see Counter
     unsigned long long *stats;           // device statistics, see StatSlot
     uint32_t *error;                     // [0] error bits, [1] first failing batch, [2] warnings,
-                                         // [3] bin entries needed, [4] clip-fan slots needed
+                                         // [3] bin entries needed, [4] clip-fan slots needed,
+                                         // [5] queue entries needed (small-draw path)
+    uint32_t debug_flags;                // kDebug* (tests only)
+    // small-draw path (one draw, no binning): per-pixel (depth, order) keys of the view, all zero
+    // between draws; queued chunks of large triangles' pixel blocks
+    unsigned long long *keys;            // [view width * height]
+    uint4 *queue;                        // [queue_capacity]: key, record slot, first block, blocks
+    uint32_t queue_capacity;
 };
 
 enum Counter : int {
     kCtrRankTicket = 0, kCtrRankDone, kCtrRankEpoch,
-    kCtrOverflow, kCtrReserved,          // per-batch: clip-fan slots used; unused
+    kCtrOverflow, kCtrQueue,             // per-batch: clip-fan slots used; small-draw queue entries used
     kCtrScanTicket, kCtrScanDone, kCtrScanEpoch,
     kCtrCount = 16
 };
@@ -171,5 +186,38 @@ enum Counter : int {
 enum StatSlot : int {
     kStatAssembled = 0, kStatActiveBins, kStatBinEntries, kStatTotal = 4, kStatCount = 8
 };
+
+// ------------------------------------------------------------------ host-side draw set-up
+// Shared by mlv_draw_indexed (api.cu) and mlv_draw_indexed_noalloc (noalloc.cu): both must plan a
+// draw identically for their results to agree bit for bit.
+
+// screen_from_ndc, main.c:825-830, with the reference's mixed float/double arithmetic.
+inline void host_screen_from_ndc(const mlv_viewport &vp, float *m) {
+    const float r[16] = {(float)(vp.width * 0.5), 0, 0, (float)(vp.width * 0.5 + vp.top_left_x),
+                         0, (float)(-vp.height * 0.5), 0, (float)(vp.height * 0.5 + vp.top_left_y),
+                         0, 0, vp.max_depth - vp.min_depth, vp.min_depth,
+                         0, 0, 0, 1};
+    memcpy(m, r, sizeof(r));
+}
+
+// The clipper's plane normals: v4f32_normalize (math.h:267-270) of the six planes of
+// main.c:652-657, evaluated with the reference's float/double mix.
+inline void host_clip_planes(float planes[6][4]) {
+    static const float raw[6][4] = {{1, 0, 0, 1}, {-1, 0, 0, 1}, {0, 1, 0, 1}, {0, -1, 0, 1}, {0, 0, 1, 1}, {0, 0, -1, 1}};
+    for (int p = 0; p < 6; ++p) {
+        const float dot = raw[p][0] * raw[p][0] + raw[p][1] * raw[p][1] + raw[p][2] * raw[p][2] + raw[p][3] * raw[p][3];
+        const float len = (float)std::sqrt((double)dot);
+        const float inv = (float)(1.0 / (double)len);
+        for (int k = 0; k < 4; ++k) planes[p][k] = raw[p][k] * inv;
+    }
+}
+
+// Whether a draw's vertices are shaded once each (k_vertex) rather than once per index (the
+// reference's way, main.c:673): when it is indexed and references most of its buffer. The outputs
+// are identical either way; this only decides where the work goes.
+inline bool host_shade_once(const void *index_buffer, uint32_t vertex_count, uint32_t tri_count) {
+    return index_buffer != nullptr && vertex_count > 0 && tri_count > 0 &&
+           (uint64_t)vertex_count <= 2ull * 3ull * tri_count;
+}
 
 }  // namespace mlv

@@ -254,15 +254,25 @@ __device__ __forceinline__ bool setup_triangle(const DrawDesc &d, const Vtx &v0,
     return true;
 }
 
-__device__ __forceinline__ void write_record(const BatchParams &bp, uint32_t rec, uint32_t draw, int ps,
-                                             bool sole_draw, const Setup &s, const Vtx &v0, const Vtx &v1,
-                                             const Vtx &v2, uint32_t extra = 0) {
-    int4 *r = bp.raster[rec].w;
+// The raster record's four words (TriRaster) of a set-up triangle.
+__device__ __forceinline__ void raster_words(const Setup &s, int4 *r) {
     r[0] = make_int4(s.e[0], s.e[1], s.e[2], s.e[3]);
     r[1] = make_int4(s.e[4], s.e[5], s.e[6], s.e[7]);
     r[2] = make_int4(s.e[8], __float_as_int(s.inv_area), __float_as_int(s.zbound), __float_as_int(s.ss[0][2]));
     r[3] = make_int4(__float_as_int(s.ss[1][2]), __float_as_int(s.ss[2][2]),
                      (s.tminx & 0xFFFF) | (s.tminy << 16), (s.tmaxx & 0xFFFF) | (s.tmaxy << 16));
+}
+
+__device__ __forceinline__ void write_record(const BatchParams &bp, uint32_t rec, uint32_t draw, int ps,
+                                             bool sole_draw, const Setup &s, const Vtx &v0, const Vtx &v1,
+                                             const Vtx &v2, uint32_t extra = 0) {
+    int4 w[4];
+    raster_words(s, w);
+    int4 *r = bp.raster[rec].w;
+    r[0] = w[0];
+    r[1] = w[1];
+    r[2] = w[2];
+    r[3] = w[3];
     if (bp.geom) {
         TriGeom &g = bp.geom[rec];
 #pragma unroll
@@ -738,7 +748,10 @@ __global__ void __launch_bounds__(kScanBlock) k_scan(BatchParams bp) {
     uint32_t total;
     uint32_t excl = block_exclusive_scan<kScanBlock>(sum, s_warp, total);
     if (threadIdx.x < 32) {
-        const uint32_t p = lookback_warp(bp.scan_status2, bid, s_epoch, total, bp.error);
+        // failure-detection tests (kDebugStallLookback): block 0 never publishes its prefix, so the
+        // bounded waits of the blocks after it run out (error bit set, they publish and go on)
+        const bool stall = bid == 0 && (bp.debug_flags & kDebugStallLookback);
+        const uint32_t p = stall ? 0u : lookback_warp(bp.scan_status2, bid, s_epoch, total, bp.error);
         if (threadIdx.x == 0) s_prefix = p;
     }
     __syncthreads();
@@ -1568,6 +1581,414 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_tile_coop(BatchParam
     pdl_trigger();
 }
 
+// ------------------------------------------------------------------ small-draw path
+//
+// A batch of one draw with few triangles (a single mesh: the plain single draw) runs as three
+// kernels instead of five, with no binning:
+//   k_direct_raster   vertex shader per index (as main.c:698-734 does), primitive assembly, clipping
+//                     and setup of 32 input triangles per CTA, then the CTA's 4 warps rasterise
+//                     those triangles over the 8x8 tiles of their sample boxes (two pixels a lane):
+//                     hierarchical Z per (tile, triangle) against the draw-start snapshot
+//                     (main.c:1005-1010), coverage (main.c:1015-1028), quantised depth
+//                     (main.c:1092-1102, 1131-1132) and the test against the draw-start depth
+//                     (main.c:1164-1168), each passing fragment folded into its pixel's 64-bit key
+//                     (depth, order) with a global atomic max (see below). Triangles over more than
+//                     4 tiles and clip fans go to a queue in chunks of 4 tiles.
+//   k_direct_queue    the queued chunks, spread over the whole GPU.
+//   k_direct_resolve  one warp per 8x8 tile: the winners' pixel shader and output merger, colour and
+//                     depth written once (main.c:1046-1189), hierarchical Z from the new depths
+//                     (write_tile, main.c:589-603), folded clears, and the keys reset to zero.
+// The per-pixel result is the same fold the tile kernel computes per draw (see the top of this
+// file), so outputs are bit-identical to the binned path. The keys live in one array per view, all
+// zero between draws: GREATER_EQUAL keeps the maximum of (depth_key << 32 | order); LESS keeps the
+// minimum, stored complemented so that both are a maximum over values that are never zero for a
+// fragment that passed (0 = no fragment). The reference's binner statistics come from the
+// triangles' bin rectangles: entries are summed, and every binned tile is marked in bin_count (one
+// word per tile for a single draw), which the resolve counts, uses to skip empty tiles, and clears.
+constexpr int kDirectBlock = 128;              // 4 warps
+constexpr int kDirectWarps = kDirectBlock / 32;
+constexpr int kDirectTris = 32;                // input triangles per CTA
+constexpr uint32_t kDirectLocalTiles = 4;      // jobs over more 8x8 tiles are queued
+constexpr uint32_t kDirectChunk = 4;           // tiles per queue entry
+constexpr int kDirectListCap = 64;             // per CTA: queued jobs and marked rectangles
+
+// A rasterisation job: one emitted triangle's coverage and depth parameters, from its raster
+// record (TriRaster) and order key.
+struct DirectJob {
+    uint32_t A[3], B[3], C[3];        // E(x, y) = A x + B y + C, A = a << 4, B = b << 4 (wrapping:
+                                      // the reference's ((a x) << 4) + ((b y) << 4) + c, main.c:1015-1025)
+    float inv_area, z0, dz1, dz2;     // quantised barycentrics and depth (main.c:1092-1102, 1131-1132)
+    float zbound;                     // depth bound for hierarchical Z (main.c:871)
+    uint32_t key, bias;               // order key; top-left bias bits (edge k needs E >= 1)
+    int32_t x0, y0, x1, y1;           // sample box
+    uint32_t tx0, ty0, ntx, nty;      // the 8x8 tiles it spans
+};
+
+__device__ __forceinline__ DirectJob direct_job(const int4 w0, const int4 w1, const int4 w2, const int4 w3,
+                                                uint32_t key) {
+    DirectJob J;
+    const uint32_t a0 = w0.x, b0 = w0.y, a1 = w0.w, b1 = w1.x, a2 = w1.z, b2 = w1.w;
+    J.A[0] = a0 << kSubpix; J.B[0] = b0 << kSubpix; J.C[0] = (uint32_t)w0.z;
+    J.A[1] = a1 << kSubpix; J.B[1] = b1 << kSubpix; J.C[1] = (uint32_t)w1.y;
+    J.A[2] = a2 << kSubpix; J.B[2] = b2 << kSubpix; J.C[2] = (uint32_t)w2.x;
+    J.inv_area = __int_as_float(w2.y);
+    J.z0 = __int_as_float(w2.w);
+    J.dz1 = __int_as_float(w3.x) - J.z0;
+    J.dz2 = __int_as_float(w3.y) - J.z0;
+    J.zbound = __int_as_float(w2.z);
+    J.key = key;
+    J.bias = ((int32_t)a0 > 0 || (a0 == 0 && (int32_t)b0 > 0) ? 0u : 1u) |
+             ((int32_t)a1 > 0 || (a1 == 0 && (int32_t)b1 > 0) ? 0u : 2u) |
+             ((int32_t)a2 > 0 || (a2 == 0 && (int32_t)b2 > 0) ? 0u : 4u);
+    J.x0 = (int16_t)(w3.z & 0xFFFF); J.y0 = w3.z >> 16;
+    J.x1 = (int16_t)(w3.w & 0xFFFF); J.y1 = w3.w >> 16;
+    J.tx0 = (uint32_t)J.x0 >> 3; J.ty0 = (uint32_t)J.y0 >> 3;
+    J.ntx = ((uint32_t)J.x1 >> 3) - J.tx0 + 1;
+    J.nty = ((uint32_t)J.y1 >> 3) - J.ty0 + 1;
+    return J;
+}
+
+// One covered-sample candidate: coverage (main.c:1028, or the top-left rule), quantised depth, the
+// test against the draw-start depth (main.c:1164-1168), and the fold into the pixel's key.
+__device__ __forceinline__ void direct_pixel(const ViewDesc &V, const DirectJob &J, uint32_t x, uint32_t y, uint32_t E0,
+                                             uint32_t E1, uint32_t E2, bool less, bool top_left, bool depth_cleared,
+                                             unsigned long long *keys) {
+    const bool covered = top_left ? (int32_t)((E0 - (J.bias & 1u)) | (E1 - ((J.bias >> 1) & 1u)) |
+                                              (E2 - ((J.bias >> 2) & 1u))) >= 0
+                                  : (int32_t)(E0 | E1 | E2) > 0;
+    if (!covered) return;
+    const float bb1 = (float)((int32_t)E1 >> (kSubpix * 2)) * J.inv_area;
+    const float bb2 = (float)((int32_t)E2 >> (kSubpix * 2)) * J.inv_area;
+    float z = J.z0 + J.dz1 * bb1;
+    z = z + J.dz2 * bb2;
+    const size_t o = (size_t)y * V.width + x;
+    const float dstart = depth_cleared ? V.clear_depth : V.depth[o];
+    if (!(less ? (z < dstart) : (z >= dstart))) return;
+    const unsigned long long k = ((unsigned long long)depth_key(z) << 32) | J.key;
+    atomicMax(keys + o, less ? ~k : k);
+}
+
+// One 8x8 tile (tx, ty) of a job: lane owns pixel (lane & 7, lane >> 3) and the one 4 rows below.
+__device__ __forceinline__ void direct_tile(const ViewDesc &V, const DirectJob &J, uint32_t tx, uint32_t ty, bool less,
+                                            bool top_left, bool depth_cleared, unsigned long long *keys, int lane) {
+    // hierarchical Z per (tile, triangle) against the draw-start snapshot (main.c:1005-1010; the
+    // mirrored maximum for LESS); a depth clear folded into this batch resets it (main.c:1212-1214)
+    const uint32_t tile = ty * V.tiles_x + tx;
+    const float hiz = depth_cleared ? (less ? 1.0f : 0.0f) : (less ? V.tile_max[tile] : V.tile_min[tile]);
+    if (less ? (J.zbound > hiz) : (J.zbound < hiz)) return;   // uniform over the warp
+    const int32_t px = (int32_t)(tx * 8 + (lane & 7)), pya = (int32_t)(ty * 8 + (lane >> 3)), pyb = pya + 4;
+    const bool in_x = px >= J.x0 && px <= J.x1;
+    const bool ina = in_x && pya >= J.y0 && pya <= J.y1, inb = in_x && pyb >= J.y0 && pyb <= J.y1;
+    const uint32_t ux = (uint32_t)px, uy = (uint32_t)pya;
+    const uint32_t E0 = J.A[0] * ux + J.B[0] * uy + J.C[0];
+    const uint32_t E1 = J.A[1] * ux + J.B[1] * uy + J.C[1];
+    const uint32_t E2 = J.A[2] * ux + J.B[2] * uy + J.C[2];
+    if (ina) direct_pixel(V, J, ux, uy, E0, E1, E2, less, top_left, depth_cleared, keys);
+    if (inb)
+        direct_pixel(V, J, ux, uy + 4, E0 + (J.B[0] << 2), E1 + (J.B[1] << 2), E2 + (J.B[2] << 2), less, top_left,
+                     depth_cleared, keys);
+}
+
+// Queues the chunks of a large job (or a clip fan): entries (key, record slot, first tile, tiles).
+__device__ __forceinline__ void direct_push(const BatchParams &bp, uint32_t key, uint32_t rec, uint32_t ntiles,
+                                            uint32_t lane_in, uint32_t lanes) {
+    const uint32_t nchunks = (ntiles + kDirectChunk - 1) / kDirectChunk;
+    uint32_t base = 0;
+    if (lane_in == 0) base = atomicAdd(bp.counters + kCtrQueue, nchunks);
+    if (lanes > 1) base = __shfl_sync(0xFFFFFFFFu, base, 0);
+    if (base + nchunks > bp.queue_capacity) {
+        if (lane_in == 0) {
+            atomicOr(bp.error, kErrQueueOverflow);
+            atomicMin(bp.error + 1, bp.batch_seq);
+            atomicMax(bp.error + 5, base + nchunks);
+        }
+        return;
+    }
+    for (uint32_t c = lane_in; c < nchunks; c += lanes)
+        bp.queue[base + c] = make_uint4(key, rec, c * kDirectChunk, min(kDirectChunk, ntiles - c * kDirectChunk));
+}
+
+__global__ void __launch_bounds__(kDirectBlock) k_direct_raster(BatchParams bp) {
+    __shared__ Vtx s_v[kDirectTris][3];
+    __shared__ DirectJob s_job[kDirectTris];
+    __shared__ uint32_t s_cnt[kDirectTris];            // tiles of each lane's local job (0: none)
+    __shared__ uint4 s_push[kDirectListCap];           // jobs to queue: key, record, tiles
+    __shared__ uint4 s_mark[kDirectListCap];           // bin rectangles to mark: tx0, ty0, nx, ny
+    __shared__ uint32_t s_npush, s_nmark;
+    pdl_wait();
+    const DrawDesc &d = bp.draws[0];
+    const ViewDesc &V = bp.views[0];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t g0 = blockIdx.x * kDirectTris;
+    if (threadIdx.x == 0) { s_npush = 0; s_nmark = 0; }
+    // vertex shader, one thread per (triangle, vertex), per index as the reference shades
+    if (threadIdx.x < 3 * kDirectTris) {
+        const uint32_t t = threadIdx.x / 3, k = threadIdx.x - 3 * t;
+        if (g0 + t < bp.total_tris) triangle_vertex(bp, d, d.start_index + 3 * (g0 + t) + k, s_v[t][k].v);
+    }
+    __syncthreads();
+    if (warp == 0) {
+        // primitive assembly, clipping and setup (main.c:736-913), one thread per input triangle
+        const uint32_t g = g0 + lane;
+        uint32_t mask = 0, entries = 0, cnt = 0;
+        if (g < bp.total_tris) {
+            const float *p0 = s_v[lane][0].v, *p1 = s_v[lane][1].v, *p2 = s_v[lane][2].v;
+            bool reject = p0[3] == 0 || p1[3] == 0 || p2[3] == 0;   // main.c:759-781
+            reject = reject || (p0[0] < -p0[3] && p1[0] < -p1[3] && p2[0] < -p2[3]) ||
+                     (p0[0] > +p0[3] && p1[0] > +p1[3] && p2[0] > +p2[3]) ||
+                     (p0[1] < -p0[3] && p1[1] < -p1[3] && p2[1] < -p2[3]) ||
+                     (p0[1] > +p0[3] && p1[1] > +p1[3] && p2[1] > +p2[3]) ||
+                     (p0[2] < 0.f && p1[2] < 0.f && p2[2] < 0.f) ||
+                     (p0[2] > +p0[3] && p1[2] > +p1[3] && p2[2] > +p2[3]);
+            if (!reject) {
+                const bool clipped = !((p0[0] >= -p0[3] && p1[0] >= -p1[3] && p2[0] >= -p2[3]) &&
+                                       (p0[0] <= +p0[3] && p1[0] <= +p1[3] && p2[0] <= +p2[3]) &&
+                                       (p0[1] >= -p0[3] && p1[1] >= -p1[3] && p2[1] >= -p2[3]) &&
+                                       (p0[1] <= +p0[3] && p1[1] <= +p1[3] && p2[1] <= +p2[3]) &&
+                                       (p0[2] >= 0.f && p1[2] >= 0.f && p2[2] >= 0.f) &&
+                                       (p0[2] <= +p0[3] && p1[2] <= +p1[3] && p2[2] <= +p2[3]));
+                // one emitted triangle: its record, its bin rectangle, its job (local or queued)
+                auto emit = [&](const Setup &su, const Vtx &a, const Vtx &b, const Vtx &c, uint32_t rec, uint32_t key,
+                                bool may_stage) {
+                    int32_t tx0, ty0, tx1, ty1;
+                    tile_range(V, su.minx, su.miny, su.maxx, su.maxy, tx0, ty0, tx1, ty1);
+                    if (tx1 < tx0 || ty1 < ty0) return;
+                    const uint32_t nx = (uint32_t)(tx1 - tx0 + 1), ny = (uint32_t)(ty1 - ty0 + 1);
+                    entries += nx * ny;
+                    if (nx * ny <= 4) {
+                        for (uint32_t y = 0; y < ny; ++y)
+                            for (uint32_t x = 0; x < nx; ++x) bp.bin_count[(ty0 + y) * V.tiles_x + tx0 + x] = 1u;
+                    } else {
+                        const uint32_t m = atomicAdd(&s_nmark, 1u);
+                        if (m < kDirectListCap) {
+                            s_mark[m] = make_uint4((uint32_t)tx0, (uint32_t)ty0, nx, ny);
+                        } else {
+                            for (uint32_t t = 0; t < nx * ny; ++t)
+                                bp.bin_count[(ty0 + t / nx) * V.tiles_x + tx0 + t % nx] = 1u;
+                        }
+                    }
+                    if (su.tminx > su.tmaxx || su.tminy > su.tmaxy) return;   // covers no sample
+                    write_record(bp, rec, 0, d.ps, true, su, a, b, c);
+                    int4 R[4];
+                    raster_words(su, R);
+                    const DirectJob J = direct_job(R[0], R[1], R[2], R[3], key);
+                    const uint32_t ntiles = J.ntx * J.nty;
+                    if (may_stage && ntiles <= kDirectLocalTiles) {
+                        s_job[lane] = J;
+                        cnt = ntiles;
+                        return;
+                    }
+                    const uint32_t m = atomicAdd(&s_npush, 1u);
+                    if (m < kDirectListCap) s_push[m] = make_uint4(key, rec, ntiles, 0u);
+                    else direct_push(bp, key, rec, ntiles, 0, 1);
+                };
+                if (!clipped) {
+                    Setup su;
+                    if (setup_triangle(d, s_v[lane][0], s_v[lane][1], s_v[lane][2], su)) {
+                        mask = 1;
+                        emit(su, s_v[lane][0], s_v[lane][1], s_v[lane][2], g, g << 3, true);
+                    }
+                } else {
+                    Vtx poly[kMaxClipVertices], tmp[kMaxClipVertices];
+                    poly[0] = s_v[lane][0]; poly[1] = s_v[lane][1]; poly[2] = s_v[lane][2];
+                    int count = 3;
+                    for (int p = 0; p < 6; ++p) clip_by_plane(poly, tmp, count, c_clip_planes[p]);
+                    const int nf = count - 2;
+                    if (nf > 0) {
+                        const uint32_t base = atomicAdd(bp.counters + kCtrOverflow, (uint32_t)nf);
+                        if (base + (uint32_t)nf > bp.overflow_capacity) {
+                            atomicOr(bp.error, kErrRecordOverflow);
+                            atomicMin(bp.error + 1, bp.batch_seq);
+                            atomicMax(bp.error + 4, base + (uint32_t)nf);
+                        } else {
+                            for (int f = 0; f < nf && f < 7; ++f) {
+                                Setup su;
+                                if (setup_triangle(d, poly[0], poly[f + 1], poly[f + 2], su)) {
+                                    mask |= 1u << f;
+                                    emit(su, poly[0], poly[f + 1], poly[f + 2], bp.total_tris + base + (uint32_t)f,
+                                         (g << 3) | (uint32_t)(f + 1), false);
+                                }
+                            }
+                            // slot g holds the fans' base, by which record_of finds them from a key
+                            bp.raster[g].w[0] = make_int4((int)base, 0, 0, 0);
+                        }
+                    }
+                }
+            }
+        }
+        s_cnt[lane] = cnt;
+        // statistics (main.c:1238 and the binner's entries, main.c:937-944), staged until the
+        // resolve commits them
+        uint32_t n = __popc(mask);
+        n = __reduce_add_sync(0xFFFFFFFFu, n);
+        entries = __reduce_add_sync(0xFFFFFFFFu, entries);
+        if (lane == 0 && n) atomicAdd(bp.stats + kStatAssembled, (unsigned long long)n);
+        if (lane == 0 && entries) atomicAdd(bp.stats + kStatBinEntries, (unsigned long long)entries);
+        __syncwarp();
+        // queued jobs, each pushed by the whole warp
+        const uint32_t np = min(s_npush, (uint32_t)kDirectListCap);
+        for (uint32_t i = 0; i < np; ++i) {
+            const uint4 e = s_push[i];
+            direct_push(bp, e.x, e.y, e.z, (uint32_t)lane, 32u);
+        }
+    }
+    __syncthreads();
+    // the binned tiles of the larger rectangles, by the whole CTA
+    const uint32_t nm = min(s_nmark, (uint32_t)kDirectListCap);
+    for (uint32_t i = 0; i < nm; ++i) {
+        const uint4 r = s_mark[i];
+        for (uint32_t t = threadIdx.x; t < r.z * r.w; t += kDirectBlock)
+            bp.bin_count[(r.y + t / r.z) * V.tiles_x + r.x + t % r.z] = 1u;
+    }
+    // the staged jobs' tiles, (job, tile) pairs dealt round-robin to the 4 warps; a warp's cursor
+    // only moves forward, and it loads a job's parameters once
+    const bool less = d.depth_less != 0;
+    const bool top_left = (d.raster_flags & kRasterTopLeft) != 0;
+    const bool depth_cleared = (V.clear_flags & kClearDepth) != 0;
+    uint32_t j = 0, b = (uint32_t)warp, cj = s_cnt[0], loaded = 0xFFFFFFFFu;
+    DirectJob J;
+    while (true) {
+        while (j < kDirectTris && b >= cj) {
+            b -= cj;
+            ++j;
+            cj = j < kDirectTris ? s_cnt[j] : 0u;
+        }
+        if (j >= kDirectTris) break;
+        if (j != loaded) {
+            J = s_job[j];
+            loaded = j;
+        }
+        const uint32_t ty = b / J.ntx, tx = b - ty * J.ntx;
+        direct_tile(V, J, J.tx0 + tx, J.ty0 + ty, less, top_left, depth_cleared, bp.keys, lane);
+        b += kDirectWarps;
+    }
+    pdl_trigger();
+}
+
+// The queued chunks (large triangles and clip fans), one warp per chunk.
+__global__ void __launch_bounds__(kDirectBlock) k_direct_queue(BatchParams bp) {
+    pdl_wait();
+    if (ld_volatile_u32(bp.error)) {   // uniform: set only by the raster kernel
+        pdl_trigger();
+        return;
+    }
+    const DrawDesc &d = bp.draws[0];
+    const ViewDesc &V = bp.views[0];
+    const int lane = threadIdx.x & 31;
+    const bool less = d.depth_less != 0;
+    const bool top_left = (d.raster_flags & kRasterTopLeft) != 0;
+    const bool depth_cleared = (V.clear_flags & kClearDepth) != 0;
+    const uint32_t n = min(ld_volatile_u32(bp.counters + kCtrQueue), bp.queue_capacity);
+    const uint32_t nwarps = gridDim.x * kDirectWarps;
+    for (uint32_t i = blockIdx.x * kDirectWarps + (threadIdx.x >> 5); i < n; i += nwarps) {
+        const uint4 e = bp.queue[i];
+        const int4 *R = bp.raster[e.y].w;
+        const DirectJob J = direct_job(__ldg(R), __ldg(R + 1), __ldg(R + 2), __ldg(R + 3), e.x);
+        for (uint32_t t = e.z; t < e.z + e.w; ++t) {
+            const uint32_t ty = t / J.ntx, tx = t - ty * J.ntx;
+            direct_tile(V, J, J.tx0 + tx, J.ty0 + ty, less, top_left, depth_cleared, bp.keys, lane);
+        }
+    }
+    pdl_trigger();
+}
+
+// One warp per 8x8 tile: the fragments the keys name are the draw's winners; shading, colour and
+// depth writes, hierarchical Z and the folded clears as k_tile does them, then the keys and the
+// tile's mark are cleared for the next draw.
+constexpr int kResolveWarps = 4;
+
+__global__ void __launch_bounds__(kResolveWarps * 32) k_direct_resolve(BatchParams bp) {
+    __shared__ uint32_t s_active;
+    pdl_wait();
+    if (ld_volatile_u32(bp.error)) return;   // uniform: set only by earlier kernels
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        // the raster kernel's staged statistics; active bins are added below by every CTA
+        for (int k : {(int)kStatAssembled, (int)kStatBinEntries}) {
+            atomicAdd(bp.stats + kStatTotal + k, bp.stats[k]);
+            bp.stats[k] = 0;
+        }
+    }
+    if (threadIdx.x == 0) s_active = 0;
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t t = blockIdx.x * kResolveWarps + warp;
+    const ViewDesc &V = bp.views[0];
+    if (t < bp.total_tiles) {
+        const DrawDesc &D = bp.draws[0];
+        const bool less = D.depth_less != 0;
+        const uint32_t tx = t % V.tiles_x, ty = t / V.tiles_x;
+        const int32_t x0 = (int32_t)tx * kTile, y0 = (int32_t)ty * kTile;
+        const int32_t px = x0 + (lane & 7), py0 = y0 + (lane >> 3), py1 = py0 + 4;
+        const bool valid0 = px < (int32_t)V.width && py0 < (int32_t)V.height;
+        const bool valid1 = px < (int32_t)V.width && py1 < (int32_t)V.height;
+        const size_t o0 = (size_t)py0 * V.width + px, o1 = (size_t)py1 * V.width + px;
+        const bool depth_cleared = (V.clear_flags & kClearDepth) != 0;
+        const uint32_t marked = bp.bin_count[t];
+        if (!marked) {   // no triangle binned here (uniform over the warp)
+            if (V.clear_flags) {
+                if (valid0) write_cleared(V, o0, V.clear_depth);
+                if (valid1) write_cleared(V, o1, V.clear_depth);
+                if (lane == 0 && depth_cleared) {   // main.c:1212-1214
+                    V.tile_min[t] = 0.0f;
+                    V.tile_max[t] = 1.0f;
+                }
+            }
+        } else {
+            if (lane == 0) {
+                bp.bin_count[t] = 0u;
+                atomicAdd(&s_active, 1u);
+            }
+            unsigned long long k0 = 0, k1 = 0;
+            if (valid0) { k0 = bp.keys[o0]; if (k0) bp.keys[o0] = 0ull; }
+            if (valid1) { k1 = bp.keys[o1]; if (k1) bp.keys[o1] = 0ull; }
+            if (less) { k0 = k0 ? ~k0 : 0ull; k1 = k1 ? ~k1 : 0ull; }
+            const uint32_t win0 = k0 ? (uint32_t)k0 : 0xFFFFFFFFu, win1 = k1 ? (uint32_t)k1 : 0xFFFFFFFFu;
+            float dcur0 = 0.0f, dcur1 = 0.0f;
+            if (valid0) dcur0 = k0 ? depth_from_key((uint32_t)(k0 >> 32)) : (depth_cleared ? V.clear_depth : V.depth[o0]);
+            if (valid1) dcur1 = k1 ? depth_from_key((uint32_t)(k1 >> 32)) : (depth_cleared ? V.clear_depth : V.depth[o1]);
+            // write_tile's bounds (main.c:589-603), in k_tile's order
+            float mn = 1.0f, mx = 0.0f;
+            if (valid0) { mn = fmin_ref(mn, dcur0); mx = fmax_ref(mx, dcur0); }
+            if (valid1) { mn = fmin_ref(mn, dcur1); mx = fmax_ref(mx, dcur1); }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const float a = __shfl_xor_sync(0xFFFFFFFFu, mn, o), b = __shfl_xor_sync(0xFFFFFFFFu, mx, o);
+                mn = fmin_ref(mn, a);
+                mx = fmax_ref(mx, b);
+            }
+            // one pixel-shader invocation per written pixel, compacted over the warp
+            const uint32_t m0 = __ballot_sync(0xFFFFFFFFu, win0 != 0xFFFFFFFFu && valid0);
+            const uint32_t m1 = __ballot_sync(0xFFFFFFFFu, win1 != 0xFFFFFFFFu && valid1);
+            const uint32_t n0 = __popc(m0), n = n0 + __popc(m1);
+            for (uint32_t q0 = 0; q0 < n; q0 += 32) {
+                const uint32_t q = q0 + lane;
+                const uint32_t half = q < n0 ? 0u : 1u;
+                uint32_t src = 0;
+                if (q < n) {
+                    const uint32_t m = half ? m1 : m0, k = half ? q - n0 : q;
+                    src = m == 0xFFFFFFFFu ? k : nth_set_bit(m, k);
+                }
+                const uint32_t wa = __shfl_sync(0xFFFFFFFFu, win0, src), wb = __shfl_sync(0xFFFFFFFFu, win1, src);
+                if (q >= n) continue;
+                shade_pixel(bp, V, half ? wb : wa, x0 + (int32_t)(src & 7), y0 + (int32_t)(src >> 3) + (half ? 4 : 0));
+            }
+            if (V.clear_flags) {
+                if (valid0 && win0 == 0xFFFFFFFFu) write_cleared(V, o0, dcur0);
+                if (valid1 && win1 == 0xFFFFFFFFu) write_cleared(V, o1, dcur1);
+            }
+            if (lane == 0) {
+                V.tile_min[t] = mn;
+                V.tile_max[t] = mx;
+            }
+        }
+    }
+    __syncthreads();
+    // active-bin statistic (main.c:937-944), straight to the totals: this kernel runs only for a
+    // batch that completed
+    if (threadIdx.x == 0 && s_active) atomicAdd(bp.stats + kStatTotal + kStatActiveBins, (unsigned long long)s_active);
+    pdl_trigger();
+}
+
 // ------------------------------------------------------------------ clears
 
 __global__ void k_fill_u32(uint32_t *p, size_t n, uint32_t value, const uint32_t *error) {
@@ -1690,6 +2111,20 @@ cudaError_t launch_scatter(const BatchParams &bp, int num_sms, cudaStream_t stre
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
     return launch_chained(k_scatter, blocks, kScatterBlock, stream, bp);
+}
+
+cudaError_t launch_direct_raster(const BatchParams &bp, cudaStream_t stream) {
+    return launch_chained(k_direct_raster, (bp.total_tris + kDirectTris - 1) / kDirectTris, (uint32_t)kDirectBlock,
+                          stream, bp);
+}
+
+cudaError_t launch_direct_queue(const BatchParams &bp, int num_sms, cudaStream_t stream) {
+    return launch_chained(k_direct_queue, (uint32_t)num_sms * 4u, (uint32_t)kDirectBlock, stream, bp);
+}
+
+cudaError_t launch_direct_resolve(const BatchParams &bp, cudaStream_t stream) {
+    return launch_chained(k_direct_resolve, (bp.total_tiles + kResolveWarps - 1) / kResolveWarps,
+                          (uint32_t)(kResolveWarps * 32), stream, bp);
 }
 
 cudaError_t launch_tile(const BatchParams &bp, uint32_t warps, uint32_t warps_per_tile, cudaStream_t stream) {

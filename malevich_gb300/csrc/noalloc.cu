@@ -109,14 +109,7 @@ mlv_status noalloc_setup(int dev, uint8_t **out) {
             return MLV_ERROR_DEVICE;
         }
         float planes[6][4];
-        static const float raw[6][4] = {{1, 0, 0, 1}, {-1, 0, 0, 1}, {0, 1, 0, 1},
-                                        {0, -1, 0, 1}, {0, 0, 1, 1}, {0, 0, -1, 1}};
-        for (int p = 0; p < 6; ++p) {
-            float dot = raw[p][0] * raw[p][0] + raw[p][1] * raw[p][1] + raw[p][2] * raw[p][2] + raw[p][3] * raw[p][3];
-            float len = (float)sqrt((double)dot);
-            float inv = (float)(1.0 / (double)len);
-            for (int k = 0; k < 4; ++k) planes[p][k] = raw[p][k] * inv;
-        }
+        host_clip_planes(planes);
         set_clip_planes(planes, 0);
         e = cudaDeviceSynchronize();
         if (e != cudaSuccess) {
@@ -177,8 +170,12 @@ extern "C" MLV_API mlv_status mlv_draw_indexed_noalloc(const mlv_noalloc_draw *a
         return fail_na(MLV_ERROR_CAPACITY_EXCEEDED, "draw has more triangles than MLV_NOALLOC_MAX_TRIANGLES");
     if (a->vertex_stride < 32 || (a->vertex_stride & 3))
         return fail_na(MLV_ERROR_INVALID_ARG, "vertex stride must be >= 32 and a multiple of 4");
-    if (a->vs < MLV_VS_BASIC || a->vs > MLV_VS_PASSTHROUGH_UV || a->ps < MLV_PS_BASIC || a->ps > MLV_PS_COLOR_TIMES_TEXEL)
+    if (a->vs < MLV_VS_BASIC || a->vs > MLV_VS_PASSTHROUGH_UV || a->ps < MLV_PS_BASIC || a->ps > MLV_PS_NONE)
         return fail_na(MLV_ERROR_INVALID_ARG, "unknown shader");
+    // the kernels read indices start_index .. start_index + index_count - 1 (as mlv_draw_indexed
+    // checks against its bound index buffer)
+    if (a->index_buffer && (uint64_t)a->start_index + a->index_count > a->index_buffer_count)
+        return fail_na(MLV_ERROR_INVALID_ARG, "draw reads past the index buffer (index_buffer_count)");
     if ((a->vs == MLV_VS_BASIC || a->vs == MLV_VS_VERTEX_LIGHTING || a->vs == MLV_VS_FULLSCREEN) && !a->per_frame_cb)
         return fail_na(MLV_ERROR_INVALID_ARG, "this vertex shader needs per_frame_cb");
     if (a->vs == MLV_VS_VERTEX_LIGHTING && !tex_valid(a->vs_texture, true, false))
@@ -229,17 +226,12 @@ extern "C" MLV_API mlv_status mlv_draw_indexed_noalloc(const mlv_noalloc_draw *a
     d.draw_in_view = 0;
     d.draw_seq = 0;
     if (a->per_frame_cb) memcpy(d.cb, a->per_frame_cb, sizeof(d.cb));
-    {
-        float r[16] = {(float)(vp.width * 0.5), 0, 0, (float)(vp.width * 0.5 + vp.top_left_x),
-                       0, (float)(-vp.height * 0.5), 0, (float)(vp.height * 0.5 + vp.top_left_y),
-                       0, 0, vp.max_depth - vp.min_depth, vp.min_depth,
-                       0, 0, 0, 1};
-        memcpy(d.screen_from_ndc, r, sizeof(r));
-    }
+    host_screen_from_ndc(vp, d.screen_from_ndc);
     d.vp_w = (int32_t)vp.width;
     d.vp_h = (int32_t)vp.height;
-    d.vs_cached = (d.ib != nullptr && d.vertex_count > 0 && tris > 0 && d.vertex_count <= kMaxVertices &&
-                   (uint64_t)d.vertex_count <= 6ull * tris) ? 1u : 0u;
+    // shaded once per vertex under the same rule as mlv_draw_indexed, while the vertices fit the
+    // scratch array's shaded-vertex area (beyond that, per index: same outputs)
+    d.vs_cached = (host_shade_once(d.ib, d.vertex_count, tris) && d.vertex_count <= kMaxVertices) ? 1u : 0u;
     d.vs_base = 0;
     d.vs_count = d.vs_cached ? d.vertex_count : 0;
     d.vs_tex = tex_of(a->vs_texture);

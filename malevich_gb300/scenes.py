@@ -454,6 +454,7 @@ def frame_to_arrays(frame, prefix="frame"):
         out[prefix + "/clear_color"] = np.array(frame.clear_color, np.float32)
     if frame.clear_depth is not None:
         out[prefix + "/clear_depth"] = np.array([frame.clear_depth], np.float32)
+    stored = {}   # texture already written: id(data) -> (draw, slot); later uses refer to it
     for i, d in enumerate(frame.draws):
         p = "%s/draw%d/" % (prefix, i)
         out[p + "ints"] = np.array([d.vs, d.ps, d.index_count, d.cull, d.depth_func, d.start_index, d.base_vertex],
@@ -464,11 +465,16 @@ def frame_to_arrays(frame, prefix="frame"):
         if d.cb is not None:
             out[p + "cb"] = d.cb
         out[p + "viewport"] = np.array(d.viewport, np.float32)
-        for name in ("vs_tex", "ps_tex"):
+        for slot, name in enumerate(("vs_tex", "ps_tex")):
             t = getattr(d, name)
-            if t is not None:
-                out[p + name] = t.data
-                out[p + name + "_fmt"] = np.array([t.format], np.int64)
+            if t is None:
+                continue
+            if id(t.data) in stored:
+                out[p + name + "_same_as"] = np.array(stored[id(t.data)], np.int64)
+                continue
+            stored[id(t.data)] = (i, slot)
+            out[p + name] = t.data
+            out[p + name + "_fmt"] = np.array([t.format], np.int64)
     return out
 
 
@@ -483,7 +489,10 @@ def frame_from_arrays(z, prefix="frame"):
         vs, ps, n, cull, df, si, bv = (int(v) for v in z[p + "ints"])
         texs = {}
         for name in ("vs_tex", "ps_tex"):
-            if p + name in z:
+            if p + name + "_same_as" in z:   # the texture of an earlier draw's slot
+                j, slot = (int(v) for v in z[p + name + "_same_as"])
+                texs[name] = getattr(fr.draws[j], ("vs_tex", "ps_tex")[slot])
+            elif p + name in z:
                 data = z[p + name]
                 key = (data.shape, data.dtype.str, hash(data.tobytes()))
                 if key not in texcache:

@@ -42,8 +42,17 @@ from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
+# Where this recipe looks for the reference's sources: $MALEVICH_REFERENCE, else the checkout this
+# build container mounts. The only place the product's files name that location.
 DEFAULT_REFERENCE = "/root/reference"
-DEFAULT_SIZES = ["1280x720", "1920x1080", "1200x720", "256x256", "512x512", "64x64", "32x32"]
+
+
+def reference_dir():
+    """The reference checkout this recipe builds from, or None when its sources are absent (as on
+    a host that only runs the prebuilt files)."""
+    d = os.environ.get("MALEVICH_REFERENCE", DEFAULT_REFERENCE)
+    return d if os.path.isdir(os.path.join(d, "source")) else None
+DEFAULT_SIZES = ["1280x720", "1920x1080", "1200x720", "480x272", "256x256", "512x512", "64x64", "32x32"]
 SHADERS = ["basic_vs.c", "vertex_lighting_vs.c", "passthrough_vs.c", "fullscreen_vs.c",
            "basic_ps.c", "passthrough_ps.c", "env_lighting_ps.c"]
 
@@ -174,7 +183,7 @@ def compile_size(srcdir, size):
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default=os.environ.get("MALEVICH_REFERENCE", DEFAULT_REFERENCE))
+    ap.add_argument("--reference", default=reference_dir() or os.environ.get("MALEVICH_REFERENCE", DEFAULT_REFERENCE))
     ap.add_argument("--sizes", default=",".join(DEFAULT_SIZES))
     args = ap.parse_args(argv)
     if not os.path.isdir(os.path.join(args.reference, "source")):

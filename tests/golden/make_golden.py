@@ -13,7 +13,7 @@ inputs - the Suprematism quads (main.c:232-254) with passthrough_vs/ps, and the 
 (main.c:255-270) with fullscreen_vs + env_lighting_ps - parsed from source/main.c at generation
 time, never written out by hand.
 
-Usage: python tests/golden/make_golden.py [--reference /root/reference]
+Usage: python tests/golden/make_golden.py [--reference DIR]   (default: oracle/ref_build.py's reference_dir())
 """
 import argparse
 import os
@@ -76,15 +76,42 @@ def scene_list():
     return out
 
 
+def scene_frame_reduced():
+    """The scene-scale frame's construction at 480x272: a 100x100-cell heightfield (20,000
+    triangles) and 11 icospheres/boxes of 800-3,000 triangles in the 20 m cube, seen from a seeded
+    pose inside it (so the ground crosses the near and side planes and is clipped heavily),
+    vertex_lighting_vs + env_lighting_ps with the reference's depth mode. Smaller textures than the
+    full frame (256x128 RGBA16F radiance) keep the fixture small; the full-size frame is pinned
+    live where the reference is built (tests/test_oracle.py)."""
+    seed = 12
+    while True:
+        rng = np.random.default_rng(seed)
+        counts = (800 + 2200 * rng.random(11)).astype(int)
+        fr = scenes.config2_scene(seed=seed, width=480, height=272, ground_cells=100, counts=counts,
+                                  radiance_size=(256, 128), irradiance_size=(64, 32), ground_tex=0)
+        st = pyoracle.render_oracle(fr)["stats"]
+        if st["clipped_triangle_count"] >= 300 and st["assembled_triangle_count"] >= 3000:
+            return {"scene_frame_480x272": fr}
+        seed += 1000
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default=ref_build.DEFAULT_REFERENCE)
+    ap.add_argument("--reference", default=ref_build.reference_dir())
+    ap.add_argument("--only", default="", help="comma-separated fixture names to (re)generate (default: all)")
     args = ap.parse_args(argv)
-    ref_build.main(["--reference", args.reference, "--sizes", "64x64,32x32"])
+    ref_build.main(["--reference", args.reference, "--sizes", "64x64,32x32,480x272"])
     frames = scene_list()
     frames.update(reference_fixed_frames(args.reference, 64, 64))
+    big = scene_frame_reduced()
+    frames.update(big)
+    only = [n for n in args.only.split(",") if n]
     for name, fr in frames.items():
-        r = pyoracle.render_reference(fr, capture=True, threads=1)
+        if only and name not in only:
+            continue
+        # the reduced scene frame keeps no per-triangle captures (they would dwarf the fixture);
+        # the small fixtures cover the setup words and TileInfo masks
+        r = pyoracle.render_reference(fr, capture=name not in big, threads=1)
         arrays = scenes.frame_to_arrays(fr)
         for k in ("color", "depth", "vis_tri", "vis_draw", "tile_min"):
             arrays["out/" + k] = r[k]

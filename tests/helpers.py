@@ -24,6 +24,21 @@ def assert_color_close(got, want, tol=COLOR_TOL, max_outlier_frac=0.0):
     return d
 
 
+def reference_nan_pixels(color):
+    """Pixels where the reference wrote NaN colour: _mm256_cvtps_epi32 turns a NaN channel into
+    0x80000000 (main.c:1176-1178), which its approximate rsqrt produces where a cosine exceeds 1
+    before acos (common_shader_core.h:232-240). Compared apart from the +-1 LSB bound."""
+    return np.ascontiguousarray(color).view(np.uint32) == 0x80000000
+
+
+def outlier_report(got, want):
+    """Counts for the colour-outlier report: pixels beyond +-1 LSB (excluding the reference's NaN
+    pixels when `want` comes from the reference), their fraction and the largest difference."""
+    d = color_diff(got, want).max(axis=-1)
+    n = int((d > COLOR_TOL).sum())
+    return {"pixels_beyond_1lsb": n, "fraction": n / d.size if d.size else 0.0, "max_diff": int(d.max()) if d.size else 0}
+
+
 def assert_bits_equal(got, want, what):
     g = np.ascontiguousarray(got).view(np.uint32)
     w = np.ascontiguousarray(want).view(np.uint32)

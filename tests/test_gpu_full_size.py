@@ -5,7 +5,7 @@ within +-1 LSB (normalising shaders: at most 0.1% of pixels beyond, see helpers)
 import numpy as np
 import pytest
 
-from helpers import assert_bits_equal, assert_color_close
+from helpers import assert_bits_equal, assert_color_close, outlier_report
 from malevich_gb300 import api, scenes
 from oracle import pyoracle
 
@@ -37,6 +37,10 @@ def test_full_scene_frame(device, scene_frame, batched):
     assert np.array_equal(got["vis_tri"], want["vis_tri"])
     assert np.array_equal(got["vis_draw"], want["vis_draw"])
     assert_bits_equal(got["vis_bary"], want["vis_bary"], "barycentrics")
+    rep = outlier_report(got["color"], want["color"])
+    print("scene frame (%s): %d of %d pixels (%.5f%%) beyond +-1 LSB of the oracle, max diff %d" % (
+        "batched" if batched else "per draw", rep["pixels_beyond_1lsb"], fr.width * fr.height,
+        100 * rep["fraction"], rep["max_diff"]))
     assert_color_close(got["color"], want["color"], max_outlier_frac=1e-3)
     for k in STATS:
         assert stats[k] == want["stats"][k], k

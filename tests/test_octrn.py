@@ -10,7 +10,10 @@ import pytest
 
 from malevich_gb300 import octrn
 
-ASSETS = os.environ.get("MALEVICH_ASSETS", "/root/reference/assets")
+from oracle import ref_build
+
+# the reference's shipped assets, when its checkout is on this machine ($MALEVICH_ASSETS overrides)
+ASSETS = os.environ.get("MALEVICH_ASSETS") or os.path.join(ref_build.reference_dir() or "", "assets")
 
 
 def test_mesh_round_trip(tmp_path):
