@@ -59,6 +59,8 @@ def parse():
                     help="--profile-once: the scene frame or the single draw (icosphere L5 at 1280x720)")
     ap.add_argument("--warps-per-tile", type=int, default=0,
                     help="--profile-once: this tile-kernel shape (1, 2, 4 or 8) instead of the default")
+    ap.add_argument("--small-draw-triangles", type=int, default=-1,
+                    help="--profile-once / --profile-diff-views: this small-draw threshold instead of the default")
     ap.add_argument("--port-vs-reference", action="store_true",
                     help="with --impl reference: time the reference's own core and the oracle port on the same "
                          "frame and threads (x86-64 only) and exit")
@@ -662,6 +664,8 @@ def main():
     torch.cuda.set_device(local)
     dev = api.Device(local)
     ctx = dev.immediate
+    if args.small_draw_triangles >= 0:
+        ctx.set_tuning(small_draw_triangles=args.small_draw_triangles)
     if args.profile_diff_views:
         print(json.dumps({"profile_diff": profile_diff(dev, args.profile_diff_views)}))
         dev.destroy()

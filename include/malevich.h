@@ -346,9 +346,10 @@ typedef struct mlv_tuning {
      * regrows the buffer and re-runs the batch, so these only trade memory for a re-run. */
     uint32_t initial_bin_entries;
     uint32_t initial_clip_fan_slots;
-    /* A batch of one draw with at most this many input triangles (and no triangle-id target and no
-     * TileInfo capture) takes the small-draw path: three kernels instead of five, no binning, the
-     * vertex shader run per index as the reference does. Same outputs; 0 disables it. */
+    /* A batch whose every view has exactly one draw, each of at most this many input triangles
+     * (default: any number), with no triangle-id target and no TileInfo capture, takes the
+     * small-draw path: three kernels instead of five, no binning, the vertex shader run per index
+     * as the reference does. Same outputs; 0 disables it. */
     uint32_t small_draw_triangles;
     uint32_t debug_flags;             /* MLV_DEBUG_*: failure-detection tests only; 0 in normal use */
 } mlv_tuning;

@@ -37,7 +37,7 @@ cudaError_t launch_scan(const BatchParams &bp, cudaStream_t stream);
 cudaError_t launch_rank(const BatchParams &bp, cudaStream_t stream);
 cudaError_t launch_scatter(const BatchParams &bp, int num_sms, cudaStream_t stream);
 cudaError_t launch_tile(const BatchParams &bp, uint32_t warps, uint32_t warps_per_tile, cudaStream_t stream);
-cudaError_t launch_direct_raster(const BatchParams &bp, cudaStream_t stream);
+cudaError_t launch_direct_raster(const BatchParams &bp, int num_sms, cudaStream_t stream);
 cudaError_t launch_direct_queue(const BatchParams &bp, int num_sms, cudaStream_t stream);
 cudaError_t launch_direct_resolve(const BatchParams &bp, cudaStream_t stream);
 }  // namespace mlv
@@ -223,8 +223,10 @@ struct PendingJob {
     uint32_t seq;
 };
 
-// Single draws of up to this many input triangles take the small-draw path by default.
-constexpr uint32_t kDefaultSmallDraw = 32768;
+// Batches of one draw per view take the small-draw path by default whatever their draws' sizes:
+// it measured faster than the binned path both on the 20,480-triangle single draw and on the
+// 256-view, 51M-triangle visibility pass.
+constexpr uint32_t kDefaultSmallDraw = 0xFFFFFFFFu;
 
 struct mlv_context_t {
     mlv_device device = nullptr;
@@ -446,7 +448,8 @@ struct Plan {
     std::vector<DrawDesc> draws;
     std::vector<ViewDesc> views;
     BatchSizes sizes;
-    bool direct = false;   // the small-draw path (one draw, no binning)
+    bool direct = false;   // the small-draw path (one draw per view, no binning)
+    bool keys_only = false;  // ... whose resolve reads no records
     std::unordered_set<mlv_texture2d> folded;   // cleared targets the tile kernel clears itself
     // upload events of the batch's inputs, waited for before the stage that first reads them
     std::vector<cudaEvent_t> wait_vertex, wait_index, wait_pixel;
@@ -494,12 +497,35 @@ static void fold_clears(const Segment &seg, const Groups &groups, Plan &p) {
     }
 }
 
-// Whether a planned batch takes the small-draw path: one draw of at most `small_draw` input
-// triangles, with no triangle-id target and no TileInfo capture (both need the binned path's ranks
-// and lists). The outputs are the same either way.
+// Whether a planned batch takes the small-draw path: every view has exactly one draw, each of at
+// most `small_draw` input triangles, with no triangle-id target and no TileInfo capture (both need
+// the binned path's ranks and lists). The outputs are the same either way.
 static bool plan_is_direct(const Plan &p, uint32_t small_draw, bool capture) {
-    return p.draws.size() == 1 && p.views.size() == 1 && p.draws[0].tri_count > 0 &&
-           p.draws[0].tri_count <= small_draw && !capture && p.views[0].vis_tri == nullptr;
+    if (capture || p.draws.empty() || p.draws.size() != p.views.size()) return false;
+    uint64_t pixels = 0, tris = 0;
+    for (const ViewDesc &v : p.views) {
+        if (v.draw_count != 1 || v.vis_tri != nullptr) return false;
+        pixels += (uint64_t)v.width * v.height;
+    }
+    for (const DrawDesc &d : p.draws) {
+        if (d.tri_count > small_draw) return false;
+        tris += d.tri_count;
+    }
+    return tris > 0 && pixels < (1ull << 31);
+}
+
+// Whether the small-draw path's resolve can take every output from the keys alone: the null pixel
+// shader, no barycentric target, and viewports whose min_depth is +0 (a depth of -0, which the
+// keys fold onto +0, cannot occur then).
+static bool plan_keys_only(const Plan &p) {
+    for (const DrawDesc &d : p.draws) {
+        uint32_t min_depth_bits;
+        memcpy(&min_depth_bits, &d.screen_from_ndc[11], 4);
+        if (d.ps != kPsNone || min_depth_bits != 0) return false;
+    }
+    for (const ViewDesc &v : p.views)
+        if (v.vis_bary != nullptr) return false;
+    return true;
 }
 
 static mlv_status plan_segment(const Segment &seg, Plan &p, uint32_t fan_slots_hint = 0, uint32_t small_draw = 0,
@@ -586,13 +612,21 @@ static mlv_status plan_segment(const Segment &seg, Plan &p, uint32_t fan_slots_h
     for (const DrawDesc &d : p.draws)
         p.sizes.shade = p.sizes.shade || d.ps != kPsNone || (d.raster_flags & kDrawSharesView);
     p.direct = plan_is_direct(p, small_draw, capture);
+    p.keys_only = false;
     if (p.direct) {
         // the vertex shader runs per index inside the raster kernel (main.c:698-734's way)
-        DrawDesc &d = p.draws[0];
-        d.vs_cached = 0;
-        d.vs_count = 0;
+        for (DrawDesc &d : p.draws) {
+            d.vs_cached = 0;
+            d.vs_count = 0;
+        }
         p.sizes.vertices = 0;
-        p.sizes.direct_pixels = (uint64_t)p.views[0].width * p.views[0].height;
+        uint64_t px = 0;
+        for (ViewDesc &v : p.views) {
+            v.key_base = (uint32_t)px;
+            px += (uint64_t)v.width * v.height;
+        }
+        p.sizes.direct_pixels = px;
+        p.keys_only = plan_keys_only(p);
     }
     return MLV_OK;
 }
@@ -730,6 +764,7 @@ static mlv_status launch_draws(mlv_context_t *c, const Plan &p, DrawDesc *d_draw
     bp.keys = w.keys;
     bp.queue = w.queue;
     bp.queue_capacity = w.queue_cap;
+    bp.keys_only = p.keys_only ? 1u : 0u;
     c->host_stats[3] += 1;
     if (bp.total_tris == 0) return MLV_OK;   // nothing to assemble: no kernel has work
     // waits on queued uploads (inside a graph capture: external event waits, evaluated at launch)
@@ -750,7 +785,7 @@ static mlv_status launch_draws(mlv_context_t *c, const Plan &p, DrawDesc *d_draw
         CUDA_TRY(wait_for(p.wait_vertex));
         CUDA_TRY(wait_for(p.wait_index));
         ev_begin(c, 1, &e);
-        CUDA_TRY(launch_direct_raster(bp, c->stream));
+        CUDA_TRY(launch_direct_raster(bp, c->device->num_sms, c->stream));
         ev_end(c, e);
         ev_begin(c, 3, &e);
         CUDA_TRY(launch_direct_queue(bp, c->device->num_sms, c->stream));

@@ -81,7 +81,7 @@ struct ViewDesc {
     uint32_t clear_flags;
     uint32_t clear_color, clear_tri, clear_draw, clear_prim, clear_bary;
     float clear_depth;
-    uint32_t pad[1];
+    uint32_t key_base;                   // small-draw path: the view's first pixel key in BatchParams::keys
 };
 
 constexpr uint32_t kClearColor = 1, kClearDepth = 2, kClearTri = 4, kClearDraw = 8, kClearPrim = 16,
@@ -167,9 +167,10 @@ struct BatchParams {
     uint32_t debug_flags;                // kDebug* (tests only)
     // small-draw path (one draw, no binning): per-pixel (depth, order) keys of the view, all zero
     // between draws; queued chunks of large triangles' pixel blocks
-    unsigned long long *keys;            // [view width * height]
-    uint4 *queue;                        // [queue_capacity]: key, record slot, first block, blocks
+    unsigned long long *keys;            // [sum of the views' width * height]
+    uint4 *queue;                        // [queue_capacity]: key, record slot, first tile, tiles
     uint32_t queue_capacity;
+    uint32_t keys_only;                  // 1: the resolve needs no records (depth and ids from the keys)
 };
 
 enum Counter : int {

@@ -1583,18 +1583,19 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_tile_coop(BatchParam
 
 // ------------------------------------------------------------------ small-draw path
 //
-// A batch of one draw with few triangles (a single mesh: the plain single draw) runs as three
+// A batch whose every view has exactly one draw (a single mesh drawn once: the plain single draw,
+// or many views of one mesh each: the differentiable loop's visibility pass) runs as three
 // kernels instead of five, with no binning:
 //   k_direct_raster   vertex shader per index (as main.c:698-734 does), primitive assembly, clipping
-//                     and setup of 32 input triangles per CTA, then the CTA's 4 warps rasterise
-//                     those triangles over the 8x8 tiles of their sample boxes (two pixels a lane):
-//                     hierarchical Z per (tile, triangle) against the draw-start snapshot
-//                     (main.c:1005-1010), coverage (main.c:1015-1028), quantised depth
-//                     (main.c:1092-1102, 1131-1132) and the test against the draw-start depth
-//                     (main.c:1164-1168), each passing fragment folded into its pixel's 64-bit key
-//                     (depth, order) with a global atomic max (see below). Triangles over more than
-//                     4 tiles and clip fans go to a queue in chunks of 4 tiles.
-//   k_direct_queue    the queued chunks, spread over the whole GPU.
+//                     and setup, then rasterisation of the CTA's triangles: hierarchical Z per
+//                     (tile, triangle) against the draw-start snapshot (main.c:1005-1010), coverage
+//                     (main.c:1015-1028), quantised depth (main.c:1092-1102, 1131-1132) and the test
+//                     against the draw-start depth (main.c:1164-1168), each passing fragment folded
+//                     into its pixel's 64-bit key (depth, order) with a global atomic max (see
+//                     below). Small triangles are rasterised by their own lane, mid-sized ones by
+//                     the CTA's warps (kDirectLanePixels* and the others below), larger ones and
+//                     clip fans go to a queue in chunks of 4 tiles.
+//   k_direct_queue    the queued chunks, spread over the whole GPU, a tile (two pixels a lane) at a time.
 //   k_direct_resolve  one warp per 8x8 tile: the winners' pixel shader and output merger, colour and
 //                     depth written once (main.c:1046-1189), hierarchical Z from the new depths
 //                     (write_tile, main.c:589-603), folded clears, and the keys reset to zero.
@@ -1604,28 +1605,35 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_tile_coop(BatchParam
 // minimum, stored complemented so that both are a maximum over values that are never zero for a
 // fragment that passed (0 = no fragment). The reference's binner statistics come from the
 // triangles' bin rectangles: entries are summed, and every binned tile is marked in bin_count (one
-// word per tile for a single draw), which the resolve counts, uses to skip empty tiles, and clears.
+// word per tile of a one-draw view), which the resolve counts, uses to skip empty tiles, and clears.
 constexpr int kDirectBlock = 128;              // 4 warps
 constexpr int kDirectWarps = kDirectBlock / 32;
-constexpr int kDirectTris = 32;                // input triangles per CTA
-constexpr uint32_t kDirectLocalTiles = 4;      // jobs over more 8x8 tiles are queued
+// How a job is rasterised, by its size (measured on the single draw and the 256-view visibility
+// pass). Small batches (one set-up warp per CTA, whose other warps are free): up to 8 sample pixels
+// by the triangle's own lane, up to 4096 by a whole warp over the spans of its rows. Large batches
+// (every warp sets up its own, mostly tiny, triangles): up to 256 pixels by the lane. Larger jobs
+// and clip fans are queued.
+constexpr uint32_t kDirectLanePixelsSmall = 8, kDirectWarpPixels = 4096;
+constexpr uint32_t kDirectLanePixelsLarge = 256;
 constexpr uint32_t kDirectChunk = 4;           // tiles per queue entry
 constexpr int kDirectListCap = 64;             // per CTA: queued jobs and marked rectangles
+constexpr uint32_t kJobLess = 1u << 8, kJobTopLeft = 1u << 9;   // DirectJob::flags above the bias bits
 
 // A rasterisation job: one emitted triangle's coverage and depth parameters, from its raster
-// record (TriRaster) and order key.
+// record (TriRaster), order key and draw.
 struct DirectJob {
     uint32_t A[3], B[3], C[3];        // E(x, y) = A x + B y + C, A = a << 4, B = b << 4 (wrapping:
                                       // the reference's ((a x) << 4) + ((b y) << 4) + c, main.c:1015-1025)
     float inv_area, z0, dz1, dz2;     // quantised barycentrics and depth (main.c:1092-1102, 1131-1132)
     float zbound;                     // depth bound for hierarchical Z (main.c:871)
-    uint32_t key, bias;               // order key; top-left bias bits (edge k needs E >= 1)
+    uint32_t key, flags;              // order key; top-left bias bits (edge k needs E >= 1) | kJob*
+    uint32_t view;
     int32_t x0, y0, x1, y1;           // sample box
     uint32_t tx0, ty0, ntx, nty;      // the 8x8 tiles it spans
 };
 
 __device__ __forceinline__ DirectJob direct_job(const int4 w0, const int4 w1, const int4 w2, const int4 w3,
-                                                uint32_t key) {
+                                                uint32_t key, const DrawDesc &d) {
     DirectJob J;
     const uint32_t a0 = w0.x, b0 = w0.y, a1 = w0.w, b1 = w1.x, a2 = w1.z, b2 = w1.w;
     J.A[0] = a0 << kSubpix; J.B[0] = b0 << kSubpix; J.C[0] = (uint32_t)w0.z;
@@ -1637,9 +1645,11 @@ __device__ __forceinline__ DirectJob direct_job(const int4 w0, const int4 w1, co
     J.dz2 = __int_as_float(w3.y) - J.z0;
     J.zbound = __int_as_float(w2.z);
     J.key = key;
-    J.bias = ((int32_t)a0 > 0 || (a0 == 0 && (int32_t)b0 > 0) ? 0u : 1u) |
-             ((int32_t)a1 > 0 || (a1 == 0 && (int32_t)b1 > 0) ? 0u : 2u) |
-             ((int32_t)a2 > 0 || (a2 == 0 && (int32_t)b2 > 0) ? 0u : 4u);
+    J.flags = ((int32_t)a0 > 0 || (a0 == 0 && (int32_t)b0 > 0) ? 0u : 1u) |
+              ((int32_t)a1 > 0 || (a1 == 0 && (int32_t)b1 > 0) ? 0u : 2u) |
+              ((int32_t)a2 > 0 || (a2 == 0 && (int32_t)b2 > 0) ? 0u : 4u) |
+              (d.depth_less ? kJobLess : 0u) | ((d.raster_flags & kRasterTopLeft) ? kJobTopLeft : 0u);
+    J.view = d.view;
     J.x0 = (int16_t)(w3.z & 0xFFFF); J.y0 = w3.z >> 16;
     J.x1 = (int16_t)(w3.w & 0xFFFF); J.y1 = w3.w >> 16;
     J.tx0 = (uint32_t)J.x0 >> 3; J.ty0 = (uint32_t)J.y0 >> 3;
@@ -1648,34 +1658,60 @@ __device__ __forceinline__ DirectJob direct_job(const int4 w0, const int4 w1, co
     return J;
 }
 
+// The fields of a view the rasteriser reads, in registers: read through the descriptor in global
+// memory they would be reloaded after every atomic.
+struct DirectView {
+    const float *depth, *hiz;         // hiz: tile_min (GREATER_EQUAL) or tile_max (LESS)
+    unsigned long long *keys;         // the view's keys
+    uint32_t width, tiles_x;
+    float clear_depth;
+    bool depth_cleared;
+};
+
+__device__ __forceinline__ DirectView direct_view(const BatchParams &bp, const ViewDesc &V, bool less) {
+    DirectView v;
+    v.depth = V.depth;
+    v.hiz = less ? V.tile_max : V.tile_min;
+    v.keys = bp.keys + V.key_base;
+    v.width = V.width;
+    v.tiles_x = V.tiles_x;
+    v.clear_depth = V.clear_depth;
+    v.depth_cleared = (V.clear_flags & kClearDepth) != 0;
+    return v;
+}
+
+// Hierarchical Z per (tile, triangle) against the draw-start snapshot (main.c:1005-1010; the
+// mirrored maximum for LESS); a depth clear folded into this batch resets it (main.c:1212-1214).
+__device__ __forceinline__ bool direct_hiz_rejects(const DirectView &V, const DirectJob &J, uint32_t tile) {
+    const bool less = (J.flags & kJobLess) != 0;
+    const float hiz = V.depth_cleared ? (less ? 1.0f : 0.0f) : V.hiz[tile];
+    return less ? (J.zbound > hiz) : (J.zbound < hiz);
+}
+
 // One covered-sample candidate: coverage (main.c:1028, or the top-left rule), quantised depth, the
 // test against the draw-start depth (main.c:1164-1168), and the fold into the pixel's key.
-__device__ __forceinline__ void direct_pixel(const ViewDesc &V, const DirectJob &J, uint32_t x, uint32_t y, uint32_t E0,
-                                             uint32_t E1, uint32_t E2, bool less, bool top_left, bool depth_cleared,
-                                             unsigned long long *keys) {
-    const bool covered = top_left ? (int32_t)((E0 - (J.bias & 1u)) | (E1 - ((J.bias >> 1) & 1u)) |
-                                              (E2 - ((J.bias >> 2) & 1u))) >= 0
-                                  : (int32_t)(E0 | E1 | E2) > 0;
+__device__ __forceinline__ void direct_pixel(const DirectView &V, const DirectJob &J, uint32_t x, uint32_t y,
+                                             uint32_t E0, uint32_t E1, uint32_t E2) {
+    const uint32_t f = J.flags;
+    const bool covered = (f & kJobTopLeft) ? (int32_t)((E0 - (f & 1u)) | (E1 - ((f >> 1) & 1u)) | (E2 - ((f >> 2) & 1u))) >= 0
+                                           : (int32_t)(E0 | E1 | E2) > 0;
     if (!covered) return;
     const float bb1 = (float)((int32_t)E1 >> (kSubpix * 2)) * J.inv_area;
     const float bb2 = (float)((int32_t)E2 >> (kSubpix * 2)) * J.inv_area;
     float z = J.z0 + J.dz1 * bb1;
     z = z + J.dz2 * bb2;
     const size_t o = (size_t)y * V.width + x;
-    const float dstart = depth_cleared ? V.clear_depth : V.depth[o];
+    const float dstart = V.depth_cleared ? V.clear_depth : V.depth[o];
+    const bool less = (f & kJobLess) != 0;
     if (!(less ? (z < dstart) : (z >= dstart))) return;
     const unsigned long long k = ((unsigned long long)depth_key(z) << 32) | J.key;
-    atomicMax(keys + o, less ? ~k : k);
+    atomicMax(V.keys + o, less ? ~k : k);
 }
 
-// One 8x8 tile (tx, ty) of a job: lane owns pixel (lane & 7, lane >> 3) and the one 4 rows below.
-__device__ __forceinline__ void direct_tile(const ViewDesc &V, const DirectJob &J, uint32_t tx, uint32_t ty, bool less,
-                                            bool top_left, bool depth_cleared, unsigned long long *keys, int lane) {
-    // hierarchical Z per (tile, triangle) against the draw-start snapshot (main.c:1005-1010; the
-    // mirrored maximum for LESS); a depth clear folded into this batch resets it (main.c:1212-1214)
-    const uint32_t tile = ty * V.tiles_x + tx;
-    const float hiz = depth_cleared ? (less ? 1.0f : 0.0f) : (less ? V.tile_max[tile] : V.tile_min[tile]);
-    if (less ? (J.zbound > hiz) : (J.zbound < hiz)) return;   // uniform over the warp
+// One 8x8 tile (tx, ty) of a job by the warp: lane owns pixel (lane & 7, lane >> 3) and the one 4
+// rows below.
+__device__ __forceinline__ void direct_tile(const DirectView &V, const DirectJob &J, uint32_t tx, uint32_t ty, int lane) {
+    if (direct_hiz_rejects(V, J, ty * V.tiles_x + tx)) return;   // uniform over the warp
     const int32_t px = (int32_t)(tx * 8 + (lane & 7)), pya = (int32_t)(ty * 8 + (lane >> 3)), pyb = pya + 4;
     const bool in_x = px >= J.x0 && px <= J.x1;
     const bool ina = in_x && pya >= J.y0 && pya <= J.y1, inb = in_x && pyb >= J.y0 && pyb <= J.y1;
@@ -1683,10 +1719,114 @@ __device__ __forceinline__ void direct_tile(const ViewDesc &V, const DirectJob &
     const uint32_t E0 = J.A[0] * ux + J.B[0] * uy + J.C[0];
     const uint32_t E1 = J.A[1] * ux + J.B[1] * uy + J.C[1];
     const uint32_t E2 = J.A[2] * ux + J.B[2] * uy + J.C[2];
-    if (ina) direct_pixel(V, J, ux, uy, E0, E1, E2, less, top_left, depth_cleared, keys);
-    if (inb)
-        direct_pixel(V, J, ux, uy + 4, E0 + (J.B[0] << 2), E1 + (J.B[1] << 2), E2 + (J.B[2] << 2), less, top_left,
-                     depth_cleared, keys);
+    if (ina) direct_pixel(V, J, ux, uy, E0, E1, E2);
+    if (inb) direct_pixel(V, J, ux, uy + 4, E0 + (J.B[0] << 2), E1 + (J.B[1] << 2), E2 + (J.B[2] << 2));
+}
+
+// The span of row y of a job where all three edge values can be >= 0, clamped to the sample box
+// (lo > hi: none), and the edge values at (x0, y). A covered sample has every edge value >= 0 (the
+// inclusive rule's (E0|E1|E2) > 0 as int32, and the top-left rule's E >= bias): with e = E(x0, y),
+// edge k allows x - x0 >= -e / A (A > 0) or x - x0 <= -e / A (A < 0), or nothing when A = 0 and
+// e < 0. The edge values are exact integers over the box (its extent is at most 1024 pixels, see
+// setup_triangle), and the crossing -e / A computed as float(-e) times a correctly rounded 1/A has a
+// relative error below 2^-22, so it is within a pixel wherever it falls inside a box (crossings
+// further out are clamped away); widened by one pixel the span is conservative, and the exact
+// integer test then decides every pixel in it.
+__device__ __forceinline__ void direct_span(const DirectJob &J, const float *rA, int32_t y, int32_t &lo, int32_t &hi,
+                                            uint32_t *E) {
+    const uint32_t uy = (uint32_t)y, ux0 = (uint32_t)J.x0;
+    lo = J.x0;
+    hi = J.x1;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        E[k] = J.A[k] * ux0 + J.B[k] * uy + J.C[k];
+        const int32_t a = (int32_t)J.A[k], e = (int32_t)E[k];
+        const int32_t cross = (int32_t)floorf(-(float)e * rA[k]);   // where E crosses 0, from x0
+        if (a > 0) lo = max(lo, J.x0 + cross - 1);
+        else if (a < 0) hi = min(hi, J.x0 + cross + 1);
+        else if (e < 0) hi = lo - 1;
+    }
+}
+
+__device__ __forceinline__ void direct_reciprocals(const DirectJob &J, float *rA) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) rA[k] = J.A[k] ? __frcp_rn((float)(int32_t)J.A[k]) : 0.0f;
+}
+
+// A small job by its own lane, row by row: the whole row of a box at most 2 pixels wide or of at
+// most 64 pixels, else the row's span (direct_span), with the edge values stepped by A along the row (E(x + 1) = E(x) + A,
+// wrapping like the reference's int32 sums) and the hierarchical-Z test once per tile the walk
+// enters.
+__device__ __forceinline__ void direct_lane(const DirectView &V, const DirectJob &J) {
+    const bool narrow = J.x1 - J.x0 < 2 || (uint32_t)(J.x1 - J.x0 + 1) * (uint32_t)(J.y1 - J.y0 + 1) <= 64u;
+    float rA[3];
+    if (!narrow) direct_reciprocals(J, rA);
+    uint32_t tile_seen = 0xFFFFFFFFu;
+    bool rejected = false;
+    for (int32_t y = J.y0; y <= J.y1; ++y) {
+        const uint32_t uy = (uint32_t)y;
+        int32_t lo = J.x0, hi = J.x1;
+        uint32_t E[3];
+        if (narrow) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) E[k] = J.A[k] * (uint32_t)J.x0 + J.B[k] * uy + J.C[k];
+        } else {
+            direct_span(J, rA, y, lo, hi, E);
+            if (lo > hi) continue;
+        }
+        const uint32_t skip = (uint32_t)(lo - J.x0);
+        uint32_t E0 = E[0] + J.A[0] * skip, E1 = E[1] + J.A[1] * skip, E2 = E[2] + J.A[2] * skip;
+        for (int32_t x = lo; x <= hi; ++x, E0 += J.A[0], E1 += J.A[1], E2 += J.A[2]) {
+            const uint32_t tile = (uy >> 3) * V.tiles_x + ((uint32_t)x >> 3);
+            if (tile != tile_seen) {
+                tile_seen = tile;
+                rejected = direct_hiz_rejects(V, J, tile);
+            }
+            if (!rejected) direct_pixel(V, J, (uint32_t)x, uy, E0, E1, E2);
+        }
+    }
+}
+
+// A job of at most kDirectWarpPixels sample pixels, by the whole warp, 32 rows at a time: lane r
+// takes the span of row r of the group, a warp scan lays the spans end to end, and their pixels
+// are dealt to the lanes 32 at a time (each lane finds its pixel's row by a binary search over the
+// scan, held in registers and read with shuffles), so that every lane tests a pixel of the
+// triangle's span rather than of its box.
+__device__ __forceinline__ void direct_warp(const DirectView &V, const DirectJob &J, int lane) {
+    float rA[3];
+    direct_reciprocals(J, rA);
+    for (int32_t ybase = J.y0; ybase <= J.y1; ybase += 32) {
+        const int32_t y = ybase + lane;
+        int32_t lo = 0, hi = -1;
+        uint32_t E[3];
+        if (y <= J.y1) direct_span(J, rA, y, lo, hi, E);
+        const uint32_t n = hi >= lo ? (uint32_t)(hi - lo + 1) : 0u;
+        uint32_t incl = n;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31), excl = incl - n;
+        for (uint32_t base = 0; base < total; base += 32) {
+            const uint32_t i = base + (uint32_t)lane;
+            // the row of pixel i: the last lane whose span starts at or before i (rows with an
+            // empty span start where the next one does, so they are never the last)
+            uint32_t r = 0;
+#pragma unroll
+            for (uint32_t step = 16; step; step >>= 1) {
+                const uint32_t s0 = __shfl_sync(0xFFFFFFFFu, excl, (int)(r + step));
+                if (s0 <= i) r += step;
+            }
+            const uint32_t s_r = __shfl_sync(0xFFFFFFFFu, excl, (int)r);
+            const int32_t lo_r = __shfl_sync(0xFFFFFFFFu, lo, (int)r);
+            if (i >= total) continue;
+            const uint32_t ux = (uint32_t)(lo_r + (int32_t)(i - s_r)), uy = (uint32_t)(ybase + (int32_t)r);
+            if (direct_hiz_rejects(V, J, (uy >> 3) * V.tiles_x + (ux >> 3))) continue;
+            direct_pixel(V, J, ux, uy, J.A[0] * ux + J.B[0] * uy + J.C[0], J.A[1] * ux + J.B[1] * uy + J.C[1],
+                         J.A[2] * ux + J.B[2] * uy + J.C[2]);
+        }
+    }
 }
 
 // Queues the chunks of a large job (or a clip fan): entries (key, record slot, first tile, tiles).
@@ -1708,31 +1848,40 @@ __device__ __forceinline__ void direct_push(const BatchParams &bp, uint32_t key,
         bp.queue[base + c] = make_uint4(key, rec, c * kDirectChunk, min(kDirectChunk, ntiles - c * kDirectChunk));
 }
 
+// SW warps of the CTA set up 32 input triangles each (the others only take part in the vertex
+// shader and the rasterisation): 1 for small batches, whose triangles spread thinly over the GPU,
+// 4 for large ones, where the set-up is the work.
+template <int SW>
 __global__ void __launch_bounds__(kDirectBlock) k_direct_raster(BatchParams bp) {
-    __shared__ Vtx s_v[kDirectTris][3];
-    __shared__ DirectJob s_job[kDirectTris];
-    __shared__ uint32_t s_cnt[kDirectTris];            // tiles of each lane's local job (0: none)
+    constexpr int NT = 32 * SW;                        // input triangles per CTA
+    __shared__ Vtx s_v[NT][3];
+    __shared__ DirectJob s_job[SW == 1 ? NT : 1];     // SW == 1: jobs for a whole warp
+    __shared__ uint32_t s_cnt[SW == 1 ? NT : 1];      // 1: staged
     __shared__ uint4 s_push[kDirectListCap];           // jobs to queue: key, record, tiles
-    __shared__ uint4 s_mark[kDirectListCap];           // bin rectangles to mark: tx0, ty0, nx, ny
+    __shared__ uint4 s_mark[kDirectListCap];           // bin rectangles to mark: first bin, nx, ny, row stride
     __shared__ uint32_t s_npush, s_nmark;
     pdl_wait();
-    const DrawDesc &d = bp.draws[0];
-    const ViewDesc &V = bp.views[0];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t g0 = blockIdx.x * kDirectTris;
+    const uint32_t g0 = blockIdx.x * NT;
     if (threadIdx.x == 0) { s_npush = 0; s_nmark = 0; }
-    // vertex shader, one thread per (triangle, vertex), per index as the reference shades
-    if (threadIdx.x < 3 * kDirectTris) {
-        const uint32_t t = threadIdx.x / 3, k = threadIdx.x - 3 * t;
-        if (g0 + t < bp.total_tris) triangle_vertex(bp, d, d.start_index + 3 * (g0 + t) + k, s_v[t][k].v);
+    // vertex shader, one invocation per (triangle, vertex), per index as the reference shades
+    for (uint32_t i = threadIdx.x; i < 3u * NT; i += kDirectBlock) {
+        const uint32_t t = i / 3, k = i - 3 * t, g = g0 + t;
+        if (g < bp.total_tris) {
+            const DrawDesc &d = bp.draws[find_draw(bp, g)];
+            triangle_vertex(bp, d, d.start_index + 3 * (g - d.tri_begin) + k, s_v[t][k].v);
+        }
     }
     __syncthreads();
-    if (warp == 0) {
+    if (warp < SW) {
         // primitive assembly, clipping and setup (main.c:736-913), one thread per input triangle
-        const uint32_t g = g0 + lane;
-        uint32_t mask = 0, entries = 0, cnt = 0;
+        const uint32_t t = (uint32_t)(warp * 32 + lane), g = g0 + t;
+        uint32_t mask = 0, entries = 0;
+        if (SW == 1) s_cnt[lane] = 0;
         if (g < bp.total_tris) {
-            const float *p0 = s_v[lane][0].v, *p1 = s_v[lane][1].v, *p2 = s_v[lane][2].v;
+            const DrawDesc &d = bp.draws[find_draw(bp, g)];
+            const ViewDesc &V = bp.views[d.view];
+            const float *p0 = s_v[t][0].v, *p1 = s_v[t][1].v, *p2 = s_v[t][2].v;
             bool reject = p0[3] == 0 || p1[3] == 0 || p2[3] == 0;   // main.c:759-781
             reject = reject || (p0[0] < -p0[3] && p1[0] < -p1[3] && p2[0] < -p2[3]) ||
                      (p0[0] > +p0[3] && p1[0] > +p1[3] && p2[0] > +p2[3]) ||
@@ -1747,50 +1896,57 @@ __global__ void __launch_bounds__(kDirectBlock) k_direct_raster(BatchParams bp) 
                                        (p0[1] <= +p0[3] && p1[1] <= +p1[3] && p2[1] <= +p2[3]) &&
                                        (p0[2] >= 0.f && p1[2] >= 0.f && p2[2] >= 0.f) &&
                                        (p0[2] <= +p0[3] && p1[2] <= +p1[3] && p2[2] <= +p2[3]));
-                // one emitted triangle: its record, its bin rectangle, its job (local or queued)
+                // one emitted triangle: its bin rectangle, its record where something reads it, and
+                // its job (the lane's own, or queued)
                 auto emit = [&](const Setup &su, const Vtx &a, const Vtx &b, const Vtx &c, uint32_t rec, uint32_t key,
                                 bool may_stage) {
                     int32_t tx0, ty0, tx1, ty1;
                     tile_range(V, su.minx, su.miny, su.maxx, su.maxy, tx0, ty0, tx1, ty1);
                     if (tx1 < tx0 || ty1 < ty0) return;
                     const uint32_t nx = (uint32_t)(tx1 - tx0 + 1), ny = (uint32_t)(ty1 - ty0 + 1);
+                    const uint32_t first = V.bin_base + (uint32_t)ty0 * V.tiles_x + (uint32_t)tx0;
                     entries += nx * ny;
                     if (nx * ny <= 4) {
                         for (uint32_t y = 0; y < ny; ++y)
-                            for (uint32_t x = 0; x < nx; ++x) bp.bin_count[(ty0 + y) * V.tiles_x + tx0 + x] = 1u;
+                            for (uint32_t x = 0; x < nx; ++x) bp.bin_count[first + y * V.tiles_x + x] = 1u;
                     } else {
                         const uint32_t m = atomicAdd(&s_nmark, 1u);
                         if (m < kDirectListCap) {
-                            s_mark[m] = make_uint4((uint32_t)tx0, (uint32_t)ty0, nx, ny);
+                            s_mark[m] = make_uint4(first, nx, ny, V.tiles_x);
                         } else {
-                            for (uint32_t t = 0; t < nx * ny; ++t)
-                                bp.bin_count[(ty0 + t / nx) * V.tiles_x + tx0 + t % nx] = 1u;
+                            for (uint32_t u = 0; u < nx * ny; ++u) bp.bin_count[first + (u / nx) * V.tiles_x + u % nx] = 1u;
                         }
                     }
                     if (su.tminx > su.tmaxx || su.tminy > su.tmaxy) return;   // covers no sample
-                    write_record(bp, rec, 0, d.ps, true, su, a, b, c);
                     int4 R[4];
                     raster_words(su, R);
-                    const DirectJob J = direct_job(R[0], R[1], R[2], R[3], key);
+                    const DirectJob J = direct_job(R[0], R[1], R[2], R[3], key, d);
+                    const uint32_t npix = (uint32_t)(J.x1 - J.x0 + 1) * (uint32_t)(J.y1 - J.y0 + 1);
                     const uint32_t ntiles = J.ntx * J.nty;
-                    if (may_stage && ntiles <= kDirectLocalTiles) {
+                    const bool local = may_stage && npix <= (SW == 1 ? kDirectWarpPixels : kDirectLanePixelsLarge);
+                    // the resolve reads a record unless the depth and ids come from the keys alone;
+                    // the queue always rebuilds its jobs from the record
+                    if (!bp.keys_only || !local) write_record(bp, rec, 0, d.ps, true, su, a, b, c);
+                    if (local && npix <= (SW == 1 ? kDirectLanePixelsSmall : kDirectLanePixelsLarge)) {
+                        direct_lane(direct_view(bp, V, d.depth_less != 0), J);
+                    } else if (SW == 1 && local) {   // (in large batches every local job is the lane's)
                         s_job[lane] = J;
-                        cnt = ntiles;
-                        return;
+                        s_cnt[lane] = 1u;
+                    } else {
+                        const uint32_t m = atomicAdd(&s_npush, 1u);
+                        if (m < kDirectListCap) s_push[m] = make_uint4(key, rec, ntiles, 0u);
+                        else direct_push(bp, key, rec, ntiles, 0, 1);
                     }
-                    const uint32_t m = atomicAdd(&s_npush, 1u);
-                    if (m < kDirectListCap) s_push[m] = make_uint4(key, rec, ntiles, 0u);
-                    else direct_push(bp, key, rec, ntiles, 0, 1);
                 };
                 if (!clipped) {
                     Setup su;
-                    if (setup_triangle(d, s_v[lane][0], s_v[lane][1], s_v[lane][2], su)) {
+                    if (setup_triangle(d, s_v[t][0], s_v[t][1], s_v[t][2], su)) {
                         mask = 1;
-                        emit(su, s_v[lane][0], s_v[lane][1], s_v[lane][2], g, g << 3, true);
+                        emit(su, s_v[t][0], s_v[t][1], s_v[t][2], g, g << 3, true);
                     }
                 } else {
                     Vtx poly[kMaxClipVertices], tmp[kMaxClipVertices];
-                    poly[0] = s_v[lane][0]; poly[1] = s_v[lane][1]; poly[2] = s_v[lane][2];
+                    poly[0] = s_v[t][0]; poly[1] = s_v[t][1]; poly[2] = s_v[t][2];
                     int count = 3;
                     for (int p = 0; p < 6; ++p) clip_by_plane(poly, tmp, count, c_clip_planes[p]);
                     const int nf = count - 2;
@@ -1816,51 +1972,32 @@ __global__ void __launch_bounds__(kDirectBlock) k_direct_raster(BatchParams bp) 
                 }
             }
         }
-        s_cnt[lane] = cnt;
         // statistics (main.c:1238 and the binner's entries, main.c:937-944), staged until the
         // resolve commits them
-        uint32_t n = __popc(mask);
-        n = __reduce_add_sync(0xFFFFFFFFu, n);
+        const uint32_t n = __reduce_add_sync(0xFFFFFFFFu, (uint32_t)__popc(mask));
         entries = __reduce_add_sync(0xFFFFFFFFu, entries);
         if (lane == 0 && n) atomicAdd(bp.stats + kStatAssembled, (unsigned long long)n);
         if (lane == 0 && entries) atomicAdd(bp.stats + kStatBinEntries, (unsigned long long)entries);
-        __syncwarp();
-        // queued jobs, each pushed by the whole warp
-        const uint32_t np = min(s_npush, (uint32_t)kDirectListCap);
-        for (uint32_t i = 0; i < np; ++i) {
-            const uint4 e = s_push[i];
-            direct_push(bp, e.x, e.y, e.z, (uint32_t)lane, 32u);
-        }
     }
     __syncthreads();
-    // the binned tiles of the larger rectangles, by the whole CTA
+    // queued jobs, each pushed by a whole warp; the binned tiles of the larger rectangles, by the CTA
+    const uint32_t np = min(s_npush, (uint32_t)kDirectListCap);
+    for (uint32_t i = (uint32_t)warp; i < np; i += kDirectWarps) {
+        const uint4 e = s_push[i];
+        direct_push(bp, e.x, e.y, e.z, (uint32_t)lane, 32u);
+    }
     const uint32_t nm = min(s_nmark, (uint32_t)kDirectListCap);
     for (uint32_t i = 0; i < nm; ++i) {
         const uint4 r = s_mark[i];
-        for (uint32_t t = threadIdx.x; t < r.z * r.w; t += kDirectBlock)
-            bp.bin_count[(r.y + t / r.z) * V.tiles_x + r.x + t % r.z] = 1u;
+        for (uint32_t u = threadIdx.x; u < r.y * r.z; u += kDirectBlock) bp.bin_count[r.x + (u / r.y) * r.w + u % r.y] = 1u;
     }
-    // the staged jobs' tiles, (job, tile) pairs dealt round-robin to the 4 warps; a warp's cursor
-    // only moves forward, and it loads a job's parameters once
-    const bool less = d.depth_less != 0;
-    const bool top_left = (d.raster_flags & kRasterTopLeft) != 0;
-    const bool depth_cleared = (V.clear_flags & kClearDepth) != 0;
-    uint32_t j = 0, b = (uint32_t)warp, cj = s_cnt[0], loaded = 0xFFFFFFFFu;
-    DirectJob J;
-    while (true) {
-        while (j < kDirectTris && b >= cj) {
-            b -= cj;
-            ++j;
-            cj = j < kDirectTris ? s_cnt[j] : 0u;
+    if (SW == 1) {
+        // the staged jobs, one at a time by a whole warp, dealt round-robin to the CTA's 4 warps
+        for (uint32_t j = (uint32_t)warp; j < (uint32_t)NT; j += kDirectWarps) {
+            if (!s_cnt[j]) continue;   // uniform over the warp
+            const DirectJob J = s_job[j];
+            direct_warp(direct_view(bp, bp.views[J.view], (J.flags & kJobLess) != 0), J, lane);
         }
-        if (j >= kDirectTris) break;
-        if (j != loaded) {
-            J = s_job[j];
-            loaded = j;
-        }
-        const uint32_t ty = b / J.ntx, tx = b - ty * J.ntx;
-        direct_tile(V, J, J.tx0 + tx, J.ty0 + ty, less, top_left, depth_cleared, bp.keys, lane);
-        b += kDirectWarps;
     }
     pdl_trigger();
 }
@@ -1872,29 +2009,28 @@ __global__ void __launch_bounds__(kDirectBlock) k_direct_queue(BatchParams bp) {
         pdl_trigger();
         return;
     }
-    const DrawDesc &d = bp.draws[0];
-    const ViewDesc &V = bp.views[0];
     const int lane = threadIdx.x & 31;
-    const bool less = d.depth_less != 0;
-    const bool top_left = (d.raster_flags & kRasterTopLeft) != 0;
-    const bool depth_cleared = (V.clear_flags & kClearDepth) != 0;
     const uint32_t n = min(ld_volatile_u32(bp.counters + kCtrQueue), bp.queue_capacity);
     const uint32_t nwarps = gridDim.x * kDirectWarps;
     for (uint32_t i = blockIdx.x * kDirectWarps + (threadIdx.x >> 5); i < n; i += nwarps) {
         const uint4 e = bp.queue[i];
+        const DrawDesc &d = bp.draws[find_draw(bp, e.x >> 3)];
         const int4 *R = bp.raster[e.y].w;
-        const DirectJob J = direct_job(__ldg(R), __ldg(R + 1), __ldg(R + 2), __ldg(R + 3), e.x);
+        const DirectJob J = direct_job(__ldg(R), __ldg(R + 1), __ldg(R + 2), __ldg(R + 3), e.x, d);
+        const DirectView V = direct_view(bp, bp.views[J.view], d.depth_less != 0);
         for (uint32_t t = e.z; t < e.z + e.w; ++t) {
             const uint32_t ty = t / J.ntx, tx = t - ty * J.ntx;
-            direct_tile(V, J, J.tx0 + tx, J.ty0 + ty, less, top_left, depth_cleared, bp.keys, lane);
+            direct_tile(V, J, J.tx0 + tx, J.ty0 + ty, lane);
         }
     }
     pdl_trigger();
 }
 
-// One warp per 8x8 tile: the fragments the keys name are the draw's winners; shading, colour and
-// depth writes, hierarchical Z and the folded clears as k_tile does them, then the keys and the
-// tile's mark are cleared for the next draw.
+// One warp per 8x8 tile of the batch's views: the fragments the keys name are the draw's winners;
+// shading, colour and depth writes, hierarchical Z and the folded clears as k_tile does them, then
+// the keys and the tile's mark are cleared for the next draw. With keys_only the winner's depth
+// and ids come from its key (the depth key is exact for every depth but -0, which a draw whose
+// viewport's min_depth is +0 never produces) and no record is read.
 constexpr int kResolveWarps = 4;
 
 __global__ void __launch_bounds__(kResolveWarps * 32) k_direct_resolve(BatchParams bp) {
@@ -1911,10 +2047,11 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_direct_resolve(BatchPara
     if (threadIdx.x == 0) s_active = 0;
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t t = blockIdx.x * kResolveWarps + warp;
-    const ViewDesc &V = bp.views[0];
-    if (t < bp.total_tiles) {
-        const DrawDesc &D = bp.draws[0];
+    const uint32_t gtile = blockIdx.x * kResolveWarps + warp;
+    if (gtile < bp.total_tiles) {
+        const ViewDesc &V = bp.views[find_view(bp, gtile)];
+        const uint32_t t = gtile - V.tile_base;
+        const DrawDesc &D = bp.draws[V.draw_begin];
         const bool less = D.depth_less != 0;
         const uint32_t tx = t % V.tiles_x, ty = t / V.tiles_x;
         const int32_t x0 = (int32_t)tx * kTile, y0 = (int32_t)ty * kTile;
@@ -1923,7 +2060,9 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_direct_resolve(BatchPara
         const bool valid1 = px < (int32_t)V.width && py1 < (int32_t)V.height;
         const size_t o0 = (size_t)py0 * V.width + px, o1 = (size_t)py1 * V.width + px;
         const bool depth_cleared = (V.clear_flags & kClearDepth) != 0;
-        const uint32_t marked = bp.bin_count[t];
+        unsigned long long *keys = bp.keys + V.key_base;
+        const uint32_t bin = V.bin_base + t;
+        const uint32_t marked = bp.bin_count[bin];
         if (!marked) {   // no triangle binned here (uniform over the warp)
             if (V.clear_flags) {
                 if (valid0) write_cleared(V, o0, V.clear_depth);
@@ -1935,12 +2074,12 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_direct_resolve(BatchPara
             }
         } else {
             if (lane == 0) {
-                bp.bin_count[t] = 0u;
+                bp.bin_count[bin] = 0u;
                 atomicAdd(&s_active, 1u);
             }
             unsigned long long k0 = 0, k1 = 0;
-            if (valid0) { k0 = bp.keys[o0]; if (k0) bp.keys[o0] = 0ull; }
-            if (valid1) { k1 = bp.keys[o1]; if (k1) bp.keys[o1] = 0ull; }
+            if (valid0) { k0 = keys[o0]; if (k0) keys[o0] = 0ull; }
+            if (valid1) { k1 = keys[o1]; if (k1) keys[o1] = 0ull; }
             if (less) { k0 = k0 ? ~k0 : 0ull; k1 = k1 ? ~k1 : 0ull; }
             const uint32_t win0 = k0 ? (uint32_t)k0 : 0xFFFFFFFFu, win1 = k1 ? (uint32_t)k1 : 0xFFFFFFFFu;
             float dcur0 = 0.0f, dcur1 = 0.0f;
@@ -1956,21 +2095,33 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_direct_resolve(BatchPara
                 mn = fmin_ref(mn, a);
                 mx = fmax_ref(mx, b);
             }
-            // one pixel-shader invocation per written pixel, compacted over the warp
-            const uint32_t m0 = __ballot_sync(0xFFFFFFFFu, win0 != 0xFFFFFFFFu && valid0);
-            const uint32_t m1 = __ballot_sync(0xFFFFFFFFu, win1 != 0xFFFFFFFFu && valid1);
-            const uint32_t n0 = __popc(m0), n = n0 + __popc(m1);
-            for (uint32_t q0 = 0; q0 < n; q0 += 32) {
-                const uint32_t q = q0 + lane;
-                const uint32_t half = q < n0 ? 0u : 1u;
-                uint32_t src = 0;
-                if (q < n) {
-                    const uint32_t m = half ? m1 : m0, k = half ? q - n0 : q;
-                    src = m == 0xFFFFFFFFu ? k : nth_set_bit(m, k);
+            if (bp.keys_only) {
+                // the null pixel shader with depth, draw-id and primitive-id outputs only
+                auto keyed = [&](size_t o, uint32_t win, float dnew) {
+                    if (V.clear_flags & kClearColor) V.color[o] = V.clear_color;
+                    V.depth[o] = dnew;
+                    if (V.vis_draw) V.vis_draw[o] = D.draw_seq;
+                    if (V.vis_prim) V.vis_prim[o] = (win >> 3) - D.tri_begin;
+                };
+                if (valid0 && win0 != 0xFFFFFFFFu) keyed(o0, win0, dcur0);
+                if (valid1 && win1 != 0xFFFFFFFFu) keyed(o1, win1, dcur1);
+            } else {
+                // one pixel-shader invocation per written pixel, compacted over the warp
+                const uint32_t m0 = __ballot_sync(0xFFFFFFFFu, win0 != 0xFFFFFFFFu && valid0);
+                const uint32_t m1 = __ballot_sync(0xFFFFFFFFu, win1 != 0xFFFFFFFFu && valid1);
+                const uint32_t n0 = __popc(m0), n = n0 + __popc(m1);
+                for (uint32_t q0 = 0; q0 < n; q0 += 32) {
+                    const uint32_t q = q0 + lane;
+                    const uint32_t half = q < n0 ? 0u : 1u;
+                    uint32_t src = 0;
+                    if (q < n) {
+                        const uint32_t m = half ? m1 : m0, k = half ? q - n0 : q;
+                        src = m == 0xFFFFFFFFu ? k : nth_set_bit(m, k);
+                    }
+                    const uint32_t wa = __shfl_sync(0xFFFFFFFFu, win0, src), wb = __shfl_sync(0xFFFFFFFFu, win1, src);
+                    if (q >= n) continue;
+                    shade_pixel(bp, V, half ? wb : wa, x0 + (int32_t)(src & 7), y0 + (int32_t)(src >> 3) + (half ? 4 : 0));
                 }
-                const uint32_t wa = __shfl_sync(0xFFFFFFFFu, win0, src), wb = __shfl_sync(0xFFFFFFFFu, win1, src);
-                if (q >= n) continue;
-                shade_pixel(bp, V, half ? wb : wa, x0 + (int32_t)(src & 7), y0 + (int32_t)(src >> 3) + (half ? 4 : 0));
             }
             if (V.clear_flags) {
                 if (valid0 && win0 == 0xFFFFFFFFu) write_cleared(V, o0, dcur0);
@@ -2113,9 +2264,11 @@ cudaError_t launch_scatter(const BatchParams &bp, int num_sms, cudaStream_t stre
     return launch_chained(k_scatter, blocks, kScatterBlock, stream, bp);
 }
 
-cudaError_t launch_direct_raster(const BatchParams &bp, cudaStream_t stream) {
-    return launch_chained(k_direct_raster, (bp.total_tris + kDirectTris - 1) / kDirectTris, (uint32_t)kDirectBlock,
-                          stream, bp);
+cudaError_t launch_direct_raster(const BatchParams &bp, int num_sms, cudaStream_t stream) {
+    // one set-up warp per CTA while that still gives every SM a few CTAs, else four
+    if (bp.total_tris <= (uint32_t)num_sms * 32u * 16u)
+        return launch_chained(k_direct_raster<1>, (bp.total_tris + 31) / 32, (uint32_t)kDirectBlock, stream, bp);
+    return launch_chained(k_direct_raster<4>, (bp.total_tris + 127) / 128, (uint32_t)kDirectBlock, stream, bp);
 }
 
 cudaError_t launch_direct_queue(const BatchParams &bp, int num_sms, cudaStream_t stream) {
