@@ -8,7 +8,9 @@ synthetic data. One step renders the whole frame (clears + 12 draws) as one batc
 
 value     input triangles per second over the K timed steps (Mtri/s), inputs resident in HBM.
 e2e       the same frame through the C ABI from host buffers: every step uploads the vertex and
-          index buffers and both textures from pinned host memory and reads the colour target back.
+          index buffers and both textures from pinned host memory and reads the colour target back;
+          two device handles alternate so that one step's readback overlaps the next one's uploads
+          (e2e.serial: one context, step after step).
 per_draw  the same frame drawn per draw on the immediate context (one launch sequence per draw).
 gpix_per_s fragments written (the oracle's count of covered, hierarchical-Z and depth-test passing
           fragments in serial order) per second.
@@ -801,61 +803,96 @@ def main():
     stage_avg = {k: (v[0] / v[1] if v[1] else 0.0) for k, v in stages.items()}
 
     # --- e2e through the C ABI from pinned host buffers
-    host_bufs = []
-    pinned = []
+    import ctypes
+    pinned = {}
 
     def pin(a):
-        t = torch.from_numpy(np.ascontiguousarray(a).view(np.uint8).reshape(-1)).pin_memory()
-        pinned.append(t)
-        return t.numpy()
+        if id(a) not in pinned:
+            t = torch.from_numpy(np.ascontiguousarray(a).view(np.uint8).reshape(-1)).pin_memory()
+            pinned[id(a)] = (t, t.numpy())
+        return pinned[id(a)][1]
 
-    # in the order the frame consumes them: the vertex stage reads vertex buffers and its texture,
-    # geometry the index buffers, the tile kernel the pixel shader's texture; each stage waits only
-    # for its own inputs' copies, so the later copies overlap the earlier stages
-    vs_tex_ids = {id(d.vs_tex.data) for d in frame.draws if d.vs_tex is not None}
-    for want in (api.BIND_VERTEX_BUFFER, api.BIND_INDEX_BUFFER):
-        for key, (buf, arr) in r._buffers.items():
-            if key[1] == want:
-                host_bufs.append((buf, pin(arr)))
-    host_tex = [(tex, pin(t.data)) for tex, t in r._textures.values()]
-    host_vs_tex = [x for x, (_, t) in zip(host_tex, r._textures.values()) if id(t.data) in vs_tex_ids]
-    host_ps_tex = [x for x, (_, t) in zip(host_tex, r._textures.values()) if id(t.data) not in vs_tex_ids]
-    n_vb = sum(1 for key in r._buffers if key[1] == api.BIND_VERTEX_BUFFER)
-    h2d = sum(a.nbytes for _, a in host_bufs) + sum(a.nbytes for _, a in host_tex)
-    rt = r.targets[0][0]
-    out_img = torch.empty((frame.height, frame.width), dtype=torch.int32).pin_memory().numpy().view(np.uint32)
-    d2h = out_img.nbytes
-    lib = api.load_library()
-    import ctypes
+    def upload_plan(rr):
+        """The renderer's resources with their pinned host sources, in the order the frame consumes
+        them: the vertex stage reads vertex buffers and its texture, geometry the index buffers, the
+        tile kernel the pixel shader's texture; each stage waits only for its own inputs' copies, so
+        the later copies overlap the earlier stages."""
+        vs_tex_ids = {id(d.vs_tex.data) for d in frame.draws if d.vs_tex is not None}
+        plan = []
+        for key, (buf, arr) in rr._buffers.items():
+            if key[1] == api.BIND_VERTEX_BUFFER:
+                plan.append(("buf", buf, pin(arr)))
+        for tex, t in rr._textures.values():
+            if id(t.data) in vs_tex_ids:
+                plan.append(("tex", tex, pin(t.data)))
+        for key, (buf, arr) in rr._buffers.items():
+            if key[1] == api.BIND_INDEX_BUFFER:
+                plan.append(("buf", buf, pin(arr)))
+        for tex, t in rr._textures.values():
+            if id(t.data) not in vs_tex_ids:
+                plan.append(("tex", tex, pin(t.data)))
+        return plan
 
-    def upload_buf(buf, a):
-        ctx.lib.mlv_update_buffer_async(ctx.handle, buf.handle, 0, a.ctypes.data_as(ctypes.c_void_p), a.nbytes)
+    def issue(rr, plan):
+        """One step's uploads (queued, from pinned memory that stays unchanged) and its frame."""
+        c = rr.device.immediate
+        for kind, res, a in plan:
+            ptr = a.ctypes.data_as(ctypes.c_void_p)
+            if kind == "buf":
+                c.lib.mlv_update_buffer_async(c.handle, res.handle, 0, ptr, a.nbytes)
+            else:
+                c.lib.mlv_update_texture2d_async(c.handle, res.handle, ptr, 0)
+        rr.render_batched()
 
-    def upload_tex(tex, a):
-        ctx.lib.mlv_update_texture2d_async(ctx.handle, tex.handle, a.ctypes.data_as(ctypes.c_void_p), 0)
+    out_imgs = [torch.empty((frame.height, frame.width), dtype=torch.int32).pin_memory().numpy().view(np.uint32)
+                for _ in range(2)]
 
-    def e2e_step():
-        # queued uploads from pinned memory (unchanged until the readback below synchronises)
-        for buf, a in host_bufs[:n_vb]:
-            upload_buf(buf, a)
-        for tex, a in host_vs_tex:
-            upload_tex(tex, a)
-        for buf, a in host_bufs[n_vb:]:
-            upload_buf(buf, a)
-        for tex, a in host_ps_tex:
-            upload_tex(tex, a)
-        r.render_batched()
-        ctx.lib.mlv_read_texture2d(ctx.handle, rt.handle, out_img.ctypes.data_as(ctypes.c_void_p), 0)
+    def read(rr, k):
+        c = rr.device.immediate
+        c.lib.mlv_read_texture2d(c.handle, rr.targets[0][0].handle, out_imgs[k % 2].ctypes.data_as(ctypes.c_void_p), 0)
 
+    plan1 = upload_plan(r)
+    h2d = sum(a.nbytes for _, _, a in plan1)
+    d2h = out_imgs[0].nbytes
+
+    # one context: upload, render and read back, step after step
     for _ in range(3):
-        e2e_step()
+        issue(r, plan1)
+        read(r, 0)
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        e2e_step()
+        issue(r, plan1)
+        read(r, 0)
+    torch.cuda.synchronize()
+    e2e_serial_s = replicas.job_time((time.perf_counter() - t0) / args.steps, dist, "cuda")
+
+    # two device handles on this GPU, each with its own copy of the frame's resources, stream and
+    # immediate context, alternating (double-buffered frames): step k's uploads and rendering are
+    # issued before step k - 1's result is read back, so one frame's readback and rendering overlap
+    # the next one's uploads. Every step still uploads all its inputs and reads its image back.
+    dev_b = api.Device(local)
+    dev_b.immediate.set_tuning(**ctx.tuning())
+    r_b = api.FrameRenderer(dev_b, frame)
+    r_b.render_batched()
+    pair = [(r, plan1), (r_b, upload_plan(r_b))]
+    for k in range(4):
+        issue(*pair[k % 2])
+        read(pair[k % 2][0], k)
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    issue(*pair[0])
+    for k in range(1, args.steps):
+        issue(*pair[k % 2])
+        read(pair[(k - 1) % 2][0], k - 1)
+    read(pair[(args.steps - 1) % 2][0], args.steps - 1)
     torch.cuda.synchronize()
     e2e_s = replicas.job_time((time.perf_counter() - t0) / args.steps, dist, "cuda")
+    e2e_same = bool(np.array_equal(out_imgs[0], out_imgs[1]) and np.array_equal(out_imgs[0], r.read(0)["color"]))
+    r_b.destroy()
+    dev_b.destroy()
 
     diff = multiview = single = None
     if not args.no_diff:
@@ -908,7 +945,14 @@ def main():
             "per_draw": {"value": round(tris / (pd_ms / 1e3) / 1e6, 3), "unit": "Mtri/s", "ms_per_frame": round(pd_ms, 4),
                          "batched_speedup": round(pd_ms / ms, 3)},
             "e2e": {"value": round(tris * world / e2e_s / 1e6, 3), "unit": "Mtri/s", "h2d_bytes_per_step": int(h2d),
-                    "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_s * 1e3, 3)},
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_s * 1e3, 3),
+                    "mode": "two device handles alternating (double-buffered frames): each step uploads its "
+                            "inputs from pinned host memory, renders, and reads its image back; a step's "
+                            "readback overlaps the next step's uploads",
+                    "images_identical": e2e_same,
+                    "serial": {"value": round(tris * world / e2e_serial_s / 1e6, 3), "unit": "Mtri/s",
+                               "ms_per_step": round(e2e_serial_s * 1e3, 3),
+                               "mode": "one context, upload, render and read back step after step"}},
             "roofline": {"bound": "hbm", "achieved": round(frame_achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(frame_achieved / peak, 4), "peak_kind": peak_kind,
                          "counts": "the whole frame: 4 I + 32 V + sampled textures (capped at 4 taps per "
