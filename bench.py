@@ -736,7 +736,9 @@ def main():
     # (the first execution sizes the workspace and captures the graph)
     from malevich_gb300 import autotune
     r.render_batched()
-    tuned = autotune.autotune(dev, r, repeats=5, warmup=2) if not args.no_autotune else None
+    # (a path forced by --small-draw-triangles stays; otherwise the tuner picks it first)
+    tuned = autotune.autotune(dev, r, repeats=5, warmup=2, choose_path=args.small_draw_triangles < 0) \
+        if not args.no_autotune else None
     for _ in range(max(args.warmup, 3)):
         r.render_batched()
     ctx.finish()

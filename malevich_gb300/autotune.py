@@ -13,8 +13,11 @@ pixels: the tile grid is observable through the reference's per-tile depth bound
 (main.c:1005-1010), so it is not tuned.
 
 `autotune` times a renderer's batched execution (its command list, replayed as a CUDA graph)
-for every point of a search space with CUDA events on the context's stream, flushing L2 between
-timed runs, and leaves the fastest point set on the context.
+with CUDA events on the context's stream, flushing L2 between timed runs, and leaves the fastest
+setting on the context. It first picks the path: the small-draw path (no binning, for batches of
+one draw per view) or the binned one (`small_draw_triangles` 0); when the small-draw path wins for
+a batch that takes it, the binned path's launch shapes have no effect and are not swept. Otherwise
+it sweeps every point of the launch-shape space.
 """
 import itertools
 
@@ -77,22 +80,51 @@ def event_timer(context, repeats=5, warmup=2, flush_bytes=256 << 20):
     return time_fn
 
 
-def autotune(device, renderer, space=None, time_fn=None, repeats=5, warmup=2):
-    """Sweeps the search space for `renderer.render_batched()` on the device's immediate
-    context, sets the fastest point and returns {"best": point, "ms": ms, "results": [...]}.
-    The outputs do not depend on the point (launch shapes only); `time_fn(fn) -> ms` may be
-    given (the default times with CUDA events)."""
+# small_draw_triangles: the binned path only, or the small-draw path wherever a batch allows it
+PATHS = (0, 0xFFFFFFFF)
+
+
+def launches_per_batch(ctx, renderer):
+    """Kernel launches one `render_batched()` makes with the context's current tuning (None when
+    the context keeps no statistics)."""
+    if not hasattr(ctx, "reset_stats"):
+        return None
+    ctx.reset_stats()
+    renderer.render_batched()
+    return ctx.stats()["kernel_launches"]
+
+
+def autotune(device, renderer, space=None, time_fn=None, repeats=5, warmup=2, choose_path=True):
+    """Tunes `renderer.render_batched()` on the device's immediate context: the path first (when
+    choose_path), then, unless the small-draw path won for this batch, every point of the
+    launch-shape space. Sets the fastest setting and returns {"best": setting, "ms": ms,
+    "results": [(point, ms)] of the sweep, "path": [(setting, ms)] of the path choice}. The outputs
+    depend on neither; `time_fn(fn) -> ms` may be given (the default times with CUDA events)."""
     ctx = device.immediate
     time_fn = time_fn or event_timer(ctx, repeats=repeats, warmup=warmup)
     base = ctx.tuning()
-    results = []
+    results, path = [], []
     try:
+        fixed = {}
+        if choose_path:
+            launches = []
+            for sd in PATHS:
+                ctx.set_tuning(small_draw_triangles=sd)
+                launches.append(launches_per_batch(ctx, renderer))
+                path.append(({"small_draw_triangles": sd}, float(time_fn(renderer.render_batched))))
+            fixed, path_ms = pick(path)
+            ctx.set_tuning(**fixed)
+            # the small-draw path runs 3 kernels a batch where the binned one runs 4 or more (and the
+            # same clears): fewer launches with it allowed means the batch takes it
+            small = None not in launches and launches[1] < launches[0]
+            if fixed["small_draw_triangles"] and small:
+                return {"best": dict(fixed), "ms": path_ms, "results": [], "path": path}
         for point in candidates(space):
-            ctx.set_tuning(**point)
-            results.append((point, float(time_fn(renderer.render_batched))))
+            ctx.set_tuning(**dict(point, **fixed))
+            results.append((dict(point, **fixed), float(time_fn(renderer.render_batched))))
     except Exception:
         ctx.set_tuning(**base)
         raise
     best, ms = pick(results)
     ctx.set_tuning(**best)
-    return {"best": best, "ms": ms, "results": results}
+    return {"best": best, "ms": ms, "results": results, "path": path}

@@ -25,7 +25,8 @@ def test_pick_takes_the_fastest_and_keeps_the_first_tie():
 
 class _FakeCtx:
     def __init__(self):
-        self.t = {"tile_warps_per_block": 4, "warps_per_tile": 1, "geometry_block": 256, "big_triangle_tiles": 16}
+        self.t = {"tile_warps_per_block": 4, "warps_per_tile": 1, "geometry_block": 256, "big_triangle_tiles": 16,
+                  "small_draw_triangles": 0xFFFFFFFF}
         self.history = []
 
     def tuning(self):
@@ -51,10 +52,28 @@ def test_autotune_sets_the_fastest_point():
     cost = lambda: dev.immediate.t["tile_warps_per_block"] * 10 + abs(dev.immediate.t["geometry_block"] - 128) + \
         dev.immediate.t["big_triangle_tiles"] * 0.1
     out = autotune.autotune(dev, _FakeRenderer(), time_fn=lambda fn: (fn(), cost())[1])
+    # the path choice ties (the cost ignores it): the binned path, first in order, then the sweep
     assert out["best"] == {"big_triangle_tiles": 4, "geometry_block": 128, "tile_warps_per_block": 2,
-                           "warps_per_tile": 1}
+                           "warps_per_tile": 1, "small_draw_triangles": 0}
     assert dev.immediate.t == out["best"]
-    assert len(out["results"]) == 72
+    assert len(out["results"]) == 72 and len(out["path"]) == 2
+
+
+def test_autotune_skips_the_sweep_when_the_small_draw_path_wins():
+    class _Ctx(_FakeCtx):
+        def reset_stats(self):
+            self.launches = 0
+
+        def stats(self):
+            return {"batch_count": 1, "kernel_launches": 3 if self.t.get("small_draw_triangles") else 4}
+
+    dev = _FakeDevice()
+    dev.immediate = _Ctx()
+    cost = lambda: 1.0 if dev.immediate.t.get("small_draw_triangles") else 2.0
+    out = autotune.autotune(dev, _FakeRenderer(), time_fn=lambda fn: (fn(), cost())[1])
+    assert out["best"] == {"small_draw_triangles": autotune.PATHS[1]} and out["results"] == []
+    assert dev.immediate.t["small_draw_triangles"] == autotune.PATHS[1]
+    assert dev.immediate.t["tile_warps_per_block"] == 4   # not swept
 
 
 def test_autotune_restores_the_tuning_on_error():
@@ -70,7 +89,7 @@ def test_autotune_restores_the_tuning_on_error():
     with pytest.raises(RuntimeError):
         autotune.autotune(dev, _FakeRenderer(), time_fn=bad_timer)
     assert dev.immediate.t == {"tile_warps_per_block": 4, "warps_per_tile": 1, "geometry_block": 256,
-                               "big_triangle_tiles": 16}
+                               "big_triangle_tiles": 16, "small_draw_triangles": 0xFFFFFFFF}
 
 
 @pytest.mark.gpu
@@ -93,3 +112,27 @@ def test_autotuned_batched_output_equals_default(device):
             assert np.array_equal(got[key].view(np.uint32), want[i][key].view(np.uint32)), (i, key)
     r.destroy()
     ctx.set_tuning(**base)
+
+
+@pytest.mark.gpu
+def test_autotune_picks_a_path_for_a_single_draw_and_keeps_the_output(device):
+    from malevich_gb300 import api
+    frame = scenes.config1_plain(seed=2, width=320, height=192, tex_size=64, level=4)
+    ctx = device.immediate
+    base = ctx.tuning()
+    r = api.FrameRenderer(device, frame, visibility=True)
+    try:
+        r.render_batched()
+        want = r.read(0)
+        out = autotune.autotune(device, r, repeats=2, warmup=1)
+        assert [p["small_draw_triangles"] for p, _ in out["path"]] == list(autotune.PATHS)
+        assert ctx.tuning()["small_draw_triangles"] == out["best"]["small_draw_triangles"]
+        # the sweep runs only when the binned path won
+        assert (out["results"] == []) == (out["best"]["small_draw_triangles"] != 0)
+        r.render_batched()
+        got = r.read(0)
+        for key in ("color", "depth", "vis_tri", "vis_draw", "vis_bary"):
+            assert np.array_equal(got[key].view(np.uint32), want[key].view(np.uint32)), key
+    finally:
+        r.destroy()
+        ctx.set_tuning(**base)
