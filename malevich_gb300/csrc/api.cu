@@ -32,7 +32,7 @@ cudaError_t launch_fill_u32(uint32_t *p, size_t n, uint32_t value, const uint32_
 cudaError_t launch_fill_many(const FillJob *d_jobs, uint32_t njobs, uint32_t nchunks, const uint32_t *error,
                              cudaStream_t stream);
 cudaError_t launch_vertex(const BatchParams &bp, cudaStream_t stream);
-cudaError_t launch_geometry(const BatchParams &bp, uint32_t block, cudaStream_t stream);
+cudaError_t launch_geometry(const BatchParams &bp, uint32_t block, int num_sms, cudaStream_t stream);
 cudaError_t launch_scan(const BatchParams &bp, cudaStream_t stream);
 cudaError_t launch_rank(const BatchParams &bp, cudaStream_t stream);
 cudaError_t launch_scatter(const BatchParams &bp, int num_sms, cudaStream_t stream);
@@ -173,6 +173,7 @@ struct Workspace {
     bool keep_geom = false;
     uint16_t *tri_info = nullptr;
     uint2 *bins_of = nullptr;
+    uint32_t *clip_list = nullptr;
     uint32_t *rank = nullptr;
     uint32_t tri_cap = 0;
     uint32_t *bin_count = nullptr, *bin_start = nullptr;
@@ -374,9 +375,12 @@ static mlv_status ensure_workspace(mlv_context_t *c, const BatchSizes &s, bool k
             w.rank = nullptr;
             cudaFree(w.bins_of);
             w.bins_of = nullptr;
-            uint32_t cap2 = 0, cap3 = 0;
+            cudaFree(w.clip_list);
+            w.clip_list = nullptr;
+            uint32_t cap2 = 0, cap3 = 0, cap4 = 0;
             MLV_TRY(grow(&w.rank, cap2, cap, sizeof(uint32_t)));
             MLV_TRY(grow(&w.bins_of, cap3, cap, sizeof(uint2)));
+            MLV_TRY(grow(&w.clip_list, cap4, cap, sizeof(uint32_t)));
             changed = true;
         }
         w.tri_cap = cap;
@@ -747,6 +751,7 @@ static mlv_status launch_draws(mlv_context_t *c, const Plan &p, DrawDesc *d_draw
     bp.geom = w.keep_geom ? w.geom : nullptr;
     bp.tri_info = w.tri_info;
     bp.bins_of = w.bins_of;
+    bp.clip_list = w.clip_list;
     bool want_rank = c->capture_infos;
     for (const ViewDesc &v : p.views) want_rank = want_rank || v.vis_tri != nullptr;
     bp.want_rank = want_rank ? 1u : 0u;
@@ -778,7 +783,7 @@ static mlv_status launch_draws(mlv_context_t *c, const Plan &p, DrawDesc *d_draw
     cudaEvent_t e;
     // the clip-fan slot counter starts at zero for every batch (reset before the first kernel, so
     // that the batch's kernels follow one another directly)
-    CUDA_TRY(cudaMemsetAsync(w.counters + kCtrOverflow, 0, 2 * sizeof(uint32_t), c->stream));
+    CUDA_TRY(cudaMemsetAsync(w.counters + kCtrOverflow, 0, 3 * sizeof(uint32_t), c->stream));
     if (p.direct) {
         // the small-draw path: raster (vertex shader, setup, small triangles), queued large
         // triangles, resolve; stages 1, 3 and 4 of the stage timers
@@ -806,8 +811,9 @@ static mlv_status launch_draws(mlv_context_t *c, const Plan &p, DrawDesc *d_draw
     }
     CUDA_TRY(wait_for(p.wait_index));
     ev_begin(c, 1, &e);
-    CUDA_TRY(launch_geometry(bp, c->tuning.geometry_block, c->stream));
+    CUDA_TRY(launch_geometry(bp, c->tuning.geometry_block, c->device->num_sms, c->stream));   // k_geometry, then k_clip
     ev_end(c, e);
+    c->host_stats[4] += 1;
     if (bp.want_rank) {
         CUDA_TRY(launch_rank(bp, c->stream));
         c->host_stats[4] += 1;
@@ -1011,6 +1017,7 @@ MLV_API mlv_status mlv_create_device(int ordinal, mlv_device *out) {
 
 static void free_workspace(Workspace &w) {
     cudaFree(w.raster); cudaFree(w.shade); cudaFree(w.geom); cudaFree(w.tri_info); cudaFree(w.bins_of); cudaFree(w.rank);
+    cudaFree(w.clip_list);
     cudaFree(w.bin_count); cudaFree(w.bin_start); cudaFree(w.list); cudaFree(w.info_mask);
     cudaFree(w.scan_status); cudaFree(w.scan_status2); cudaFree(w.counters); cudaFree(w.stats);
     cudaFree(w.error); cudaFree(w.d_draws); cudaFree(w.d_views); cudaFree(w.d_fills); cudaFree(w.vs_out);

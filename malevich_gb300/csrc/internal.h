@@ -150,6 +150,7 @@ struct BatchParams {
     TriShade *shade;
     TriGeom *geom;                       // nullptr unless the geometry is kept
     uint16_t *tri_info;                  // [total_tris]: emitted-fan mask | clipped << 8
+    uint32_t *clip_list;                 // [total_tris]: the input triangles k_geometry leaves to k_clip
     uint2 *bins_of;                      // [total_tris]: an unclipped triangle's (first bin, nx | ny << 16);
                                          // (0, 0) no bins, (0, kBinsClipped) clipped: see its fans
     uint32_t *rank;                      // [total_tris]: assembled triangles before g (exclusive)
@@ -175,7 +176,8 @@ struct BatchParams {
 
 enum Counter : int {
     kCtrRankTicket = 0, kCtrRankDone, kCtrRankEpoch,
-    kCtrOverflow, kCtrQueue,             // per-batch: clip-fan slots used; small-draw queue entries used
+    kCtrOverflow, kCtrQueue, kCtrClip,   // per-batch: clip-fan slots used; small-draw queue entries
+                                         // used; triangles listed for clipping (clip_list)
     kCtrScanTicket, kCtrScanDone, kCtrScanEpoch,
     kCtrCount = 16
 };

@@ -6,7 +6,9 @@
 //   k_geometry  IA + primitive assembly/clip/setup + per-(tile, draw) bin counts
 //               (main.c:662-913 and the counting half of the binner, 924-936). One thread per input
 //               triangle; records go to slots indexed by input triangle (see BatchParams), so the
-//               reference's serial order is the slot order and no compaction is needed.
+//               reference's serial order is the slot order and no compaction is needed. Triangles
+//               that need clipping are listed instead, for
+//   k_clip      one warp per listed triangle: clipping (main.c:649-661) and its fans' setup.
 //   k_rank      only when visibility or TileInfo outputs are requested: the reference's compact
 //               triangle index (its `out_triangle_index`, main.c:873-875), by an exclusive scan of
 //               the per-input-triangle output counts.
@@ -291,14 +293,21 @@ __device__ __forceinline__ void write_record(const BatchParams &bp, uint32_t rec
     h[4] = make_float4(v0.v[8], v1.v[8], v2.v[8], __uint_as_float(extra));
 }
 
-// clip_by_plane, main.c:609-647 (Sutherland-Hodgman on one normalised plane, plane_d = 0)
+// clip_by_plane, main.c:609-647 (Sutherland-Hodgman on one normalised plane, plane_d = 0), on
+// poly (count vertices), with tmp as scratch. A polygon with every vertex inside (distance > -0)
+// comes out of the reference's pass unchanged, vertex for vertex and in order, so that pass is
+// skipped: most planes of a clipped triangle then cost its distances only, not two copies of it.
 __device__ void clip_by_plane(Vtx *poly, Vtx *tmp, int &count, const float *n) {
-    int nv = count, out = 0;
+    const int nv = count;
     if (nv <= 0) return;
+    bool all_in = true;
+    for (int i = 0; i < nv; ++i) all_in = all_in && dot4_lr(n, poly[i].v[0], poly[i].v[1], poly[i].v[2], poly[i].v[3]) > -0.0f;
+    if (all_in) return;
+    int out = 0;
     float cd = dot4_lr(n, poly[0].v[0], poly[0].v[1], poly[0].v[2], poly[0].v[3]);
     bool cin = cd > -0.0f;
     for (int i = 0; i < nv; ++i) {
-        int next = (i + 1) % nv;
+        const int next = i + 1 == nv ? 0 : i + 1;
         if (cin && out < kMaxClipVertices) tmp[out++] = poly[i];
         const Vtx &pn = poly[next];
         float nd = dot4_lr(n, pn.v[0], pn.v[1], pn.v[2], pn.v[3]);
@@ -315,6 +324,45 @@ __device__ void clip_by_plane(Vtx *poly, Vtx *tmp, int &count, const float *n) {
     }
     count = out;
     for (int i = 0; i < out; ++i) poly[i] = tmp[i];
+}
+
+// The same pass run by a whole warp on a polygon in shared memory (poly: count vertices, at most
+// kMaxClipVertices), into out. Lane i takes vertex i and the edge from it to the next: the same
+// distances, t and interpolations as the serial pass, written where the serial pass would put them
+// (an exclusive scan of the lanes' emission counts); emissions past kMaxClipVertices are dropped,
+// as the serial pass drops them. Returns false, out untouched, when every vertex is inside (the
+// pass would give the polygon back unchanged). Every lane calls it with the same count and plane.
+__device__ bool clip_by_plane_warp(const Vtx *poly, Vtx *out, int &count, const float *n, int lane) {
+    const int nv = count;
+    if (nv <= 0) return false;
+    const bool mine = lane < nv;
+    const float dist = mine ? dot4_lr(n, poly[lane].v[0], poly[lane].v[1], poly[lane].v[2], poly[lane].v[3]) : 0.0f;
+    const bool in = mine && dist > -0.0f;
+    const uint32_t inm = __ballot_sync(0xFFFFFFFFu, in);
+    if (inm == (nv >= 32 ? 0xFFFFFFFFu : (1u << nv) - 1u)) return false;
+    const int next = lane + 1 >= nv ? 0 : lane + 1;
+    const float dnext = __shfl_sync(0xFFFFFFFFu, dist, next);
+    const bool cross = mine && in != (((inm >> next) & 1u) != 0);
+    const uint32_t emits = (in ? 1u : 0u) + (cross ? 1u : 0u);
+    uint32_t incl = emits;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    uint32_t at = incl - emits;
+    if (in && at < (uint32_t)kMaxClipVertices) out[at] = poly[lane];
+    if (in) ++at;
+    if (cross && at < (uint32_t)kMaxClipVertices) {
+        const float t = (0.0f + dist) / (dist - dnext);
+        const float omt = 1.f - t;
+#pragma unroll
+        for (int c = 0; c < 9; ++c) out[at].v[c] = poly[lane].v[c] * omt + poly[next].v[c] * t;
+    }
+    count = (int)min(total, (uint32_t)kMaxClipVertices);
+    __syncwarp();
+    return true;
 }
 
 __device__ __forceinline__ uint32_t find_draw(const BatchParams &bp, uint32_t tri) {
@@ -495,13 +543,10 @@ constexpr int kFanQueue = 16;
 
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK, MLV_GEOMETRY_THREADS_PER_SM / BLOCK) k_geometry(BatchParams bp) {
-    __shared__ BinJob s_q[BLOCK / 32][kFanQueue];
-    __shared__ uint32_t s_qn[BLOCK / 32];
     pdl_wait();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane == 0) s_qn[warp] = 0;
-    __syncwarp();
+    const int lane = threadIdx.x & 31;
     const uint32_t g = blockIdx.x * BLOCK + threadIdx.x;
+    bool clipped = false;       // left to k_clip
     uint32_t mask = 0;
     BinJob own;                 // the bins of an unclipped triangle, counted warp-wide below
     bool have_own = false;
@@ -525,7 +570,6 @@ __global__ void __launch_bounds__(BLOCK, MLV_GEOMETRY_THREADS_PER_SM / BLOCK) k_
                  (p0[1] > +p0[3] && p1[1] > +p1[3] && p2[1] > +p2[3]) ||
                  (p0[2] < 0.f && p1[2] < 0.f && p2[2] < 0.f) ||
                  (p0[2] > +p0[3] && p1[2] > +p1[3] && p2[2] > +p2[3]);
-        bool clipped = false;
         if (!reject) {
             clipped = !((p0[0] >= -p0[3] && p1[0] >= -p1[3] && p2[0] >= -p2[3]) &&
                         (p0[0] <= +p0[3] && p1[0] <= +p1[3] && p2[0] <= +p2[3]) &&
@@ -560,49 +604,21 @@ __global__ void __launch_bounds__(BLOCK, MLV_GEOMETRY_THREADS_PER_SM / BLOCK) k_
                         }
                     }
                 }
-            } else {
-#pragma unroll
-                for (int k = 0; k < 3; ++k) triangle_attributes(bp, slot[k], v[k].v);
-                Vtx poly[kMaxClipVertices], tmp[kMaxClipVertices];
-                poly[0] = v[0]; poly[1] = v[1]; poly[2] = v[2];
-                int count = 3;
-                for (int p = 0; p < 6; ++p) clip_by_plane(poly, tmp, count, c_clip_planes[p]);
-                const int nf = count - 2;
-                if (nf > 0) {
-                    const uint32_t base = atomicAdd(bp.counters + kCtrOverflow, (uint32_t)nf);
-                    if (base + (uint32_t)nf > bp.overflow_capacity) {
-                        atomicOr(bp.error, kErrRecordOverflow);
-                        atomicMin(bp.error + 1, bp.batch_seq);
-                        atomicMax(bp.error + 4, base + (uint32_t)nf);
-                    } else {
-                        uint32_t deltas[2] = {0u, 0u};   // 6 bits a fan: fans 0-4, then 5-6
-                        for (int f = 0; f < nf && f < 7; ++f) {
-                            Setup su;
-                            if (setup_triangle(d, poly[0], poly[f + 1], poly[f + 2], su)) {
-                                const uint32_t slot = bp.total_tris + base + (uint32_t)f;
-                                write_record(bp, slot, draw, d.ps, !(d.raster_flags & kDrawSharesView), su, poly[0],
-                                             poly[f + 1], poly[f + 2]);
-                                mask |= 1u << f;
-                                deltas[f < 5 ? 0 : 1] |= su.box_delta << (6 * (f < 5 ? f : f - 5));
-                                BinJob job;
-                                if (!bin_job(vw, d.draw_in_view, su.minx, su.miny, su.maxx, su.maxy, 0u, job)) continue;
-                                const uint32_t nt = job.nx * job.ny;
-                                if (nt > bp.big_tiles) {
-                                    const uint32_t q = atomicAdd(&s_qn[warp], 1u);
-                                    if (q < kFanQueue) { s_q[warp][q] = job; continue; }
-                                }
-                                for (uint32_t t = 0; t < nt; ++t) atomicAdd(bp.bin_count + job_bin(job, t), 1u);
-                            }
-                        }
-                        // slot g (no record of its own) holds the fans' base and box deltas
-                        bp.raster[g].w[0] = make_int4((int)base, (int)deltas[0], (int)deltas[1], 0);
-                    }
-                }
             }
+            // a triangle that needs clipping is listed for k_clip, which writes its fans, tri_info
+            // and bins_of after this kernel
         }
-        bp.tri_info[g] = (uint16_t)(mask | (clipped ? 0x100u : 0u));
-        bp.bins_of[g] = have_own ? make_uint2(own.first_bin, own.nx | (own.ny << 16))
-                                 : make_uint2(0u, clipped && mask ? kBinsClipped : 0u);
+        if (!clipped) {
+            bp.tri_info[g] = (uint16_t)mask;
+            bp.bins_of[g] = have_own ? make_uint2(own.first_bin, own.nx | (own.ny << 16)) : make_uint2(0u, 0u);
+        }
+    }
+    const uint32_t clip_lanes = __ballot_sync(0xFFFFFFFFu, clipped);
+    if (clip_lanes) {   // one position per warp in the clip list
+        uint32_t at = 0;
+        if (lane == 0) at = atomicAdd(bp.counters + kCtrClip, (uint32_t)__popc(clip_lanes));
+        at = __shfl_sync(0xFFFFFFFFu, at, 0);
+        if (clipped) bp.clip_list[at + __popc(clip_lanes & ((1u << lane) - 1u))] = g;
     }
     if (!__any_sync(0xFFFFFFFFu, mask != 0u)) {   // the warp assembled nothing: nothing to count
         pdl_trigger();
@@ -644,12 +660,94 @@ __global__ void __launch_bounds__(BLOCK, MLV_GEOMETRY_THREADS_PER_SM / BLOCK) k_
         j.row_stride = __shfl_sync(0xFFFFFFFFu, own.row_stride, src);
         for (uint32_t t = lane; t < j.nx * j.ny; t += 32) atomicAdd(bp.bin_count + job_bin(j, t), 1u);
     }
-    __syncwarp();
-    const uint32_t nq = min(s_qn[warp], (uint32_t)kFanQueue);
-    for (uint32_t b = 0; b < nq; ++b) {
-        const BinJob j = s_q[warp][b];
-        for (uint32_t t = lane; t < j.nx * j.ny; t += 32) atomicAdd(bp.bin_count + job_bin(j, t), 1u);
+    pdl_trigger();
+}
+
+// Clipping (main.c:649-661) of the triangles k_geometry listed, one warp per triangle: lanes 0-2
+// fetch its vertices again, the warp clips them plane by plane (clip_by_plane_warp), and lane f sets
+// up fan f (main.c:662-913): its record in slot total_tris + base + f, its bins counted (by the warp
+// together when it spans more than big_tiles). Then the triangle's fan mask, clipped bit and box
+// deltas are written where k_geometry writes an unclipped triangle's. Spread over the whole GPU,
+// the clipped triangles' serial work no longer lengthens the warps of k_geometry that hold them.
+constexpr int kClipBlock = 128;
+
+__global__ void __launch_bounds__(kClipBlock) k_clip(BatchParams bp) {
+    __shared__ Vtx s_poly[kClipBlock / 32][2][kMaxClipVertices];
+    pdl_wait();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t n = ld_volatile_u32(bp.counters + kCtrClip);
+    uint32_t assembled = 0;
+    for (uint32_t i = blockIdx.x * (kClipBlock / 32) + warp; i < n; i += gridDim.x * (kClipBlock / 32)) {
+        const uint32_t g = bp.clip_list[i];
+        const uint32_t draw = find_draw(bp, g);
+        const DrawDesc &d = bp.draws[draw];
+        Vtx *poly = s_poly[warp][0], *other = s_poly[warp][1];
+        if (lane < 3) triangle_vertex(bp, d, d.start_index + 3 * (g - d.tri_begin) + (uint32_t)lane, poly[lane].v);
+        __syncwarp();
+        int count = 3;
+        for (int p = 0; p < 6; ++p)
+            if (clip_by_plane_warp(poly, other, count, c_clip_planes[p], lane)) {
+                Vtx *t = poly;
+                poly = other;
+                other = t;
+            }
+        const int nf = count - 2;
+        uint32_t fans = 0;
+        if (nf > 0) {
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(bp.counters + kCtrOverflow, (uint32_t)nf);
+            base = __shfl_sync(0xFFFFFFFFu, base, 0);
+            if (base + (uint32_t)nf > bp.overflow_capacity) {
+                if (lane == 0) {
+                    atomicOr(bp.error, kErrRecordOverflow);
+                    atomicMin(bp.error + 1, bp.batch_seq);
+                    atomicMax(bp.error + 4, base + (uint32_t)nf);
+                }
+            } else {
+                Setup su;
+                bool ok = false;
+                BinJob job;
+                uint32_t nt = 0;
+                if (lane < min(nf, 7)) {
+                    ok = setup_triangle(d, poly[0], poly[lane + 1], poly[lane + 2], su);
+                    if (ok) {
+                        write_record(bp, bp.total_tris + base + (uint32_t)lane, draw, d.ps,
+                                     !(d.raster_flags & kDrawSharesView), su, poly[0], poly[lane + 1], poly[lane + 2]);
+                        if (bin_job(bp.views[d.view], d.draw_in_view, su.minx, su.miny, su.maxx, su.maxy, 0u, job))
+                            nt = job.nx * job.ny;
+                        if (nt <= bp.big_tiles)
+                            for (uint32_t t = 0; t < nt; ++t) atomicAdd(bp.bin_count + job_bin(job, t), 1u);
+                    }
+                }
+                fans = __ballot_sync(0xFFFFFFFFu, ok);
+                // fans over many tiles: their bins counted by the whole warp
+                uint32_t big = __ballot_sync(0xFFFFFFFFu, nt > bp.big_tiles);
+                while (big) {
+                    const int src = __ffs(big) - 1;
+                    big &= big - 1;
+                    BinJob j;
+                    j.first_bin = __shfl_sync(0xFFFFFFFFu, job.first_bin, src);
+                    j.nx = __shfl_sync(0xFFFFFFFFu, job.nx, src);
+                    j.ny = __shfl_sync(0xFFFFFFFFu, job.ny, src);
+                    j.col_stride = __shfl_sync(0xFFFFFFFFu, job.col_stride, src);
+                    j.row_stride = __shfl_sync(0xFFFFFFFFu, job.row_stride, src);
+                    for (uint32_t t = lane; t < j.nx * j.ny; t += 32) atomicAdd(bp.bin_count + job_bin(j, t), 1u);
+                }
+                // slot g (no record of its own) holds the fans' base and box deltas, 6 bits a fan:
+                // fans 0-4 in one word, 5-6 in the next
+                const uint32_t d0 = __reduce_or_sync(0xFFFFFFFFu, ok && lane < 5 ? su.box_delta << (6 * lane) : 0u);
+                const uint32_t d1 = __reduce_or_sync(0xFFFFFFFFu, ok && lane >= 5 ? su.box_delta << (6 * (lane - 5)) : 0u);
+                if (lane == 0) bp.raster[g].w[0] = make_int4((int)base, (int)d0, (int)d1, 0);
+            }
+        }
+        if (lane == 0) {
+            bp.tri_info[g] = (uint16_t)(fans | 0x100u);
+            bp.bins_of[g] = make_uint2(0u, fans ? kBinsClipped : 0u);
+        }
+        assembled += (uint32_t)__popc(fans);
+        __syncwarp();
     }
+    if (lane == 0 && assembled) atomicAdd(bp.stats + kStatAssembled, (unsigned long long)assembled);   // main.c:1238
     pdl_trigger();
 }
 
@@ -882,9 +980,32 @@ __device__ __forceinline__ bool record_job(const BatchParams &bp, const ViewDesc
                    key, job);
 }
 
-__device__ __forceinline__ void put(const BatchParams &bp, uint32_t bin, uint32_t key) {
-    const uint32_t pos = atomicSub(bp.bin_count + bin, 1u) - 1u;
-    bp.list[__ldg(bp.bin_start + bin) + pos] = key;
+// Puts key[k] into bin[k] for the k (of 4) whose bit is set in m: the list positions (atomics on
+// the bin counters) and the bins' starts are all requested before any is used, so one thread's
+// fills take one round trip instead of one each.
+__device__ __forceinline__ void put4(const BatchParams &bp, const uint32_t *bin, const uint32_t *key, uint32_t m) {
+    uint32_t pos[4], st[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (m >> k & 1u) {
+            pos[k] = atomicSub(bp.bin_count + bin[k], 1u) - 1u;
+            st[k] = __ldg(bp.bin_start + bin[k]);
+        }
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (m >> k & 1u) bp.list[st[k] + pos[k]] = key[k];
+}
+
+// The bins t, t + step, ... (below nt) of one job, four at a time.
+__device__ __forceinline__ void put_job(const BatchParams &bp, const BinJob &j, uint32_t t, uint32_t step) {
+    const uint32_t nt = j.nx * j.ny;
+    const uint32_t key[4] = {j.key, j.key, j.key, j.key};
+    for (; t < nt; t += 4 * step) {
+        uint32_t bin[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) bin[k] = job_bin(j, min(t + (uint32_t)k * step, nt - 1));
+        put4(bp, bin, key, (1u << min(4u, (nt - t + step - 1) / step)) - 1u);
+    }
 }
 
 __global__ void __launch_bounds__(kScatterBlock) k_scatter(BatchParams bp) {
@@ -946,7 +1067,7 @@ __global__ void __launch_bounds__(kScatterBlock) k_scatter(BatchParams bp) {
                     const uint32_t q = atomicAdd(&s_qn[warp], 1u);
                     if (q < kFanQueue) { s_q[warp][q] = job; continue; }
                 }
-                for (uint32_t t = 0; t < nt; ++t) put(bp, job_bin(job, t), job.key);
+                put_job(bp, job, 0, 1);
             }
         }
         const uint32_t single = nt_own == 1 ? own.first_bin : 0xFFFFFFFFu;
@@ -959,22 +1080,7 @@ __global__ void __launch_bounds__(kScatterBlock) k_scatter(BatchParams bp) {
             const uint32_t r = (uint32_t)__popc(peers & ((1u << lane) - 1u));
             bp.list[__ldg(bp.bin_start + single) + top - 1u - r] = own.key;
         } else if (nt_own > 1 && nt_own <= bp.big_tiles) {
-            // up to 4 bins at a time: the atomics and bin_start loads are independent, so they
-            // are all in flight together instead of one round trip after another
-            for (uint32_t t0 = 0; t0 < nt_own; t0 += 4) {
-                uint32_t bin[4], pos[4], st[4];
-#pragma unroll
-                for (int k = 0; k < 4; ++k) bin[k] = job_bin(own, min(t0 + k, nt_own - 1));
-#pragma unroll
-                for (int k = 0; k < 4; ++k)
-                    if (t0 + k < nt_own) {
-                        pos[k] = atomicSub(bp.bin_count + bin[k], 1u) - 1u;
-                        st[k] = __ldg(bp.bin_start + bin[k]);
-                    }
-#pragma unroll
-                for (int k = 0; k < 4; ++k)
-                    if (t0 + k < nt_own) bp.list[st[k] + pos[k]] = own.key;
-            }
+            put_job(bp, own, 0, 1);
         }
         // triangles over more than big_tiles bins are filled by the whole warp, 32 (triangle, bin)
         // pairs per round. Each big triangle normally starts a new round (its pair count is padded
@@ -1000,27 +1106,38 @@ __global__ void __launch_bounds__(kScatterBlock) k_scatter(BatchParams bp) {
             }
             __syncwarp();
             // each lane's pairs are item = lane, lane + 32, ...: its triangle only moves forward,
-            // so the job stays in registers until the lane crosses the end of a triangle
+            // so the job stays in registers until the lane crosses the end of a triangle; four
+            // pairs are filled together
             uint32_t jb = 0, base = 0, end = s_bigpref[warp][0];
             BinJob job = s_big[warp][0];
-            for (uint32_t item = lane; item < total_big; item += 32) {
-                if (item >= end) {
-                    do {
-                        ++jb;
-                        base = end;
-                        end = s_bigpref[warp][jb];
-                    } while (item >= end);
-                    job = s_big[warp][jb];
+            for (uint32_t item0 = lane; item0 < total_big; item0 += 128) {
+                uint32_t bin[4], key[4], m = 0;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const uint32_t item = item0 + 32u * (uint32_t)k;
+                    bin[k] = 0;
+                    key[k] = 0;
+                    if (item >= total_big) continue;
+                    if (item >= end) {
+                        do {
+                            ++jb;
+                            base = end;
+                            end = s_bigpref[warp][jb];
+                        } while (item >= end);
+                        job = s_big[warp][jb];
+                    }
+                    if (item - base < job.nx * job.ny) {   // not padding
+                        bin[k] = job_bin(job, item - base);
+                        key[k] = job.key;
+                        m |= 1u << k;
+                    }
                 }
-                if (item - base < job.nx * job.ny) put(bp, job_bin(job, item - base), job.key);
+                put4(bp, bin, key, m);
             }
         }
         __syncwarp();
         const uint32_t nq = min(s_qn[warp], (uint32_t)kFanQueue);
-        for (uint32_t b = 0; b < nq; ++b) {
-            const BinJob j = s_q[warp][b];
-            for (uint32_t t = lane; t < j.nx * j.ny; t += 32) put(bp, job_bin(j, t), j.key);
-        }
+        for (uint32_t b = 0; b < nq; ++b) put_job(bp, s_q[warp][b], lane, 32);
         __syncwarp();
     }
     pdl_trigger();
@@ -2232,13 +2349,20 @@ cudaError_t launch_vertex(const BatchParams &bp, cudaStream_t stream) {
     return launch_chained(k_vertex, (bp.total_vertices + kVertexBlock - 1) / kVertexBlock, kVertexBlock, stream, bp);
 }
 
-cudaError_t launch_geometry(const BatchParams &bp, uint32_t block, cudaStream_t stream) {
+// k_geometry, then k_clip (a grid of up to 8 CTAs per SM: one warp for each listed triangle, in
+// one round for up to 32 a SM)
+cudaError_t launch_geometry(const BatchParams &bp, uint32_t block, int num_sms, cudaStream_t stream) {
     if (bp.total_tris == 0) return cudaSuccess;
+    cudaError_t e;
     switch (block) {
-        case 128: return launch_chained(k_geometry<128>, (bp.total_tris + 127) / 128, 128, stream, bp);
-        case 512: return launch_chained(k_geometry<512>, (bp.total_tris + 511) / 512, 512, stream, bp);
-        default: return launch_chained(k_geometry<256>, (bp.total_tris + 255) / 256, 256, stream, bp);
+        case 128: e = launch_chained(k_geometry<128>, (bp.total_tris + 127) / 128, 128, stream, bp); break;
+        case 512: e = launch_chained(k_geometry<512>, (bp.total_tris + 511) / 512, 512, stream, bp); break;
+        default: e = launch_chained(k_geometry<256>, (bp.total_tris + 255) / 256, 256, stream, bp); break;
     }
+    if (e != cudaSuccess) return e;
+    const uint32_t blocks_needed = (bp.total_tris + kClipBlock / 32 - 1) / (kClipBlock / 32);
+    const uint32_t cap = 8u * (uint32_t)(num_sms > 0 ? num_sms : 1);
+    return launch_chained(k_clip, blocks_needed < cap ? blocks_needed : cap, kClipBlock, stream, bp);
 }
 
 cudaError_t launch_rank(const BatchParams &bp, cudaStream_t stream) {

@@ -21,7 +21,7 @@ namespace mlv {
 void set_clip_planes(const float planes[6][4], cudaStream_t stream);
 cudaError_t launch_fill_u32(uint32_t *p, size_t n, uint32_t value, const uint32_t *error, cudaStream_t stream);
 cudaError_t launch_vertex(const BatchParams &bp, cudaStream_t stream);
-cudaError_t launch_geometry(const BatchParams &bp, uint32_t block, cudaStream_t stream);
+cudaError_t launch_geometry(const BatchParams &bp, uint32_t block, int num_sms, cudaStream_t stream);
 cudaError_t launch_scan(const BatchParams &bp, cudaStream_t stream);
 cudaError_t launch_scatter(const BatchParams &bp, int num_sms, cudaStream_t stream);
 cudaError_t launch_tile(const BatchParams &bp, uint32_t warps, uint32_t warps_per_tile, cudaStream_t stream);
@@ -59,6 +59,7 @@ constexpr size_t kOffVsOut = align256(kOffShade + sizeof(TriShade) * (kMaxTriang
 constexpr size_t kOffList = align256(kOffVsOut + sizeof(float4) * 3 * kMaxVertices);
 constexpr size_t kScratchBytes = align256(kOffList + sizeof(uint32_t) * kMaxBinEntries);
 static_assert(kScratchBytes == MLV_NOALLOC_SCRATCH_BYTES, "header and layout disagree on the scratch size");
+static_assert(kMaxBinEntries >= kMaxTriangles, "the clip list lives in the bin-list region");
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
@@ -274,6 +275,9 @@ extern "C" MLV_API mlv_status mlv_draw_indexed_noalloc(const mlv_noalloc_draw *a
     bp.bin_count = (uint32_t *)(base + kOffBinCount);
     bp.bin_start = (uint32_t *)(base + kOffBinStart);
     bp.list = (uint32_t *)(base + kOffList);
+    // the list is written only by k_scatter, after k_clip is done with the clip list it holds
+    // (MLV_NOALLOC_MAX_BIN_ENTRIES >= MLV_NOALLOC_MAX_TRIANGLES entries)
+    bp.clip_list = bp.list;
     bp.scan_status2 = (unsigned long long *)(base + kOffStatus);
     bp.counters = (uint32_t *)(base + kOffCounters);
     bp.stats = (unsigned long long *)(base + kOffStats);
@@ -289,7 +293,7 @@ extern "C" MLV_API mlv_status mlv_draw_indexed_noalloc(const mlv_noalloc_draw *a
     }
     if (tris) {
         NA_CUDA(launch_vertex(bp, stream));
-        NA_CUDA(launch_geometry(bp, 128, stream));
+        NA_CUDA(launch_geometry(bp, 128, g_num_sms[dev] ? g_num_sms[dev] : 152, stream));
         NA_CUDA(launch_scan(bp, stream));
         NA_CUDA(launch_scatter(bp, g_num_sms[dev] ? g_num_sms[dev] : 152, stream));
         NA_CUDA(launch_tile(bp, 4, 1, stream));
