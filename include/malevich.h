@@ -451,7 +451,7 @@ MLV_API mlv_status mlv_om_set_primitive_id_target(mlv_context context, mlv_textu
 #define MLV_NOALLOC_MAX_TILES 16384u
 #define MLV_NOALLOC_MAX_CLIP_FANS 8192u
 #define MLV_NOALLOC_MAX_BIN_ENTRIES 131072u
-#define MLV_NOALLOC_SCRATCH_BYTES 8456704u
+#define MLV_NOALLOC_SCRATCH_BYTES 8849920u
 #define MLV_NOALLOC_RESET_HIERARCHICAL_Z 0x1u
 
 typedef struct mlv_noalloc_texture {

@@ -172,8 +172,9 @@ struct Workspace {
     uint32_t overflow_cap = 0;        // overflow slots the last sizing reserved
     bool keep_geom = false;
     uint16_t *tri_info = nullptr;
-    uint2 *bins_of = nullptr;
-    uint32_t *clip_list = nullptr;
+    uint4 *jobs = nullptr;
+    uint2 *clip_list = nullptr;       // [clip_cap]
+    uint32_t clip_cap = 0;
     uint32_t *rank = nullptr;
     uint32_t tri_cap = 0;
     uint32_t *bin_count = nullptr, *bin_start = nullptr;
@@ -332,6 +333,7 @@ static mlv_status ensure_fixed(mlv_context_t *c) {
 struct BatchSizes {
     uint64_t tris = 0, overflow = 0, bins = 0, tiles = 0, draws = 0, views = 0, vertices = 0;
     uint64_t direct_pixels = 0;   // small-draw path: the view's pixels (one key each)
+    bool binned = false;  // some batch takes the binned path: bin jobs and the clip list are needed
     bool shade = false;   // some draw has a pixel shader: the 80-byte shading records are needed
 };
 
@@ -351,14 +353,16 @@ static mlv_status ensure_workspace(mlv_context_t *c, const BatchSizes &s, bool k
     // shading records only once a batch has a pixel shader (a depth or visibility pass with the
     // null pixel shader needs none: 80 of its 144 bytes per triangle slot)
     const bool shade = s.shade || w.shade != nullptr;
-    if (slots > w.record_cap || !w.raster || (keep_geom && !w.geom) || (shade && !w.shade)) {
+    const bool binned = s.binned || w.jobs != nullptr;   // (the small-draw path lists no bin jobs)
+    if (slots > w.record_cap || !w.raster || (keep_geom && !w.geom) || (shade && !w.shade) || (binned && !w.jobs)) {
         uint64_t n = std::max<uint64_t>(slots, (uint64_t)w.record_cap + w.record_cap / 2);
         if (slots <= w.record_cap && w.raster) n = w.record_cap;   // only the shading records are new
         n = std::max<uint64_t>(n, 4096);
         if (n > 0x7FFFFFFFull) return fail(MLV_ERROR_CAPACITY_EXCEEDED, "more than 2^31 triangle slots");
-        cudaFree(w.raster); cudaFree(w.shade); cudaFree(w.geom);
-        w.raster = nullptr; w.shade = nullptr; w.geom = nullptr;
+        cudaFree(w.raster); cudaFree(w.shade); cudaFree(w.geom); cudaFree(w.jobs);
+        w.raster = nullptr; w.shade = nullptr; w.geom = nullptr; w.jobs = nullptr;
         MLV_TRY(dev_alloc((void **)&w.raster, n * sizeof(TriRaster)));
+        if (binned) MLV_TRY(dev_alloc((void **)&w.jobs, n * sizeof(uint4)));
         if (shade) MLV_TRY(dev_alloc((void **)&w.shade, n * sizeof(TriShade)));
         w.keep_geom = keep_geom || w.keep_geom;
         if (w.keep_geom) MLV_TRY(dev_alloc((void **)&w.geom, n * sizeof(TriGeom)));
@@ -373,17 +377,16 @@ static mlv_status ensure_workspace(mlv_context_t *c, const BatchSizes &s, bool k
         if (before != w.tri_info) {
             cudaFree(w.rank);
             w.rank = nullptr;
-            cudaFree(w.bins_of);
-            w.bins_of = nullptr;
-            cudaFree(w.clip_list);
-            w.clip_list = nullptr;
-            uint32_t cap2 = 0, cap3 = 0, cap4 = 0;
+            uint32_t cap2 = 0;
             MLV_TRY(grow(&w.rank, cap2, cap, sizeof(uint32_t)));
-            MLV_TRY(grow(&w.bins_of, cap3, cap, sizeof(uint2)));
-            MLV_TRY(grow(&w.clip_list, cap4, cap, sizeof(uint32_t)));
             changed = true;
         }
         w.tri_cap = cap;
+    }
+    if (binned) {
+        uint2 *before = w.clip_list;
+        MLV_TRY(grow(&w.clip_list, w.clip_cap, s.tris + 1, sizeof(uint2)));
+        changed = changed || before != w.clip_list;
     }
     {
         uint32_t *before = w.bin_count;
@@ -616,6 +619,7 @@ static mlv_status plan_segment(const Segment &seg, Plan &p, uint32_t fan_slots_h
     for (const DrawDesc &d : p.draws)
         p.sizes.shade = p.sizes.shade || d.ps != kPsNone || (d.raster_flags & kDrawSharesView);
     p.direct = plan_is_direct(p, small_draw, capture);
+    p.sizes.binned = !p.direct;
     p.keys_only = false;
     if (p.direct) {
         // the vertex shader runs per index inside the raster kernel (main.c:698-734's way)
@@ -750,7 +754,8 @@ static mlv_status launch_draws(mlv_context_t *c, const Plan &p, DrawDesc *d_draw
     bp.shade = w.shade;
     bp.geom = w.keep_geom ? w.geom : nullptr;
     bp.tri_info = w.tri_info;
-    bp.bins_of = w.bins_of;
+    bp.jobs = w.jobs;
+    bp.jobs_capacity = w.record_cap;
     bp.clip_list = w.clip_list;
     bool want_rank = c->capture_infos;
     for (const ViewDesc &v : p.views) want_rank = want_rank || v.vis_tri != nullptr;
@@ -783,7 +788,7 @@ static mlv_status launch_draws(mlv_context_t *c, const Plan &p, DrawDesc *d_draw
     cudaEvent_t e;
     // the clip-fan slot counter starts at zero for every batch (reset before the first kernel, so
     // that the batch's kernels follow one another directly)
-    CUDA_TRY(cudaMemsetAsync(w.counters + kCtrOverflow, 0, 3 * sizeof(uint32_t), c->stream));
+    CUDA_TRY(cudaMemsetAsync(w.counters + kCtrOverflow, 0, 4 * sizeof(uint32_t), c->stream));
     if (p.direct) {
         // the small-draw path: raster (vertex shader, setup, small triangles), queued large
         // triangles, resolve; stages 1, 3 and 4 of the stage timers
@@ -1016,7 +1021,7 @@ MLV_API mlv_status mlv_create_device(int ordinal, mlv_device *out) {
 }
 
 static void free_workspace(Workspace &w) {
-    cudaFree(w.raster); cudaFree(w.shade); cudaFree(w.geom); cudaFree(w.tri_info); cudaFree(w.bins_of); cudaFree(w.rank);
+    cudaFree(w.raster); cudaFree(w.shade); cudaFree(w.geom); cudaFree(w.tri_info); cudaFree(w.jobs); cudaFree(w.rank);
     cudaFree(w.clip_list);
     cudaFree(w.bin_count); cudaFree(w.bin_start); cudaFree(w.list); cudaFree(w.info_mask);
     cudaFree(w.scan_status); cudaFree(w.scan_status2); cudaFree(w.counters); cudaFree(w.stats);
@@ -1719,6 +1724,7 @@ static mlv_status run_list(mlv_context_t *c, mlv_command_list l, uint32_t seq, b
         maxs.views = std::max(maxs.views, s.views);
         maxs.vertices = std::max(maxs.vertices, s.vertices);
         maxs.shade = maxs.shade || s.shade;
+        maxs.binned = maxs.binned || s.binned;
         nd += plans[i].draws.size();
         nv += plans[i].views.size();
     }

@@ -12,7 +12,6 @@ namespace mlv {
 constexpr int kTile = 8;                 // 8x8 pixel tiles: the reference's bins (main.c:24-25)
 constexpr int kSubpix = 4;               // 28.4 fixed point (main.c:39)
 constexpr int kPsNone = 5;               // MLV_PS_NONE: depth and visibility only
-constexpr uint32_t kBinsClipped = 0xFFFFFFFFu;
 constexpr int kRasterTopLeft = 1;        // MLV_FILL_TOP_LEFT
 constexpr int kRasterCenter = 2;         // MLV_SAMPLE_PIXEL_CENTER
 constexpr int kDrawSharesView = 4;       // (DrawDesc::raster_flags) the view has other draws too
@@ -150,9 +149,10 @@ struct BatchParams {
     TriShade *shade;
     TriGeom *geom;                       // nullptr unless the geometry is kept
     uint16_t *tri_info;                  // [total_tris]: emitted-fan mask | clipped << 8
-    uint32_t *clip_list;                 // [total_tris]: the input triangles k_geometry leaves to k_clip
-    uint2 *bins_of;                      // [total_tris]: an unclipped triangle's (first bin, nx | ny << 16);
-                                         // (0, 0) no bins, (0, kBinsClipped) clipped: see its fans
+    uint2 *clip_list;                    // [total_tris]: (input triangle, draw) that k_geometry leaves to k_clip
+    uint4 *jobs;                         // [jobs_capacity] bin jobs, one per triangle or fan with bins:
+                                         // (key, first bin, nx | ny << 16, view), counted by kCtrJobs
+    uint32_t jobs_capacity;              // = raster record slots
     uint32_t *rank;                      // [total_tris]: assembled triangles before g (exclusive)
     uint32_t *bin_count;                 // [total_bins], zero between batches
     uint32_t *bin_start;                 // [total_bins + 1]
@@ -176,8 +176,9 @@ struct BatchParams {
 
 enum Counter : int {
     kCtrRankTicket = 0, kCtrRankDone, kCtrRankEpoch,
-    kCtrOverflow, kCtrQueue, kCtrClip,   // per-batch: clip-fan slots used; small-draw queue entries
-                                         // used; triangles listed for clipping (clip_list)
+    kCtrOverflow, kCtrQueue, kCtrClip, kCtrJobs,   // per batch: clip-fan slots used; small-draw queue
+                                         // entries used; triangles listed for clipping (clip_list);
+                                         // bin jobs listed (jobs)
     kCtrScanTicket, kCtrScanDone, kCtrScanEpoch,
     kCtrCount = 16
 };

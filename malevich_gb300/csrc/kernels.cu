@@ -157,7 +157,6 @@ struct Setup {
     float rw[3];
     int32_t minx, miny, maxx, maxy;      // the reference's pixel box: binning
     int32_t tminx, tminy, tmaxx, tmaxy;  // the same box shrunk to the samples it can cover: tile kernel
-    uint32_t box_delta;                  // the shrink: x min | y min << 1 (0-1), x max << 2 | y max << 4 (0-3)
 };
 
 // set_edge_function, main.c:563-575 (wrapping int32)
@@ -231,7 +230,7 @@ __device__ __forceinline__ bool setup_triangle(const DrawDesc &d, const Vtx &v0,
     mxy = min(mxy + 1, d.vp_h - 1);
     // Every maximum <= -8 bins nowhere and covers no pixel (C division truncates -1..-7 to tile 0,
     // main.c:928), so clamping it there changes nothing and keeps the bounds exact in the 16-bit
-    // fields of TriRaster, which the scatter kernel re-reads to find the same tiles.
+    // fields of TriRaster, where the tile kernels read the box.
     mxx = max(mxx, -8);
     mxy = max(mxy, -8);
     s.minx = mnx; s.miny = mny; s.maxx = mxx; s.maxy = mxy;
@@ -240,7 +239,7 @@ __device__ __forceinline__ bool setup_triangle(const DrawDesc &d, const Vtx &v0,
     // mixed sign off its line and all 0 on it.) That holds while the edge values are exact, which
     // they are for vertex extents up to 1024 pixels: |E| stays below 2^31 over the box, so the
     // wrapping sums equal the true values. The box shrinks by at most 1 at the minimum and 3 at the
-    // maximum, so the deltas fit 6 bits and give the reference box back (k_scatter, clip fans).
+    // maximum.
     const int32_t xlo = min(x[0], min(x[1], x[2])), xhi = max(x[0], max(x[1], x[2]));
     const int32_t ylo = min(y[0], min(y[1], y[2])), yhi = max(y[0], max(y[1], y[2]));
     int32_t dlx = 0, dly = 0, dhx = 0, dhy = 0;
@@ -252,7 +251,6 @@ __device__ __forceinline__ bool setup_triangle(const DrawDesc &d, const Vtx &v0,
         dhy = min(max(mxy - ((yhi - off) >> kSubpix), 0), 3);
     }
     s.tminx = mnx + dlx; s.tminy = mny + dly; s.tmaxx = mxx - dhx; s.tmaxy = mxy - dhy;
-    s.box_delta = (uint32_t)(dlx | dly << 1 | dhx << 2 | dhy << 4);
     return true;
 }
 
@@ -532,9 +530,20 @@ __device__ __forceinline__ uint32_t job_bin(const BinJob &j, uint32_t t) {
     return j.first_bin + y * j.row_stride + x * j.col_stride;
 }
 
-// Clip-fan triangles of a warp spanning more than big_tiles tiles, handled by the whole warp; when
-// the queue is full the lane handles its fan alone.
-constexpr int kFanQueue = 16;
+
+// Appends the bin job of every lane with one (has) to the batch's job list, one atomic per warp:
+// its key, first bin, tile counts and view, which k_scatter fills from. Lanes of a warp hold
+// neighbouring triangles, which stay neighbours in the list. Every lane of the warp calls it.
+__device__ __forceinline__ void push_jobs(const BatchParams &bp, bool has, const BinJob &job, uint32_t view, int lane) {
+    const uint32_t lanes = __ballot_sync(0xFFFFFFFFu, has);
+    if (!lanes) return;
+    uint32_t at = 0;
+    if (lane == 0) at = atomicAdd(bp.counters + kCtrJobs, (uint32_t)__popc(lanes));
+    at = __shfl_sync(0xFFFFFFFFu, at, 0) + (uint32_t)__popc(lanes & ((1u << lane) - 1u));
+    if (!has) return;
+    if (at < bp.jobs_capacity) bp.jobs[at] = make_uint4(job.key, job.first_bin, job.nx | (job.ny << 16), view);
+    else atomicOr(bp.error, kErrRecordOverflow);   // cannot happen: a job per record slot at most
+}
 
 // Resident threads per SM the geometry kernel's register budget is sized for (1024: 64 registers).
 #ifndef MLV_GEOMETRY_THREADS_PER_SM
@@ -546,6 +555,7 @@ __global__ void __launch_bounds__(BLOCK, MLV_GEOMETRY_THREADS_PER_SM / BLOCK) k_
     pdl_wait();
     const int lane = threadIdx.x & 31;
     const uint32_t g = blockIdx.x * BLOCK + threadIdx.x;
+    uint32_t draw = 0, view = 0;
     bool clipped = false;       // left to k_clip
     uint32_t mask = 0;
     BinJob own;                 // the bins of an unclipped triangle, counted warp-wide below
@@ -553,9 +563,10 @@ __global__ void __launch_bounds__(BLOCK, MLV_GEOMETRY_THREADS_PER_SM / BLOCK) k_
     uint32_t ghost_entries = 0; // bins of a triangle that covers no sample (statistics only)
     uint32_t ghost_bin = 0xFFFFFFFFu;   // its bin when it has one, marked warp-wide below
     if (g < bp.total_tris) {
-        const uint32_t draw = find_draw(bp, g);
+        draw = find_draw(bp, g);
         const DrawDesc &d = bp.draws[draw];
-        const ViewDesc &vw = bp.views[d.view];
+        view = d.view;
+        const ViewDesc &vw = bp.views[view];
         const uint32_t local = g - d.tri_begin;
         Vtx v[3];
         uint32_t slot[3];
@@ -605,20 +616,18 @@ __global__ void __launch_bounds__(BLOCK, MLV_GEOMETRY_THREADS_PER_SM / BLOCK) k_
                     }
                 }
             }
-            // a triangle that needs clipping is listed for k_clip, which writes its fans, tri_info
-            // and bins_of after this kernel
+            // a triangle that needs clipping is listed for k_clip, which writes its fans, their
+            // bin jobs and its tri_info after this kernel
         }
-        if (!clipped) {
-            bp.tri_info[g] = (uint16_t)mask;
-            bp.bins_of[g] = have_own ? make_uint2(own.first_bin, own.nx | (own.ny << 16)) : make_uint2(0u, 0u);
-        }
+        if (!clipped) bp.tri_info[g] = (uint16_t)mask;
     }
+    push_jobs(bp, have_own, own, view, lane);
     const uint32_t clip_lanes = __ballot_sync(0xFFFFFFFFu, clipped);
     if (clip_lanes) {   // one position per warp in the clip list
         uint32_t at = 0;
         if (lane == 0) at = atomicAdd(bp.counters + kCtrClip, (uint32_t)__popc(clip_lanes));
         at = __shfl_sync(0xFFFFFFFFu, at, 0);
-        if (clipped) bp.clip_list[at + __popc(clip_lanes & ((1u << lane) - 1u))] = g;
+        if (clipped) bp.clip_list[at + __popc(clip_lanes & ((1u << lane) - 1u))] = make_uint2(g, draw);
     }
     if (!__any_sync(0xFFFFFFFFu, mask != 0u)) {   // the warp assembled nothing: nothing to count
         pdl_trigger();
@@ -678,8 +687,8 @@ __global__ void __launch_bounds__(kClipBlock) k_clip(BatchParams bp) {
     const uint32_t n = ld_volatile_u32(bp.counters + kCtrClip);
     uint32_t assembled = 0;
     for (uint32_t i = blockIdx.x * (kClipBlock / 32) + warp; i < n; i += gridDim.x * (kClipBlock / 32)) {
-        const uint32_t g = bp.clip_list[i];
-        const uint32_t draw = find_draw(bp, g);
+        const uint2 entry = bp.clip_list[i];
+        const uint32_t g = entry.x, draw = entry.y;
         const DrawDesc &d = bp.draws[draw];
         Vtx *poly = s_poly[warp][0], *other = s_poly[warp][1];
         if (lane < 3) triangle_vertex(bp, d, d.start_index + 3 * (g - d.tri_begin) + (uint32_t)lane, poly[lane].v);
@@ -713,7 +722,8 @@ __global__ void __launch_bounds__(kClipBlock) k_clip(BatchParams bp) {
                     if (ok) {
                         write_record(bp, bp.total_tris + base + (uint32_t)lane, draw, d.ps,
                                      !(d.raster_flags & kDrawSharesView), su, poly[0], poly[lane + 1], poly[lane + 2]);
-                        if (bin_job(bp.views[d.view], d.draw_in_view, su.minx, su.miny, su.maxx, su.maxy, 0u, job))
+                        if (bin_job(bp.views[d.view], d.draw_in_view, su.minx, su.miny, su.maxx, su.maxy,
+                                    (g << 3) | (uint32_t)(lane + 1), job))
                             nt = job.nx * job.ny;
                         if (nt <= bp.big_tiles)
                             for (uint32_t t = 0; t < nt; ++t) atomicAdd(bp.bin_count + job_bin(job, t), 1u);
@@ -733,17 +743,12 @@ __global__ void __launch_bounds__(kClipBlock) k_clip(BatchParams bp) {
                     j.row_stride = __shfl_sync(0xFFFFFFFFu, job.row_stride, src);
                     for (uint32_t t = lane; t < j.nx * j.ny; t += 32) atomicAdd(bp.bin_count + job_bin(j, t), 1u);
                 }
-                // slot g (no record of its own) holds the fans' base and box deltas, 6 bits a fan:
-                // fans 0-4 in one word, 5-6 in the next
-                const uint32_t d0 = __reduce_or_sync(0xFFFFFFFFu, ok && lane < 5 ? su.box_delta << (6 * lane) : 0u);
-                const uint32_t d1 = __reduce_or_sync(0xFFFFFFFFu, ok && lane >= 5 ? su.box_delta << (6 * (lane - 5)) : 0u);
-                if (lane == 0) bp.raster[g].w[0] = make_int4((int)base, (int)d0, (int)d1, 0);
+                push_jobs(bp, nt != 0, job, d.view, lane);
+                // slot g (no record of its own) holds the fans' base
+                if (lane == 0) bp.raster[g].w[0] = make_int4((int)base, 0, 0, 0);
             }
         }
-        if (lane == 0) {
-            bp.tri_info[g] = (uint16_t)(fans | 0x100u);
-            bp.bins_of[g] = make_uint2(0u, fans ? kBinsClipped : 0u);
-        }
+        if (lane == 0) bp.tri_info[g] = (uint16_t)(fans | 0x100u);
         assembled += (uint32_t)__popc(fans);
         __syncwarp();
     }
@@ -964,22 +969,6 @@ __global__ void __launch_bounds__(kSmallScanBlock) k_scan_small(BatchParams bp) 
 
 constexpr int kScatterBlock = 256;
 
-// Fills the bin lists (main.c:950-962): one thread per input triangle. An unclipped triangle's
-// tile range comes from the 8-byte descriptor k_geometry wrote for it (bins_of); a clipped one's
-// fans' ranges are rebuilt from the boxes in their records widened by the shrinks k_geometry kept,
-// which gives back the boxes k_geometry binned. The key goes to the list of every bin of the range
-// (the order inside a bin does not matter, see k_tile). One-tile triangles of a warp that share a
-// bin take their list positions with one atomic; triangles over more than big_tiles bins are
-// filled by the whole warp.
-__device__ __forceinline__ bool record_job(const BatchParams &bp, const ViewDesc &vw, uint32_t draw_in_view,
-                                           uint32_t rec, uint32_t key, uint32_t delta, BinJob &job) {
-    // the record holds the shrunk box (Setup::box_delta): widen it back to the reference's
-    const int4 w3 = bp.raster[rec].w[3];
-    return bin_job(vw, draw_in_view, (int16_t)(w3.z & 0xFFFF) - (int32_t)(delta & 1u), (w3.z >> 16) - (int32_t)(delta >> 1 & 1u),
-                   (int16_t)(w3.w & 0xFFFF) + (int32_t)(delta >> 2 & 3u), (w3.w >> 16) + (int32_t)(delta >> 4 & 3u),
-                   key, job);
-}
-
 // Puts key[k] into bin[k] for the k (of 4) whose bit is set in m: the list positions (atomics on
 // the bin counters) and the bins' starts are all requested before any is used, so one thread's
 // fills take one round trip instead of one each.
@@ -1008,10 +997,13 @@ __device__ __forceinline__ void put_job(const BatchParams &bp, const BinJob &j, 
     }
 }
 
+// Fills the bin lists (main.c:950-962) from the bin jobs k_geometry and k_clip listed (one per
+// triangle or fan with bins: its key, first bin, tile counts and view), one thread per job: the key
+// goes to the list of every bin of its range (the order inside a bin does not matter, see k_tile).
+// One-tile jobs of a warp that share a bin take their list positions with one atomic; jobs over
+// more than big_tiles bins are filled by the whole warp.
 __global__ void __launch_bounds__(kScatterBlock) k_scatter(BatchParams bp) {
-    __shared__ BinJob s_q[kScatterBlock / 32][kFanQueue];
-    __shared__ uint32_t s_qn[kScatterBlock / 32];
-    __shared__ BinJob s_big[kScatterBlock / 32][32];      // the warp's triangles over many bins
+    __shared__ BinJob s_big[kScatterBlock / 32][32];      // the warp's jobs over many bins
     __shared__ uint32_t s_bigpref[kScatterBlock / 32][32]; // inclusive prefix of their bin counts
     pdl_wait();
     if (ld_volatile_u32(bp.error)) return;
@@ -1025,60 +1017,36 @@ __global__ void __launch_bounds__(kScatterBlock) k_scatter(BatchParams bp) {
         return;
     }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t njobs = ld_volatile_u32(bp.counters + kCtrJobs);
     const uint32_t stride = gridDim.x * kScatterBlock;
-    uint32_t g_first = blockIdx.x * kScatterBlock + threadIdx.x;
-    uint2 bd_next = g_first < bp.total_tris ? bp.bins_of[g_first] : make_uint2(0u, 0u);
-    for (uint32_t base = blockIdx.x * kScatterBlock; base < bp.total_tris; base += stride) {
-        if (lane == 0) s_qn[warp] = 0;
-        __syncwarp();
-        const uint32_t g = base + threadIdx.x;
-        const uint2 bd = bd_next;
-        // the next iteration's descriptor is in flight while this one's bins are filled
-        bd_next = g + stride < bp.total_tris ? bp.bins_of[g + stride] : make_uint2(0u, 0u);
-        if (!__any_sync(0xFFFFFFFFu, bd.y != 0u)) continue;   // none of the warp's triangles has bins
+    const uint32_t j_first = blockIdx.x * kScatterBlock + threadIdx.x;
+    uint4 e_next = j_first < njobs ? bp.jobs[j_first] : make_uint4(0u, 0u, 0u, 0u);
+    for (uint32_t base = blockIdx.x * kScatterBlock; base < njobs; base += stride) {
+        const uint32_t j = base + threadIdx.x;
+        const uint4 e = e_next;
+        // the next iteration's job is in flight while this one's bins are filled
+        e_next = j + stride < njobs ? bp.jobs[j + stride] : make_uint4(0u, 0u, 0u, 0u);
         BinJob own;
-        uint32_t nt_own = 0;
-        if (bd.y != 0u && bd.y != kBinsClipped) {
-            own.key = g << 3;
-            own.first_bin = bd.x;
-            own.nx = bd.y & 0xFFFFu;
-            own.ny = bd.y >> 16;
-            nt_own = own.nx * own.ny;
-            if (nt_own > 1) {   // the bin strides of its view (a one-tile triangle needs none)
-                const ViewDesc &vw = bp.views[bp.draws[find_draw(bp, g)].view];
-                own.col_stride = vw.draw_count;
-                own.row_stride = vw.tiles_x * vw.draw_count;
-            }
-        } else if (bd.y == kBinsClipped) {
-            const uint32_t info = bp.tri_info[g];
-            const DrawDesc &d = bp.draws[find_draw(bp, g)];
-            const ViewDesc &vw = bp.views[d.view];
-            const uint32_t fbase = (uint32_t)__ldg(&bp.raster[g].w[0].x);
-            for (uint32_t f = 0; f < 7; ++f) {
-                if (!(info >> f & 1u)) continue;
-                BinJob job;
-                // the fan's box deltas: slot g's words y (fans 0-4) and z (fans 5-6), 6 bits each
-                const uint32_t dw = (uint32_t)__ldg(f < 5 ? &bp.raster[g].w[0].y : &bp.raster[g].w[0].z);
-                if (!record_job(bp, vw, d.draw_in_view, bp.total_tris + fbase + f, (g << 3) | (f + 1),
-                                (dw >> (6 * (f < 5 ? f : f - 5))) & 63u, job))
-                    continue;
-                const uint32_t nt = job.nx * job.ny;
-                if (nt > bp.big_tiles) {
-                    const uint32_t q = atomicAdd(&s_qn[warp], 1u);
-                    if (q < kFanQueue) { s_q[warp][q] = job; continue; }
-                }
-                put_job(bp, job, 0, 1);
-            }
+        own.key = e.x;
+        own.first_bin = e.y;
+        own.nx = e.z & 0xFFFFu;
+        own.ny = e.z >> 16;
+        const uint32_t nt_own = j < njobs ? own.nx * own.ny : 0u;
+        if (nt_own > 1) {   // the bin strides of its view (a one-tile job needs none)
+            const ViewDesc &vw = bp.views[e.w];
+            own.col_stride = vw.draw_count;
+            own.row_stride = vw.tiles_x * vw.draw_count;
         }
         const uint32_t single = nt_own == 1 ? own.first_bin : 0xFFFFFFFFu;
         const uint32_t peers = __match_any_sync(0xFFFFFFFFu, single);
         if (single != 0xFFFFFFFFu) {
             const int leader = __ffs(peers) - 1;
+            const uint32_t st = __ldg(bp.bin_start + single);
             uint32_t top = 0;
             if (lane == leader) top = atomicSub(bp.bin_count + single, (uint32_t)__popc(peers));
             top = __shfl_sync(peers, top, leader);
             const uint32_t r = (uint32_t)__popc(peers & ((1u << lane) - 1u));
-            bp.list[__ldg(bp.bin_start + single) + top - 1u - r] = own.key;
+            bp.list[st + top - 1u - r] = own.key;
         } else if (nt_own > 1 && nt_own <= bp.big_tiles) {
             put_job(bp, own, 0, 1);
         }
@@ -1108,7 +1076,7 @@ __global__ void __launch_bounds__(kScatterBlock) k_scatter(BatchParams bp) {
             // each lane's pairs are item = lane, lane + 32, ...: its triangle only moves forward,
             // so the job stays in registers until the lane crosses the end of a triangle; four
             // pairs are filled together
-            uint32_t jb = 0, base = 0, end = s_bigpref[warp][0];
+            uint32_t jb = 0, first = 0, end = s_bigpref[warp][0];
             BinJob job = s_big[warp][0];
             for (uint32_t item0 = lane; item0 < total_big; item0 += 128) {
                 uint32_t bin[4], key[4], m = 0;
@@ -1121,13 +1089,13 @@ __global__ void __launch_bounds__(kScatterBlock) k_scatter(BatchParams bp) {
                     if (item >= end) {
                         do {
                             ++jb;
-                            base = end;
+                            first = end;
                             end = s_bigpref[warp][jb];
                         } while (item >= end);
                         job = s_big[warp][jb];
                     }
-                    if (item - base < job.nx * job.ny) {   // not padding
-                        bin[k] = job_bin(job, item - base);
+                    if (item - first < job.nx * job.ny) {   // not padding
+                        bin[k] = job_bin(job, item - first);
                         key[k] = job.key;
                         m |= 1u << k;
                     }
@@ -1135,9 +1103,6 @@ __global__ void __launch_bounds__(kScatterBlock) k_scatter(BatchParams bp) {
                 put4(bp, bin, key, m);
             }
         }
-        __syncwarp();
-        const uint32_t nq = min(s_qn[warp], (uint32_t)kFanQueue);
-        for (uint32_t b = 0; b < nq; ++b) put_job(bp, s_q[warp][b], lane, 32);
         __syncwarp();
     }
     pdl_trigger();

@@ -52,14 +52,14 @@ constexpr size_t kStatusWords = kMaxTiles / 4096 + 2;
 constexpr size_t kOffBinCount = align256(kOffStatus + sizeof(unsigned long long) * kStatusWords);
 constexpr size_t kOffBinStart = align256(kOffBinCount + sizeof(uint32_t) * (kMaxTiles + 1));
 constexpr size_t kOffTriInfo = align256(kOffBinStart + sizeof(uint32_t) * (kMaxTiles + 1));
-constexpr size_t kOffBinsOf = align256(kOffTriInfo + sizeof(uint16_t) * (kMaxTriangles + 1));
-constexpr size_t kOffRaster = align256(kOffBinsOf + sizeof(uint2) * kMaxTriangles);
+constexpr size_t kOffJobs = align256(kOffTriInfo + sizeof(uint16_t) * (kMaxTriangles + 1));
+constexpr size_t kOffRaster = align256(kOffJobs + sizeof(uint4) * (kMaxTriangles + kMaxFanSlots));
 constexpr size_t kOffShade = align256(kOffRaster + sizeof(TriRaster) * (kMaxTriangles + kMaxFanSlots));
 constexpr size_t kOffVsOut = align256(kOffShade + sizeof(TriShade) * (kMaxTriangles + kMaxFanSlots));
 constexpr size_t kOffList = align256(kOffVsOut + sizeof(float4) * 3 * kMaxVertices);
 constexpr size_t kScratchBytes = align256(kOffList + sizeof(uint32_t) * kMaxBinEntries);
 static_assert(kScratchBytes == MLV_NOALLOC_SCRATCH_BYTES, "header and layout disagree on the scratch size");
-static_assert(kMaxBinEntries >= kMaxTriangles, "the clip list lives in the bin-list region");
+static_assert(kMaxBinEntries >= 2 * kMaxTriangles, "the clip list lives in the bin-list region");
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
@@ -271,13 +271,14 @@ extern "C" MLV_API mlv_status mlv_draw_indexed_noalloc(const mlv_noalloc_draw *a
     bp.raster = (TriRaster *)(base + kOffRaster);
     bp.shade = (TriShade *)(base + kOffShade);
     bp.tri_info = (uint16_t *)(base + kOffTriInfo);
-    bp.bins_of = (uint2 *)(base + kOffBinsOf);
+    bp.jobs = (uint4 *)(base + kOffJobs);
+    bp.jobs_capacity = kMaxTriangles + kMaxFanSlots;
     bp.bin_count = (uint32_t *)(base + kOffBinCount);
     bp.bin_start = (uint32_t *)(base + kOffBinStart);
     bp.list = (uint32_t *)(base + kOffList);
     // the list is written only by k_scatter, after k_clip is done with the clip list it holds
-    // (MLV_NOALLOC_MAX_BIN_ENTRIES >= MLV_NOALLOC_MAX_TRIANGLES entries)
-    bp.clip_list = bp.list;
+    // (MLV_NOALLOC_MAX_BIN_ENTRIES words hold MLV_NOALLOC_MAX_TRIANGLES entries of two)
+    bp.clip_list = (uint2 *)(base + kOffList);
     bp.scan_status2 = (unsigned long long *)(base + kOffStatus);
     bp.counters = (uint32_t *)(base + kOffCounters);
     bp.stats = (unsigned long long *)(base + kOffStats);
