@@ -372,6 +372,15 @@ __device__ __forceinline__ uint32_t find_draw(const BatchParams &bp, uint32_t tr
     return lo;
 }
 
+// The draw of every input triangle in [first, last] when they share one, else kNoDraw: the
+// triangles a CTA sets up almost always do, and one search then serves them all.
+constexpr uint32_t kNoDraw = 0xFFFFFFFFu;
+
+__device__ __forceinline__ uint32_t common_draw(const BatchParams &bp, uint32_t first, uint32_t last) {
+    const uint32_t a = find_draw(bp, first);
+    return a == find_draw(bp, last) ? a : kNoDraw;
+}
+
 __device__ __forceinline__ void fetch_vertex(const DrawDesc &d, uint32_t idx_pos, float *in, uint32_t *warn) {
     int64_t idx = d.ib ? (int64_t)__ldg(d.ib + idx_pos) : (int64_t)idx_pos;
     idx += d.base_vertex;
@@ -1942,15 +1951,22 @@ __global__ void __launch_bounds__(kDirectBlock) k_direct_raster(BatchParams bp) 
     __shared__ uint4 s_push[kDirectListCap];           // jobs to queue: key, record, tiles
     __shared__ uint4 s_mark[kDirectListCap];           // bin rectangles to mark: first bin, nx, ny, row stride
     __shared__ uint32_t s_npush, s_nmark;
+    __shared__ uint32_t s_draw;
     pdl_wait();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t g0 = blockIdx.x * NT;
-    if (threadIdx.x == 0) { s_npush = 0; s_nmark = 0; }
+    if (threadIdx.x == 0) {
+        s_npush = 0;
+        s_nmark = 0;
+        s_draw = common_draw(bp, g0, min(g0 + NT, bp.total_tris) - 1);
+    }
+    __syncthreads();
+    const uint32_t cta_draw = s_draw;
     // vertex shader, one invocation per (triangle, vertex), per index as the reference shades
     for (uint32_t i = threadIdx.x; i < 3u * NT; i += kDirectBlock) {
         const uint32_t t = i / 3, k = i - 3 * t, g = g0 + t;
         if (g < bp.total_tris) {
-            const DrawDesc &d = bp.draws[find_draw(bp, g)];
+            const DrawDesc &d = bp.draws[cta_draw != kNoDraw ? cta_draw : find_draw(bp, g)];
             triangle_vertex(bp, d, d.start_index + 3 * (g - d.tri_begin) + k, s_v[t][k].v);
         }
     }
@@ -1961,7 +1977,7 @@ __global__ void __launch_bounds__(kDirectBlock) k_direct_raster(BatchParams bp) 
         uint32_t mask = 0, entries = 0;
         if (SW == 1) s_cnt[lane] = 0;
         if (g < bp.total_tris) {
-            const DrawDesc &d = bp.draws[find_draw(bp, g)];
+            const DrawDesc &d = bp.draws[cta_draw != kNoDraw ? cta_draw : find_draw(bp, g)];
             const ViewDesc &V = bp.views[d.view];
             const float *p0 = s_v[t][0].v, *p1 = s_v[t][1].v, *p2 = s_v[t][2].v;
             bool reject = p0[3] == 0 || p1[3] == 0 || p2[3] == 0;   // main.c:759-781
