@@ -120,19 +120,38 @@ def test_autotune_picks_a_path_for_a_single_draw_and_keeps_the_output(device):
     frame = scenes.config1_plain(seed=2, width=320, height=192, tex_size=64, level=4)
     ctx = device.immediate
     base = ctx.tuning()
-    r = api.FrameRenderer(device, frame, visibility=True)
+    r = api.FrameRenderer(device, frame)   # no triangle-id targets: the small-draw path applies
     try:
         r.render_batched()
         want = r.read(0)
         out = autotune.autotune(device, r, repeats=2, warmup=1)
         assert [p["small_draw_triangles"] for p, _ in out["path"]] == list(autotune.PATHS)
         assert ctx.tuning()["small_draw_triangles"] == out["best"]["small_draw_triangles"]
-        # the sweep runs only when the binned path won
-        assert (out["results"] == []) == (out["best"]["small_draw_triangles"] != 0)
+        # no sweep when the small-draw path won; a sweep when the binned path did
+        if out["best"]["small_draw_triangles"] == 0:
+            assert out["results"]
+        else:
+            assert out["results"] == []
         r.render_batched()
         got = r.read(0)
-        for key in ("color", "depth", "vis_tri", "vis_draw", "vis_bary"):
+        for key in ("color", "depth"):
             assert np.array_equal(got[key].view(np.uint32), want[key].view(np.uint32)), key
+    finally:
+        r.destroy()
+        ctx.set_tuning(**base)
+
+
+@pytest.mark.gpu
+def test_autotune_sweeps_when_the_small_draw_path_does_not_apply(device):
+    from malevich_gb300 import api
+    frame = scenes.config1_plain(seed=3, width=160, height=96, tex_size=32, level=3)
+    ctx = device.immediate
+    base = ctx.tuning()
+    r = api.FrameRenderer(device, frame, visibility=True)   # triangle ids: binned path only
+    try:
+        r.render_batched()
+        out = autotune.autotune(device, r, space={"tile_warps_per_block": (2, 4)}, repeats=1, warmup=1)
+        assert len(out["results"]) == 2
     finally:
         r.destroy()
         ctx.set_tuning(**base)
