@@ -1705,12 +1705,12 @@ MLV_API mlv_status mlv_destroy_command_list(mlv_command_list l) {
     return MLV_OK;
 }
 
-// Builds the list's device descriptors, sizes the workspace for its largest segment and
-// records all of its kernels on the context stream (eagerly, or into a graph being captured).
-static mlv_status run_list(mlv_context_t *c, mlv_command_list l, uint32_t seq, bool upload) {
-    std::vector<Plan> plans(l->segments.size());
-    BatchSizes maxs;
-    size_t nd = 0, nv = 0;
+// Plans every segment of the list with the context's tuning; maxs: the largest of their sizes.
+static mlv_status plan_list(mlv_context_t *c, mlv_command_list l, std::vector<Plan> &plans, BatchSizes &maxs,
+                            size_t &nd, size_t &nv) {
+    plans.assign(l->segments.size(), Plan());
+    maxs = BatchSizes();
+    nd = nv = 0;
     for (size_t i = 0; i < l->segments.size(); ++i) {
         MLV_TRY(plan_segment(l->segments[i], plans[i], c->tuning.initial_clip_fan_slots,
                              c->tuning.small_draw_triangles, c->capture_infos));
@@ -1728,6 +1728,28 @@ static mlv_status run_list(mlv_context_t *c, mlv_command_list l, uint32_t seq, b
         nd += plans[i].draws.size();
         nv += plans[i].views.size();
     }
+    return MLV_OK;
+}
+
+// Sizes the workspace for the list as the context's tuning plans it. Run before a graph capture:
+// the captured kernels keep the workspace's pointers, and a tuning change can move the list to
+// another path with buffers of its own (the small-draw path's keys, the binned path's job list).
+static mlv_status size_list(mlv_context_t *c, mlv_command_list l) {
+    std::vector<Plan> plans;
+    BatchSizes maxs;
+    size_t nd = 0, nv = 0;
+    MLV_TRY(plan_list(c, l, plans, maxs, nd, nv));
+    return ensure_workspace(c, maxs, false);
+}
+
+// Builds the list's device descriptors, sizes the workspace for its largest segment and
+// records all of its kernels on the context stream (eagerly, or into a graph being captured,
+// after size_list).
+static mlv_status run_list(mlv_context_t *c, mlv_command_list l, uint32_t seq, bool upload) {
+    std::vector<Plan> plans;
+    BatchSizes maxs;
+    size_t nd = 0, nv = 0;
+    MLV_TRY(plan_list(c, l, plans, maxs, nd, nv));
     if (!c->capturing_graph) MLV_TRY(ensure_workspace(c, maxs, false));
     std::vector<std::vector<FillJob>> fills(l->segments.size());
     std::vector<uint32_t> fill_chunks(l->segments.size());
@@ -1813,6 +1835,7 @@ MLV_API mlv_status mlv_execute_command_list(mlv_context c, mlv_command_list l) {
         l->exec_tuning != c->tuning_generation || l->exec_uploads != uploads) {
         if (l->exec) cudaGraphExecDestroy(l->exec);
         l->exec = nullptr;
+        MLV_TRY(size_list(c, l));
         cudaGraph_t g = nullptr;
         uint64_t saved[8];
         memcpy(saved, c->host_stats, sizeof(saved));

@@ -155,3 +155,30 @@ def test_autotune_sweeps_when_the_small_draw_path_does_not_apply(device):
     finally:
         r.destroy()
         ctx.set_tuning(**base)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("first,then", [(autotune.PATHS[1], 0), (0, autotune.PATHS[1])])
+def test_a_tuning_change_that_moves_the_path_sizes_its_buffers_before_the_capture(first, then):
+    """A fresh context that has run a command list on one path only: a tuning change moves the list
+    to the other path, whose buffers (the binned path's job and clip lists, the small-draw path's
+    keys) did not exist yet, and the graph captured for it must see them allocated."""
+    from malevich_gb300 import api
+    dev = api.Device(0)
+    try:
+        ctx = dev.immediate
+        ctx.set_tuning(small_draw_triangles=first)
+        frame = scenes.config1_plain(seed=4, width=192, height=128, tex_size=32, level=3)
+        r = api.FrameRenderer(dev, frame)
+        r.render_batched()   # eager: sizes the workspace for the first path only
+        r.render_batched()   # graph
+        want = r.read(0)
+        ctx.set_tuning(small_draw_triangles=then)
+        r.render_batched()   # captured again, on the other path
+        r.render_batched()
+        got = r.read(0)
+        for key in ("color", "depth"):
+            assert np.array_equal(got[key].view(np.uint32), want[key].view(np.uint32)), key
+        r.destroy()
+    finally:
+        dev.destroy()
