@@ -9,7 +9,8 @@ synthetic data. One step renders the whole frame (clears + 12 draws) as one batc
 value     input triangles per second over the K timed steps (Mtri/s), inputs resident in HBM.
 e2e       the same frame through the C ABI from host buffers: every step uploads the vertex and
           index buffers and both textures from pinned host memory and reads the colour target back;
-          two device handles alternate so that one step's readback overlaps the next one's uploads
+          two device handles alternate so that one step's readback overlaps the next one's uploads;
+          the inputs go up as one grouped upload (mlv_update_resources_async): one copy a step
           (e2e.serial: one context, step after step).
 per_draw  the same frame drawn per draw on the immediate context (one launch sequence per draw).
 gpix_per_s fragments written (the oracle's count of covered, hierarchical-Z and depth-test passing
@@ -814,36 +815,50 @@ def main():
             pinned[id(a)] = (t, t.numpy())
         return pinned[id(a)][1]
 
-    def upload_plan(rr):
-        """The renderer's resources with their pinned host sources, in the order the frame consumes
-        them: the vertex stage reads vertex buffers and its texture, geometry the index buffers, the
-        tile kernel the pixel shader's texture; each stage waits only for its own inputs' copies, so
-        the later copies overlap the earlier stages."""
+    blocks = {}
+
+    def upload_plan(rr, by_stage):
+        """The renderer's resources as grouped uploads, each group one pinned block moved by one
+        copy and placed by one kernel, built once and shared by the renderers of the same frame.
+        by_stage: three groups, in the order the frame reads them (the vertex stage's inputs, the
+        index buffers, the pixel shader's texture), so that a lone frame's earlier stages overlap
+        the later copies; else one group, which with two frames in flight was faster (0.247
+        against 0.263 ms per step)."""
         vs_tex_ids = {id(d.vs_tex.data) for d in frame.draws if d.vs_tex is not None}
+        groups = [[], [], []] if by_stage else [[]]
+        for key, (buf, arr) in rr._buffers.items():
+            groups[(0 if key[1] == api.BIND_VERTEX_BUFFER else 1) if by_stage else 0].append((buf, arr))
+        for tex, t in rr._textures.values():
+            groups[(0 if id(t.data) in vs_tex_ids else 2) if by_stage else 0].append((tex, t.data))
         plan = []
-        for key, (buf, arr) in rr._buffers.items():
-            if key[1] == api.BIND_VERTEX_BUFFER:
-                plan.append(("buf", buf, pin(arr)))
-        for tex, t in rr._textures.values():
-            if id(t.data) in vs_tex_ids:
-                plan.append(("tex", tex, pin(t.data)))
-        for key, (buf, arr) in rr._buffers.items():
-            if key[1] == api.BIND_INDEX_BUFFER:
-                plan.append(("buf", buf, pin(arr)))
-        for tex, t in rr._textures.values():
-            if id(t.data) not in vs_tex_ids:
-                plan.append(("tex", tex, pin(t.data)))
+        for g in groups:
+            if not g:
+                continue
+            key = tuple(id(a) for _, a in g)
+            if key not in blocks:
+                offs, at = [], 0
+                for _, a in g:
+                    offs.append(at)
+                    at += (a.nbytes + 15) // 16 * 16
+                t = torch.empty(at, dtype=torch.uint8).pin_memory()
+                block = t.numpy()
+                for (_, a), o in zip(g, offs):
+                    block[o:o + a.nbytes] = np.ascontiguousarray(a).view(np.uint8).reshape(-1)
+                blocks[key] = (t, block, offs)
+            _, block, offs = blocks[key]
+            ups = (api.Upload * len(g))()
+            for i, ((res, a), o) in enumerate(zip(g, offs)):
+                kind = api.UPLOAD_TEXTURE2D if isinstance(res, api.Texture2D) else api.UPLOAD_BUFFER
+                ups[i] = api.Upload(kind, 0, res.handle, o, 0, a.nbytes)
+            plan.append((block, ups, len(g)))
         return plan
 
     def issue(rr, plan):
-        """One step's uploads (queued, from pinned memory that stays unchanged) and its frame."""
+        """One step's uploads (grouped copies from pinned blocks that stay unchanged) and its
+        frame."""
         c = rr.device.immediate
-        for kind, res, a in plan:
-            ptr = a.ctypes.data_as(ctypes.c_void_p)
-            if kind == "buf":
-                c.lib.mlv_update_buffer_async(c.handle, res.handle, 0, ptr, a.nbytes)
-            else:
-                c.lib.mlv_update_texture2d_async(c.handle, res.handle, ptr, 0)
+        for block, ups, n in plan:
+            c.lib.mlv_update_resources_async(c.handle, block.ctypes.data_as(ctypes.c_void_p), block.nbytes, ups, n)
         rr.render_batched()
 
     out_imgs = [torch.empty((frame.height, frame.width), dtype=torch.int32).pin_memory().numpy().view(np.uint32)
@@ -853,8 +868,8 @@ def main():
         c = rr.device.immediate
         c.lib.mlv_read_texture2d(c.handle, rr.targets[0][0].handle, out_imgs[k % 2].ctypes.data_as(ctypes.c_void_p), 0)
 
-    plan1 = upload_plan(r)
-    h2d = sum(a.nbytes for _, _, a in plan1)
+    plan1 = upload_plan(r, by_stage=True)
+    h2d = sum(block.nbytes for block, _, _ in upload_plan(r, by_stage=False))
     d2h = out_imgs[0].nbytes
 
     # one context: upload, render and read back, step after step
@@ -878,7 +893,7 @@ def main():
     dev_b.immediate.set_tuning(**ctx.tuning())
     r_b = api.FrameRenderer(dev_b, frame)
     r_b.render_batched()
-    pair = [(r, plan1), (r_b, upload_plan(r_b))]
+    pair = [(r, upload_plan(r, by_stage=False)), (r_b, upload_plan(r_b, by_stage=False))]
     for k in range(4):
         issue(*pair[k % 2])
         read(pair[k % 2][0], k)
@@ -949,12 +964,14 @@ def main():
             "e2e": {"value": round(tris * world / e2e_s / 1e6, 3), "unit": "Mtri/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_s * 1e3, 3),
                     "mode": "two device handles alternating (double-buffered frames): each step uploads its "
-                            "inputs from pinned host memory, renders, and reads its image back; a step's "
-                            "readback overlaps the next step's uploads",
+                            "inputs from pinned host memory (one grouped upload of the vertex and index buffers "
+                            "and both textures: one copy, one placement kernel), renders, and reads its image "
+                            "back; a step's readback overlaps the next step's uploads",
                     "images_identical": e2e_same,
                     "serial": {"value": round(tris * world / e2e_serial_s / 1e6, 3), "unit": "Mtri/s",
                                "ms_per_step": round(e2e_serial_s * 1e3, 3),
-                               "mode": "one context, upload, render and read back step after step"}},
+                               "mode": "one context, upload, render and read back step after step; the uploads "
+                                       "as three grouped copies, one per stage that reads them"}},
             "roofline": {"bound": "hbm", "achieved": round(frame_achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(frame_achieved / peak, 4), "peak_kind": peak_kind,
                          "counts": "the whole frame: 4 I + 32 V + sampled textures (capped at 4 taps per "

@@ -36,7 +36,7 @@ EXPORTS = [
     "mlv_get_immediate_context", "mlv_create_deferred_context", "mlv_destroy_context", "mlv_create_buffer",
     "mlv_destroy_buffer", "mlv_create_texture2d", "mlv_create_texture2d_on_memory", "mlv_destroy_texture2d", "mlv_buffer_device_pointer",
     "mlv_texture2d_device_pointer", "mlv_update_buffer", "mlv_update_texture2d", "mlv_read_texture2d",
-    "mlv_update_buffer_async", "mlv_update_texture2d_async",
+    "mlv_update_buffer_async", "mlv_update_texture2d_async", "mlv_update_resources_async",
     "mlv_ia_set_primitive_topology", "mlv_ia_set_index_buffer", "mlv_ia_set_vertex_buffers",
     "mlv_vs_set_shader", "mlv_vs_set_constant_buffers", "mlv_vs_set_shader_resources", "mlv_ps_set_shader",
     "mlv_ps_set_shader_resources", "mlv_rs_set_viewports", "mlv_rs_set_state", "mlv_om_set_depth_stencil_state",
@@ -53,6 +53,15 @@ class MalevichError(RuntimeError):
     def __init__(self, status, message):
         super().__init__("%s: %s" % (STATUS_NAMES.get(status, status), message))
         self.status = status
+
+
+UPLOAD_BUFFER, UPLOAD_TEXTURE2D = 0, 1
+
+
+class Upload(ctypes.Structure):
+    """One range of a grouped upload (mlv_upload)."""
+    _fields_ = [("kind", ctypes.c_uint32), ("pad", ctypes.c_uint32), ("resource", ctypes.c_void_p),
+                ("src_offset", ctypes.c_uint64), ("dst_offset", ctypes.c_uint64), ("size", ctypes.c_uint64)]
 
 
 class BufferDesc(ctypes.Structure):
@@ -130,6 +139,7 @@ def load_library(path=LIB_PATH):
     lib.mlv_update_texture2d.argtypes = [vp, vp, vp, ctypes.c_uint32]
     lib.mlv_update_buffer_async.argtypes = [vp, vp, ctypes.c_uint64, vp, ctypes.c_uint64]
     lib.mlv_update_texture2d_async.argtypes = [vp, vp, vp, ctypes.c_uint32]
+    lib.mlv_update_resources_async.argtypes = [vp, vp, ctypes.c_uint64, ctypes.POINTER(Upload), ctypes.c_uint32]
     lib.mlv_read_texture2d.argtypes = [vp, vp, vp, ctypes.c_uint32]
     lib.mlv_ia_set_primitive_topology.argtypes = [vp, ctypes.c_int]
     lib.mlv_ia_set_index_buffer.argtypes = [vp, vp, ctypes.c_int, ctypes.c_uint32]
@@ -335,6 +345,22 @@ class Context:
             raise ValueError("update_texture_async needs a C-contiguous array it can keep")
         _check(self.lib.mlv_update_texture2d_async(self.handle, tex.handle, _ptr(arr), 0))
         self._queued.append(arr)
+
+    def update_resources_async(self, block, uploads):
+        """Queued uploads of several resources from one C-contiguous byte array `block`:
+        `uploads` is a list of (resource, src_offset, size) for Buffer/Texture objects (buffers may
+        add a dst_offset as a fourth item). One copy moves the block, one kernel places the ranges;
+        the context keeps `block` alive until its next synchronisation."""
+        if not block.flags["C_CONTIGUOUS"]:
+            raise ValueError("update_resources_async needs a C-contiguous array it can keep")
+        arr = (Upload * max(len(uploads), 1))()
+        for i, u in enumerate(uploads):
+            res, src, size = u[0], u[1], u[2]
+            dst = u[3] if len(u) > 3 else 0
+            kind = UPLOAD_TEXTURE2D if isinstance(res, Texture2D) else UPLOAD_BUFFER
+            arr[i] = Upload(kind, 0, res.handle, src, dst, size)
+        _check(self.lib.mlv_update_resources_async(self.handle, _ptr(block), block.nbytes, arr, len(uploads)))
+        self._queued.append(block)
 
     def finish_command_list(self):
         h = ctypes.c_void_p()

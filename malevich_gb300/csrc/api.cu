@@ -33,6 +33,8 @@ cudaError_t launch_fill_many(const FillJob *d_jobs, uint32_t njobs, uint32_t nch
                              cudaStream_t stream);
 cudaError_t launch_vertex(const BatchParams &bp, cudaStream_t stream);
 cudaError_t launch_geometry(const BatchParams &bp, uint32_t block, int num_sms, cudaStream_t stream);
+cudaError_t launch_upload_scatter(const uint8_t *staging, const UploadJobs &jobs, uint32_t njobs, uint64_t max_size,
+                                  int num_sms, cudaStream_t stream);
 cudaError_t launch_scan(const BatchParams &bp, cudaStream_t stream);
 cudaError_t launch_rank(const BatchParams &bp, cudaStream_t stream);
 cudaError_t launch_scatter(const BatchParams &bp, int num_sms, cudaStream_t stream);
@@ -256,6 +258,8 @@ struct mlv_context_t {
     // index buffers before geometry, PS textures before the tile kernel)
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t work_mark = nullptr;   // the context stream's work so far, which uploads follow
+    uint8_t *upload_staging = nullptr; // grouped uploads (mlv_update_resources_async) land here first
+    uint64_t upload_staging_cap = 0;
     // last single-draw segment, for mlv_get_tile_infos
     bool last_single = false;
     uint32_t last_total_bins = 0, last_tiles_x = 0, last_draw_count = 0;
@@ -1042,6 +1046,7 @@ static void destroy_context_internal(mlv_context_t *c) {
     if (c->h_error) cudaFreeHost(c->h_error);
     if (c->copy_stream) {
         cudaStreamSynchronize(c->copy_stream);
+        cudaFree(c->upload_staging);
         cudaStreamDestroy(c->copy_stream);
     }
     if (c->work_mark) cudaEventDestroy(c->work_mark);
@@ -1289,15 +1294,22 @@ MLV_API mlv_status mlv_update_texture2d(mlv_context c, mlv_texture2d t, const vo
 // context first synchronises if anything is pending; otherwise the copy is only queued, on the
 // context's copy stream behind everything already issued on its stream, and the resource's event
 // marks its completion for the batches that read it (Plan::wait_*).
+// A resource's first queued upload gives it its ready event, which captured graphs must then wait
+// for: that changes the upload generation, so command lists re-capture.
+static mlv_status ensure_ready_event(mlv_context_t *c, cudaEvent_t *ready) {
+    if (!*ready) {
+        CUDA_TRY(cudaEventCreateWithFlags(ready, cudaEventDisableTiming));
+        c->device->upload_generation.fetch_add(1);
+    }
+    return MLV_OK;
+}
+
 static mlv_status begin_upload(mlv_context_t *c, cudaEvent_t *ready) {
     if (!c->copy_stream) {
         CUDA_TRY(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
         CUDA_TRY(cudaEventCreateWithFlags(&c->work_mark, cudaEventDisableTiming));
     }
-    if (!*ready) {
-        CUDA_TRY(cudaEventCreateWithFlags(ready, cudaEventDisableTiming));
-        c->device->upload_generation.fetch_add(1);
-    }
+    if (ready) MLV_TRY(ensure_ready_event(c, ready));
     CUDA_TRY(cudaEventRecord(c->work_mark, c->stream));
     CUDA_TRY(cudaStreamWaitEvent(c->copy_stream, c->work_mark, 0));
     return MLV_OK;
@@ -1327,6 +1339,75 @@ MLV_API mlv_status mlv_update_texture2d_async(mlv_context c, mlv_texture2d t, co
     CUDA_TRY(cudaMemcpy2DAsync(t->ptr, row, data, row_pitch ? row_pitch : row, row, t->height, cudaMemcpyHostToDevice,
                                c->copy_stream));
     CUDA_TRY(cudaEventRecord(t->ready, c->copy_stream));
+    return MLV_OK;
+}
+
+// One host-to-device copy of the block into the context's staging area, then k_upload_scatter
+// places the ranges (kUploadJobsPerLaunch a launch), all on the copy stream; each resource's ready
+// event is recorded after the last placement.
+MLV_API mlv_status mlv_update_resources_async(mlv_context c, const void *block, uint64_t block_bytes,
+                                              const mlv_upload *ups, uint32_t count) {
+    MLV_TRY(need_immediate(c));
+    if (count == 0) return MLV_OK;
+    if (!block || !ups) return fail(MLV_ERROR_INVALID_ARG, "NULL argument");
+    std::vector<UploadJob> jobs(count);
+    for (uint32_t i = 0; i < count; ++i) {
+        const mlv_upload &u = ups[i];
+        if (!u.resource) return fail(MLV_ERROR_INVALID_ARG, "upload " + std::to_string(i) + ": NULL resource");
+        if (u.src_offset % 16) return fail(MLV_ERROR_INVALID_ARG, "upload " + std::to_string(i) + ": src_offset must be a multiple of 16");
+        if (u.src_offset > block_bytes || u.size > block_bytes - u.src_offset)
+            return fail(MLV_ERROR_INVALID_ARG, "upload " + std::to_string(i) + ": range outside the block");
+        uint8_t *dst = nullptr;
+        if (u.kind == MLV_UPLOAD_BUFFER) {
+            mlv_buffer b = (mlv_buffer)u.resource;
+            if (b->device != c->device) return fail(MLV_ERROR_INVALID_ARG, "upload " + std::to_string(i) + ": another device's buffer");
+            if (u.dst_offset > b->size || u.size > b->size - u.dst_offset)
+                return fail(MLV_ERROR_INVALID_ARG, "upload " + std::to_string(i) + ": update outside the buffer");
+            dst = b->ptr + u.dst_offset;
+        } else if (u.kind == MLV_UPLOAD_TEXTURE2D) {
+            mlv_texture2d t = (mlv_texture2d)u.resource;
+            if (t->device != c->device) return fail(MLV_ERROR_INVALID_ARG, "upload " + std::to_string(i) + ": another device's texture");
+            if (u.dst_offset != 0 || u.size != (uint64_t)t->width * t->height * t->texel_bytes)
+                return fail(MLV_ERROR_INVALID_ARG, "upload " + std::to_string(i) + ": a texture takes its whole size at offset 0");
+            dst = t->ptr;
+        } else {
+            return fail(MLV_ERROR_INVALID_ARG, "upload " + std::to_string(i) + ": unknown kind");
+        }
+        if ((uintptr_t)dst % 16) return fail(MLV_ERROR_INVALID_ARG, "upload " + std::to_string(i) + ": destination not 16-byte aligned");
+        jobs[i] = UploadJob{dst, u.src_offset, u.size};
+    }
+    MLV_TRY(set_device(c->device));
+    if (!c->pending.empty()) MLV_TRY(sync_context(c));
+    MLV_TRY(begin_upload(c, nullptr));
+    if (block_bytes > c->upload_staging_cap) {
+        CUDA_TRY(cudaStreamSynchronize(c->copy_stream));   // earlier grouped uploads still read it
+        cudaFree(c->upload_staging);
+        c->upload_staging = nullptr;
+        c->upload_staging_cap = 0;
+        MLV_TRY(dev_alloc((void **)&c->upload_staging, block_bytes));
+        c->upload_staging_cap = block_bytes;
+    }
+    CUDA_TRY(cudaMemcpyAsync(c->upload_staging, block, block_bytes, cudaMemcpyHostToDevice, c->copy_stream));
+    for (uint32_t first = 0; first < count; first += kUploadJobsPerLaunch) {
+        UploadJobs part = {};
+        const uint32_t n = std::min<uint32_t>(kUploadJobsPerLaunch, count - first);
+        uint64_t largest = 0;
+        for (uint32_t k = 0; k < n; ++k) {
+            part.job[k] = jobs[first + k];
+            largest = std::max<uint64_t>(largest, jobs[first + k].size);
+        }
+        CUDA_TRY(launch_upload_scatter(c->upload_staging, part, n, largest, c->device->num_sms, c->copy_stream));
+    }
+    for (uint32_t i = 0; i < count; ++i) {
+        const mlv_upload &u = ups[i];
+        cudaEvent_t *ready = u.kind == MLV_UPLOAD_BUFFER ? &((mlv_buffer)u.resource)->ready : &((mlv_texture2d)u.resource)->ready;
+        MLV_TRY(ensure_ready_event(c, ready));
+        CUDA_TRY(cudaEventRecord(*ready, c->copy_stream));
+        if (u.kind == MLV_UPLOAD_BUFFER) {
+            mlv_buffer b = (mlv_buffer)u.resource;
+            if (!b->shadow.empty()) memcpy(b->shadow.data() + u.dst_offset, (const uint8_t *)block + u.src_offset, u.size);
+        }
+    }
     return MLV_OK;
 }
 

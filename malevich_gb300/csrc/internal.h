@@ -120,6 +120,16 @@ constexpr uint32_t kFillChunk = 8192;
 // One emitted triangle's share of the binner (main.c:924-962), rebuilt from its record's bounds
 // where needed (never stored): its key and the bins of its tile rectangle,
 // bin(x, y) = first_bin + y * row_stride + x * col_stride.
+// One range of a grouped upload (mlv_update_resources_async): size bytes from staging + src to dst.
+struct UploadJob {
+    uint8_t *dst;
+    uint64_t src, size;
+};
+constexpr uint32_t kUploadJobsPerLaunch = 64;
+struct UploadJobs {
+    UploadJob job[kUploadJobsPerLaunch];
+};
+
 struct BinJob {
     uint32_t key, first_bin, nx, ny;
     uint32_t col_stride, row_stride, pad0, pad1;

@@ -2240,6 +2240,20 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_direct_resolve(BatchPara
 
 // ------------------------------------------------------------------ clears
 
+// A grouped upload's placement: job blockIdx.y's range, 16 bytes a thread per step (the bytes past
+// the last whole 16 one at a time). Sources are 16-byte aligned in the staging area, destinations
+// in their resources (checked on the host).
+__global__ void __launch_bounds__(256) k_upload_scatter(const uint8_t *staging, UploadJobs jobs) {
+    const UploadJob j = jobs.job[blockIdx.y];
+    const uint4 *src = reinterpret_cast<const uint4 *>(staging + j.src);
+    uint4 *dst = reinterpret_cast<uint4 *>(j.dst);
+    const uint64_t n16 = j.size >> 4;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += (uint64_t)gridDim.x * blockDim.x)
+        dst[i] = __ldg(src + i);
+    if (blockIdx.x == 0 && threadIdx.x < (j.size & 15u))
+        j.dst[(n16 << 4) + threadIdx.x] = staging[j.src + (n16 << 4) + threadIdx.x];
+}
+
 __global__ void k_fill_u32(uint32_t *p, size_t n, uint32_t value, const uint32_t *error) {
     pdl_wait();
     if (error && ld_volatile_u32(error)) return;
@@ -2328,6 +2342,18 @@ cudaError_t launch_fill_u32(uint32_t *p, size_t n, uint32_t value, const uint32_
 cudaError_t launch_vertex(const BatchParams &bp, cudaStream_t stream) {
     if (bp.total_vertices == 0) return cudaSuccess;
     return launch_chained(k_vertex, (bp.total_vertices + kVertexBlock - 1) / kVertexBlock, kVertexBlock, stream, bp);
+}
+
+// up to kUploadJobsPerLaunch ranges; x: CTAs per range (the largest range's 16-byte units over 256
+// threads, at most 2 per SM)
+cudaError_t launch_upload_scatter(const uint8_t *staging, const UploadJobs &jobs, uint32_t njobs, uint64_t max_size,
+                                  int num_sms, cudaStream_t stream) {
+    if (njobs == 0) return cudaSuccess;
+    uint64_t x = (max_size / 16 + 255) / 256;
+    const uint64_t cap = 2u * (uint64_t)(num_sms > 0 ? num_sms : 1);
+    x = x < 1 ? 1 : (x > cap ? cap : x);
+    k_upload_scatter<<<dim3((uint32_t)x, njobs), 256, 0, stream>>>(staging, jobs);
+    return cudaGetLastError();
 }
 
 // k_geometry, then k_clip (a grid of up to 8 CTAs per SM: one warp for each listed triangle, in

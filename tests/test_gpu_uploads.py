@@ -88,3 +88,88 @@ def test_readback_after_a_queued_upload_sees_it(device):
     ctx.update_texture_async(tex, data)
     assert np.array_equal(ctx.read_texture(tex), data)
     tex.destroy()
+
+
+def _pack(arrays, align=16):
+    """One byte block holding the arrays at 16-byte aligned offsets, and those offsets."""
+    offs, at = [], 0
+    for a in arrays:
+        offs.append(at)
+        at += (a.nbytes + align - 1) // align * align
+    block = np.zeros(max(at, 1), np.uint8)
+    for a, o in zip(arrays, offs):
+        block[o:o + a.nbytes] = np.ascontiguousarray(a).view(np.uint8).reshape(-1)
+    return block, offs
+
+
+def _upload_grouped(ctx, r, frame, new):
+    """The same contents as _upload, in three grouped uploads (vertex-stage inputs, index buffers,
+    the pixel shader's texture), each one copy and one placement kernel."""
+    groups = [[], [], []]
+    for d_old, d_new in zip(frame.draws, new.draws):
+        groups[0].append((r._buffers[(id(d_old.vb), api.BIND_VERTEX_BUFFER)][0], d_new.vb))
+        groups[1].append((r._buffers[(id(d_old.ib), api.BIND_INDEX_BUFFER)][0], d_new.ib))
+    groups[0].append((r._textures[id(frame.draws[0].vs_tex.data)][0], new.draws[0].vs_tex.data))
+    groups[2].append((r._textures[id(frame.draws[0].ps_tex.data)][0], new.draws[0].ps_tex.data))
+    for g in groups:
+        block, offs = _pack([a for _, a in g])
+        ctx.update_resources_async(block, [(res, o, a.nbytes) for (res, a), o in zip(g, offs)])
+
+
+def test_grouped_uploads_reach_eager_and_replayed_batches(device):
+    rng = np.random.default_rng(53)
+    fr = scenes.small_scene(54, 96, 64, vs=scenes.VS_VERTEX_LIGHTING, ps=scenes.PS_ENV_LIGHTING, n_objects=3, level=3)
+    new = _changed(fr, rng)
+    want_old, want_new = pyoracle.render_oracle(fr), pyoracle.render_oracle(new)
+    ctx = device.immediate
+    r = api.FrameRenderer(device, fr)
+    r.render_batched()
+    r.render_batched()
+    _check(r.read(0), want_old)
+    for k in range(4):
+        src = new if k % 2 == 0 else fr
+        _upload_grouped(ctx, r, fr, src)
+        r.render_batched()
+        _check(r.read(0), want_new if k % 2 == 0 else want_old)
+    # grouped and per-resource uploads give the same image
+    _upload(ctx, r, fr, new)
+    r.render_batched()
+    one = r.read(0)
+    _upload_grouped(ctx, r, fr, new)
+    r.render_batched()
+    two = r.read(0)
+    assert np.array_equal(one["color"], two["color"]) and np.array_equal(one["depth"].view(np.uint32), two["depth"].view(np.uint32))
+    r.destroy()
+
+
+def test_grouped_upload_places_ranges_and_partial_tails(device):
+    ctx = device.immediate
+    a = np.arange(37 * 11, dtype=np.uint32).reshape(11, 37)           # 1,628 bytes: a 12-byte tail
+    b = (np.arange(8 * 8, dtype=np.uint32) * 2654435761).astype(np.uint32).reshape(8, 8)
+    ta = api.Texture2D(device, 37, 11, api.FORMAT_R8G8B8A8_UNORM)
+    tb = api.Texture2D(device, 8, 8, api.FORMAT_R8G8B8A8_UNORM)
+    block, offs = _pack([b, a])
+    ctx.update_resources_async(block, [(ta, offs[1], a.nbytes), (tb, offs[0], b.nbytes)])
+    assert np.array_equal(ctx.read_texture(ta), a)
+    assert np.array_equal(ctx.read_texture(tb), b)
+    ta.destroy()
+    tb.destroy()
+
+
+def test_grouped_upload_checks_its_arguments(device):
+    ctx = device.immediate
+    t = api.Texture2D(device, 8, 8, api.FORMAT_R8G8B8A8_UNORM)
+    buf = api.Buffer(device, byte_width=256, bind=api.BIND_VERTEX_BUFFER)
+    block = np.zeros(512, np.uint8)
+    for bad in ([(t, 8, 256)],            # source not 16-byte aligned
+                [(t, 0, 255)],            # a texture takes its whole size
+                [(buf, 0, 16, 8)],        # destination not 16-byte aligned
+                [(buf, 0, 512)],          # beyond the buffer
+                [(buf, 400, 256)]):       # beyond the block
+        with pytest.raises(api.MalevichError):
+            ctx.update_resources_async(block, bad)
+    ctx.update_resources_async(block, [(buf, 16, 240, 16), (t, 256, 256)])
+    ctx.update_resources_async(block, [])
+    ctx.finish()
+    t.destroy()
+    buf.destroy()
