@@ -212,6 +212,11 @@ struct mlv_command_list_t {
     uint64_t exec_generation = ~0ull, exec_tuning = ~0ull, exec_uploads = ~0ull;
     mlv_context_t *exec_context = nullptr;
     int executions = 0;
+    // what the descriptors in d_draws/d_views/d_fills were planned for: a tuning change can move
+    // the list to the other path, whose descriptors differ
+    uint64_t desc_tuning = ~0ull;
+    mlv_context_t *desc_context = nullptr;
+    bool desc_capture = false;
     DrawDesc *d_draws = nullptr;   // per-segment descriptor copies owned by the list
     ViewDesc *d_views = nullptr;
     FillJob *d_fills = nullptr;    // per-segment batched clears
@@ -279,6 +284,23 @@ static mlv_status dev_alloc(void **p, size_t bytes) {
     return MLV_OK;
 }
 
+// Zeroes device memory and waits for it: cudaMemset runs on the legacy default stream, which the
+// library's non-blocking streams do not wait for, so work queued next (a graph captured right
+// after a workspace grows, a first batch) could otherwise read the old contents.
+static cudaError_t zero_now(void *p, size_t bytes) {
+    cudaError_t e = cudaMemset(p, 0, bytes);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(cudaStreamLegacy);
+}
+
+// The same for a copy from (pageable) host memory: cudaMemcpy may return once the data is staged,
+// before it reaches the device.
+static cudaError_t copy_to_device_now(void *dst, const void *src, size_t bytes) {
+    cudaError_t e = cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(cudaStreamLegacy);
+}
+
 template <class T>
 static mlv_status grow(T **p, uint32_t &cap, uint64_t need, uint64_t elem = sizeof(T), bool zero = false) {
     if (need <= cap && *p) return MLV_OK;
@@ -289,7 +311,7 @@ static mlv_status grow(T **p, uint32_t &cap, uint64_t need, uint64_t elem = size
     if (*p) cudaFree(*p);
     *p = nullptr;
     MLV_TRY(dev_alloc((void **)p, n * elem));
-    if (zero) CUDA_TRY(cudaMemset(*p, 0, n * elem));
+    if (zero) CUDA_TRY(zero_now(*p, n * elem));
     cap = (uint32_t)n;
     return MLV_OK;
 }
@@ -315,7 +337,7 @@ static TexDesc tex_desc(mlv_texture2d t) {
 // entries a list overflow needed, [4] clip-fan slots a record overflow needed
 static mlv_status reset_error_words(Workspace &w) {
     const uint32_t init[8] = {0, 0xFFFFFFFFu, 0, 0, 0, 0, 0, 0};
-    CUDA_TRY(cudaMemcpy(w.error, init, sizeof(init), cudaMemcpyHostToDevice));
+    CUDA_TRY(copy_to_device_now(w.error, init, sizeof(init)));
     return MLV_OK;
 }
 
@@ -325,8 +347,8 @@ static mlv_status ensure_fixed(mlv_context_t *c) {
         MLV_TRY(dev_alloc((void **)&w.counters, sizeof(uint32_t) * kCtrCount));
         MLV_TRY(dev_alloc((void **)&w.stats, sizeof(unsigned long long) * kStatCount));
         MLV_TRY(dev_alloc((void **)&w.error, sizeof(uint32_t) * 8));
-        CUDA_TRY(cudaMemset(w.counters, 0, sizeof(uint32_t) * kCtrCount));
-        CUDA_TRY(cudaMemset(w.stats, 0, sizeof(unsigned long long) * kStatCount));
+        CUDA_TRY(zero_now(w.counters, sizeof(uint32_t) * kCtrCount));
+        CUDA_TRY(zero_now(w.stats, sizeof(unsigned long long) * kStatCount));
         MLV_TRY(reset_error_words(w));
         CUDA_TRY(cudaMallocHost((void **)&c->h_error, sizeof(uint32_t) * 32));
         memset(c->h_error, 0, sizeof(uint32_t) * 32);
@@ -343,9 +365,9 @@ struct BatchSizes {
 
 static mlv_status reset_scan_state(Workspace &w) {
     // fresh look-back state: every status word "not ready" in epoch 0, counters at epoch 0
-    CUDA_TRY(cudaMemset(w.scan_status, 0, sizeof(unsigned long long) * w.status_cap));
-    CUDA_TRY(cudaMemset(w.scan_status2, 0, sizeof(unsigned long long) * w.status2_cap));
-    CUDA_TRY(cudaMemset(w.counters, 0, sizeof(uint32_t) * kCtrCount));
+    CUDA_TRY(zero_now(w.scan_status, sizeof(unsigned long long) * w.status_cap));
+    CUDA_TRY(zero_now(w.scan_status2, sizeof(unsigned long long) * w.status2_cap));
+    CUDA_TRY(zero_now(w.counters, sizeof(uint32_t) * kCtrCount));
     return MLV_OK;
 }
 
@@ -897,7 +919,7 @@ static mlv_status check_and_recover(mlv_context_t *c, bool fetched = false, bool
         if (c->h_error[2]) {
             // out-of-range indices read zeros, as Direct3D 11 does; report once
             uint32_t z = 0;
-            CUDA_TRY(cudaMemcpy(c->ws.error + 2, &z, 4, cudaMemcpyHostToDevice));
+            CUDA_TRY(copy_to_device_now(c->ws.error + 2, &z, 4));
             g_last_error = "a draw read vertices outside its vertex buffer (zeros were used)";
         }
         if (err == 0) {
@@ -906,8 +928,8 @@ static mlv_status check_and_recover(mlv_context_t *c, bool fetched = false, bool
         }
         if (err & kErrLookbackTimeout) {
             MLV_TRY(reset_error_words(c->ws));
-            CUDA_TRY(cudaMemset(c->ws.bin_count, 0, sizeof(uint32_t) * c->ws.bin_cap));
-            if (c->ws.keys) CUDA_TRY(cudaMemset(c->ws.keys, 0, sizeof(unsigned long long) * c->ws.keys_cap));
+            CUDA_TRY(zero_now(c->ws.bin_count, sizeof(uint32_t) * c->ws.bin_cap));
+            if (c->ws.keys) CUDA_TRY(zero_now(c->ws.keys, sizeof(unsigned long long) * c->ws.keys_cap));
             MLV_TRY(reset_scan_state(c->ws));
             c->pending.clear();
             return fail(MLV_ERROR_TIMEOUT, "a bounded device-side wait gave up (decoupled look-back)");
@@ -941,9 +963,9 @@ static mlv_status check_and_recover(mlv_context_t *c, bool fetched = false, bool
         }
         // reset the device state the skipped kernels left behind (and the failed batches' staged
         // statistics, which the re-run stages again)
-        CUDA_TRY(cudaMemset(w.stats, 0, sizeof(unsigned long long) * kStatTotal));
-        CUDA_TRY(cudaMemset(w.bin_count, 0, sizeof(uint32_t) * w.bin_cap));
-        if (w.keys) CUDA_TRY(cudaMemset(w.keys, 0, sizeof(unsigned long long) * w.keys_cap));
+        CUDA_TRY(zero_now(w.stats, sizeof(unsigned long long) * kStatTotal));
+        CUDA_TRY(zero_now(w.bin_count, sizeof(uint32_t) * w.bin_cap));
+        if (w.keys) CUDA_TRY(zero_now(w.keys, sizeof(unsigned long long) * w.keys_cap));
         MLV_TRY(reset_scan_state(w));
         MLV_TRY(reset_error_words(w));
         // Jobs before the first failing batch completed; from it on every kernel that writes a
@@ -1124,7 +1146,7 @@ MLV_API mlv_status mlv_create_buffer(mlv_device d, const mlv_buffer_desc *desc, 
     }
     if (desc->bind_flags & MLV_BIND_CONSTANT_BUFFER) b->shadow.assign(desc->byte_width, 0);
     if (init) {
-        cudaError_t e = cudaMemcpy(b->ptr, init, desc->byte_width, cudaMemcpyHostToDevice);
+        cudaError_t e = copy_to_device_now(b->ptr, init, desc->byte_width);
         if (e != cudaSuccess) {
             cudaFree(b->ptr);
             delete b;
@@ -1199,9 +1221,9 @@ static mlv_status create_texture2d(mlv_device d, const mlv_texture2d_desc *desc,
             delete t;
             return st;
         }
-        cudaMemset(t->tile_min, 0, nt * 4);
+        zero_now(t->tile_min, nt * 4);
         std::vector<float> ones(nt, 1.0f);
-        cudaMemcpy(t->tile_max, ones.data(), nt * 4, cudaMemcpyHostToDevice);
+        copy_to_device_now(t->tile_max, ones.data(), nt * 4);
     }
     if (init) {
         size_t row = (size_t)desc->width * tb;
@@ -1215,7 +1237,7 @@ static mlv_status create_texture2d(mlv_device d, const mlv_texture2d_desc *desc,
             return fail(MLV_ERROR_DEVICE, cudaGetErrorString(e));
         }
     } else if (!placed) {
-        cudaMemset(t->ptr, 0, bytes);
+        zero_now(t->ptr, bytes);
     }
     *out = t;
     return MLV_OK;
@@ -1273,7 +1295,7 @@ MLV_API mlv_status mlv_update_buffer(mlv_context c, mlv_buffer b, uint64_t offse
     if (offset > b->size || size > b->size - offset) return fail(MLV_ERROR_INVALID_ARG, "update outside the buffer");
     MLV_TRY(set_device(c->device));
     MLV_TRY(sync_context(c));   // queued draws may still read the old contents
-    CUDA_TRY(cudaMemcpy(b->ptr + offset, data, size, cudaMemcpyHostToDevice));
+    CUDA_TRY(copy_to_device_now(b->ptr + offset, data, size));
     if (!b->shadow.empty()) memcpy(b->shadow.data() + offset, data, size);
     return MLV_OK;
 }
@@ -1812,77 +1834,111 @@ static mlv_status plan_list(mlv_context_t *c, mlv_command_list l, std::vector<Pl
     return MLV_OK;
 }
 
-// Sizes the workspace for the list as the context's tuning plans it. Run before a graph capture:
-// the captured kernels keep the workspace's pointers, and a tuning change can move the list to
-// another path with buffers of its own (the small-draw path's keys, the binned path's job list).
+// Sizes the workspace for the list as the context's tuning plans it, and uploads its descriptors
+// if they were planned otherwise. Run before a graph capture: the captured kernels keep the
+// workspace's pointers, and a tuning change can move the list to another path with buffers and
+// descriptors of its own (the small-draw path's keys, the binned path's job list; whether the
+// vertices are shaded once or per index).
+static mlv_status upload_list(mlv_context_t *c, mlv_command_list l, const std::vector<Plan> &plans,
+                              const std::vector<std::vector<FillJob>> &fills, size_t nd, size_t nv);
+static bool list_descriptors_current(const mlv_context_t *c, mlv_command_list l);
+static void build_list_fills(mlv_command_list l, const std::vector<Plan> &plans,
+                             std::vector<std::vector<FillJob>> &fills, std::vector<uint32_t> &chunks);
+
 static mlv_status size_list(mlv_context_t *c, mlv_command_list l) {
     std::vector<Plan> plans;
     BatchSizes maxs;
     size_t nd = 0, nv = 0;
     MLV_TRY(plan_list(c, l, plans, maxs, nd, nv));
-    return ensure_workspace(c, maxs, false);
+    MLV_TRY(ensure_workspace(c, maxs, false));
+    // the descriptors too: planned for another tuning, they may describe the other path
+    if (!list_descriptors_current(c, l)) {
+        std::vector<std::vector<FillJob>> fills;
+        std::vector<uint32_t> chunks;
+        build_list_fills(l, plans, fills, chunks);
+        MLV_TRY(upload_list(c, l, plans, fills, nd, nv));
+    }
+    return MLV_OK;
 }
 
 // Builds the list's device descriptors, sizes the workspace for its largest segment and
 // records all of its kernels on the context stream (eagerly, or into a graph being captured,
 // after size_list).
+// Uploads the list's fill jobs and draw and view descriptors as planned (before any capture: the
+// copies are synchronous).
+static mlv_status upload_list(mlv_context_t *c, mlv_command_list l, const std::vector<Plan> &plans,
+                              const std::vector<std::vector<FillJob>> &fills, size_t nd, size_t nv) {
+    size_t nf = 0;
+    for (auto &f : fills) nf += f.size();
+    if (nf > l->fills_total || !l->d_fills) {
+        cudaFree(l->d_fills);
+        l->d_fills = nullptr;
+        MLV_TRY(dev_alloc((void **)&l->d_fills, std::max<size_t>(nf, 1) * sizeof(FillJob)));
+        l->fills_total = nf;
+    }
+    l->fill_off.clear();
+    size_t of = 0;
+    for (auto &f : fills) {
+        l->fill_off.push_back(of);
+        if (!f.empty()) CUDA_TRY(copy_to_device_now(l->d_fills + of, f.data(), sizeof(FillJob) * f.size()));
+        of += f.size();
+    }
+    if (nd > l->draws_total || !l->d_draws) {
+        cudaFree(l->d_draws);
+        l->d_draws = nullptr;
+        MLV_TRY(dev_alloc((void **)&l->d_draws, std::max<size_t>(nd, 1) * sizeof(DrawDesc)));
+        l->draws_total = nd;
+    }
+    if (nv > l->views_total || !l->d_views) {
+        cudaFree(l->d_views);
+        l->d_views = nullptr;
+        MLV_TRY(dev_alloc((void **)&l->d_views, std::max<size_t>(nv, 1) * sizeof(ViewDesc)));
+        l->views_total = nv;
+    }
+    l->draw_off.clear();
+    l->view_off.clear();
+    size_t od = 0, ov = 0;
+    for (auto &p : plans) {
+        l->draw_off.push_back(od);
+        l->view_off.push_back(ov);
+        if (!p.draws.empty())
+            CUDA_TRY(copy_to_device_now(l->d_draws + od, p.draws.data(), sizeof(DrawDesc) * p.draws.size()));
+        if (!p.views.empty())
+            CUDA_TRY(copy_to_device_now(l->d_views + ov, p.views.data(), sizeof(ViewDesc) * p.views.size()));
+        od += p.draws.size();
+        ov += p.views.size();
+    }
+    l->desc_tuning = c->tuning_generation;
+    l->desc_context = c;
+    l->desc_capture = c->capture_infos;
+    return MLV_OK;
+}
+
+// Whether the list's uploaded descriptors were planned with the context's current tuning.
+static bool list_descriptors_current(const mlv_context_t *c, mlv_command_list l) {
+    return l->d_draws && l->d_fills && l->desc_tuning == c->tuning_generation && l->desc_context == c &&
+           l->desc_capture == c->capture_infos;
+}
+
+static void build_list_fills(mlv_command_list l, const std::vector<Plan> &plans,
+                             std::vector<std::vector<FillJob>> &fills, std::vector<uint32_t> &chunks) {
+    fills.assign(l->segments.size(), {});
+    chunks.assign(l->segments.size(), 0);
+    for (size_t i = 0; i < l->segments.size(); ++i) chunks[i] = build_fills(l->segments[i], fills[i], &plans[i].folded);
+}
+
 static mlv_status run_list(mlv_context_t *c, mlv_command_list l, uint32_t seq, bool upload) {
     std::vector<Plan> plans;
     BatchSizes maxs;
     size_t nd = 0, nv = 0;
     MLV_TRY(plan_list(c, l, plans, maxs, nd, nv));
     if (!c->capturing_graph) MLV_TRY(ensure_workspace(c, maxs, false));
-    std::vector<std::vector<FillJob>> fills(l->segments.size());
-    std::vector<uint32_t> fill_chunks(l->segments.size());
-    size_t nf = 0;
-    for (size_t i = 0; i < l->segments.size(); ++i) {
-        fill_chunks[i] = build_fills(l->segments[i], fills[i], &plans[i].folded);
-        nf += fills[i].size();
-    }
-    if (upload || !l->d_fills) {
-        if (nf > l->fills_total || !l->d_fills) {
-            cudaFree(l->d_fills);
-            l->d_fills = nullptr;
-            MLV_TRY(dev_alloc((void **)&l->d_fills, std::max<size_t>(nf, 1) * sizeof(FillJob)));
-            l->fills_total = nf;
-        }
-        l->fill_off.clear();
-        size_t of = 0;
-        for (auto &f : fills) {
-            l->fill_off.push_back(of);
-            if (!f.empty())
-                CUDA_TRY(cudaMemcpy(l->d_fills + of, f.data(), sizeof(FillJob) * f.size(), cudaMemcpyHostToDevice));
-            of += f.size();
-        }
-    }
-    if (upload || !l->d_draws) {
-        if (nd > l->draws_total || !l->d_draws) {
-            cudaFree(l->d_draws);
-            l->d_draws = nullptr;
-            MLV_TRY(dev_alloc((void **)&l->d_draws, std::max<size_t>(nd, 1) * sizeof(DrawDesc)));
-            l->draws_total = nd;
-        }
-        if (nv > l->views_total || !l->d_views) {
-            cudaFree(l->d_views);
-            l->d_views = nullptr;
-            MLV_TRY(dev_alloc((void **)&l->d_views, std::max<size_t>(nv, 1) * sizeof(ViewDesc)));
-            l->views_total = nv;
-        }
-        l->draw_off.clear();
-        l->view_off.clear();
-        size_t od = 0, ov = 0;
-        for (auto &p : plans) {
-            l->draw_off.push_back(od);
-            l->view_off.push_back(ov);
-            if (!p.draws.empty())
-                CUDA_TRY(cudaMemcpy(l->d_draws + od, p.draws.data(), sizeof(DrawDesc) * p.draws.size(),
-                                    cudaMemcpyHostToDevice));
-            if (!p.views.empty())
-                CUDA_TRY(cudaMemcpy(l->d_views + ov, p.views.data(), sizeof(ViewDesc) * p.views.size(),
-                                    cudaMemcpyHostToDevice));
-            od += p.draws.size();
-            ov += p.views.size();
-        }
+    std::vector<std::vector<FillJob>> fills;
+    std::vector<uint32_t> fill_chunks;
+    build_list_fills(l, plans, fills, fill_chunks);
+    if (upload || !list_descriptors_current(c, l)) {
+        if (c->capturing_graph) return fail(MLV_ERROR_INVALID_STATE, "command list descriptors not uploaded before a capture");
+        MLV_TRY(upload_list(c, l, plans, fills, nd, nv));
     }
     for (size_t i = 0; i < l->segments.size(); ++i) {
         MLV_TRY(run_fills(c, fills[i], fill_chunks[i], l->d_fills + l->fill_off[i]));
@@ -1978,7 +2034,7 @@ MLV_API mlv_status mlv_reset_stats(mlv_context c) {
     MLV_TRY(set_device(c->device));
     MLV_TRY(sync_context(c));
     MLV_TRY(ensure_fixed(c));
-    CUDA_TRY(cudaMemset(c->ws.stats, 0, sizeof(unsigned long long) * kStatCount));
+    CUDA_TRY(zero_now(c->ws.stats, sizeof(unsigned long long) * kStatCount));
     memset(c->host_stats, 0, sizeof(c->host_stats));
     memset(c->stage_ms, 0, sizeof(c->stage_ms));
     memset(c->stage_launches, 0, sizeof(c->stage_launches));
