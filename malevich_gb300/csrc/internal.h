@@ -154,7 +154,8 @@ struct BatchParams {
     uint32_t batch_seq;
     uint32_t total_vertices;             // sum of vs_count
     uint32_t want_rank;                  // 1: compute assembled-triangle ranks (visibility, capture)
-    float4 *vs_out;                      // 3 float4 per shaded vertex: SV_POSITION, reg1, (reg2.x, 0, 0, 0)
+    float4 *vs_out;                      // [total_vertices] SV_POSITION, then [total_vertices][2] attributes:
+                                         // reg1, (reg2.x, 0, 0, 0)
     TriRaster *raster;                   // [total_tris + overflow_capacity]
     TriShade *shade;
     TriGeom *geom;                       // nullptr unless the geometry is kept

@@ -442,15 +442,14 @@ __global__ void __launch_bounds__(kVertexBlock) k_vertex(BatchParams bp) {
     }
     float o[9];
     run_vs(d.vs, in, d.cb, d.vs_tex, o);
-    if (d.ps == kPsNone) {
-        // a null pixel shader reads no attributes: positions only, packed densely at the start of
-        // the draw's range (a third of the bytes, and neighbours share cache sectors)
-        bp.vs_out[3 * (size_t)d.vs_base + local] = make_float4(o[0], o[1], o[2], o[3]);
-    } else {
-        float4 *out = bp.vs_out + 3 * (size_t)v;
-        out[0] = make_float4(o[0], o[1], o[2], o[3]);
-        out[1] = make_float4(o[4], o[5], o[6], o[7]);
-        out[2] = make_float4(o[8], 0.0f, 0.0f, 0.0f);
+    // positions densely first (the gathers of the clip tests and setup read nothing else, and
+    // neighbouring vertices share cache sectors), the attributes after all positions; a null pixel
+    // shader reads no attributes
+    bp.vs_out[v] = make_float4(o[0], o[1], o[2], o[3]);
+    if (d.ps != kPsNone) {
+        float4 *attr = bp.vs_out + bp.total_vertices + 2 * (size_t)v;
+        attr[0] = make_float4(o[4], o[5], o[6], o[7]);
+        attr[1] = make_float4(o[8], 0.0f, 0.0f, 0.0f);
     }
     pdl_trigger();
 }
@@ -462,15 +461,15 @@ __device__ __forceinline__ void triangle_vertex(const BatchParams &bp, const Dra
         int64_t idx = d.ib ? (int64_t)__ldg(d.ib + idx_pos) : (int64_t)idx_pos;
         idx += d.base_vertex;
         if (idx >= 0 && idx < (int64_t)d.vertex_count) {
+            const size_t slot = (size_t)d.vs_base + (size_t)idx;
+            const float4 a = __ldg(bp.vs_out + slot);
+            o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
             if (d.ps == kPsNone) {   // positions only (see k_vertex)
-                const float4 a = __ldg(bp.vs_out + 3 * (size_t)d.vs_base + (size_t)idx);
-                o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
                 o[4] = o[5] = o[6] = o[7] = o[8] = 0.0f;
                 return;
             }
-            const float4 *src = bp.vs_out + 3 * ((size_t)d.vs_base + (size_t)idx);
-            const float4 a = __ldg(src), b = __ldg(src + 1), c = __ldg(src + 2);
-            o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+            const float4 *attr = bp.vs_out + bp.total_vertices + 2 * slot;
+            const float4 b = __ldg(attr), c = __ldg(attr + 1);
             o[4] = b.x; o[5] = b.y; o[6] = b.z; o[7] = b.w; o[8] = c.x;
             return;
         }
@@ -493,7 +492,7 @@ __device__ __forceinline__ uint32_t triangle_position(const BatchParams &bp, con
         idx += d.base_vertex;
         if (idx >= 0 && idx < (int64_t)d.vertex_count) {
             const uint32_t slot = d.vs_base + (uint32_t)idx;
-            const float4 a = __ldg(bp.vs_out + 3 * (size_t)slot);
+            const float4 a = __ldg(bp.vs_out + slot);
             o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
             return slot;
         }
@@ -504,8 +503,8 @@ __device__ __forceinline__ uint32_t triangle_position(const BatchParams &bp, con
 
 __device__ __forceinline__ void triangle_attributes(const BatchParams &bp, uint32_t slot, float *o) {
     if (slot == kNoSlot) return;
-    const float4 *src = bp.vs_out + 3 * (size_t)slot;
-    const float4 b = __ldg(src + 1), c = __ldg(src + 2);
+    const float4 *attr = bp.vs_out + bp.total_vertices + 2 * (size_t)slot;
+    const float4 b = __ldg(attr), c = __ldg(attr + 1);
     o[4] = b.x; o[5] = b.y; o[6] = b.z; o[7] = b.w; o[8] = c.x;
 }
 
