@@ -1962,11 +1962,52 @@ __global__ void __launch_bounds__(kDirectBlock) k_direct_raster(BatchParams bp) 
     __syncthreads();
     const uint32_t cta_draw = s_draw;
     // vertex shader, one invocation per (triangle, vertex), per index as the reference shades
-    for (uint32_t i = threadIdx.x; i < 3u * NT; i += kDirectBlock) {
-        const uint32_t t = i / 3, k = i - 3 * t, g = g0 + t;
-        if (g < bp.total_tris) {
-            const DrawDesc &d = bp.draws[cta_draw != kNoDraw ? cta_draw : find_draw(bp, g)];
-            triangle_vertex(bp, d, d.start_index + 3 * (g - d.tri_begin) + k, s_v[t][k].v);
+    if (cta_draw != kNoDraw && !bp.draws[cta_draw].vs_cached) {
+        // the CTA's triangles share a draw: a thread's invocations load all their indices, then
+        // all their vertices, then shade, so that its loads are in flight together
+        constexpr int kPer = (3 * NT + kDirectBlock - 1) / kDirectBlock;
+        const DrawDesc &d = bp.draws[cta_draw];
+        int64_t idx[kPer];
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+            const uint32_t i = threadIdx.x + (uint32_t)j * kDirectBlock, t = i / 3, g = g0 + t;
+            idx[j] = -1;
+            if (i < 3u * NT && g < bp.total_tris) {
+                const uint32_t at = d.start_index + 3 * (g - d.tri_begin) + (i - 3 * t);
+                idx[j] = (d.ib ? (int64_t)__ldg(d.ib + at) : (int64_t)at) + d.base_vertex;
+            }
+        }
+        float in[kPer][8];
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+#pragma unroll
+            for (int c = 0; c < 8; ++c) in[j][c] = 0.0f;   // D3D11: out-of-range vertex fetch reads zeros
+            if (idx[j] >= 0 && idx[j] < (int64_t)d.vertex_count) {
+                const uint8_t *p = d.vb + (size_t)idx[j] * d.vb_stride;
+                if ((((uintptr_t)p) & 15) == 0) {
+                    const float4 a = __ldg((const float4 *)p), b = __ldg((const float4 *)p + 1);
+                    in[j][0] = a.x; in[j][1] = a.y; in[j][2] = a.z; in[j][3] = a.w;
+                    in[j][4] = b.x; in[j][5] = b.y; in[j][6] = b.z; in[j][7] = b.w;
+                } else {
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) in[j][c] = __ldg((const float *)p + c);
+                }
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+            const uint32_t i = threadIdx.x + (uint32_t)j * kDirectBlock, t = i / 3, g = g0 + t;
+            if (i >= 3u * NT || g >= bp.total_tris) continue;
+            if (idx[j] < 0 || idx[j] >= (int64_t)d.vertex_count) atomicOr(bp.error + 2, kErrBadIndex);
+            run_vs(d.vs, in[j], d.cb, d.vs_tex, s_v[t][i - 3 * t].v);
+        }
+    } else {
+        for (uint32_t i = threadIdx.x; i < 3u * NT; i += kDirectBlock) {
+            const uint32_t t = i / 3, k = i - 3 * t, g = g0 + t;
+            if (g < bp.total_tris) {
+                const DrawDesc &d = bp.draws[cta_draw != kNoDraw ? cta_draw : find_draw(bp, g)];
+                triangle_vertex(bp, d, d.start_index + 3 * (g - d.tri_begin) + k, s_v[t][k].v);
+            }
         }
     }
     __syncthreads();
