@@ -1951,12 +1951,15 @@ __global__ void __launch_bounds__(kDirectBlock) k_direct_raster(BatchParams bp) 
     __shared__ uint4 s_mark[kDirectListCap];           // bin rectangles to mark: first bin, nx, ny, row stride
     __shared__ uint32_t s_npush, s_nmark;
     __shared__ uint32_t s_draw;
+    __shared__ uint32_t s_clip[NT], s_nclip;          // the CTA's triangles that need clipping
+    __shared__ Vtx s_poly[kDirectWarps][2][kMaxClipVertices];
     pdl_wait();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t g0 = blockIdx.x * NT;
     if (threadIdx.x == 0) {
         s_npush = 0;
         s_nmark = 0;
+        s_nclip = 0;
         s_draw = common_draw(bp, g0, min(g0 + NT, bp.total_tris) - 1);
     }
     __syncthreads();
@@ -2083,30 +2086,7 @@ __global__ void __launch_bounds__(kDirectBlock) k_direct_raster(BatchParams bp) 
                         emit(su, s_v[t][0], s_v[t][1], s_v[t][2], g, g << 3, true);
                     }
                 } else {
-                    Vtx poly[kMaxClipVertices], tmp[kMaxClipVertices];
-                    poly[0] = s_v[t][0]; poly[1] = s_v[t][1]; poly[2] = s_v[t][2];
-                    int count = 3;
-                    for (int p = 0; p < 6; ++p) clip_by_plane(poly, tmp, count, c_clip_planes[p]);
-                    const int nf = count - 2;
-                    if (nf > 0) {
-                        const uint32_t base = atomicAdd(bp.counters + kCtrOverflow, (uint32_t)nf);
-                        if (base + (uint32_t)nf > bp.overflow_capacity) {
-                            atomicOr(bp.error, kErrRecordOverflow);
-                            atomicMin(bp.error + 1, bp.batch_seq);
-                            atomicMax(bp.error + 4, base + (uint32_t)nf);
-                        } else {
-                            for (int f = 0; f < nf && f < 7; ++f) {
-                                Setup su;
-                                if (setup_triangle(d, poly[0], poly[f + 1], poly[f + 2], su)) {
-                                    mask |= 1u << f;
-                                    emit(su, poly[0], poly[f + 1], poly[f + 2], bp.total_tris + base + (uint32_t)f,
-                                         (g << 3) | (uint32_t)(f + 1), false);
-                                }
-                            }
-                            // slot g holds the fans' base, by which record_of finds them from a key
-                            bp.raster[g].w[0] = make_int4((int)base, 0, 0, 0);
-                        }
-                    }
+                    s_clip[atomicAdd(&s_nclip, 1u)] = t;   // clipped below by a whole warp
                 }
             }
         }
@@ -2118,6 +2098,71 @@ __global__ void __launch_bounds__(kDirectBlock) k_direct_raster(BatchParams bp) 
         if (lane == 0 && entries) atomicAdd(bp.stats + kStatBinEntries, (unsigned long long)entries);
     }
     __syncthreads();
+    const uint32_t nclip = s_nclip;
+    if (nclip) {   // uniform over the CTA
+        // the triangles that need clipping, one warp each (main.c:649-661, then 662-913): the warp
+        // clips (clip_by_plane_warp), lane f sets up fan f, records it and queues it
+        for (uint32_t q = (uint32_t)warp; q < nclip; q += kDirectWarps) {
+            const uint32_t t = s_clip[q], g = g0 + t;
+            const DrawDesc &d = bp.draws[cta_draw != kNoDraw ? cta_draw : find_draw(bp, g)];
+            const ViewDesc &V = bp.views[d.view];
+            Vtx *poly = s_poly[warp][0], *other = s_poly[warp][1];
+            if (lane < 3) poly[lane] = s_v[t][lane];
+            __syncwarp();
+            int count = 3;
+            for (int p = 0; p < 6; ++p)
+                if (clip_by_plane_warp(poly, other, count, c_clip_planes[p], lane)) {
+                    Vtx *tp = poly;
+                    poly = other;
+                    other = tp;
+                }
+            const int nf = count - 2;
+            if (nf <= 0) continue;
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(bp.counters + kCtrOverflow, (uint32_t)nf);
+            base = __shfl_sync(0xFFFFFFFFu, base, 0);
+            if (base + (uint32_t)nf > bp.overflow_capacity) {
+                if (lane == 0) {
+                    atomicOr(bp.error, kErrRecordOverflow);
+                    atomicMin(bp.error + 1, bp.batch_seq);
+                    atomicMax(bp.error + 4, base + (uint32_t)nf);
+                }
+                continue;
+            }
+            bool ok = false;
+            uint32_t entries = 0;
+            if (lane < min(nf, 7)) {
+                Setup su;
+                ok = setup_triangle(d, poly[0], poly[lane + 1], poly[lane + 2], su);
+                int32_t tx0, ty0, tx1, ty1;
+                if (ok) tile_range(V, su.minx, su.miny, su.maxx, su.maxy, tx0, ty0, tx1, ty1);
+                if (ok && tx1 >= tx0 && ty1 >= ty0) {
+                    const uint32_t rec = bp.total_tris + base + (uint32_t)lane, key = (g << 3) | (uint32_t)(lane + 1);
+                    const uint32_t nx = (uint32_t)(tx1 - tx0 + 1), ny = (uint32_t)(ty1 - ty0 + 1);
+                    const uint32_t first = V.bin_base + (uint32_t)ty0 * V.tiles_x + (uint32_t)tx0;
+                    entries = nx * ny;
+                    for (uint32_t u = 0; u < nx * ny; ++u) bp.bin_count[first + (u / nx) * V.tiles_x + u % nx] = 1u;
+                    if (su.tminx <= su.tmaxx && su.tminy <= su.tmaxy) {   // covers some sample
+                        int4 R[4];
+                        raster_words(su, R);
+                        const DirectJob J = direct_job(R[0], R[1], R[2], R[3], key, d);
+                        write_record(bp, rec, 0, d.ps, true, su, poly[0], poly[lane + 1], poly[lane + 2]);
+                        direct_push(bp, key, rec, J.ntx * J.nty, 0, 1);
+                    }
+                }
+            }
+            const uint32_t fans = __ballot_sync(0xFFFFFFFFu, ok);
+            entries = __reduce_add_sync(0xFFFFFFFFu, entries);
+            if (lane == 0) {
+                // slot g holds the fans' base, by which record_of finds them from a key
+                bp.raster[g].w[0] = make_int4((int)base, 0, 0, 0);
+                if (fans) atomicAdd(bp.stats + kStatAssembled, (unsigned long long)__popc(fans));   // main.c:1238
+                if (entries) atomicAdd(bp.stats + kStatBinEntries, (unsigned long long)entries);
+            }
+            __syncwarp();
+        }
+        __syncthreads();
+    }
     // queued jobs, each pushed by a whole warp; the binned tiles of the larger rectangles, by the CTA
     const uint32_t np = min(s_npush, (uint32_t)kDirectListCap);
     for (uint32_t i = (uint32_t)warp; i < np; i += kDirectWarps) {
