@@ -291,45 +291,13 @@ __device__ __forceinline__ void write_record(const BatchParams &bp, uint32_t rec
     h[4] = make_float4(v0.v[8], v1.v[8], v2.v[8], __uint_as_float(extra));
 }
 
-// clip_by_plane, main.c:609-647 (Sutherland-Hodgman on one normalised plane, plane_d = 0), on
-// poly (count vertices), with tmp as scratch. A polygon with every vertex inside (distance > -0)
-// comes out of the reference's pass unchanged, vertex for vertex and in order, so that pass is
-// skipped: most planes of a clipped triangle then cost its distances only, not two copies of it.
-__device__ void clip_by_plane(Vtx *poly, Vtx *tmp, int &count, const float *n) {
-    const int nv = count;
-    if (nv <= 0) return;
-    bool all_in = true;
-    for (int i = 0; i < nv; ++i) all_in = all_in && dot4_lr(n, poly[i].v[0], poly[i].v[1], poly[i].v[2], poly[i].v[3]) > -0.0f;
-    if (all_in) return;
-    int out = 0;
-    float cd = dot4_lr(n, poly[0].v[0], poly[0].v[1], poly[0].v[2], poly[0].v[3]);
-    bool cin = cd > -0.0f;
-    for (int i = 0; i < nv; ++i) {
-        const int next = i + 1 == nv ? 0 : i + 1;
-        if (cin && out < kMaxClipVertices) tmp[out++] = poly[i];
-        const Vtx &pn = poly[next];
-        float nd = dot4_lr(n, pn.v[0], pn.v[1], pn.v[2], pn.v[3]);
-        bool nin = nd > -0.0f;
-        if (cin != nin && out < kMaxClipVertices) {
-            float t = (0.0f + cd) / (cd - nd);
-            float omt = 1.f - t;
-#pragma unroll
-            for (int c = 0; c < 9; ++c) tmp[out].v[c] = poly[i].v[c] * omt + pn.v[c] * t;
-            ++out;
-        }
-        cd = nd;
-        cin = nin;
-    }
-    count = out;
-    for (int i = 0; i < out; ++i) poly[i] = tmp[i];
-}
-
-// The same pass run by a whole warp on a polygon in shared memory (poly: count vertices, at most
-// kMaxClipVertices), into out. Lane i takes vertex i and the edge from it to the next: the same
-// distances, t and interpolations as the serial pass, written where the serial pass would put them
-// (an exclusive scan of the lanes' emission counts); emissions past kMaxClipVertices are dropped,
-// as the serial pass drops them. Returns false, out untouched, when every vertex is inside (the
-// pass would give the polygon back unchanged). Every lane calls it with the same count and plane.
+// clip_by_plane, main.c:609-647 (Sutherland-Hodgman on one normalised plane, plane_d = 0), run by a
+// whole warp on a polygon in shared memory (poly: count vertices, at most kMaxClipVertices), into
+// out. Lane i takes vertex i and the edge from it to the next: the reference's distance, t and
+// lerps, each output written where the reference's serial loop puts it (an exclusive warp scan of
+// the lanes' emission counts); outputs past kMaxClipVertices are dropped. Returns false, out
+// untouched, when every vertex is inside (distance > -0): the reference's pass then gives the
+// polygon back unchanged. Every lane calls it with the same count and plane.
 __device__ bool clip_by_plane_warp(const Vtx *poly, Vtx *out, int &count, const float *n, int lane) {
     const int nv = count;
     if (nv <= 0) return false;
