@@ -17,7 +17,8 @@ with CUDA events on the context's stream, flushing L2 between timed runs, and le
 setting on the context. It first picks the path: the small-draw path (no binning, for batches of
 one draw per view) or the binned one (`small_draw_triangles` 0); when the small-draw path wins for
 a batch that takes it, the binned path's launch shapes have no effect and are not swept. Otherwise
-it sweeps every point of the launch-shape space.
+it sweeps every point of the launch-shape space. A batch the small-draw path cannot take (views
+of several draws) leaves the context's path setting as it was.
 """
 import itertools
 
@@ -112,12 +113,17 @@ def autotune(device, renderer, space=None, time_fn=None, repeats=5, warmup=2, ch
                 ctx.set_tuning(small_draw_triangles=sd)
                 launches.append(launches_per_batch(ctx, renderer))
                 path.append(({"small_draw_triangles": sd}, float(time_fn(renderer.render_batched))))
-            fixed, path_ms = pick(path)
-            ctx.set_tuning(**fixed)
-            # the small-draw path runs 3 kernels a batch where the binned one runs 4 or more (and the
-            # same clears): fewer launches with it allowed means the batch takes it
+            # the small-draw path runs 3 kernels a batch where the binned one runs 6 (and the same
+            # clears): fewer launches with it allowed means the batch takes it. Where it does not,
+            # the two settings run the same kernels, and the context keeps its own setting (which
+            # decides the path of other batches, such as single draws, that were not timed)
             small = None not in launches and launches[1] < launches[0]
-            if fixed["small_draw_triangles"] and small:
+            if small:
+                fixed, path_ms = pick(path)
+            else:
+                fixed = {"small_draw_triangles": base["small_draw_triangles"]}
+            ctx.set_tuning(**fixed)
+            if small and fixed["small_draw_triangles"]:
                 return {"best": dict(fixed), "ms": path_ms, "results": [], "path": path}
         for point in candidates(space):
             ctx.set_tuning(**dict(point, **fixed))

@@ -52,9 +52,10 @@ def test_autotune_sets_the_fastest_point():
     cost = lambda: dev.immediate.t["tile_warps_per_block"] * 10 + abs(dev.immediate.t["geometry_block"] - 128) + \
         dev.immediate.t["big_triangle_tiles"] * 0.1
     out = autotune.autotune(dev, _FakeRenderer(), time_fn=lambda fn: (fn(), cost())[1])
-    # the path choice ties (the cost ignores it): the binned path, first in order, then the sweep
+    # a context without launch statistics cannot tell whether the small-draw path applies: its
+    # path setting stays, and the sweep runs
     assert out["best"] == {"big_triangle_tiles": 4, "geometry_block": 128, "tile_warps_per_block": 2,
-                           "warps_per_tile": 1, "small_draw_triangles": 0}
+                           "warps_per_tile": 1, "small_draw_triangles": 0xFFFFFFFF}
     assert dev.immediate.t == out["best"]
     assert len(out["results"]) == 72 and len(out["path"]) == 2
 
@@ -139,6 +140,22 @@ def test_autotune_picks_a_path_for_a_single_draw_and_keeps_the_output(device):
     finally:
         r.destroy()
         ctx.set_tuning(**base)
+
+
+def test_autotune_keeps_the_path_setting_when_the_small_draw_path_does_not_apply():
+    class _Ctx(_FakeCtx):
+        def reset_stats(self):
+            pass
+
+        def stats(self):
+            return {"batch_count": 1, "kernel_launches": 6}   # the same kernels either way
+
+    dev = _FakeDevice()
+    dev.immediate = _Ctx()
+    cost = lambda: 1.0 if not dev.immediate.t.get("small_draw_triangles") else 2.0   # noise favouring 0
+    out = autotune.autotune(dev, _FakeRenderer(), space={"geometry_block": (128, 256)},
+                            time_fn=lambda fn: (fn(), cost())[1])
+    assert dev.immediate.t["small_draw_triangles"] == 0xFFFFFFFF and len(out["results"]) == 2
 
 
 @pytest.mark.gpu

@@ -95,6 +95,22 @@ int main(int argc, char **argv) {
     CHECK(mlv_create_texture2d(dev, &td, NULL, 0, &rt));
     td.format = MLV_FORMAT_D32_FLOAT; td.bind_flags = MLV_BIND_DEPTH_STENCIL;
     CHECK(mlv_create_texture2d(dev, &td, NULL, 0, &ds));
+    {
+        /* the same inputs once more as one grouped upload (no reference counterpart): one block,
+           the index buffer at a 16-byte aligned offset; the image must not change */
+        const uint64_t vb_bytes = (uint64_t)head[2] * 32, ib_at = (vb_bytes + 15) / 16 * 16;
+        const uint64_t ib_bytes = (uint64_t)head[3] * 4;
+        unsigned char *block = (unsigned char *)calloc(1, (size_t)(ib_at + ib_bytes));
+        mlv_upload ups[2];
+        memcpy(block, vb, (size_t)vb_bytes);
+        memcpy(block + ib_at, ib, (size_t)ib_bytes);
+        memset(ups, 0, sizeof(ups));
+        ups[0].kind = MLV_UPLOAD_BUFFER; ups[0].resource = vbuf; ups[0].src_offset = 0; ups[0].size = vb_bytes;
+        ups[1].kind = MLV_UPLOAD_BUFFER; ups[1].resource = ibuf; ups[1].src_offset = ib_at; ups[1].size = ib_bytes;
+        CHECK(mlv_update_resources_async(ctx, block, ib_at + ib_bytes, ups, 2));
+        CHECK(mlv_finish(ctx));
+        free(block);
+    }
 
     /* render(): clear, viewport, targets, shaders, buffers, draw_indexed (main.c:1268-1296) */
     CHECK(mlv_reset_stats(ctx));
