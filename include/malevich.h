@@ -27,7 +27,7 @@ extern "C" {
 #define MLV_API
 #endif
 
-#define MLV_ABI_VERSION 4
+#define MLV_ABI_VERSION 5
 
 /* ------------------------------------------------------------------ status */
 
@@ -374,6 +374,12 @@ typedef struct mlv_tuning {
      * as the reference does. Same outputs; 0 disables it. */
     uint32_t small_draw_triangles;
     uint32_t debug_flags;             /* MLV_DEBUG_*: failure-detection tests only; 0 in normal use */
+    /* 1: a batch on the binned path runs as one persistent launch instead of a kernel per stage
+     * (vertex shading, geometry, clipping, bin scan, scatter, tiles): a grid of as many CTAs as the
+     * GPU holds at once, with a grid-wide barrier between the stages. Same outputs. It uses 8 warps
+     * (tiles) per CTA, or one tile per CTA shared by 8 warps when warps_per_tile > 1;
+     * tile_warps_per_block and geometry_block do not apply. The stage timers count it as stage 4. */
+    uint32_t persistent_launch;
 } mlv_tuning;
 
 /* The bin scan's first block never publishes its prefix, so the bounded waits of the blocks after
@@ -381,6 +387,10 @@ typedef struct mlv_tuning {
  * after which the context works again. Takes effect on batches with more than 16,384 bins that
  * use the binned path (a 1920x1080 target, for instance). */
 #define MLV_DEBUG_STALL_LOOKBACK 0x1u
+/* Persistent launch: its first CTA leaves before the first grid barrier, so the bounded waits of
+ * all the others run out (shortened under this flag to milliseconds): the batch writes nothing and
+ * the next synchronisation returns MLV_ERROR_TIMEOUT, after which the context works again. */
+#define MLV_DEBUG_STALL_GRID 0x2u
 
 MLV_API mlv_status mlv_get_tuning(mlv_context context, mlv_tuning *out_tuning);
 MLV_API mlv_status mlv_set_tuning(mlv_context context, const mlv_tuning *tuning);

@@ -99,10 +99,12 @@ class Tuning(ctypes.Structure):
     _fields_ = [("tile_warps_per_block", ctypes.c_uint32), ("warps_per_tile", ctypes.c_uint32),
                 ("big_triangle_tiles", ctypes.c_uint32), ("geometry_block", ctypes.c_uint32),
                 ("initial_bin_entries", ctypes.c_uint32), ("initial_clip_fan_slots", ctypes.c_uint32),
-                ("small_draw_triangles", ctypes.c_uint32), ("debug_flags", ctypes.c_uint32)]
+                ("small_draw_triangles", ctypes.c_uint32), ("debug_flags", ctypes.c_uint32),
+                ("persistent_launch", ctypes.c_uint32)]
 
 
 DEBUG_STALL_LOOKBACK = 0x1
+DEBUG_STALL_GRID = 0x2
 
 
 _lib = None

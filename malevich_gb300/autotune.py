@@ -8,7 +8,9 @@ warps share one tile's triangles (for frames whose triangles crowd into few tile
 kernel's CTA size (how
 many input triangles one CTA sets up and bins), and the threshold above which a triangle's bins
 are counted and scattered cooperatively by a whole warp instead of by its own thread
-(triangles-per-warp against warps-per-triangle). The hierarchical-Z tile and the bins stay 8x8
+(triangles-per-warp against warps-per-triangle), and whether the binned pipeline runs as a kernel
+per stage or as one persistent launch (a grid of resident CTAs with grid-wide barriers between the
+stages). The hierarchical-Z tile and the bins stay 8x8
 pixels: the tile grid is observable through the reference's per-tile depth bounds
 (main.c:1005-1010), so it is not tuned.
 
@@ -27,21 +29,40 @@ SPACE = {
     "warps_per_tile": (1, 2, 4, 8),
     "geometry_block": (128, 256, 512),
     "big_triangle_tiles": (4, 8, 16, 32),
+    "persistent_launch": (0, 1),
 }
+
+# The persistent launch's fixed shapes: 8 warps a CTA (8 tiles, or one tile shared by all 8 when
+# warps_per_tile > 1) and 256 triangles a geometry block.
+PERSISTENT_SHAPE = {"tile_warps_per_block": 8, "geometry_block": 256}
+
+
+def _one_value(space, key, prefer):
+    vals = space[key]
+    return prefer if prefer in vals else vals[0]
 
 
 def candidates(space=None):
     """Every point of the search space as a dict, in a fixed order. With several warps per tile
     the tile kernel runs one tile per CTA and tile_warps_per_block has no effect, so those points
-    are kept for one value of it only (4 when the space has it, else its first)."""
+    are kept for one value of it only (4 when the space has it, else its first). The persistent
+    launch has fixed shapes (PERSISTENT_SHAPE; any warps_per_tile above 1 shares a tile among all 8
+    warps), so its points are kept for those values, and for warps_per_tile 1 and its largest."""
     space = SPACE if space is None else space
     keys = sorted(space)
     points = [dict(zip(keys, vals)) for vals in itertools.product(*(space[k] for k in keys))]
-    if "warps_per_tile" in space and "tile_warps_per_block" in space:
-        tw = space["tile_warps_per_block"]
-        keep = 4 if 4 in tw else tw[0]
-        points = [p for p in points if p["warps_per_tile"] == 1 or p["tile_warps_per_block"] == keep]
-    return points
+
+    def keep(p):
+        if p.get("persistent_launch"):
+            for k, v in PERSISTENT_SHAPE.items():
+                if k in space and p[k] != _one_value(space, k, v):
+                    return False
+            return "warps_per_tile" not in p or p["warps_per_tile"] in (1, max(space["warps_per_tile"]))
+        if "warps_per_tile" in space and "tile_warps_per_block" in space:
+            return p["warps_per_tile"] == 1 or p["tile_warps_per_block"] == _one_value(space, "tile_warps_per_block", 4)
+        return True
+
+    return [p for p in points if keep(p)]
 
 
 def pick(results):
@@ -109,8 +130,11 @@ def autotune(device, renderer, space=None, time_fn=None, repeats=5, warmup=2, ch
         fixed = {}
         if choose_path:
             launches = []
+            # the binned path as a kernel per stage while the path is chosen (its launch count
+            # tells the paths apart)
+            chained = {"persistent_launch": 0} if "persistent_launch" in base else {}
             for sd in PATHS:
-                ctx.set_tuning(small_draw_triangles=sd)
+                ctx.set_tuning(small_draw_triangles=sd, **chained)
                 launches.append(launches_per_batch(ctx, renderer))
                 path.append(({"small_draw_triangles": sd}, float(time_fn(renderer.render_batched))))
             # the small-draw path runs 3 kernels a batch where the binned one runs 6 (and the same
@@ -122,9 +146,11 @@ def autotune(device, renderer, space=None, time_fn=None, repeats=5, warmup=2, ch
                 fixed, path_ms = pick(path)
             else:
                 fixed = {"small_draw_triangles": base["small_draw_triangles"]}
-            ctx.set_tuning(**fixed)
             if small and fixed["small_draw_triangles"]:
+                restore = {k: base[k] for k in chained}   # other batches keep the context's form
+                ctx.set_tuning(**fixed, **restore)
                 return {"best": dict(fixed), "ms": path_ms, "results": [], "path": path}
+            ctx.set_tuning(**fixed)
         for point in candidates(space):
             ctx.set_tuning(**dict(point, **fixed))
             results.append((dict(point, **fixed), float(time_fn(renderer.render_batched))))

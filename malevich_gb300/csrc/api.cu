@@ -39,6 +39,7 @@ cudaError_t launch_scan(const BatchParams &bp, cudaStream_t stream);
 cudaError_t launch_rank(const BatchParams &bp, cudaStream_t stream);
 cudaError_t launch_scatter(const BatchParams &bp, int num_sms, cudaStream_t stream);
 cudaError_t launch_tile(const BatchParams &bp, uint32_t warps, uint32_t warps_per_tile, cudaStream_t stream);
+cudaError_t launch_persistent(const BatchParams &bp, uint32_t warps_per_tile, int num_sms, cudaStream_t stream);
 cudaError_t launch_direct_raster(const BatchParams &bp, int num_sms, cudaStream_t stream);
 cudaError_t launch_direct_queue(const BatchParams &bp, int num_sms, cudaStream_t stream);
 cudaError_t launch_direct_resolve(const BatchParams &bp, cudaStream_t stream);
@@ -244,7 +245,7 @@ struct mlv_context_t {
     PipelineState st;
     std::vector<Segment> recorded;     // deferred contexts
     Workspace ws;
-    mlv_tuning tuning = {4, 1, 16, 128, 0, 0, kDefaultSmallDraw, 0};   // measured defaults; the autotuner refines them
+    mlv_tuning tuning = {4, 1, 16, 128, 0, 0, kDefaultSmallDraw, 0, 0};   // measured defaults; the autotuner refines them
     uint64_t tuning_generation = 0;    // bumped by mlv_set_tuning: captured graphs re-capture
     uint64_t host_stats[8] = {};       // vertex_count, input triangles, draws, batches, launches
     bool profiling = false;
@@ -814,7 +815,7 @@ static mlv_status launch_draws(mlv_context_t *c, const Plan &p, DrawDesc *d_draw
     cudaEvent_t e;
     // the clip-fan slot counter starts at zero for every batch (reset before the first kernel, so
     // that the batch's kernels follow one another directly)
-    CUDA_TRY(cudaMemsetAsync(w.counters + kCtrOverflow, 0, 4 * sizeof(uint32_t), c->stream));
+    CUDA_TRY(cudaMemsetAsync(w.counters + kCtrOverflow, 0, kCtrPerBatch * sizeof(uint32_t), c->stream));
     if (p.direct) {
         // the small-draw path: raster (vertex shader, setup, small triangles), queued large
         // triangles, resolve; stages 1, 3 and 4 of the stage timers
@@ -831,6 +832,18 @@ static mlv_status launch_draws(mlv_context_t *c, const Plan &p, DrawDesc *d_draw
         CUDA_TRY(launch_direct_resolve(bp, c->stream));
         ev_end(c, e);
         c->host_stats[4] += 3;
+        return MLV_OK;
+    }
+    if (c->tuning.persistent_launch) {
+        // the binned pipeline as one persistent launch (k_batch), timed as the tile stage; it
+        // reads every input, so it waits for all of the batch's queued uploads
+        CUDA_TRY(wait_for(p.wait_vertex));
+        CUDA_TRY(wait_for(p.wait_index));
+        CUDA_TRY(wait_for(p.wait_pixel));
+        ev_begin(c, 4, &e);
+        CUDA_TRY(launch_persistent(bp, c->tuning.warps_per_tile, c->device->num_sms, c->stream));
+        ev_end(c, e);
+        c->host_stats[4] += 1;
         return MLV_OK;
     }
     CUDA_TRY(wait_for(p.wait_vertex));
@@ -926,13 +939,15 @@ static mlv_status check_and_recover(mlv_context_t *c, bool fetched = false, bool
             c->pending.clear();
             return MLV_OK;
         }
-        if (err & kErrLookbackTimeout) {
+        if (err & (kErrLookbackTimeout | kErrGridTimeout)) {
             MLV_TRY(reset_error_words(c->ws));
             CUDA_TRY(zero_now(c->ws.bin_count, sizeof(uint32_t) * c->ws.bin_cap));
             if (c->ws.keys) CUDA_TRY(zero_now(c->ws.keys, sizeof(unsigned long long) * c->ws.keys_cap));
             MLV_TRY(reset_scan_state(c->ws));
             c->pending.clear();
-            return fail(MLV_ERROR_TIMEOUT, "a bounded device-side wait gave up (decoupled look-back)");
+            return fail(MLV_ERROR_TIMEOUT, (err & kErrGridTimeout)
+                                               ? "a bounded device-side wait gave up (persistent launch grid barrier)"
+                                               : "a bounded device-side wait gave up (decoupled look-back)");
         }
         // regrow: records from the device's assembled count, list from the reported entry count
         const uint32_t need_list = c->h_error[3];
@@ -2056,7 +2071,9 @@ MLV_API mlv_status mlv_set_tuning(mlv_context c, const mlv_tuning *t) {
     if (t->geometry_block != 128 && t->geometry_block != 256 && t->geometry_block != 512)
         return fail(MLV_ERROR_INVALID_ARG, "geometry_block must be 128, 256 or 512");
     if (t->big_triangle_tiles < 1) return fail(MLV_ERROR_INVALID_ARG, "big_triangle_tiles must be >= 1");
-    if (t->debug_flags & ~(uint32_t)MLV_DEBUG_STALL_LOOKBACK) return fail(MLV_ERROR_INVALID_ARG, "unknown debug flag");
+    if (t->persistent_launch > 1) return fail(MLV_ERROR_INVALID_ARG, "persistent_launch must be 0 or 1");
+    if (t->debug_flags & ~(uint32_t)(MLV_DEBUG_STALL_LOOKBACK | MLV_DEBUG_STALL_GRID))
+        return fail(MLV_ERROR_INVALID_ARG, "unknown debug flag");
     if (memcmp(&c->tuning, t, sizeof(*t)) != 0) ++c->tuning_generation;
     c->tuning = *t;
     return MLV_OK;

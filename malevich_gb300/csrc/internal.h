@@ -27,10 +27,12 @@ enum : uint32_t {
     kErrBigOverflow = 1u << 3,
     kErrBadIndex = 1u << 4,
     kErrQueueOverflow = 1u << 5,         // small-draw path: more large-triangle chunks than the queue holds
+    kErrGridTimeout = 1u << 6,           // persistent launch: a grid barrier's bounded wait gave up
 };
 
 // Debug flags (mlv_tuning::debug_flags, MLV_DEBUG_*), for failure-detection tests only.
 constexpr uint32_t kDebugStallLookback = 1u;
+constexpr uint32_t kDebugStallGrid = 2u;     // persistent launch: CTA 0 leaves before the first grid barrier
 
 struct TexDesc {
     const void *data;
@@ -187,12 +189,16 @@ struct BatchParams {
 
 enum Counter : int {
     kCtrRankTicket = 0, kCtrRankDone, kCtrRankEpoch,
-    kCtrOverflow, kCtrQueue, kCtrClip, kCtrJobs,   // per batch: clip-fan slots used; small-draw queue
-                                         // entries used; triangles listed for clipping (clip_list);
-                                         // bin jobs listed (jobs)
+    kCtrOverflow, kCtrQueue, kCtrClip, kCtrJobs, kCtrGrid, kCtrClaimGeometry, kCtrClaimTiles,
+                                         // per batch (zeroed before each): clip-fan slots used;
+                                         // small-draw queue entries used; triangles listed for
+                                         // clipping (clip_list); bin jobs listed (jobs); arrivals at
+                                         // the persistent launch's grid barriers; its geometry and
+                                         // tile blocks claimed
     kCtrScanTicket, kCtrScanDone, kCtrScanEpoch,
     kCtrCount = 16
 };
+constexpr int kCtrPerBatch = kCtrClaimTiles - kCtrOverflow + 1;
 
 
 // Statistics are staged per batch (slots kStat*) and added to the totals (kStat* + kStatTotal)

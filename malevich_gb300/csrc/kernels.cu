@@ -56,6 +56,24 @@ __device__ __forceinline__ uint32_t ld_volatile_u32(const uint32_t *p) {
     return *(const volatile uint32_t *)p;
 }
 
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t *p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// A load of what an earlier stage of the same batch wrote (shaded vertices, clip-fan bases, bin
+// starts). The separate kernels read it through the read-only path: its writer was an earlier
+// kernel. In the persistent launch (k_batch) the writer is the same kernel, and the read-only path
+// is only for data that no thread writes while the kernel runs, so its copies of the stage bodies
+// (COHERENT) use an ordinary load with the cache-all-levels hint, which the grid barrier's fences
+// make see the other CTAs' writes.
+template <bool COHERENT, typename T>
+__device__ __forceinline__ T ld_stage(const T *p) {
+    if constexpr (COHERENT) return __ldca(p);
+    else return __ldg(p);
+}
+
 // Programmatic dependent launch: the pipeline's kernels are launched so that the next one may be
 // scheduled while the previous one finishes. Each waits for its predecessor's completion (and the
 // visibility of its writes) before touching any of its outputs, and lets its dependents launch
@@ -393,9 +411,9 @@ __device__ __forceinline__ uint32_t find_vertex_draw(const BatchParams &bp, uint
     return lo;
 }
 
-__global__ void __launch_bounds__(kVertexBlock) k_vertex(BatchParams bp) {
-    pdl_wait();
-    const uint32_t v = blockIdx.x * kVertexBlock + threadIdx.x;
+// The vertex shading of block blk (kVertexBlock vertices); k_vertex and the persistent launch run it.
+__device__ __forceinline__ void vertex_body(const BatchParams &bp, uint32_t blk) {
+    const uint32_t v = blk * kVertexBlock + threadIdx.x;
     if (v >= bp.total_vertices) return;
     const DrawDesc &d = bp.draws[find_vertex_draw(bp, v)];
     const uint32_t local = v - d.vs_base;
@@ -419,25 +437,31 @@ __global__ void __launch_bounds__(kVertexBlock) k_vertex(BatchParams bp) {
         attr[0] = make_float4(o[4], o[5], o[6], o[7]);
         attr[1] = make_float4(o[8], 0.0f, 0.0f, 0.0f);
     }
+}
+
+__global__ void __launch_bounds__(kVertexBlock) k_vertex(BatchParams bp) {
+    pdl_wait();
+    vertex_body(bp, blockIdx.x);
     pdl_trigger();
 }
 
 // Vertex k of a triangle: from the shaded-vertex buffer, or shaded here (per-index path, and for
 // out-of-range indices, which read zeros as in Direct3D 11).
+template <bool COHERENT = false>
 __device__ __forceinline__ void triangle_vertex(const BatchParams &bp, const DrawDesc &d, uint32_t idx_pos, float *o) {
     if (d.vs_cached) {
         int64_t idx = d.ib ? (int64_t)__ldg(d.ib + idx_pos) : (int64_t)idx_pos;
         idx += d.base_vertex;
         if (idx >= 0 && idx < (int64_t)d.vertex_count) {
             const size_t slot = (size_t)d.vs_base + (size_t)idx;
-            const float4 a = __ldg(bp.vs_out + slot);
+            const float4 a = ld_stage<COHERENT>(bp.vs_out + slot);
             o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
             if (d.ps == kPsNone) {   // positions only (see k_vertex)
                 o[4] = o[5] = o[6] = o[7] = o[8] = 0.0f;
                 return;
             }
             const float4 *attr = bp.vs_out + bp.total_vertices + 2 * slot;
-            const float4 b = __ldg(attr), c = __ldg(attr + 1);
+            const float4 b = ld_stage<COHERENT>(attr), c = ld_stage<COHERENT>(attr + 1);
             o[4] = b.x; o[5] = b.y; o[6] = b.z; o[7] = b.w; o[8] = c.x;
             return;
         }
@@ -453,6 +477,7 @@ __device__ __forceinline__ void triangle_vertex(const BatchParams &bp, const Dra
 // the whole vertex (shaded here, or a null pixel shader, which reads no attributes).
 constexpr uint32_t kNoSlot = 0xFFFFFFFFu;
 
+template <bool COHERENT = false>
 __device__ __forceinline__ uint32_t triangle_position(const BatchParams &bp, const DrawDesc &d, uint32_t idx_pos,
                                                       float *o) {
     if (d.vs_cached && d.ps != kPsNone) {
@@ -460,27 +485,29 @@ __device__ __forceinline__ uint32_t triangle_position(const BatchParams &bp, con
         idx += d.base_vertex;
         if (idx >= 0 && idx < (int64_t)d.vertex_count) {
             const uint32_t slot = d.vs_base + (uint32_t)idx;
-            const float4 a = __ldg(bp.vs_out + slot);
+            const float4 a = ld_stage<COHERENT>(bp.vs_out + slot);
             o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
             return slot;
         }
     }
-    triangle_vertex(bp, d, idx_pos, o);
+    triangle_vertex<COHERENT>(bp, d, idx_pos, o);
     return kNoSlot;
 }
 
+template <bool COHERENT = false>
 __device__ __forceinline__ void triangle_attributes(const BatchParams &bp, uint32_t slot, float *o) {
     if (slot == kNoSlot) return;
     const float4 *attr = bp.vs_out + bp.total_vertices + 2 * (size_t)slot;
-    const float4 b = __ldg(attr), c = __ldg(attr + 1);
+    const float4 b = ld_stage<COHERENT>(attr), c = ld_stage<COHERENT>(attr + 1);
     o[4] = b.x; o[5] = b.y; o[6] = b.z; o[7] = b.w; o[8] = c.x;
 }
 
 // Slot of the record a triangle key names (see BatchParams).
+template <bool COHERENT = false>
 __device__ __forceinline__ uint32_t record_of(const BatchParams &bp, uint32_t key) {
     const uint32_t g = key >> 3, c = key & 7u;
     if (c == 0) return g;
-    return bp.total_tris + (uint32_t)__ldg(&bp.raster[g].w[0].x) + (c - 1);
+    return bp.total_tris + (uint32_t)ld_stage<COHERENT>(&bp.raster[g].w[0].x) + (c - 1);
 }
 
 // The tiles (bins) of one emitted triangle from its clamped pixel bounds: the binner's tile range
@@ -526,11 +553,11 @@ __device__ __forceinline__ void push_jobs(const BatchParams &bp, bool has, const
 #define MLV_GEOMETRY_THREADS_PER_SM 1024
 #endif
 
-template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK, MLV_GEOMETRY_THREADS_PER_SM / BLOCK) k_geometry(BatchParams bp) {
-    pdl_wait();
+// Input triangle g of each lane (32 consecutive ones), by one whole warp; k_geometry and the
+// persistent launch run it.
+template <bool COHERENT = false>
+__device__ __forceinline__ void geometry_warp(const BatchParams &bp, uint32_t g) {
     const int lane = threadIdx.x & 31;
-    const uint32_t g = blockIdx.x * BLOCK + threadIdx.x;
     uint32_t draw = 0, view = 0;
     bool clipped = false;       // left to k_clip
     uint32_t mask = 0;
@@ -547,7 +574,7 @@ __global__ void __launch_bounds__(BLOCK, MLV_GEOMETRY_THREADS_PER_SM / BLOCK) k_
         Vtx v[3];
         uint32_t slot[3];
 #pragma unroll
-        for (int k = 0; k < 3; ++k) slot[k] = triangle_position(bp, d, d.start_index + 3 * local + k, v[k].v);
+        for (int k = 0; k < 3; ++k) slot[k] = triangle_position<COHERENT>(bp, d, d.start_index + 3 * local + k, v[k].v);
         const float *p0 = v[0].v, *p1 = v[1].v, *p2 = v[2].v;
         // main.c:759-781
         bool reject = p0[3] == 0 || p1[3] == 0 || p2[3] == 0;
@@ -575,7 +602,7 @@ __global__ void __launch_bounds__(BLOCK, MLV_GEOMETRY_THREADS_PER_SM / BLOCK) k_
                     mask = 1;
                     if (!ghost) {
 #pragma unroll
-                        for (int k = 0; k < 3; ++k) triangle_attributes(bp, slot[k], v[k].v);
+                        for (int k = 0; k < 3; ++k) triangle_attributes<COHERENT>(bp, slot[k], v[k].v);
                         write_record(bp, g, draw, d.ps, !(d.raster_flags & kDrawSharesView), su, v[0], v[1], v[2]);
                         have_own = bin_job(vw, d.draw_in_view, su.minx, su.miny, su.maxx, su.maxy, g << 3, own);
                     } else {
@@ -605,10 +632,7 @@ __global__ void __launch_bounds__(BLOCK, MLV_GEOMETRY_THREADS_PER_SM / BLOCK) k_
         at = __shfl_sync(0xFFFFFFFFu, at, 0);
         if (clipped) bp.clip_list[at + __popc(clip_lanes & ((1u << lane) - 1u))] = make_uint2(g, draw);
     }
-    if (!__any_sync(0xFFFFFFFFu, mask != 0u)) {   // the warp assembled nothing: nothing to count
-        pdl_trigger();
-        return;
-    }
+    if (!__any_sync(0xFFFFFFFFu, mask != 0u)) return;   // the warp assembled nothing: nothing to count
     // assembled-triangle statistic (main.c:1238)
     uint32_t n = __popc(mask);
 #pragma unroll
@@ -645,6 +669,12 @@ __global__ void __launch_bounds__(BLOCK, MLV_GEOMETRY_THREADS_PER_SM / BLOCK) k_
         j.row_stride = __shfl_sync(0xFFFFFFFFu, own.row_stride, src);
         for (uint32_t t = lane; t < j.nx * j.ny; t += 32) atomicAdd(bp.bin_count + job_bin(j, t), 1u);
     }
+}
+
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK, MLV_GEOMETRY_THREADS_PER_SM / BLOCK) k_geometry(BatchParams bp) {
+    pdl_wait();
+    geometry_warp(bp, blockIdx.x * BLOCK + threadIdx.x);
     pdl_trigger();
 }
 
@@ -656,18 +686,24 @@ __global__ void __launch_bounds__(BLOCK, MLV_GEOMETRY_THREADS_PER_SM / BLOCK) k_
 // the clipped triangles' serial work no longer lengthens the warps of k_geometry that hold them.
 constexpr int kClipBlock = 128;
 
-__global__ void __launch_bounds__(kClipBlock) k_clip(BatchParams bp) {
-    __shared__ Vtx s_poly[kClipBlock / 32][2][kMaxClipVertices];
-    pdl_wait();
+template <int WARPS>
+struct ClipSmem {
+    Vtx poly[WARPS][2][kMaxClipVertices];   // each warp's polygon and its clipped copy
+};
+
+// The listed triangles of CTA blk of nblk, a warp per triangle (WARPS warps a CTA); k_clip and the
+// persistent launch run it.
+template <int WARPS, bool COHERENT = false>
+__device__ __forceinline__ void clip_body(const BatchParams &bp, uint32_t blk, uint32_t nblk, ClipSmem<WARPS> &sm) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t n = ld_volatile_u32(bp.counters + kCtrClip);
     uint32_t assembled = 0;
-    for (uint32_t i = blockIdx.x * (kClipBlock / 32) + warp; i < n; i += gridDim.x * (kClipBlock / 32)) {
+    for (uint32_t i = blk * WARPS + warp; i < n; i += nblk * WARPS) {
         const uint2 entry = bp.clip_list[i];
         const uint32_t g = entry.x, draw = entry.y;
         const DrawDesc &d = bp.draws[draw];
-        Vtx *poly = s_poly[warp][0], *other = s_poly[warp][1];
-        if (lane < 3) triangle_vertex(bp, d, d.start_index + 3 * (g - d.tri_begin) + (uint32_t)lane, poly[lane].v);
+        Vtx *poly = sm.poly[warp][0], *other = sm.poly[warp][1];
+        if (lane < 3) triangle_vertex<COHERENT>(bp, d, d.start_index + 3 * (g - d.tri_begin) + (uint32_t)lane, poly[lane].v);
         __syncwarp();
         int count = 3;
         for (int p = 0; p < 6; ++p)
@@ -729,6 +765,12 @@ __global__ void __launch_bounds__(kClipBlock) k_clip(BatchParams bp) {
         __syncwarp();
     }
     if (lane == 0 && assembled) atomicAdd(bp.stats + kStatAssembled, (unsigned long long)assembled);   // main.c:1238
+}
+
+__global__ void __launch_bounds__(kClipBlock) k_clip(BatchParams bp) {
+    __shared__ ClipSmem<kClipBlock / 32> sm;
+    pdl_wait();
+    clip_body<kClipBlock / 32>(bp, blockIdx.x, gridDim.x, sm);
     pdl_trigger();
 }
 
@@ -736,14 +778,27 @@ __global__ void __launch_bounds__(kClipBlock) k_clip(BatchParams bp) {
 
 constexpr int kRankBlock = 256, kRankItems = 8;
 
+// Shared state of one block of a decoupled look-back scan (k_rank, k_scan).
+struct ScanSmem {
+    uint32_t bid, epoch, prefix;
+    uint32_t warp[8];
+};
+
+// The scans' block order: a separate kernel takes it from a ticket, in the order its blocks start,
+// so that a block only ever waits on blocks that already run. The persistent launch gives block
+// b = CTA + k * CTAs to its CTAs in increasing k: all of them are resident and each finishes its
+// blocks in order, so every block a block waits on is done or running.
+constexpr uint32_t kTicket = 0xFFFFFFFFu;
+
 // rank[g] = number of triangles input triangles 0..g-1 of the batch assembled (exclusive scan of
-// the popcount of tri_info's fan masks), same decoupled look-back as k_scan.
-__global__ void __launch_bounds__(kRankBlock) k_rank(BatchParams bp) {
-    __shared__ uint32_t s_bid, s_epoch, s_prefix;
-    __shared__ uint32_t s_warp[kRankBlock / 32];
-    pdl_wait();
+// the popcount of tri_info's fan masks), same decoupled look-back as k_scan. Block `block` of
+// nblk (kTicket: from the ticket counter).
+__device__ __forceinline__ void rank_body(const BatchParams &bp, uint32_t block, uint32_t nblk, ScanSmem &sm) {
+    uint32_t &s_bid = sm.bid, &s_epoch = sm.epoch, &s_prefix = sm.prefix;
+    uint32_t *s_warp = sm.warp;
+    static_assert(kRankBlock / 32 <= 8, "ScanSmem::warp");
     if (threadIdx.x == 0) {
-        s_bid = atomicAdd(bp.counters + kCtrRankTicket, 1u);
+        s_bid = block == kTicket ? atomicAdd(bp.counters + kCtrRankTicket, 1u) : block;
         s_epoch = ld_volatile_u32(bp.counters + kCtrRankEpoch);
     }
     __syncthreads();
@@ -775,13 +830,19 @@ __global__ void __launch_bounds__(kRankBlock) k_rank(BatchParams bp) {
     if (threadIdx.x == 0) {
         __threadfence();
         uint32_t done = atomicAdd(bp.counters + kCtrRankDone, 1u);
-        if (done == gridDim.x - 1) {
+        if (done == nblk - 1) {
             bp.counters[kCtrRankTicket] = 0;
             bp.counters[kCtrRankDone] = 0;
             bp.counters[kCtrRankEpoch] = s_epoch + 1;
             __threadfence();
         }
     }
+}
+
+__global__ void __launch_bounds__(kRankBlock) k_rank(BatchParams bp) {
+    __shared__ ScanSmem sm;
+    pdl_wait();
+    rank_body(bp, kTicket, gridDim.x, sm);
     pdl_trigger();
 }
 
@@ -789,13 +850,13 @@ __global__ void __launch_bounds__(kRankBlock) k_rank(BatchParams bp) {
 
 constexpr int kScanBlock = 256, kScanItems = 16;   // 4096 bins per block, read as 4 x uint4 per thread
 
-__global__ void __launch_bounds__(kScanBlock) k_scan(BatchParams bp) {
-    __shared__ uint32_t s_bid, s_epoch, s_prefix;
-    __shared__ uint32_t s_warp[kScanBlock / 32];
-    pdl_wait();
-    if (ld_volatile_u32(bp.error)) return;   // uniform: set only by earlier kernels
+// Block `block` of nblk of the bin scan (kTicket: from the ticket counter).
+__device__ __forceinline__ void scan_body(const BatchParams &bp, uint32_t block, uint32_t nblk, ScanSmem &sm) {
+    uint32_t &s_bid = sm.bid, &s_epoch = sm.epoch, &s_prefix = sm.prefix;
+    uint32_t *s_warp = sm.warp;
+    static_assert(kScanBlock / 32 <= 8, "ScanSmem::warp");
     if (threadIdx.x == 0) {
-        s_bid = atomicAdd(bp.counters + kCtrScanTicket, 1u);
+        s_bid = block == kTicket ? atomicAdd(bp.counters + kCtrScanTicket, 1u) : block;
         s_epoch = ld_volatile_u32(bp.counters + kCtrScanEpoch);
     }
     __syncthreads();
@@ -861,19 +922,26 @@ __global__ void __launch_bounds__(kScanBlock) k_scan(BatchParams bp) {
     for (int o = 16; o > 0; o >>= 1) active += __shfl_xor_sync(0xFFFFFFFFu, active, o);
     if ((threadIdx.x & 31) == 0 && active) atomicAdd(bp.stats + kStatActiveBins, (unsigned long long)active);
     if (threadIdx.x == 0) {
-        if (bid == gridDim.x - 1) {
+        if (bid == nblk - 1) {
             bp.bin_start[n] = s_prefix + total;
             atomicAdd(bp.stats + kStatBinEntries, (unsigned long long)(s_prefix + total));
         }
         __threadfence();
         uint32_t done = atomicAdd(bp.counters + kCtrScanDone, 1u);
-        if (done == gridDim.x - 1) {
+        if (done == nblk - 1) {
             bp.counters[kCtrScanTicket] = 0;
             bp.counters[kCtrScanDone] = 0;
             bp.counters[kCtrScanEpoch] = s_epoch + 1;
             __threadfence();
         }
     }
+}
+
+__global__ void __launch_bounds__(kScanBlock) k_scan(BatchParams bp) {
+    __shared__ ScanSmem sm;
+    pdl_wait();
+    if (ld_volatile_u32(bp.error)) return;   // uniform: set only by earlier kernels
+    scan_body(bp, kTicket, gridDim.x, sm);
     pdl_trigger();
 }
 
@@ -948,13 +1016,14 @@ constexpr int kScatterBlock = 256;
 // Puts key[k] into bin[k] for the k (of 4) whose bit is set in m: the list positions (atomics on
 // the bin counters) and the bins' starts are all requested before any is used, so one thread's
 // fills take one round trip instead of one each.
+template <bool COHERENT = false>
 __device__ __forceinline__ void put4(const BatchParams &bp, const uint32_t *bin, const uint32_t *key, uint32_t m) {
     uint32_t pos[4], st[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k)
         if (m >> k & 1u) {
             pos[k] = atomicSub(bp.bin_count + bin[k], 1u) - 1u;
-            st[k] = __ldg(bp.bin_start + bin[k]);
+            st[k] = ld_stage<COHERENT>(bp.bin_start + bin[k]);
         }
 #pragma unroll
     for (int k = 0; k < 4; ++k)
@@ -962,6 +1031,7 @@ __device__ __forceinline__ void put4(const BatchParams &bp, const uint32_t *bin,
 }
 
 // The bins t, t + step, ... (below nt) of one job, four at a time.
+template <bool COHERENT = false>
 __device__ __forceinline__ void put_job(const BatchParams &bp, const BinJob &j, uint32_t t, uint32_t step) {
     const uint32_t nt = j.nx * j.ny;
     const uint32_t key[4] = {j.key, j.key, j.key, j.key};
@@ -969,7 +1039,7 @@ __device__ __forceinline__ void put_job(const BatchParams &bp, const BinJob &j, 
         uint32_t bin[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) bin[k] = job_bin(j, min(t + (uint32_t)k * step, nt - 1));
-        put4(bp, bin, key, (1u << min(4u, (nt - t + step - 1) / step)) - 1u);
+        put4<COHERENT>(bp, bin, key, (1u << min(4u, (nt - t + step - 1) / step)) - 1u);
     }
 }
 
@@ -978,14 +1048,21 @@ __device__ __forceinline__ void put_job(const BatchParams &bp, const BinJob &j, 
 // goes to the list of every bin of its range (the order inside a bin does not matter, see k_tile).
 // One-tile jobs of a warp that share a bin take their list positions with one atomic; jobs over
 // more than big_tiles bins are filled by the whole warp.
-__global__ void __launch_bounds__(kScatterBlock) k_scatter(BatchParams bp) {
-    __shared__ BinJob s_big[kScatterBlock / 32][32];      // the warp's jobs over many bins
-    __shared__ uint32_t s_bigpref[kScatterBlock / 32][32]; // inclusive prefix of their bin counts
-    pdl_wait();
-    if (ld_volatile_u32(bp.error)) return;
+struct ScatterSmem {
+    BinJob big[kScatterBlock / 32][32];       // the warp's jobs over many bins
+    uint32_t bigpref[kScatterBlock / 32][32]; // inclusive prefix of their bin counts
+};
+
+// CTA blk of nblk (kScatterBlock threads); k_scatter and the persistent launch run it (which
+// reads the error word at its grid barrier instead, where no CTA can be setting it).
+template <bool CHECK_ERROR = true, bool COHERENT = false>
+__device__ __forceinline__ void scatter_body(const BatchParams &bp, uint32_t blk, uint32_t nblk, ScatterSmem &sm) {
+    auto &s_big = sm.big;
+    auto &s_bigpref = sm.bigpref;
+    if (CHECK_ERROR && ld_volatile_u32(bp.error)) return;
     const uint32_t total = bp.bin_start[bp.total_bins];
     if (total > bp.list_capacity) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (blk == 0 && threadIdx.x == 0) {
             atomicOr(bp.error, kErrListOverflow);
             atomicMin(bp.error + 1, bp.batch_seq);
             atomicMax(bp.error + 3, total);
@@ -994,10 +1071,10 @@ __global__ void __launch_bounds__(kScatterBlock) k_scatter(BatchParams bp) {
     }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t njobs = ld_volatile_u32(bp.counters + kCtrJobs);
-    const uint32_t stride = gridDim.x * kScatterBlock;
-    const uint32_t j_first = blockIdx.x * kScatterBlock + threadIdx.x;
+    const uint32_t stride = nblk * kScatterBlock;
+    const uint32_t j_first = blk * kScatterBlock + threadIdx.x;
     uint4 e_next = j_first < njobs ? bp.jobs[j_first] : make_uint4(0u, 0u, 0u, 0u);
-    for (uint32_t base = blockIdx.x * kScatterBlock; base < njobs; base += stride) {
+    for (uint32_t base = blk * kScatterBlock; base < njobs; base += stride) {
         const uint32_t j = base + threadIdx.x;
         const uint4 e = e_next;
         // the next iteration's job is in flight while this one's bins are filled
@@ -1017,14 +1094,14 @@ __global__ void __launch_bounds__(kScatterBlock) k_scatter(BatchParams bp) {
         const uint32_t peers = __match_any_sync(0xFFFFFFFFu, single);
         if (single != 0xFFFFFFFFu) {
             const int leader = __ffs(peers) - 1;
-            const uint32_t st = __ldg(bp.bin_start + single);
+            const uint32_t st = ld_stage<COHERENT>(bp.bin_start + single);
             uint32_t top = 0;
             if (lane == leader) top = atomicSub(bp.bin_count + single, (uint32_t)__popc(peers));
             top = __shfl_sync(peers, top, leader);
             const uint32_t r = (uint32_t)__popc(peers & ((1u << lane) - 1u));
             bp.list[st + top - 1u - r] = own.key;
         } else if (nt_own > 1 && nt_own <= bp.big_tiles) {
-            put_job(bp, own, 0, 1);
+            put_job<COHERENT>(bp, own, 0, 1);
         }
         // triangles over more than big_tiles bins are filled by the whole warp, 32 (triangle, bin)
         // pairs per round. Each big triangle normally starts a new round (its pair count is padded
@@ -1076,11 +1153,17 @@ __global__ void __launch_bounds__(kScatterBlock) k_scatter(BatchParams bp) {
                         m |= 1u << k;
                     }
                 }
-                put4(bp, bin, key, m);
+                put4<COHERENT>(bp, bin, key, m);
             }
         }
         __syncwarp();
     }
+}
+
+__global__ void __launch_bounds__(kScatterBlock) k_scatter(BatchParams bp) {
+    __shared__ ScatterSmem sm;
+    pdl_wait();
+    scatter_body(bp, blockIdx.x, gridDim.x, sm);
     pdl_trigger();
 }
 
@@ -1168,6 +1251,7 @@ __device__ __forceinline__ unsigned long long better_key(bool less, unsigned lon
 // LESS) on best[pixel], for whole-tile tests the lane's own fa (pixel lane) and fb (pixel lane + 32),
 // which the caller folds into best after the draw. best and depth are the tile's 64 pixels,
 // row-major; stage, pref and mask are the warp's own.
+template <bool COHERENT = false>
 __device__ __forceinline__ void tile_chunk(const BatchParams &bp, uint32_t chunk, uint32_t e, int32_t x0, int32_t y0,
                                            bool less, bool top_left, float hiz, uint32_t *stage, uint32_t *pref,
                                            unsigned long long *mask, unsigned long long *best, const float *depth,
@@ -1176,7 +1260,7 @@ __device__ __forceinline__ void tile_chunk(const BatchParams &bp, uint32_t chunk
     uint32_t cnt = 0;   // work items of this lane's triangle in the tile
     if (i < e) {
         const uint32_t key = bp.list[i];
-        const uint32_t rec = record_of(bp, key);
+        const uint32_t rec = record_of<COHERENT>(bp, key);
         const int4 *R = bp.raster[rec].w;
         const int4 w2 = R[2], w3 = R[3];
         const float zb = __int_as_float(w2.z);
@@ -1323,10 +1407,11 @@ __device__ __forceinline__ void tile_chunk(const BatchParams &bp, uint32_t chunk
 // the reference's quantised barycentrics and perspective correction (main.c:1089-1160), the
 // shader (main.c:1172), packing (main.c:1176-1178), the colour and depth write (main.c:1180-1181)
 // and the visibility outputs.
+template <bool COHERENT = false>
 __device__ __forceinline__ void shade_pixel(const BatchParams &bp, const ViewDesc &V, uint32_t key, int32_t x,
                                             int32_t y) {
     const size_t o = (size_t)y * V.width + x;
-    const uint32_t rec = record_of(bp, key);
+    const uint32_t rec = record_of<COHERENT>(bp, key);
     const int4 *R = bp.raster[rec].w;
     const int4 w0 = R[0], w1 = R[1], w2 = R[2], w3 = R[3];
     // the winner's draw: the view's only one, or the index its shading record keeps
@@ -1378,8 +1463,8 @@ __device__ __forceinline__ void shade_pixel(const BatchParams &bp, const ViewDes
 }
 
 // Commits the batch's staged statistics (k_geometry and k_scan finished before the tile kernel).
-__device__ __forceinline__ void commit_stats(const BatchParams &bp) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+__device__ __forceinline__ void commit_stats(const BatchParams &bp, uint32_t blk) {
+    if (blk == 0 && threadIdx.x == 0) {
         for (int k = 0; k < 3; ++k) {
             bp.stats[kStatTotal + k] += bp.stats[k];
             bp.stats[k] = 0;
@@ -1387,19 +1472,25 @@ __device__ __forceinline__ void commit_stats(const BatchParams &bp) {
     }
 }
 
-// One warp per tile, WARPS tiles per CTA.
 template <int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
-    __shared__ unsigned long long s_best[WARPS][64];
-    __shared__ float s_depth[WARPS][64];
-    __shared__ __align__(16) uint32_t s_stage[WARPS][32 * kStage];
-    __shared__ uint32_t s_pref[WARPS][32];
-    __shared__ unsigned long long s_mask[WARPS][32];
-    pdl_wait();
-    if (ld_volatile_u32(bp.error)) return;
-    commit_stats(bp);
+struct TileSmem {
+    __align__(16) uint32_t stage[WARPS][32 * kStage];
+    unsigned long long best[WARPS][64];
+    float depth[WARPS][64];
+    uint32_t pref[WARPS][32];
+    unsigned long long mask[WARPS][32];
+};
+
+// Tile gtile of the batch by one warp, with the warp's slices of sm; k_tile (WARPS tiles per CTA)
+// and the persistent launch run it.
+template <int WARPS, bool COHERENT = false>
+__device__ __forceinline__ void tile_warp(const BatchParams &bp, uint32_t gtile, TileSmem<WARPS> &sm) {
+    auto &s_best = sm.best;
+    auto &s_depth = sm.depth;
+    auto &s_stage = sm.stage;
+    auto &s_pref = sm.pref;
+    auto &s_mask = sm.mask;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t gtile = blockIdx.x * WARPS + warp;
     if (gtile >= bp.total_tiles) return;
     const uint32_t vi = find_view(bp, gtile);
     const ViewDesc &V = bp.views[vi];
@@ -1408,8 +1499,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
     const uint32_t bin0 = V.bin_base + t * V.draw_count;
     const uint32_t dc = V.draw_count;
     // the bin boundaries of this tile's draws, one per lane (lane d holds bin_start[bin0 + d])
-    const uint32_t my_start = lane <= dc ? __ldg(bp.bin_start + bin0 + lane) : 0u;
-    const uint32_t last = dc < 32 ? __shfl_sync(0xFFFFFFFFu, my_start, dc) : __ldg(bp.bin_start + bin0 + dc);
+    const uint32_t my_start = lane <= dc ? ld_stage<COHERENT>(bp.bin_start + bin0 + lane) : 0u;
+    const uint32_t last = dc < 32 ? __shfl_sync(0xFFFFFFFFu, my_start, dc) : ld_stage<COHERENT>(bp.bin_start + bin0 + dc);
 
     const int32_t x0 = (int32_t)tx * kTile, y0 = (int32_t)ty * kTile;
     // lane owns pixels p0 = lane (rows 0-3) and p1 = lane + 32 (rows 4-7)
@@ -1450,8 +1541,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
             s = __shfl_sync(0xFFFFFFFFu, my_start, dd);
             e = __shfl_sync(0xFFFFFFFFu, my_start, dd + 1);
         } else {
-            s = __ldg(bp.bin_start + bin0 + dd);
-            e = __ldg(bp.bin_start + bin0 + dd + 1);
+            s = ld_stage<COHERENT>(bp.bin_start + bin0 + dd);
+            e = ld_stage<COHERENT>(bp.bin_start + bin0 + dd + 1);
         }
         if (s == e) continue;
         const DrawDesc &D = bp.draws[V.draw_begin + dd];
@@ -1463,7 +1554,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
         const float hiz = less ? hiz_max : hiz_min;
         unsigned long long fa = sentinel, fb = sentinel;
         for (uint32_t chunk = s; chunk < e; chunk += 32)
-            tile_chunk(bp, chunk, e, x0, y0, less, top_left, hiz, s_stage[warp], s_pref[warp], s_mask[warp],
+            tile_chunk<COHERENT>(bp, chunk, e, x0, y0, less, top_left, hiz, s_stage[warp], s_pref[warp], s_mask[warp],
                        s_best[warp], s_depth[warp], capture, lane, fa, fb);
         // fold this draw's winners into the running state; hierarchical Z update (write_tile, main.c:589-603)
         const unsigned long long k0 = better_key(less, s_best[warp][lane], fa);
@@ -1501,7 +1592,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
         }
         const uint32_t wa = __shfl_sync(0xFFFFFFFFu, win0, src), wb = __shfl_sync(0xFFFFFFFFu, win1, src);
         if (q >= n) continue;
-        shade_pixel(bp, V, half ? wb : wa, x0 + (int32_t)(src & 7), y0 + (int32_t)(src >> 3) + (half ? 4 : 0));
+        shade_pixel<COHERENT>(bp, V, half ? wb : wa, x0 + (int32_t)(src & 7), y0 + (int32_t)(src >> 3) + (half ? 4 : 0));
     }
     // pixels no draw wrote still owe their folded clears
     if (V.clear_flags) {
@@ -1512,6 +1603,15 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
         V.tile_min[t] = hiz_min;
         V.tile_max[t] = hiz_max;
     }
+}
+
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
+    __shared__ TileSmem<WARPS> sm;
+    pdl_wait();
+    if (ld_volatile_u32(bp.error)) return;
+    commit_stats(bp, blockIdx.x);
+    tile_warp<WARPS>(bp, blockIdx.x * WARPS + (threadIdx.x >> 5), sm);
     pdl_trigger();
 }
 
@@ -1522,19 +1622,31 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
 // as k_tile: the per-pixel max (min) of (depth, key) does not depend on which warp finds it, and
 // thread t < 64 owns pixel t for the fold, the hierarchical-Z bounds and the pixel shader.
 template <int WARPS>
-__global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_tile_coop(BatchParams bp) {
+struct CoopSmem {
+    __align__(16) uint32_t stage[WARPS][32 * kStage];
+    unsigned long long best[64];
+    float depth[64];
+    float hiz[2];
+    uint32_t pref[WARPS][32];
+    unsigned long long mask[WARPS][32];
+};
+
+// Tile blk, shared by the CTA's WARPS warps; k_tile_coop and the persistent launch run it. Every
+// return and barrier is uniform over the CTA (the error word is read only where no kernel of the
+// batch can still set it: k_tile_coop's start; the persistent launch checks it at its barrier).
+template <int WARPS, bool CHECK_ERROR = true, bool COHERENT = false>
+__device__ __forceinline__ void tile_coop_body(const BatchParams &bp, uint32_t blk, CoopSmem<WARPS> &sm) {
     static_assert(WARPS >= 2, "threads 0-63 own the tile's pixels");
-    __shared__ unsigned long long s_best[64];
-    __shared__ float s_depth[64];
-    __shared__ float s_hiz[2];
-    __shared__ __align__(16) uint32_t s_stage[WARPS][32 * kStage];
-    __shared__ uint32_t s_pref[WARPS][32];
-    __shared__ unsigned long long s_mask[WARPS][32];
-    pdl_wait();
-    if (ld_volatile_u32(bp.error)) return;   // uniform: set only by earlier kernels
-    commit_stats(bp);
+    auto &s_best = sm.best;
+    auto &s_depth = sm.depth;
+    auto &s_hiz = sm.hiz;
+    auto &s_stage = sm.stage;
+    auto &s_pref = sm.pref;
+    auto &s_mask = sm.mask;
+    if (CHECK_ERROR && ld_volatile_u32(bp.error)) return;   // uniform: set only by earlier kernels
+    commit_stats(bp, blk);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t gtile = blockIdx.x;
+    const uint32_t gtile = blk;
     if (gtile >= bp.total_tiles) return;
     const uint32_t vi = find_view(bp, gtile);
     const ViewDesc &V = bp.views[vi];
@@ -1542,8 +1654,8 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_tile_coop(BatchParam
     const uint32_t tx = t % V.tiles_x, ty = t / V.tiles_x;
     const uint32_t bin0 = V.bin_base + t * V.draw_count;
     const uint32_t dc = V.draw_count;
-    const uint32_t my_start = lane <= dc ? __ldg(bp.bin_start + bin0 + lane) : 0u;
-    const uint32_t last = dc < 32 ? __shfl_sync(0xFFFFFFFFu, my_start, dc) : __ldg(bp.bin_start + bin0 + dc);
+    const uint32_t my_start = lane <= dc ? ld_stage<COHERENT>(bp.bin_start + bin0 + lane) : 0u;
+    const uint32_t last = dc < 32 ? __shfl_sync(0xFFFFFFFFu, my_start, dc) : ld_stage<COHERENT>(bp.bin_start + bin0 + dc);
 
     const int32_t x0 = (int32_t)tx * kTile, y0 = (int32_t)ty * kTile;
     const int pix = (int)threadIdx.x;           // pixel of threads 0-63: row-major in the tile
@@ -1581,8 +1693,8 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_tile_coop(BatchParam
             s = __shfl_sync(0xFFFFFFFFu, my_start, dd);
             e = __shfl_sync(0xFFFFFFFFu, my_start, dd + 1);
         } else {
-            s = __ldg(bp.bin_start + bin0 + dd);
-            e = __ldg(bp.bin_start + bin0 + dd + 1);
+            s = ld_stage<COHERENT>(bp.bin_start + bin0 + dd);
+            e = ld_stage<COHERENT>(bp.bin_start + bin0 + dd + 1);
         }
         if (s == e) continue;   // uniform over the CTA
         const DrawDesc &D = bp.draws[V.draw_begin + dd];
@@ -1596,7 +1708,7 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_tile_coop(BatchParam
         const uint32_t ws = s + min(n, per * (uint32_t)warp), we = s + min(n, per * (uint32_t)(warp + 1));
         unsigned long long fa = sentinel, fb = sentinel;
         for (uint32_t chunk = ws; chunk < we; chunk += 32)
-            tile_chunk(bp, chunk, we, x0, y0, less, top_left, hiz, s_stage[warp], s_pref[warp], s_mask[warp],
+            tile_chunk<COHERENT>(bp, chunk, we, x0, y0, less, top_left, hiz, s_stage[warp], s_pref[warp], s_mask[warp],
                        s_best, s_depth, capture, lane, fa, fb);
         // the warp's whole-tile results: lane holds pixels lane and lane + 32
         if (fa != sentinel) { if (less) atomicMin(&s_best[lane], fa); else atomicMax(&s_best[lane], fa); }
@@ -1630,11 +1742,146 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_tile_coop(BatchParam
         hiz_max = s_hiz[1];
     }
 
-    if (valid && win != 0xFFFFFFFFu) shade_pixel(bp, V, win, px, py);
+    if (valid && win != 0xFFFFFFFFu) shade_pixel<COHERENT>(bp, V, win, px, py);
     if (valid && win == 0xFFFFFFFFu && V.clear_flags) write_cleared(V, o, dcur);
     if (threadIdx.x == 0) {
         V.tile_min[t] = hiz_min;
         V.tile_max[t] = hiz_max;
+    }
+}
+
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_tile_coop(BatchParams bp) {
+    __shared__ CoopSmem<WARPS> sm;
+    pdl_wait();
+    tile_coop_body<WARPS>(bp, blockIdx.x, sm);
+    pdl_trigger();
+}
+
+// ------------------------------------------------------------------ persistent launch
+//
+// The binned pipeline of a batch as one launch: a grid of as many CTAs as fit on the GPU at once
+// (a cooperative launch, which guarantees that they are all resident) runs the stages in turn, with
+// a grid-wide barrier where the separate kernels have a launch boundary:
+//   vertex shading (k_vertex) | geometry (k_geometry) | clipping (k_clip) | ranks (k_rank, when
+//   requested) and the bin scan (k_scan) | scatter (k_scatter) | tiles (k_tile<8>, or k_tile_coop<8>
+//   when tiles are shared by warps)
+// Each stage runs the same body as its kernel, over the same blocks, so the results are the same.
+// The scans take their blocks in a fixed order instead of from tickets (see kTicket).
+constexpr int kBatchBlock = 256;                     // 8 warps
+constexpr uint32_t kGridSpinLimit = 1u << 22;        // a second or more of waiting, with the backoff
+constexpr uint32_t kGridSpinLimitDebug = 1u << 14;   // kDebugStallGrid: milliseconds
+
+union BatchSmem {
+    TileSmem<kBatchBlock / 32> tile;
+    CoopSmem<kBatchBlock / 32> coop;
+    ScatterSmem scatter;
+    ClipSmem<kBatchBlock / 32> clip;
+    ScanSmem scan;
+};
+
+// Grid barrier `round` (1, 2, ...) of the persistent launch. The arrival counter starts at zero
+// for every batch and counts up over the launch's barriers, so barrier `round` is passed once it
+// reaches round * gridDim.x. Thread 0 of each CTA makes the CTA's writes visible (fence), arrives
+// and waits; the wait is bounded, and when it runs out the error bit is set. Returns false,
+// uniformly over the CTA, when the CTA must leave: its wait ran out, or an error bit is set (an
+// earlier stage overflowed or timed out; the separate kernels return early on it too).
+__device__ __forceinline__ bool grid_barrier(const BatchParams &bp, uint32_t round, uint32_t *s_go) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t go = 0;
+        // failure-detection tests (kDebugStallGrid): CTA 0 leaves without arriving, so the waits of
+        // all the others run out
+        if (!((bp.debug_flags & kDebugStallGrid) && blockIdx.x == 0)) {
+            go = 1;
+            __threadfence();
+            atomicAdd(bp.counters + kCtrGrid, 1u);
+            const uint32_t target = round * gridDim.x;
+            const uint32_t limit = (bp.debug_flags & kDebugStallGrid) ? kGridSpinLimitDebug : kGridSpinLimit;
+            uint32_t spins = 0;
+            while (ld_acquire_u32(bp.counters + kCtrGrid) < target) {
+                if (++spins > limit) {
+                    atomicOr(bp.error, kErrGridTimeout);
+                    go = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+            __threadfence();
+            if (ld_volatile_u32(bp.error)) go = 0;
+        }
+        *s_go = go;
+    }
+    __syncthreads();
+    return *s_go != 0;
+}
+
+// Runs body(b) for every block b in [0, nb) on the persistent grid: each CTA first takes block
+// blockIdx.x, then claims the next unclaimed one from the counter, one ahead (the claim is in
+// flight while the current block runs). Blocks of uneven cost (tiles, triangles of a frame's
+// visible and culled regions) then balance over the CTAs as a separate kernel's blocks do on the
+// hardware's block scheduler. Every thread of the CTA calls it; the loop is uniform over the CTA.
+template <typename Body>
+__device__ __forceinline__ void claim_blocks(uint32_t *counter, uint32_t nb, uint32_t *s_next, Body &&body) {
+    uint32_t b = blockIdx.x;
+    while (b < nb) {
+        uint32_t next = 0;
+        if (threadIdx.x == 0) next = gridDim.x + atomicAdd(counter, 1u);
+        body(b);
+        __syncthreads();   // every thread has read the previous block number
+        if (threadIdx.x == 0) *s_next = next;
+        __syncthreads();
+        b = *s_next;
+    }
+}
+
+template <bool COOP>
+__global__ void __launch_bounds__(kBatchBlock, 4) k_batch(BatchParams bp) {
+    __shared__ BatchSmem sm;
+    __shared__ uint32_t s_go, s_next;
+    constexpr int W = kBatchBlock / 32;
+    const uint32_t nctas = gridDim.x;
+    uint32_t round = 0;
+    if (bp.total_vertices) {   // draws whose vertices are shaded once
+        const uint32_t nb = (bp.total_vertices + kVertexBlock - 1) / kVertexBlock;
+        static_assert(kVertexBlock == kBatchBlock, "one vertex a thread");
+        for (uint32_t b = blockIdx.x; b < nb; b += nctas) vertex_body(bp, b);
+        if (!grid_barrier(bp, ++round, &s_go)) return;
+    }
+    claim_blocks(bp.counters + kCtrClaimGeometry, (bp.total_tris + kBatchBlock - 1) / kBatchBlock, &s_next,
+                 [&](uint32_t b) { geometry_warp<true>(bp, b * kBatchBlock + threadIdx.x); });
+    if (!grid_barrier(bp, ++round, &s_go)) return;
+    clip_body<W, true>(bp, blockIdx.x, nctas, sm.clip);
+    if (!grid_barrier(bp, ++round, &s_go)) return;
+    if (bp.want_rank) {
+        static_assert(kRankBlock == kBatchBlock, "rank block");
+        const uint32_t per = kRankBlock * kRankItems;
+        const uint32_t nb = bp.total_tris > per ? (bp.total_tris + per - 1) / per : 1u;
+        for (uint32_t b = blockIdx.x; b < nb; b += nctas) {
+            rank_body(bp, b, nb, sm.scan);
+            __syncthreads();
+        }
+    }
+    {
+        static_assert(kScanBlock == kBatchBlock, "scan block");
+        const uint32_t per = kScanBlock * kScanItems;
+        const uint32_t nb = bp.total_bins > per ? (bp.total_bins + per - 1) / per : 1u;
+        for (uint32_t b = blockIdx.x; b < nb; b += nctas) {
+            scan_body(bp, b, nb, sm.scan);
+            __syncthreads();
+        }
+    }
+    if (!grid_barrier(bp, ++round, &s_go)) return;
+    static_assert(kScatterBlock == kBatchBlock, "scatter block");
+    scatter_body<false, true>(bp, blockIdx.x, nctas, sm.scatter);
+    if (!grid_barrier(bp, ++round, &s_go)) return;
+    if (COOP) {
+        claim_blocks(bp.counters + kCtrClaimTiles, bp.total_tiles, &s_next,
+                     [&](uint32_t b) { tile_coop_body<W, false, true>(bp, b, sm.coop); });
+    } else {
+        commit_stats(bp, blockIdx.x);
+        claim_blocks(bp.counters + kCtrClaimTiles, (bp.total_tiles + W - 1) / W, &s_next,
+                     [&](uint32_t b) { tile_warp<W, true>(bp, b * W + (threadIdx.x >> 5), sm.tile); });
     }
     pdl_trigger();
 }
@@ -2462,6 +2709,32 @@ cudaError_t launch_direct_queue(const BatchParams &bp, int num_sms, cudaStream_t
 cudaError_t launch_direct_resolve(const BatchParams &bp, cudaStream_t stream) {
     return launch_chained(k_direct_resolve, (bp.total_tiles + kResolveWarps - 1) / kResolveWarps,
                           (uint32_t)(kResolveWarps * 32), stream, bp);
+}
+
+// The persistent launch: as many CTAs as are resident at once (cooperative: the launch fails
+// rather than start a grid whose CTAs could not all run together).
+cudaError_t launch_persistent(const BatchParams &bp, uint32_t warps_per_tile, int num_sms, cudaStream_t stream) {
+    const bool coop = warps_per_tile > 1;
+    void (*kernel)(BatchParams) = coop ? k_batch<true> : k_batch<false>;
+    static int resident[2] = {0, 0};   // CTAs per SM, the same on every device of this build's arch
+    if (resident[coop] == 0) {
+        int n = 0;
+        const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, kBatchBlock, 0);
+        if (e != cudaSuccess) return e;
+        if (n < 1) return cudaErrorInvalidConfiguration;
+        resident[coop] = n;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((uint32_t)(resident[coop] * (num_sms > 0 ? num_sms : 1)));
+    cfg.blockDim = dim3(kBatchBlock);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, bp);
 }
 
 cudaError_t launch_tile(const BatchParams &bp, uint32_t warps, uint32_t warps_per_tile, cudaStream_t stream) {

@@ -33,7 +33,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 def test_abi_version(lib):
     # 2: mlv_rasterizer_desc gained fill_rule and sample_position
-    assert lib.mlv_get_abi_version() == 4
+    assert lib.mlv_get_abi_version() == 5
 
 
 def test_null_handles_are_rejected(lib):

@@ -11,11 +11,54 @@ def test_candidates_cover_the_space_in_order():
     pts = autotune.candidates(space)
     assert len(pts) == 6
     assert pts[0] == {"a": 3, "b": 1} and pts[-1] == {"a": 5, "b": 2}
-    # several warps per tile make the warps-per-CTA knob moot: (3 + 3) tile shapes
-    assert len(autotune.candidates()) == (3 + 3) * 3 * 4
+    # several warps per tile make the warps-per-CTA knob moot: (3 + 3) tile shapes; the persistent
+    # launch has fixed shapes but for warps per tile (1 or all 8) and the big-triangle threshold
+    assert len(autotune.candidates()) == (3 + 3) * 3 * 4 + 2 * 4
     pts = autotune.candidates({"tile_warps_per_block": (2, 8), "warps_per_tile": (1, 4)})
     assert pts == [{"tile_warps_per_block": 2, "warps_per_tile": 1}, {"tile_warps_per_block": 2, "warps_per_tile": 4},
                    {"tile_warps_per_block": 8, "warps_per_tile": 1}]
+
+
+def test_persistent_points_take_its_fixed_shapes():
+    pts = [p for p in autotune.candidates() if p["persistent_launch"]]
+    assert len(pts) == 8
+    assert all(p["tile_warps_per_block"] == 8 and p["geometry_block"] == 256 for p in pts)
+    assert sorted({p["warps_per_tile"] for p in pts}) == [1, 8]
+    assert sorted({p["big_triangle_tiles"] for p in pts}) == [4, 8, 16, 32]
+    # without the knobs it fixes, only warps per tile is filtered
+    pts = autotune.candidates({"persistent_launch": (0, 1), "warps_per_tile": (1, 2, 4)})
+    assert pts == [{"persistent_launch": 0, "warps_per_tile": 1}, {"persistent_launch": 0, "warps_per_tile": 2},
+                   {"persistent_launch": 0, "warps_per_tile": 4}, {"persistent_launch": 1, "warps_per_tile": 1},
+                   {"persistent_launch": 1, "warps_per_tile": 4}]
+
+
+def test_autotune_picks_the_persistent_launch_when_it_is_fastest():
+    dev = _FakeDevice()
+    cost = lambda: (1.0 if dev.immediate.t["persistent_launch"] else 2.0) + dev.immediate.t["big_triangle_tiles"] * 0.01
+    out = autotune.autotune(dev, _FakeRenderer(), time_fn=lambda fn: (fn(), cost())[1])
+    assert out["best"]["persistent_launch"] == 1 and out["best"]["big_triangle_tiles"] == 4
+    assert dev.immediate.t["persistent_launch"] == 1 and dev.immediate.t["tile_warps_per_block"] == 8
+
+
+def test_the_path_choice_counts_launches_of_the_chained_form():
+    # a context left on the persistent launch runs 1 binned launch a batch: the path choice must
+    # compare the chained form's 6 with the small-draw path's 3, and keep the context's form after
+    class _Ctx(_FakeCtx):
+        def reset_stats(self):
+            pass
+
+        def stats(self):
+            if self.t.get("small_draw_triangles"):
+                return {"kernel_launches": 3}
+            return {"kernel_launches": 1 if self.t.get("persistent_launch") else 6}
+
+    dev = _FakeDevice()
+    dev.immediate = _Ctx()
+    dev.immediate.t["persistent_launch"] = 1
+    cost = lambda: 1.0 if dev.immediate.t.get("small_draw_triangles") else 2.0
+    out = autotune.autotune(dev, _FakeRenderer(), time_fn=lambda fn: (fn(), cost())[1])
+    assert out["results"] == [] and out["best"] == {"small_draw_triangles": autotune.PATHS[1]}
+    assert dev.immediate.t["persistent_launch"] == 1
 
 
 def test_pick_takes_the_fastest_and_keeps_the_first_tie():
@@ -26,7 +69,7 @@ def test_pick_takes_the_fastest_and_keeps_the_first_tie():
 class _FakeCtx:
     def __init__(self):
         self.t = {"tile_warps_per_block": 4, "warps_per_tile": 1, "geometry_block": 256, "big_triangle_tiles": 16,
-                  "small_draw_triangles": 0xFFFFFFFF}
+                  "small_draw_triangles": 0xFFFFFFFF, "persistent_launch": 0}
         self.history = []
 
     def tuning(self):
@@ -55,9 +98,9 @@ def test_autotune_sets_the_fastest_point():
     # a context without launch statistics cannot tell whether the small-draw path applies: its
     # path setting stays, and the sweep runs
     assert out["best"] == {"big_triangle_tiles": 4, "geometry_block": 128, "tile_warps_per_block": 2,
-                           "warps_per_tile": 1, "small_draw_triangles": 0xFFFFFFFF}
+                           "warps_per_tile": 1, "persistent_launch": 0, "small_draw_triangles": 0xFFFFFFFF}
     assert dev.immediate.t == out["best"]
-    assert len(out["results"]) == 72 and len(out["path"]) == 2
+    assert len(out["results"]) == 80 and len(out["path"]) == 2
 
 
 def test_autotune_skips_the_sweep_when_the_small_draw_path_wins():
@@ -90,7 +133,7 @@ def test_autotune_restores_the_tuning_on_error():
     with pytest.raises(RuntimeError):
         autotune.autotune(dev, _FakeRenderer(), time_fn=bad_timer)
     assert dev.immediate.t == {"tile_warps_per_block": 4, "warps_per_tile": 1, "geometry_block": 256,
-                               "big_triangle_tiles": 16, "small_draw_triangles": 0xFFFFFFFF}
+                               "big_triangle_tiles": 16, "small_draw_triangles": 0xFFFFFFFF, "persistent_launch": 0}
 
 
 @pytest.mark.gpu
