@@ -60,6 +60,8 @@ def parse():
                     help="render the frame once (batched, eager) and exit: a short launch sequence for ncu")
     ap.add_argument("--profile-workload", default="scene", choices=["scene", "single"],
                     help="--profile-once: the scene frame or the single draw (icosphere L5 at 1280x720)")
+    ap.add_argument("--persistent", action="store_true",
+                    help="--profile-once: the batch as one persistent launch (k_batch)")
     ap.add_argument("--warps-per-tile", type=int, default=0,
                     help="--profile-once: this tile-kernel shape (1, 2, 4 or 8) instead of the default")
     ap.add_argument("--small-draw-triangles", type=int, default=-1,
@@ -318,6 +320,37 @@ def run_single_draw_section(dev, args):
                          "traffic": ncu_traffic("single_draw_frame")}}
 
 
+def persistent_point(tuned):
+    """The autotuner's fastest persistent-launch point (the defaults when it did not run)."""
+    best = None
+    for point, ms in (tuned or {}).get("results", []):
+        if point.get("persistent_launch") and (best is None or ms < best[1]):
+            best = (point, ms)
+    return dict(best[0]) if best else {"persistent_launch": 1, "warps_per_tile": 1}
+
+
+def time_persistent(ctx, r, point, timed, steps, reference, n_views=1):
+    """The renderer's batch as one persistent launch (the binned pipeline's stages in one
+    cooperative launch with grid barriers between them, `point`'s shapes): ms per batch by the
+    caller's `timed`, kernel launches per batch, and whether every view's colour and depth equal
+    `reference` (the kernel-per-stage outputs) bit for bit. The context's tuning is restored."""
+    base = ctx.tuning()
+    try:
+        ctx.set_tuning(**point)
+        r.render_batched()
+        ms = timed(r.render_batched, steps)
+        ctx.reset_stats()
+        r.render_batched()
+        launches = ctx.stats()["kernel_launches"]
+        same = all(np.array_equal(r.read(i)[k].view(np.uint32), reference[i][k].view(np.uint32))
+                   for i in range(n_views) for k in ("color", "depth"))
+    finally:
+        ctx.set_tuning(**base)
+    return {"ms": round(ms, 4), "launches": int(launches), "images_identical": bool(same),
+            "launch_shapes": {k: v for k, v in point.items() if k in ("persistent_launch", "warps_per_tile",
+                                                                        "big_triangle_tiles")}}
+
+
 def run_multiview_section(dev, args):
     """Batched multi-view: 64 views at seeded resolutions in {256..1024}^2, 16 icosphere/heightfield
     meshes of 2k-200k triangles, 4-16 draws per view, basic_vs + basic_ps. Launch shapes come from
@@ -355,6 +388,8 @@ def run_multiview_section(dev, args):
     batched_ms = timed(r.render_batched, args.steps)
     st = ctx.stats()
     batched = [r.read(i) for i in range(len(frames))]
+    pers = time_persistent(ctx, r, persistent_point(tuned), timed, max(3, args.steps // 2), batched,
+                           n_views=len(frames))
     per_draw_ms = timed(r.render_per_draw, max(3, args.steps // 2))
     same = 0
     for i in range(len(frames)):
@@ -371,6 +406,8 @@ def run_multiview_section(dev, args):
             "batched_mtri_per_s": round(tris / (batched_ms / 1e3) / 1e6, 1),
             "assembled_per_run": st["assembled_triangle_count"] // runs,
             "views_identical_to_per_draw": "%d/%d" % (same, len(frames)),
+            "persistent_launch": dict(pers, kernel_per_stage_ms=round(batched_ms, 4),
+                                      speed_vs_kernel_per_stage=round(batched_ms / pers["ms"], 3)),
             "autotuned": tuned["best"], "autotune_points": len(tuned["results"]),
             "l2": "flushed between steps (256 MB write outside the timed events)"}
 
@@ -720,6 +757,8 @@ def main():
     if args.profile_once:
         if args.warps_per_tile:
             ctx.set_tuning(warps_per_tile=args.warps_per_tile)
+        if args.persistent:
+            ctx.set_tuning(persistent_launch=1, small_draw_triangles=0)
         r.render_batched()
         ctx.finish()
         print(json.dumps({"profile_once": True, "stats": ctx.stats()}))
@@ -792,6 +831,26 @@ def main():
         pd.append((a, b))
     ctx.finish()
     pd_ms = float(np.mean([a.elapsed_time(b) for a, b in pd]))
+
+    # --- the same frame as one persistent launch, timed the same way
+    def timed_frames(fn, n):
+        for _ in range(3):
+            fn()
+        ctx.finish()
+        evs2 = []
+        for i in range(n):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                flush.fill_(i)
+                a.record(stream)
+            fn()
+            with torch.cuda.stream(stream):
+                b.record(stream)
+            evs2.append((a, b))
+        ctx.finish()
+        return float(np.mean([a.elapsed_time(b) for a, b in evs2]))
+
+    pers = time_persistent(ctx, r, persistent_point(tuned), timed_frames, args.steps, [timed_out])
 
     # --- per-kernel durations (stage events on the context stream), same frame, eager launches
     ctx.set_profiling(True)
@@ -969,6 +1028,9 @@ def main():
             "gpix_per_s": round(fragments / (ms / 1e3) / 1e9, 4) if fragments else None,
             "per_draw": {"value": round(tris / (pd_ms / 1e3) / 1e6, 3), "unit": "Mtri/s", "ms_per_frame": round(pd_ms, 4),
                          "batched_speedup": round(pd_ms / ms, 3)},
+            "persistent_launch": dict(pers, speed_vs_kernel_per_stage=round(ms / pers["ms"], 3),
+                                      mode="the batch's binned pipeline as one cooperative launch, grid barriers "
+                                           "between its stages (the autotuner's fastest such point)"),
             "e2e": {"value": round(tris * world / e2e_s / 1e6, 3), "unit": "Mtri/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_s * 1e3, 3),
                     "mode": "three device handles in turn (triple-buffered frames): each step uploads its "
