@@ -31,6 +31,7 @@
 // the tile kernel computes with shared-memory atomics, then shades only the winner.
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <algorithm>
 #include <utility>
 
 #include "internal.h"
@@ -1800,8 +1801,8 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_tile_coop(BatchParam
 
 // ------------------------------------------------------------------ persistent launch
 //
-// The binned pipeline of a batch as one launch: a grid of as many CTAs as fit on the GPU at once
-// (a cooperative launch, which guarantees that they are all resident) runs the stages in turn, with
+// The binned pipeline of a batch as one launch: a grid of at most as many CTAs as fit on the GPU at
+// once (a cooperative launch, which guarantees that they are all resident) runs the stages in turn, with
 // a grid-wide barrier where the separate kernels have a launch boundary:
 //   vertex shading (k_vertex) | geometry (k_geometry) | clipping (k_clip) | ranks (k_rank, when
 //   requested) and the bin scan (k_scan) | scatter (k_scatter) | tiles (k_tile<8>, or k_tile_coop<8>
@@ -2758,8 +2759,8 @@ cudaError_t launch_direct_resolve(const BatchParams &bp, cudaStream_t stream) {
                           (uint32_t)(kResolveWarps * 32), stream, bp);
 }
 
-// The persistent launch: as many CTAs as are resident at once (cooperative: the launch fails
-// rather than start a grid whose CTAs could not all run together).
+// The persistent launch: at most as many CTAs as are resident at once (cooperative: the launch
+// fails rather than start a grid whose CTAs could not all run together).
 cudaError_t launch_persistent(const BatchParams &bp, uint32_t warps_per_tile, int num_sms, cudaStream_t stream) {
     const bool coop = warps_per_tile > 1;
     void (*kernel)(BatchParams) = coop ? k_batch<true> : k_batch<false>;
@@ -2771,8 +2772,15 @@ cudaError_t launch_persistent(const BatchParams &bp, uint32_t warps_per_tile, in
         if (n < 1) return cudaErrorInvalidConfiguration;
         resident[coop] = n;
     }
+    // no more CTAs than the batch's largest stage has blocks for: a small batch's barriers then
+    // gather a few CTAs instead of every SM's (the other stages stride over whatever grid there is)
+    constexpr uint32_t W = kBatchBlock / 32;
+    uint64_t want = std::max<uint64_t>((bp.total_vertices + kBatchBlock - 1) / kBatchBlock,
+                                       (bp.total_tris + kBatchBlock - 1) / kBatchBlock);
+    want = std::max<uint64_t>(want, coop ? bp.total_tiles : (bp.total_tiles + W - 1) / W);
+    const uint64_t fit = (uint64_t)resident[coop] * (uint64_t)(num_sms > 0 ? num_sms : 1);
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((uint32_t)(resident[coop] * (num_sms > 0 ? num_sms : 1)));
+    cfg.gridDim = dim3((uint32_t)std::max<uint64_t>(1, std::min(want, fit)));
     cfg.blockDim = dim3(kBatchBlock);
     cfg.dynamicSmemBytes = 0;
     cfg.stream = stream;

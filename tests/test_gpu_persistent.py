@@ -256,6 +256,28 @@ def test_bounded_lookback_wait_in_the_persistent_launch(device):
         r.destroy()
 
 
+def test_autotune_searches_the_persistent_launch(device):
+    # the sweep times the persistent points too; whichever form wins, the image is the same
+    from malevich_gb300 import autotune
+    fr = scenes.small_scene(56, 64, 64, n_objects=2, level=2)
+    (want,), _ = render(device, [fr], 0)
+    ctx = device.immediate
+    base = ctx.tuning()
+    r = api.FrameRenderer(device, fr, visibility=True)
+    try:
+        ctx.set_tuning(small_draw_triangles=0)
+        r.render_batched()
+        out = autotune.autotune(device, r, repeats=3, warmup=1, choose_path=False)
+        assert sum(1 for p, _ in out["results"] if p["persistent_launch"]) == 8
+        assert ctx.tuning()["persistent_launch"] == out["best"]["persistent_launch"]
+        r.render_batched()
+        r.render_batched()
+        check_same(r.read(0), want)
+    finally:
+        ctx.set_tuning(**base)
+        r.destroy()
+
+
 def test_persistent_launch_is_validated(device):
     ctx = device.immediate
     with pytest.raises(api.MalevichError):
