@@ -813,9 +813,10 @@ static mlv_status launch_draws(mlv_context_t *c, const Plan &p, DrawDesc *d_draw
         return cudaSuccess;
     };
     cudaEvent_t e;
-    // the clip-fan slot counter starts at zero for every batch (reset before the first kernel, so
-    // that the batch's kernels follow one another directly)
-    CUDA_TRY(cudaMemsetAsync(w.counters + kCtrOverflow, 0, kCtrPerBatch * sizeof(uint32_t), c->stream));
+    // the per-batch counters (clip-fan slots, queue entries, clip list, bin jobs, the persistent
+    // launch's arrivals and claims) are zero here: every batch's last kernel zeroes them for the
+    // next one (reset_batch_counters), and a failed batch's recovery zeroes every counter, so the
+    // batch's kernels follow one another with no memset in front of them
     if (p.direct) {
         // the small-draw path: raster (vertex shader, setup, small triangles), queued large
         // triangles, resolve; stages 1, 3 and 4 of the stage timers

@@ -671,7 +671,10 @@ __device__ __forceinline__ void geometry_warp(const BatchParams &bp, uint32_t g)
         uint32_t at = 0;
         if (lane == 0) at = atomicAdd(bp.counters + kCtrClip, (uint32_t)__popc(clip_lanes));
         at = __shfl_sync(0xFFFFFFFFu, at, 0);
-        if (clipped) bp.clip_list[at + __popc(clip_lanes & ((1u << lane) - 1u))] = make_uint2(g, draw);
+        const uint32_t slot = at + __popc(clip_lanes & ((1u << lane) - 1u));
+        // below total_tris (the list's size) while the per-batch counters start at zero, as they
+        // do except behind a failed batch (error word set; such batches are re-run)
+        if (clipped && slot < bp.total_tris) bp.clip_list[slot] = make_uint2(g, draw);
     }
     if (!__any_sync(0xFFFFFFFFu, mask != 0u)) return;   // the warp assembled nothing: nothing to count
     // assembled-triangle statistic (main.c:1238)
@@ -737,7 +740,11 @@ struct ClipSmem {
 template <int WARPS, bool COHERENT = false>
 __device__ __forceinline__ void clip_body(const BatchParams &bp, uint32_t blk, uint32_t nblk, ClipSmem<WARPS> &sm) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t n = ld_volatile_u32(bp.counters + kCtrClip);
+    // behind a failed batch (error word set) the counters need not have started at zero, and the
+    // batch is re-run anyway: nothing to clip. Decided per warp (another warp's clip may set the
+    // word meanwhile, and the warp's lanes clip together)
+    if (__any_sync(0xFFFFFFFFu, ld_volatile_u32(bp.error) != 0u)) return;
+    const uint32_t n = min(ld_volatile_u32(bp.counters + kCtrClip), bp.total_tris);
     uint32_t assembled = 0;
     for (uint32_t i = blk * WARPS + warp; i < n; i += nblk * WARPS) {
         const uint2 entry = bp.clip_list[i];
@@ -1503,6 +1510,16 @@ __device__ __forceinline__ void shade_pixel(const BatchParams &bp, const ViewDes
     if (V.vis_bary) reinterpret_cast<float2 *>(V.vis_bary)[o] = make_float2(b1, b2);
 }
 
+// Zeroes the per-batch counters (kCtrOverflow ... kCtrClaimTiles) for the next batch. The batch's
+// last kernel does it once its predecessors are done with them, so that a batch needs no memset of
+// its own in front of its first kernel (in a graph, a memset node there keeps the first kernel
+// from being launched early). The counters are zero on allocation and after a failed batch's
+// recovery, which zeroes every counter.
+__device__ __forceinline__ void reset_batch_counters(const BatchParams &bp) {
+#pragma unroll
+    for (int k = 0; k < kCtrPerBatch; ++k) bp.counters[kCtrOverflow + k] = 0u;
+}
+
 // Commits the batch's staged statistics (k_geometry and k_scan finished before the tile kernel).
 __device__ __forceinline__ void commit_stats(const BatchParams &bp, uint32_t blk) {
     if (blk == 0 && threadIdx.x == 0) {
@@ -1652,6 +1669,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile(BatchParams bp) {
     pdl_wait();
     if (ld_volatile_u32(bp.error)) return;
     commit_stats(bp, blockIdx.x);
+    if (blockIdx.x == 0 && threadIdx.x == 0) reset_batch_counters(bp);
     tile_warp<WARPS>(bp, blockIdx.x * WARPS + (threadIdx.x >> 5), sm);
     pdl_trigger();
 }
@@ -1795,6 +1813,7 @@ template <int WARPS>
 __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_tile_coop(BatchParams bp) {
     __shared__ CoopSmem<WARPS> sm;
     pdl_wait();
+    if (blockIdx.x == 0 && threadIdx.x == 0 && !ld_volatile_u32(bp.error)) reset_batch_counters(bp);
     tile_coop_body<WARPS>(bp, blockIdx.x, sm);
     pdl_trigger();
 }
@@ -1923,6 +1942,13 @@ __global__ void __launch_bounds__(kBatchBlock, 4) k_batch(BatchParams bp) {
         commit_stats(bp, blockIdx.x);
         claim_blocks(bp.counters + kCtrClaimTiles, (bp.total_tiles + W - 1) / W, &s_next,
                      [&](uint32_t b) { tile_warp<W, true>(bp, b * W + (threadIdx.x >> 5), sm.tile); });
+    }
+    // the last CTA to finish (one more arrival on the barrier counter) zeroes the per-batch
+    // counters for the next batch, claims and arrivals included
+    __syncthreads();
+    if (threadIdx.x == 0 && atomicAdd(bp.counters + kCtrGrid, 1u) == (round + 1) * gridDim.x - 1) {
+        __threadfence();
+        reset_batch_counters(bp);
     }
     pdl_trigger();
 }
@@ -2484,6 +2510,7 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_direct_resolve(BatchPara
     pdl_wait();
     if (ld_volatile_u32(bp.error)) return;   // uniform: set only by earlier kernels
     if (blockIdx.x == 0 && threadIdx.x == 0) {
+        reset_batch_counters(bp);
         // the raster kernel's staged statistics; active bins are added below by every CTA
         for (int k : {(int)kStatAssembled, (int)kStatBinEntries}) {
             atomicAdd(bp.stats + kStatTotal + k, bp.stats[k]);
