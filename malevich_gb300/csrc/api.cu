@@ -43,6 +43,8 @@ cudaError_t launch_persistent(const BatchParams &bp, uint32_t warps_per_tile, in
 cudaError_t launch_direct_raster(const BatchParams &bp, int num_sms, cudaStream_t stream);
 cudaError_t launch_direct_queue(const BatchParams &bp, int num_sms, cudaStream_t stream);
 cudaError_t launch_direct_resolve(const BatchParams &bp, cudaStream_t stream);
+cudaError_t launch_put_descriptors(const void *a, uint32_t a_bytes, void *dst_a, const void *b, uint32_t b_bytes,
+                                   void *dst_b, cudaStream_t stream);
 }  // namespace mlv
 
 using namespace mlv;
@@ -887,10 +889,18 @@ static mlv_status execute_segment_eager(mlv_context_t *c, const Segment &seg, ui
         MLV_TRY(run_fills(c, jobs, chunks, nullptr));
     }
     MLV_TRY(ensure_workspace(c, p.sizes, false));
-    CUDA_TRY(cudaMemcpyAsync(c->ws.d_draws, p.draws.data(), sizeof(DrawDesc) * p.draws.size(),
-                             cudaMemcpyHostToDevice, c->stream));
-    CUDA_TRY(cudaMemcpyAsync(c->ws.d_views, p.views.data(), sizeof(ViewDesc) * p.views.size(),
-                             cudaMemcpyHostToDevice, c->stream));
+    // the descriptors: in a kernel's parameter block when they fit (a batch of a few draws), so
+    // that the batch's kernels follow the previous batch's directly; else two copies
+    const size_t draw_bytes = sizeof(DrawDesc) * p.draws.size(), view_bytes = sizeof(ViewDesc) * p.views.size();
+    static_assert(sizeof(DrawDesc) % 4 == 0 && sizeof(ViewDesc) % 4 == 0, "descriptors are copied as words");
+    if (draw_bytes + view_bytes <= kDescParamWords * 4u) {
+        CUDA_TRY(launch_put_descriptors(p.draws.data(), (uint32_t)draw_bytes, c->ws.d_draws, p.views.data(),
+                                        (uint32_t)view_bytes, c->ws.d_views, c->stream));
+        c->host_stats[4] += 1;
+    } else {
+        CUDA_TRY(cudaMemcpyAsync(c->ws.d_draws, p.draws.data(), draw_bytes, cudaMemcpyHostToDevice, c->stream));
+        CUDA_TRY(cudaMemcpyAsync(c->ws.d_views, p.views.data(), view_bytes, cudaMemcpyHostToDevice, c->stream));
+    }
     MLV_TRY(launch_draws(c, p, c->ws.d_draws, c->ws.d_views, seq));
     if (!rerun) {
         c->host_stats[0] += seg.vertex_count;

@@ -200,6 +200,10 @@ enum Counter : int {
 };
 constexpr int kCtrPerBatch = kCtrClaimTiles - kCtrOverflow + 1;
 
+// Words of descriptors an eager batch passes in a kernel's parameter block (with the kernel's other
+// parameters under the 4 KB limit): a batch of up to 9 draws of one view.
+constexpr uint32_t kDescParamWords = 992;
+
 
 // Statistics are staged per batch (slots kStat*) and added to the totals (kStat* + kStatTotal)
 // by the tile kernel, which runs only for batches that completed; a batch that is re-run after

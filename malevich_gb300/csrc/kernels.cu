@@ -32,6 +32,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <algorithm>
+#include <cstring>
 #include <utility>
 
 #include "internal.h"
@@ -2629,6 +2630,24 @@ __global__ void __launch_bounds__(256) k_upload_scatter(const uint8_t *staging, 
         j.dst[(n16 << 4) + threadIdx.x] = staging[j.src + (n16 << 4) + threadIdx.x];
 }
 
+// An eager batch's draw and view descriptors, passed in the launch's parameter block and written
+// to the workspace by one CTA, so that no copy-engine transfers stand in front of the batch's
+// kernels (the kernel is chained to the previous batch's like the pipeline's own: it waits until
+// that batch is done reading the descriptors it overwrites).
+struct DescWords {
+    uint32_t w[kDescParamWords];
+};
+
+__global__ void __launch_bounds__(256) k_put_descriptors(const __grid_constant__ DescWords src, uint32_t na,
+                                                         uint32_t *dst_a, uint32_t nb, uint32_t *dst_b) {
+    pdl_wait();
+    for (uint32_t i = threadIdx.x; i < na + nb; i += blockDim.x) {
+        if (i < na) dst_a[i] = src.w[i];
+        else dst_b[i - na] = src.w[i];
+    }
+    pdl_trigger();
+}
+
 __global__ void k_fill_u32(uint32_t *p, size_t n, uint32_t value, const uint32_t *error) {
     pdl_wait();
     if (error && ld_volatile_u32(error)) return;
@@ -2692,6 +2711,16 @@ static cudaError_t launch_chained(void (*kernel)(Params...), uint32_t grid, uint
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
+// a_bytes + b_bytes at most kDescParamWords * 4, both multiples of 4 (checked by the caller)
+cudaError_t launch_put_descriptors(const void *a, uint32_t a_bytes, void *dst_a, const void *b, uint32_t b_bytes,
+                                   void *dst_b, cudaStream_t stream) {
+    DescWords src;
+    memcpy(src.w, a, a_bytes);
+    memcpy(src.w + a_bytes / 4, b, b_bytes);
+    return launch_chained(k_put_descriptors, 1u, 256u, stream, src, a_bytes / 4, (uint32_t *)dst_a, b_bytes / 4,
+                          (uint32_t *)dst_b);
 }
 
 cudaError_t launch_fill_many(const FillJob *d_jobs, uint32_t njobs, uint32_t nchunks, const uint32_t *error,
