@@ -21,6 +21,8 @@
 //               write-back; the segment's clears of the batch's targets are folded in.
 //               k_tile_coop: the same with 2, 4 or 8 warps sharing each tile's triangles.
 //   k_fill_many the clears that are not folded (one launch per segment).
+//   k_put_descriptors  an eager batch's draw and view descriptors, from the launch's parameters.
+//   k_batch     the six stages above as one persistent launch (mlv_tuning::persistent_launch).
 // The kernels are launched with programmatic stream serialisation (see pdl_wait).
 //
 // Why the order inside a bin does not matter: there is no blending (main.c:1180-1181) and pixel
