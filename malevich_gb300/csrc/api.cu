@@ -42,7 +42,7 @@ cudaError_t launch_tile(const BatchParams &bp, uint32_t warps, uint32_t warps_pe
 cudaError_t launch_persistent(const BatchParams &bp, uint32_t warps_per_tile, int num_sms, cudaStream_t stream);
 cudaError_t launch_direct_raster(const BatchParams &bp, int num_sms, cudaStream_t stream);
 cudaError_t launch_direct_queue(const BatchParams &bp, int num_sms, cudaStream_t stream);
-cudaError_t launch_direct_resolve(const BatchParams &bp, cudaStream_t stream);
+cudaError_t launch_direct_resolve(const BatchParams &bp, int num_sms, cudaStream_t stream);
 cudaError_t launch_put_descriptors(const void *a, uint32_t a_bytes, void *dst_a, const void *b, uint32_t b_bytes,
                                    void *dst_b, cudaStream_t stream);
 }  // namespace mlv
@@ -202,6 +202,8 @@ struct Workspace {
     // small-draw path: the view's per-pixel keys (zero between draws) and the large-triangle queue
     unsigned long long *keys = nullptr;
     uint32_t keys_cap = 0;
+    uint32_t *marked = nullptr;       // [marked_cap]: small-draw path, the tiles a batch marked
+    uint32_t marked_cap = 0;
     uint4 *queue = nullptr;
     uint32_t queue_cap = 0;
     uint64_t generation = 0;
@@ -465,7 +467,9 @@ static mlv_status ensure_workspace(mlv_context_t *c, const BatchSizes &s, bool k
         MLV_TRY(grow(&w.keys, w.keys_cap, s.direct_pixels, sizeof(unsigned long long), true));
         uint4 *qb = w.queue;
         MLV_TRY(grow(&w.queue, w.queue_cap, std::max<uint64_t>(s.tris, 16384), sizeof(uint4)));
-        if (before != w.keys || qb != w.queue) changed = true;
+        uint32_t *mb = w.marked;
+        MLV_TRY(grow(&w.marked, w.marked_cap, std::max<uint64_t>(s.tiles, 1), sizeof(uint32_t)));
+        if (before != w.keys || qb != w.queue || mb != w.marked) changed = true;
     }
     {
         DrawDesc *b1 = w.d_draws;
@@ -486,6 +490,7 @@ struct Plan {
     BatchSizes sizes;
     bool direct = false;   // the small-draw path (one draw per view, no binning)
     bool keys_only = false;  // ... whose resolve reads no records
+    bool mark_list = false;  // ... whose views fold no clear: the resolve visits the marked tiles only
     std::unordered_set<mlv_texture2d> folded;   // cleared targets the tile kernel clears itself
     // upload events of the batch's inputs, waited for before the stage that first reads them
     std::vector<cudaEvent_t> wait_vertex, wait_index, wait_pixel;
@@ -650,6 +655,7 @@ static mlv_status plan_segment(const Segment &seg, Plan &p, uint32_t fan_slots_h
     p.direct = plan_is_direct(p, small_draw, capture);
     p.sizes.binned = !p.direct;
     p.keys_only = false;
+    p.mark_list = false;
     if (p.direct) {
         // the vertex shader runs per index inside the raster kernel (main.c:698-734's way)
         for (DrawDesc &d : p.draws) {
@@ -664,6 +670,8 @@ static mlv_status plan_segment(const Segment &seg, Plan &p, uint32_t fan_slots_h
         }
         p.sizes.direct_pixels = px;
         p.keys_only = plan_keys_only(p);
+        p.mark_list = true;
+        for (const ViewDesc &v : p.views) p.mark_list = p.mark_list && v.clear_flags == 0;
     }
     return MLV_OK;
 }
@@ -804,6 +812,8 @@ static mlv_status launch_draws(mlv_context_t *c, const Plan &p, DrawDesc *d_draw
     bp.queue = w.queue;
     bp.queue_capacity = w.queue_cap;
     bp.keys_only = p.keys_only ? 1u : 0u;
+    bp.mark_list = p.mark_list ? 1u : 0u;
+    bp.marked = w.marked;
     c->host_stats[3] += 1;
     if (bp.total_tris == 0) return MLV_OK;   // nothing to assemble: no kernel has work
     // waits on queued uploads (inside a graph capture: external event waits, evaluated at launch)
@@ -832,7 +842,7 @@ static mlv_status launch_draws(mlv_context_t *c, const Plan &p, DrawDesc *d_draw
         ev_end(c, e);
         CUDA_TRY(wait_for(p.wait_pixel));
         ev_begin(c, 4, &e);
-        CUDA_TRY(launch_direct_resolve(bp, c->stream));
+        CUDA_TRY(launch_direct_resolve(bp, c->device->num_sms, c->stream));
         ev_end(c, e);
         c->host_stats[4] += 3;
         return MLV_OK;
@@ -1078,7 +1088,7 @@ static void free_workspace(Workspace &w) {
     cudaFree(w.bin_count); cudaFree(w.bin_start); cudaFree(w.list); cudaFree(w.info_mask);
     cudaFree(w.scan_status); cudaFree(w.scan_status2); cudaFree(w.counters); cudaFree(w.stats);
     cudaFree(w.error); cudaFree(w.d_draws); cudaFree(w.d_views); cudaFree(w.d_fills); cudaFree(w.vs_out);
-    cudaFree(w.keys); cudaFree(w.queue);
+    cudaFree(w.keys); cudaFree(w.queue); cudaFree(w.marked);
     w = Workspace();
 }
 

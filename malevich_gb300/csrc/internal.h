@@ -185,6 +185,10 @@ struct BatchParams {
     uint4 *queue;                        // [queue_capacity]: key, record slot, first tile, tiles
     uint32_t queue_capacity;
     uint32_t keys_only;                  // 1: the resolve needs no records (depth and ids from the keys)
+    // 1 (a small-draw batch whose views fold no clear): the queue kernel lists the tiles the raster
+    // kernel marked in `marked`, and the resolve visits only those (an unmarked tile owes nothing)
+    uint32_t mark_list;
+    uint32_t *marked;                    // [total_tiles]
 };
 
 enum Counter : int {
@@ -196,6 +200,9 @@ enum Counter : int {
                                          // the persistent launch's grid barriers; its geometry and
                                          // tile blocks claimed
     kCtrScanTicket, kCtrScanDone, kCtrScanEpoch,
+    kCtrMarked, kCtrMarkedDone,          // small-draw batches with a marked-tile list: tiles listed (by
+                                         // the queue kernel);
+                                         // resolve CTAs finished (its last CTA zeroes both)
     kCtrCount = 16
 };
 constexpr int kCtrPerBatch = kCtrClaimTiles - kCtrOverflow + 1;

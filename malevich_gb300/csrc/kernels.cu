@@ -2498,6 +2498,23 @@ __global__ void __launch_bounds__(kDirectBlock) k_direct_queue(BatchParams bp) {
             direct_tile(V, J, J.tx0 + tx, J.ty0 + ty, lane);
         }
     }
+    if (bp.mark_list) {
+        // the tiles the raster kernel marked (all marks are set: it has finished), listed for the
+        // resolve, 32 tiles a warp round: one load a lane, one atomic a warp. On the small-draw
+        // path a view's bins are its tiles, so a bin index is the batch's tile index.
+        const uint32_t nwarps2 = gridDim.x * kDirectWarps;
+        for (uint32_t base = (blockIdx.x * kDirectWarps + (threadIdx.x >> 5)) * 32u; base < bp.total_tiles;
+             base += nwarps2 * 32u) {
+            const uint32_t tile = base + (uint32_t)lane;
+            const bool marked = tile < bp.total_tiles && bp.bin_count[tile] != 0u;
+            const uint32_t m = __ballot_sync(0xFFFFFFFFu, marked);
+            if (!m) continue;
+            uint32_t at = 0;
+            if (lane == 0) at = atomicAdd(bp.counters + kCtrMarked, (uint32_t)__popc(m));
+            at = __shfl_sync(0xFFFFFFFFu, at, 0) + (uint32_t)__popc(m & ((1u << lane) - 1u));
+            if (marked && at < bp.total_tiles) bp.marked[at] = tile;
+        }
+    }
     pdl_trigger();
 }
 
@@ -2523,8 +2540,8 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_direct_resolve(BatchPara
     if (threadIdx.x == 0) s_active = 0;
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t gtile = blockIdx.x * kResolveWarps + warp;
-    if (gtile < bp.total_tiles) {
+    // tile gtile of the batch, by the whole warp
+    auto resolve_tile = [&](uint32_t gtile) {
         const ViewDesc &V = bp.views[find_view(bp, gtile)];
         const uint32_t t = gtile - V.tile_base;
         const DrawDesc &D = bp.draws[V.draw_begin];
@@ -2608,11 +2625,29 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_direct_resolve(BatchPara
                 V.tile_max[t] = mx;
             }
         }
+    };
+    if (bp.mark_list) {
+        // only the tiles the raster kernel listed (no view folds a clear, so an unmarked tile
+        // owes nothing), a warp per listed tile
+        const uint32_t n = min(ld_volatile_u32(bp.counters + kCtrMarked), bp.total_tiles);
+        for (uint32_t i = blockIdx.x * kResolveWarps + warp; i < n; i += gridDim.x * kResolveWarps)
+            resolve_tile(bp.marked[i]);
+    } else {
+        const uint32_t gtile = blockIdx.x * kResolveWarps + warp;
+        if (gtile < bp.total_tiles) resolve_tile(gtile);
     }
     __syncthreads();
     // active-bin statistic (main.c:937-944), straight to the totals: this kernel runs only for a
     // batch that completed
     if (threadIdx.x == 0 && s_active) atomicAdd(bp.stats + kStatTotal + kStatActiveBins, (unsigned long long)s_active);
+    // the list's counter is read by every CTA, so the last one to finish zeroes it
+    if (bp.mark_list && threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(bp.counters + kCtrMarkedDone, 1u) == gridDim.x - 1) {
+            bp.counters[kCtrMarked] = 0u;
+            bp.counters[kCtrMarkedDone] = 0u;
+        }
+    }
     pdl_trigger();
 }
 
@@ -2812,9 +2847,12 @@ cudaError_t launch_direct_queue(const BatchParams &bp, int num_sms, cudaStream_t
     return launch_chained(k_direct_queue, (uint32_t)num_sms * 4u, (uint32_t)kDirectBlock, stream, bp);
 }
 
-cudaError_t launch_direct_resolve(const BatchParams &bp, cudaStream_t stream) {
-    return launch_chained(k_direct_resolve, (bp.total_tiles + kResolveWarps - 1) / kResolveWarps,
-                          (uint32_t)(kResolveWarps * 32), stream, bp);
+cudaError_t launch_direct_resolve(const BatchParams &bp, int num_sms, cudaStream_t stream) {
+    uint32_t grid = (bp.total_tiles + kResolveWarps - 1) / kResolveWarps;
+    // with a marked-tile list the CTAs stride over the listed tiles, whose number only the device
+    // knows: up to 8 CTAs an SM
+    if (bp.mark_list) grid = std::min<uint32_t>(grid, 8u * (uint32_t)(num_sms > 0 ? num_sms : 1));
+    return launch_chained(k_direct_resolve, grid, (uint32_t)(kResolveWarps * 32), stream, bp);
 }
 
 // The persistent launch: at most as many CTAs as are resident at once (cooperative: the launch
