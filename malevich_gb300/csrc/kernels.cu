@@ -1970,8 +1970,10 @@ __global__ void __launch_bounds__(kBatchBlock, 4) k_batch(BatchParams bp) {
 //                     below). Small triangles are rasterised by their own lane, mid-sized ones by
 //                     the CTA's warps (kDirectLanePixels* and the others below), larger ones and
 //                     clip fans go to a queue in chunks of 4 tiles.
-//   k_direct_queue    the queued chunks, spread over the whole GPU, a tile (two pixels a lane) at a time.
-//   k_direct_resolve  one warp per 8x8 tile: the winners' pixel shader and output merger, colour and
+//   k_direct_queue    the queued chunks, spread over the whole GPU, a tile (two pixels a lane) at a time;
+//                     in a batch that folds no clear, also the list of the marked tiles.
+//   k_direct_resolve  one warp per 8x8 tile (per listed tile when the batch folds no clear): the
+//                     winners' pixel shader and output merger, colour and
 //                     depth written once (main.c:1046-1189), hierarchical Z from the new depths
 //                     (write_tile, main.c:589-603), folded clears, and the keys reset to zero.
 // The per-pixel result is the same fold the tile kernel computes per draw (see the top of this
