@@ -238,7 +238,7 @@ def algorithmic_bytes(frame, dev_stats, written_pixels):
 def run_single_draw_section(dev, args):
     """The plain single draw: a level-5 icosphere (20,480 triangles) with basic_vs + basic_ps over a
     1024x1024 RGBA8 noise texture into 1280x720 RGBA8 + D32 (depth LESS, cleared to 1.0). The frame
-    (both clears and the draw) is timed as 100 back-to-back frames recorded in one command list
+    (both clears and the draw) is timed as 1,000 back-to-back frames recorded in one command list
     (one CUDA graph launch; its 8 MB working set stays in L2, which is stated) and as single-frame
     graph launches with L2 flushed before each (these include the launch latency). Algorithmic bytes per frame: indices + unique vertices (32 B) + the
     texture footprint (min(size, 4 taps x 4 B x fragments)) + colour and depth written once."""
@@ -257,8 +257,8 @@ def run_single_draw_section(dev, args):
     for _ in range(5):
         r.render_batched()
     ctx.finish()
-    # 100 frames back to back in one command list (one graph launch): the device time per frame
-    n = 100
+    # 1,000 frames back to back in one command list (one graph launch): the device time per frame
+    n = 1000
     rep = r.record_repeated(n)
     for _ in range(3):
         ctx.execute_command_list(rep)
