@@ -745,7 +745,8 @@ def main():
     if world > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
+        if args.impl == "gb300":   # the reference arm runs on the host cores only
+            torch.cuda.set_device(local)
         dist.init_process_group("nccl" if args.impl == "gb300" else "gloo")
     if args.impl == "reference" and args.port_vs_reference:
         return port_vs_reference(args) if rank == 0 else 0
