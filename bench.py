@@ -58,8 +58,9 @@ def parse():
     ap.add_argument("--diff-steps", type=int, default=100)
     ap.add_argument("--profile-once", action="store_true",
                     help="render the frame once (batched, eager) and exit: a short launch sequence for ncu")
-    ap.add_argument("--profile-workload", default="scene", choices=["scene", "single"],
-                    help="--profile-once: the scene frame or the single draw (icosphere L5 at 1280x720)")
+    ap.add_argument("--profile-workload", default="scene", choices=["scene", "single", "multiview"],
+                    help="--profile-once: the scene frame, the single draw (icosphere L5 at 1280x720) or "
+                         "the 64-view batch (one batched execution at the default launch shapes)")
     ap.add_argument("--persistent", action="store_true",
                     help="--profile-once: the batch as one persistent launch (k_batch)")
     ap.add_argument("--warps-per-tile", type=int, default=0,
@@ -769,8 +770,12 @@ def main():
         print(json.dumps({"profile_diff": profile_diff(dev, args.profile_diff_views)}))
         dev.destroy()
         return 0
-    frame = scenes.config1_plain() if args.profile_once and args.profile_workload == "single" \
-        else scenes.config2_scene(seed=args.seed)
+    if args.profile_once and args.profile_workload == "single":
+        frame = scenes.config1_plain()
+    elif args.profile_once and args.profile_workload == "multiview":
+        frame = scenes.config3_batched(seed=3)
+    else:
+        frame = scenes.config2_scene(seed=args.seed)
     r = api.FrameRenderer(dev, frame)
     if args.profile_once:
         if args.warps_per_tile:
