@@ -789,6 +789,10 @@ static mlv_status launch_draws(mlv_context_t *c, const Plan &p, DrawDesc *d_draw
     bp.vs_out = w.vs_out;
     bp.raster = w.raster;
     bp.shade = w.shade;
+    // the 48-byte shading record when every pixel shader of the batch reads only U and V
+    bool uv_only = true;
+    for (const DrawDesc &d : p.draws) uv_only = uv_only && (d.ps == MLV_PS_BASIC || d.ps == kPsNone);
+    bp.shade_stride = uv_only ? kShadeUV : kShadeFull;
     bp.geom = w.keep_geom ? w.geom : nullptr;
     bp.tri_info = w.tri_info;
     bp.jobs = w.jobs;

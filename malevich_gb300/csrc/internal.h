@@ -98,12 +98,18 @@ struct TriRaster {
     int4 w[4];
 };
 
-// Per assembled triangle, read once per shaded pixel: 80 bytes.
+// Per assembled triangle, read once per shaded pixel: 80 bytes (kShadeFull float4s).
 //   s0 = rw0, rw1, rw2, draw          s1..s3 = reg1 (xyzw) of vertices 0..2
 //   s4 = reg2.x of vertices 0..2, pad
+// In a batch whose pixel shaders read only U and V (basic_ps, or none), 48 bytes (kShadeUV):
+//   s0 = rw0, rw1, rw2, draw          s1 = U of vertices 0..2, V of vertex 0
+//   s2 = V of vertices 1 and 2, pad
+// The records of a batch are BatchParams::shade_stride float4s apart; the workspace is sized for
+// the full form.
 struct TriShade {
     float4 s[5];
 };
+constexpr uint32_t kShadeFull = 5, kShadeUV = 3;
 
 // Screen-space positions (reg0 after the viewport transform), for the differentiable path.
 struct TriGeom {
@@ -159,7 +165,8 @@ struct BatchParams {
     float4 *vs_out;                      // [total_vertices] SV_POSITION, then [total_vertices][2] attributes:
                                          // reg1, (reg2.x, 0, 0, 0)
     TriRaster *raster;                   // [total_tris + overflow_capacity]
-    TriShade *shade;
+    TriShade *shade;                     // records shade_stride float4s apart (see TriShade)
+    uint32_t shade_stride;               // kShadeFull, or kShadeUV
     TriGeom *geom;                       // nullptr unless the geometry is kept
     uint16_t *tri_info;                  // [total_tris]: emitted-fan mask | clipped << 8
     uint2 *clip_list;                    // [total_tris]: (input triangle, draw) that k_geometry leaves to k_clip

@@ -287,7 +287,7 @@ __device__ __forceinline__ void raster_words(const Setup &s, int4 *r) {
 
 __device__ __forceinline__ void write_record(const BatchParams &bp, uint32_t rec, uint32_t draw, int ps,
                                              bool sole_draw, const Setup &s, const Vtx &v0, const Vtx &v1,
-                                             const Vtx &v2, uint32_t extra = 0) {
+                                             const Vtx &v2) {
     int4 w[4];
     raster_words(s, w);
     int4 *r = bp.raster[rec].w;
@@ -305,12 +305,17 @@ __device__ __forceinline__ void write_record(const BatchParams &bp, uint32_t rec
     // A null pixel shader reads no 1/w and no attributes; the tile kernel still takes the draw
     // index from the record when the view has several draws (sole_draw: it has one)
     if (ps == kPsNone && sole_draw) return;
-    float4 *h = bp.shade[rec].s;
+    float4 *h = reinterpret_cast<float4 *>(bp.shade) + (size_t)rec * bp.shade_stride;
     h[0] = make_float4(s.rw[0], s.rw[1], s.rw[2], __uint_as_float(draw));
+    if (bp.shade_stride == kShadeUV) {   // the batch's pixel shaders read U (reg1.w) and V (reg2.x) only
+        h[1] = make_float4(v0.v[7], v1.v[7], v2.v[7], v0.v[8]);
+        h[2] = make_float4(v1.v[8], v2.v[8], 0.0f, 0.0f);
+        return;
+    }
     h[1] = make_float4(v0.v[4], v0.v[5], v0.v[6], v0.v[7]);
     h[2] = make_float4(v1.v[4], v1.v[5], v1.v[6], v1.v[7]);
     h[3] = make_float4(v2.v[4], v2.v[5], v2.v[6], v2.v[7]);
-    h[4] = make_float4(v0.v[8], v1.v[8], v2.v[8], __uint_as_float(extra));
+    h[4] = make_float4(v0.v[8], v1.v[8], v2.v[8], 0.0f);
 }
 
 // clip_by_plane, main.c:609-647 (Sutherland-Hodgman on one normalised plane, plane_d = 0), run by a
@@ -1467,8 +1472,9 @@ __device__ __forceinline__ void shade_pixel(const BatchParams &bp, const ViewDes
     const int4 w0 = R[0], w1 = R[1], w2 = R[2], w3 = R[3];
     // the winner's draw: the view's only one, or the index its shading record keeps
     const bool sole = V.draw_count == 1;
+    const float4 *S = reinterpret_cast<const float4 *>(bp.shade) + (size_t)rec * bp.shade_stride;
     float4 s0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    if (!sole) s0 = bp.shade[rec].s[0];
+    if (!sole) s0 = S[0];
     const DrawDesc &D = bp.draws[sole ? V.draw_begin : __float_as_uint(s0.w)];
     const uint32_t E1 = (((uint32_t)w0.w * (uint32_t)x) << kSubpix) + (((uint32_t)w1.x * (uint32_t)y) << kSubpix) + (uint32_t)w1.y;
     const uint32_t E2 = (((uint32_t)w1.z * (uint32_t)x) << kSubpix) + (((uint32_t)w1.w * (uint32_t)y) << kSubpix) + (uint32_t)w2.x;
@@ -1479,7 +1485,6 @@ __device__ __forceinline__ void shade_pixel(const BatchParams &bp, const ViewDes
     float z = z0 + (z1 - z0) * b1;
     z = z + (z2 - z0) * b2;
     if (D.ps != kPsNone) {
-        const float4 *S = bp.shade[rec].s;
         if (sole) s0 = S[0];
         // perspective correction, main.c:1106-1115
         float den = (1.0f - (b1 + b2)) * s0.x;
@@ -1488,13 +1493,23 @@ __device__ __forceinline__ void shade_pixel(const BatchParams &bp, const ViewDes
         den = 1.0f / den;
         const float pb1 = (b1 * s0.y) * den;
         const float pb2 = (b2 * s0.z) * den;
-        const float4 r0 = S[1], r1 = S[2], r2 = S[3], uv2 = S[4];
         auto interp = [&](float v0, float v1, float v2) {
             float tmp = v0 + (v1 - v0) * pb1;
             return tmp + (v2 - v0) * pb2;
         };
-        const float a0 = interp(r0.x, r1.x, r2.x), a1 = interp(r0.y, r1.y, r2.y), a2 = interp(r0.z, r1.z, r2.z);
-        const float u = interp(r0.w, r1.w, r2.w), v = interp(uv2.x, uv2.y, uv2.z);
+        float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, u, v;
+        if (bp.shade_stride == kShadeUV) {   // U and V only (basic_ps reads nothing else)
+            const float4 q1 = S[1], q2 = S[2];
+            u = interp(q1.x, q1.y, q1.z);
+            v = interp(q1.w, q2.x, q2.y);
+        } else {
+            const float4 r0 = S[1], r1 = S[2], r2 = S[3], uv2 = S[4];
+            a0 = interp(r0.x, r1.x, r2.x);
+            a1 = interp(r0.y, r1.y, r2.y);
+            a2 = interp(r0.z, r1.z, r2.z);
+            u = interp(r0.w, r1.w, r2.w);
+            v = interp(uv2.x, uv2.y, uv2.z);
+        }
         const float3 c = run_ps(D.ps, a0, a1, a2, u, v, D.ps_tex);
         V.color[o] = pack_color(c.x, c.y, c.z);
     } else if (V.clear_flags & kClearColor) {

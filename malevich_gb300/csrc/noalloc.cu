@@ -270,6 +270,7 @@ extern "C" MLV_API mlv_status mlv_draw_indexed_noalloc(const mlv_noalloc_draw *a
     bp.vs_out = (float4 *)(base + kOffVsOut);
     bp.raster = (TriRaster *)(base + kOffRaster);
     bp.shade = (TriShade *)(base + kOffShade);
+    bp.shade_stride = kShadeFull;
     bp.tri_info = (uint16_t *)(base + kOffTriInfo);
     bp.jobs = (uint4 *)(base + kOffJobs);
     bp.jobs_capacity = kMaxTriangles + kMaxFanSlots;
