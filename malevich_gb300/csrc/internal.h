@@ -163,7 +163,8 @@ struct BatchParams {
     uint32_t total_vertices;             // sum of vs_count
     uint32_t want_rank;                  // 1: compute assembled-triangle ranks (visibility, capture)
     float4 *vs_out;                      // [total_vertices] SV_POSITION, then [total_vertices][2] attributes:
-                                         // reg1, (reg2.x, 0, 0, 0)
+                                         // reg1, (reg2.x, 0, 0, 0); with shade_stride kShadeUV,
+                                         // [total_vertices] float2 (reg1.w, reg2.x) instead
     TriRaster *raster;                   // [total_tris + overflow_capacity]
     TriShade *shade;                     // records shade_stride float4s apart (see TriShade)
     uint32_t shade_stride;               // kShadeFull, or kShadeUV

@@ -481,9 +481,13 @@ __device__ __forceinline__ void vertex_body(const BatchParams &bp, uint32_t blk)
     // shader reads no attributes
     bp.vs_out[v] = make_float4(o[0], o[1], o[2], o[3]);
     if (d.ps != kPsNone) {
-        float4 *attr = bp.vs_out + bp.total_vertices + 2 * (size_t)v;
-        attr[0] = make_float4(o[4], o[5], o[6], o[7]);
-        attr[1] = make_float4(o[8], 0.0f, 0.0f, 0.0f);
+        if (bp.shade_stride == kShadeUV) {   // the batch's pixel shaders read U and V only
+            reinterpret_cast<float2 *>(bp.vs_out + bp.total_vertices)[v] = make_float2(o[7], o[8]);
+        } else {
+            float4 *attr = bp.vs_out + bp.total_vertices + 2 * (size_t)v;
+            attr[0] = make_float4(o[4], o[5], o[6], o[7]);
+            attr[1] = make_float4(o[8], 0.0f, 0.0f, 0.0f);
+        }
     }
 }
 
@@ -491,6 +495,23 @@ __global__ void __launch_bounds__(kVertexBlock) k_vertex(BatchParams bp) {
     pdl_wait();
     vertex_body(bp, blockIdx.x);
     pdl_trigger();
+}
+
+// The attributes of shaded vertex `slot` (o[4..8]: reg1.xyzw, reg2.x) from the shaded-vertex
+// buffer: two float4s a vertex, or in a batch whose pixel shaders read only U and V, (U, V), with
+// reg1.xyz, which no such shader reads, left zero.
+template <bool COHERENT = false>
+__device__ __forceinline__ void load_attributes(const BatchParams &bp, size_t slot, float *o) {
+    if (bp.shade_stride == kShadeUV) {
+        const float2 uv = ld_stage<COHERENT>(reinterpret_cast<const float2 *>(bp.vs_out + bp.total_vertices) + slot);
+        o[4] = o[5] = o[6] = 0.0f;
+        o[7] = uv.x;
+        o[8] = uv.y;
+        return;
+    }
+    const float4 *attr = bp.vs_out + bp.total_vertices + 2 * slot;
+    const float4 b = ld_stage<COHERENT>(attr), c = ld_stage<COHERENT>(attr + 1);
+    o[4] = b.x; o[5] = b.y; o[6] = b.z; o[7] = b.w; o[8] = c.x;
 }
 
 // Vertex k of a triangle: from the shaded-vertex buffer, or shaded here (per-index path, and for
@@ -508,9 +529,7 @@ __device__ __forceinline__ void triangle_vertex(const BatchParams &bp, const Dra
                 o[4] = o[5] = o[6] = o[7] = o[8] = 0.0f;
                 return;
             }
-            const float4 *attr = bp.vs_out + bp.total_vertices + 2 * slot;
-            const float4 b = ld_stage<COHERENT>(attr), c = ld_stage<COHERENT>(attr + 1);
-            o[4] = b.x; o[5] = b.y; o[6] = b.z; o[7] = b.w; o[8] = c.x;
+            load_attributes<COHERENT>(bp, slot, o);
             return;
         }
     }
@@ -545,9 +564,7 @@ __device__ __forceinline__ uint32_t triangle_position(const BatchParams &bp, con
 template <bool COHERENT = false>
 __device__ __forceinline__ void triangle_attributes(const BatchParams &bp, uint32_t slot, float *o) {
     if (slot == kNoSlot) return;
-    const float4 *attr = bp.vs_out + bp.total_vertices + 2 * (size_t)slot;
-    const float4 b = ld_stage<COHERENT>(attr), c = ld_stage<COHERENT>(attr + 1);
-    o[4] = b.x; o[5] = b.y; o[6] = b.z; o[7] = b.w; o[8] = c.x;
+    load_attributes<COHERENT>(bp, slot, o);
 }
 
 // Slot of the record a triangle key names (see BatchParams).
